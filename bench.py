@@ -1,0 +1,256 @@
+"""Benchmark of the srp draw path on GB300.
+
+Workload (one "step" = one frame): the ~2M-triangle soup of random geodesic
+spheres at 1920x1080 (1024^2 random texture, scissor = central 80%, stencil
+INCR on depth pass, depth LESS, mixed perspective/affine/flat varyings),
+followed by 100k lines and 100k points -- three srp draw calls.
+
+  value   Mfrag/s with vertex/index data already resident in HBM; the frame's
+          draws are timed with CUDA events on the library's stream, the L2 is
+          flushed and the framebuffer re-initialised between frames, outside
+          the events.
+  e2e     the same frame through the public API from host memory: the vertex
+          and index bytes are copied in with srpVertexBufferCopyData /
+          srpIndexBufferCopyData (uploaded by the draw), and the framebuffer
+          planes are read back to the host, all inside the timed region.
+A fragment is a pixel that passed coverage and the scissor test (before depth
+and stencil), counted the same way by the CPU oracle.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's algorithm on the host cores: the CPU
+oracle (a restatement of the reference, bit-identical to it) rendering the
+same frame, one process per core. N > 1 runs independent replicas (the path
+does not shard across GPUs within a frame).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SCENE = "soup"
+SEED = 1
+WORKLOAD = "soup: 2.0M-triangle geodesic-sphere soup, 1920x1080, 100k lines, 100k points"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    def __init__(self, index):
+        self.index, self.samples, self.proc = index, [], None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm = []
+        mx = 0.0
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[0]))
+                mx = max(mx, float(s[1]))
+                for n, v in zip(names, s[3:7]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+            except Exception:
+                pass
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_frame(scale, frames, seed=SEED):
+    exe = os.path.join(ROOT, "oracle", "_build", "port_scenes")
+    out = subprocess.check_output([exe, "time", SCENE, str(seed), repr(float(scale)), str(frames)]).decode()
+    return json.loads(out.strip().splitlines()[-1])
+
+
+def run_reference(args):
+    """The reference algorithm (CPU oracle) on all host cores, one frame per
+    core per step."""
+    import concurrent.futures as cf
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from srp_gb300.build import build_oracle
+    build_oracle()
+    cores = os.cpu_count() or 1
+    frames = max(1, args.warmup + args.steps)
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=cores) as ex:
+        res = list(ex.map(lambda i: cpu_frame(1.0, frames, SEED + i % 4), range(cores)))
+    wall = time.perf_counter() - t0
+    # throughput over the timed frames: each worker reports its mean frame time
+    frags = sum(r["fragments"] for r in res) / cores
+    per_core_fps = [1.0 / r["mean_s"] for r in res]
+    value = frags * sum(per_core_fps) / 1e6
+    line = {"impl": "reference", "metric": "Mfrag/s", "value": round(value, 3), "unit": "Mfrag/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1000.0 * sum(r["mean_s"] for r in res) / cores, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "seed": SEED},
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mfrag/s", "cores": cores, "kind": "port",
+                             "sample": f"{frames} full frames per core, {cores} processes, wall {wall:.1f}s"},
+            "e2e": {"value": round(value, 3), "unit": "Mfrag/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import ctypes
+    import torch
+    import srp_gb300
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    srp_gb300.build()
+    L = srp_gb300.lib()
+    L.srpGpuSetFramebufferMode(srp_gb300.SRP_GPU_FB_DEVICE)
+    stream = torch.cuda.Stream()
+    L.srpGpuSetStream(ctypes.c_void_p(stream.cuda_stream))
+    sc = srp_gb300.Scene(SCENE, SEED + rank, args.scale)
+    info = sc.info
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def frame():
+        sc.render()
+
+    # warm-up
+    for _ in range(max(args.warmup, 1)):
+        with torch.cuda.stream(stream):
+            sc.prepare()
+            frame()
+    torch.cuda.synchronize()
+    L.srpGpuResetStats()
+    st0 = srp_gb300.SRPGpuStats()
+    clocks = ClockSampler(local)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    times = []
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            sc.prepare()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            frame()
+            e1.record(stream)
+        stream.synchronize()
+        times.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall0
+    L.srpGpuGetStats(ctypes.byref(st0))
+    frags_per_frame = st0.fragments / max(args.steps, 1)
+    launches = st0.kernelLaunches
+    # end-to-end through the API from host memory
+    e2e_times = []
+    for _ in range(max(2, args.steps // 2)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sc.upload()
+        sc.prepare()
+        frame()
+        sc.sync()
+        e2e_times.append(time.perf_counter() - t0)
+    clk = clocks.stop()
+    total_ms = sum(times)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = frags_per_frame * args.steps * world / (total_ms / 1000.0) / 1e6
+    e2e_s = sum(e2e_times) / len(e2e_times)
+    h2d = info.vertexBytes + info.indexBytes
+    d2h = info.width * info.height * 9
+    peak, peak_kind = peaks()
+    algo_bytes = (info.vertexBytes + info.indexBytes + info.width * info.height * 9 * 2 + info.textureBytes)
+    achieved = algo_bytes / (total_ms / args.steps / 1000.0) / 1e9
+    line = {
+        "metric": "Mfrag/s", "value": round(value, 3), "unit": "Mfrag/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "seed": SEED, "width": info.width, "height": info.height,
+                   "triangles": info.inputTriangles, "lines": info.inputLines, "points": info.inputPoints,
+                   "fragments_per_frame": frags_per_frame, "l2": "flushed between frames (256 MB write)",
+                   "frames_per_s": round(args.steps / (total_ms / 1000.0), 2),
+                   "mtri_per_s": round(info.inputTriangles * args.steps / (total_ms / 1000.0) / 1e6, 2)},
+        "clocks": clk,
+        "e2e": {"value": round(frags_per_frame / e2e_s / 1e6, 3), "unit": "Mfrag/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None,
+                     "note": f"whole frame, algorithmic bytes {algo_bytes}, peak {peak_kind}"},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        from srp_gb300.build import build_oracle
+        build_oracle()
+        r = cpu_frame(1.0, 3)
+        line["cpu_baseline"] = {"value": round(r["fragments"] / r["mean_s"] / 1e6, 3), "unit": "Mfrag/s",
+                                "cores": 1, "kind": "port",
+                                "sample": "3 full frames of the same workload on 1 host core"}
+    if rank == 0:
+        print(json.dumps(line))
+    sc.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

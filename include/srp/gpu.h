@@ -1,0 +1,87 @@
+/* srp-gb300: additions to the srp API for the GPU implementation.
+ *
+ * Nothing here has a counterpart in kitrofimov/srp; the reference API itself
+ * (srp/srp.h) is implemented unchanged. These entry points cover what a GPU
+ * build needs beyond it: mapping host shader functions to device shaders,
+ * controlling when the framebuffer's host mirrors are refreshed, choosing the
+ * CUDA stream, and reading counters. All are plain C (extern "C"). */
+#pragma once
+
+#include <stddef.h>
+#include <stdint.h>
+#include "srp/srp.h"
+#include "srp/shaderlib.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ shaders */
+
+/** Map a host vertex shader function to a built-in device shader. The
+ *  built-in host functions of srp/shaderlib.h are mapped already. */
+void srpGpuRegisterVertexShader(void (*hostShader)(SRPVertexShaderIn*, SRPVertexShaderOut*),
+                                SRPGpuVertexShaderId deviceShader);
+/** Map a host fragment shader function to a built-in device shader. */
+void srpGpuRegisterFragmentShader(void (*hostShader)(SRPFragmentShaderIn*, SRPFragmentShaderOut*),
+                                  SRPGpuFragmentShaderId deviceShader);
+
+/* -------------------------------------------------------- framebuffer */
+
+typedef enum SRPGpuFramebufferMode
+{
+	/** Default, for unmodified srp programs: every draw first uploads the
+	 *  host planes (which the program may have edited) and afterwards
+	 *  downloads the result, and every clear is mirrored, so the public
+	 *  color/depth/stencil arrays are always current. */
+	SRP_GPU_FB_COHERENT = 0,
+	/** The device planes are authoritative. Host arrays are refreshed only by
+	 *  srpGpuFramebufferSync and pushed only by srpGpuFramebufferUpload. */
+	SRP_GPU_FB_DEVICE = 1
+} SRPGpuFramebufferMode;
+
+void srpGpuSetFramebufferMode(SRPGpuFramebufferMode mode);
+SRPGpuFramebufferMode srpGpuGetFramebufferMode(void);
+
+/** Copy the device planes into the host arrays (waits for the GPU). */
+void srpGpuFramebufferSync(const SRPFramebuffer* fb);
+/** Copy the host arrays to the device planes. */
+void srpGpuFramebufferUpload(const SRPFramebuffer* fb);
+
+#define SRP_GPU_FILL_COLOR   1u
+#define SRP_GPU_FILL_DEPTH   2u
+#define SRP_GPU_FILL_STENCIL 4u
+/** Fill the selected device planes with constants (stream-ordered). */
+void srpGpuFramebufferFill(const SRPFramebuffer* fb, uint32_t color, float depth, uint8_t stencil,
+                           unsigned planes);
+
+/* ------------------------------------------------------ stream, stats */
+
+/** Launch all work on `stream` (a cudaStream_t; NULL = the library's own
+ *  stream). Must be called outside of any draw. */
+void srpGpuSetStream(void* stream);
+void* srpGpuGetStream(void);
+/** Block until all queued work has finished; reports pending device errors
+ *  through the message callback. Returns 0 if no error was pending. */
+int srpGpuSynchronize(void);
+
+typedef struct SRPGpuStats
+{
+	uint64_t fragments;          /* fragments that passed coverage + scissor */
+	uint64_t primitives;         /* primitives after clipping and culling */
+	uint64_t binEntries;         /* (tile, primitive) pairs binned */
+	uint64_t clipOverflows;      /* clipped polygons with more than 6 vertices */
+	uint64_t draws;
+	uint64_t kernelLaunches;     /* kernels launched by the library */
+} SRPGpuStats;
+
+/** Read the counters accumulated since the last reset (waits for the GPU). */
+void srpGpuGetStats(SRPGpuStats* stats);
+void srpGpuResetStats(void);
+
+/** Tile edge in pixels used by the binning and raster stages (8 or 16). */
+void srpGpuSetTileSize(int tileSize);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,187 @@
+"""srp_gb300: the srp draw path on GB300 (sm_103a), behind srp's own C API.
+
+The product is the shared library ``srp_gb300/lib/libsrp_gb300.so`` whose
+exported symbols are the reference's public C API (include/srp/*.h) plus the
+GPU additions of include/srp/gpu.h. This package only builds it and binds it
+with ctypes for Python callers (tests, benchmarks). There is no CPU fallback:
+when the library is missing or no GPU is present, calls that need the GPU fail
+loudly.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .build import LIB, ROOT, build  # noqa: F401
+
+_lib = None
+_scenes = None
+
+SRP_GPU_FB_COHERENT = 0
+SRP_GPU_FB_DEVICE = 1
+
+
+class SRPGpuStats(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_uint64) for n in
+                ("fragments", "primitives", "binEntries", "clipOverflows", "draws", "kernelLaunches")]
+
+
+class SceneInfo(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int), ("height", ctypes.c_int),
+                ("inputTriangles", ctypes.c_size_t), ("inputLines", ctypes.c_size_t),
+                ("inputPoints", ctypes.c_size_t), ("vertexBytes", ctypes.c_size_t),
+                ("indexBytes", ctypes.c_size_t), ("textureBytes", ctypes.c_size_t),
+                ("draws", ctypes.c_int), ("usesStencil", ctypes.c_int)]
+
+
+MESSAGE_CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p,
+                                    ctypes.c_void_p)
+
+
+class SRPMessageCallback(ctypes.Structure):
+    _fields_ = [("func", MESSAGE_CALLBACK), ("userParameter", ctypes.c_void_p)]
+
+
+def library_path():
+    return os.path.join(LIB, "libsrp_gb300.so")
+
+
+def lib():
+    """The GPU library (C ABI). Raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: run srp_gb300.build() (nvcc, sm_103a) first")
+        L = ctypes.CDLL(path)
+        L.srpGpuGetStats.argtypes = [ctypes.POINTER(SRPGpuStats)]
+        L.srpGpuSetFramebufferMode.argtypes = [ctypes.c_int]
+        L.srpGpuSetStream.argtypes = [ctypes.c_void_p]
+        L.srpGpuGetStream.restype = ctypes.c_void_p
+        L.srpGpuSynchronize.restype = ctypes.c_int
+        L.srpSetMessageCallback.argtypes = [SRPMessageCallback]
+        _lib = L
+    return _lib
+
+
+def scenes():
+    """The seeded scene library, driving the GPU library through the srp API."""
+    global _scenes
+    if _scenes is None:
+        lib()  # the scene library resolves srp* (and srpContext) against it
+        path = os.path.join(LIB, "libsrp_scenes_gpu.so")
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is missing: run srp_gb300.build() first")
+        S = ctypes.CDLL(path)
+        S.sceneCreate.restype = ctypes.c_void_p
+        S.sceneCreate.argtypes = [ctypes.c_char_p, ctypes.c_uint64, ctypes.c_double]
+        S.sceneDestroy.argtypes = [ctypes.c_void_p]
+        S.sceneGetInfo.argtypes = [ctypes.c_void_p, ctypes.POINTER(SceneInfo)]
+        S.sceneInputHash.restype = ctypes.c_uint64
+        S.sceneInputHash.argtypes = [ctypes.c_void_p]
+        S.sceneUpload.argtypes = [ctypes.c_void_p]
+        S.scenePrepareFramebuffer.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        S.sceneRender.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        S.sceneNames.restype = ctypes.POINTER(ctypes.c_char_p)
+        S.srpNewFramebuffer.restype = ctypes.c_void_p
+        S.srpNewFramebuffer.argtypes = [ctypes.c_size_t, ctypes.c_size_t]
+        S.srpFreeFramebuffer.argtypes = [ctypes.c_void_p]
+        S.srpGpuFramebufferSync.argtypes = [ctypes.c_void_p]
+        _scenes = S
+    return _scenes
+
+
+def scene_names():
+    S = scenes()
+    out, p = [], S.sceneNames()
+    i = 0
+    while p[i]:
+        out.append(p[i].decode())
+        i += 1
+    return out
+
+
+class FramebufferView(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_size_t), ("height", ctypes.c_size_t), ("size", ctypes.c_size_t),
+                ("color", ctypes.POINTER(ctypes.c_uint32)), ("depth", ctypes.POINTER(ctypes.c_float)),
+                ("stencil", ctypes.POINTER(ctypes.c_uint8))]
+
+
+def framebuffer_arrays(fb):
+    """Copies of the host planes of an SRPFramebuffer* (after a sync)."""
+    v = ctypes.cast(fb, ctypes.POINTER(FramebufferView)).contents
+    n = v.size
+    color = np.ctypeslib.as_array(v.color, shape=(n,)).copy()
+    depth = np.ctypeslib.as_array(v.depth, shape=(n,)).copy()
+    stencil = np.ctypeslib.as_array(v.stencil, shape=(n,)).copy()
+    return color, depth, stencil
+
+
+class Scene:
+    """A seeded scene whose draws run on the GPU through the srp API."""
+
+    def __init__(self, name, seed=1, scale=1.0):
+        self.S = scenes()
+        self.ptr = self.S.sceneCreate(name.encode(), seed, scale)
+        if not self.ptr:
+            raise ValueError(f"unknown scene {name}")
+        self.info = SceneInfo()
+        self.S.sceneGetInfo(self.ptr, ctypes.byref(self.info))
+        self.name, self.seed, self.scale = name, seed, scale
+        self.fb = self.S.srpNewFramebuffer(self.info.width, self.info.height)
+        if not self.fb:
+            raise RuntimeError("srpNewFramebuffer failed (no GPU?)")
+
+    @property
+    def input_hash(self):
+        return self.S.sceneInputHash(self.ptr)
+
+    def upload(self):
+        self.S.sceneUpload(self.ptr)
+
+    def prepare(self):
+        self.S.scenePrepareFramebuffer(self.ptr, self.fb)
+
+    def render(self):
+        self.S.sceneRender(self.ptr, self.fb)
+
+    def sync(self):
+        self.S.srpGpuFramebufferSync(self.fb)
+
+    def planes(self):
+        self.sync()
+        return framebuffer_arrays(self.fb)
+
+    def close(self):
+        if self.fb:
+            self.S.srpFreeFramebuffer(self.fb)
+            self.fb = None
+        if self.ptr:
+            self.S.sceneDestroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def render_scene(name, seed=1, scale=1.0):
+    """Render one frame of a scene on the GPU; returns (color, depth, stencil,
+    width, height, stats, input_hash)."""
+    L = lib()
+    L.srpGpuSetFramebufferMode(SRP_GPU_FB_DEVICE)
+    sc = Scene(name, seed, scale)
+    try:
+        sc.prepare()
+        L.srpGpuResetStats()
+        sc.render()
+        c, d, s = sc.planes()
+        st = SRPGpuStats()
+        L.srpGpuGetStats(ctypes.byref(st))
+        if L.srpGpuSynchronize() != 0:
+            raise RuntimeError("GPU error during the draw")
+        return c, d, s, sc.info.width, sc.info.height, st, sc.input_hash
+    finally:
+        sc.close()

@@ -1,0 +1,146 @@
+/* Types shared by the host side of the library and its CUDA kernels. */
+#pragma once
+
+#include <stdint.h>
+#include <stddef.h>
+
+namespace srpg {
+
+/* Largest user uniform block the GPU path accepts (it travels as a kernel
+ * parameter, so shaders read it from the constant bank). */
+constexpr int kMaxUniformBytes = 1024;
+/* Largest vertex record / varying block handled by the kernels. */
+constexpr int kMaxVertexWords = 32;
+constexpr int kMaxVaryingWords = 32;
+constexpr int kMaxVaryings = 16;
+/* Vertices a Sutherland-Hodgman polygon can reach (3 + one per plane). */
+constexpr int kMaxPoly = 9;
+
+enum VaryingMode : uint8_t { kPerspective = 0, kAffine = 1, kFlat = 2 };
+
+/* One varying attribute: nItems elements of `type` at byte offset `offset`. */
+struct VaryingAttr {
+	uint16_t offset;
+	uint16_t nItems;
+	uint8_t type;        /* SRPType */
+	uint8_t mode;        /* VaryingMode */
+	uint8_t elemSize;
+	uint8_t pad;
+};
+
+struct VaryingLayout {
+	int nAttr;
+	int sizeBytes;
+	int nWords;          /* ceil(sizeBytes / 4) */
+	int floatOnly;       /* every attribute is 4-byte float/int at a 4-aligned offset */
+	VaryingAttr attr[kMaxVaryings];
+	uint8_t wordMode[kMaxVaryingWords];   /* floatOnly: per-word VaryingMode */
+	uint8_t wordIsFloat[kMaxVaryingWords];
+};
+
+struct StencilFace {
+	int func, sfail, dfail, pass;
+	uint32_t ref, mask, writeMask, pad;
+};
+
+/* Pipeline state for one draw (a snapshot of SRPContext plus derived values). */
+struct DrawState {
+	int W, H;
+	int frontFaceCW;
+	int cullFace;        /* SRPFace */
+	int polygonMode;
+	float pointSize;
+	int provokingFirst;
+	int scissorEnabled;
+	uint64_t sx0, sx1, sy0, sy1;   /* [x0, x0 + width) with size_t wrap-around */
+	int stencilEnabled;
+	int depthTest, depthWrite, depthOp;
+	int earlyZ;          /* !mayOverwriteDepth */
+	int pad0;
+	StencilFace front, back;
+	int tile;            /* tile edge in pixels */
+	int tilesX, tilesY;
+	int pad1;
+};
+
+/* Device texture descriptor (RGBA8 texels, alpha unused: the reference keeps
+ * three channels and reads alpha as 1). */
+struct TextureDesc {
+	const uint32_t* texels;
+	int width, height, wm1, hm1;
+	int wrapX, wrapY;
+};
+
+/* Triangle record read by the tile resolve kernel (64 bytes). */
+struct __align__(16) TriRaster {
+	float l0[3];         /* barycentrics at the centre of the bbox-min pixel */
+	float dx[3], dy[3];  /* per-pixel and per-row increments */
+	float c[3];          /* z_ndc * invW per vertex (depth = sum c_i * lambda_i) */
+	uint16_t minX, minY, maxX, maxY;   /* bbox, max exclusive */
+	uint32_t flags;      /* bit0 front facing, bits1..3 top-left flags */
+	uint32_t pad;
+};
+
+/* Triangle data needed only for shading (32 bytes). */
+struct __align__(16) TriAttr {
+	float invW[3];
+	uint32_t vref[3];    /* rows of the post-VS vertex arrays */
+	uint32_t id;         /* primitiveID */
+	uint32_t pad;
+};
+
+/* Line record after setup (48 bytes). */
+struct __align__(16) LineRec {
+	float x0, y0, xInc, yInc;
+	float tInc;
+	int32_t steps;
+	float c[2];          /* z_ndc * invW */
+	float invW[2];
+	uint32_t vref[2];
+	uint32_t id;
+	uint32_t fragBase;   /* first fragment slot */
+	uint32_t pad[2];
+};
+
+/* One line fragment (16 bytes). */
+struct __align__(16) LineFrag {
+	float depth;
+	float t;
+	uint32_t line;       /* index into the line records */
+	int16_t px, py;      /* logical pixel (px may equal the width) */
+};
+
+/* Point record after setup (32 bytes). */
+struct __align__(16) PointRec {
+	float mnx, mny, mxx, mxy;   /* coverage square, [mn, mx) */
+	float z;
+	uint32_t vref;
+	uint32_t id;
+	int16_t x0, y0, x1, y1;     /* raster bounds, inclusive, clamped to the framebuffer */
+};
+
+enum PrimKind { kKindTri = 0, kKindLineFrag = 1, kKindPoint = 2 };
+
+/* Counters written by the kernels, read back by the host. */
+struct DeviceCounters {
+	unsigned long long fragments;
+	unsigned long long prims;        /* primitives emitted by setup */
+	unsigned long long entries;      /* (tile, primitive) pairs */
+	unsigned long long bigJobs;
+	unsigned long long clipVerts;    /* clip-generated vertices */
+	unsigned long long lineFrags;
+	unsigned long long clipOverflow;
+	unsigned int errors;             /* bit mask, see kErr* */
+	unsigned int lookbackTicket;
+	unsigned int nonEmptyTiles;
+	unsigned int pad;
+};
+
+enum : unsigned {
+	kErrBadIndex = 1u,        /* vertex index outside the vertex buffer */
+	kErrCapacity = 2u,        /* a scratch buffer was too small (draw is retried) */
+	kErrSpin = 4u,            /* a bounded wait gave up */
+	kErrUnsupported = 8u,
+};
+
+}  // namespace srpg

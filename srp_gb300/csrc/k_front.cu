@@ -1,0 +1,824 @@
+/* Front end of a draw: vertex range, vertex shading, primitive assembly with
+ * clipping and setup, ordered compaction, tile-pair emission, line DDA.
+ *
+ * Reference behaviour restated here (kitrofimov/srp):
+ *   topology            src/pipeline/topology.c:14-83
+ *   post-VS cache       src/pipeline/vertex_processing.c:23-74, 90-112
+ *   clipping            src/pipeline/clipping.c:68-277
+ *   triangle setup      src/raster/triangle.c:113-238
+ *   line setup / DDA    src/raster/line.c:34-96
+ *   point setup         src/raster/point.c:32-118
+ *   numbering           src/pipeline/primitive_assembly.c:37-254
+ * The reference numbers surviving primitives serially (post-clip, post-cull,
+ * in submission order). Here one thread handles one input primitive; block
+ * scans plus a decoupled look-back across blocks give every survivor the
+ * same number, and the offset of its (tile, primitive) pairs, in one pass. */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "device_common.cuh"
+#include "kernels.h"
+#include "srp/buffer.h"
+
+namespace srpg {
+__device__ __forceinline__ void devTexSample(const void* tex, float u, float v, float out[4])
+{
+	textureSample((const TextureDesc*) tex, u, v, out);
+}
+}  // namespace srpg
+#define SRP_DEVICE_TEXTURE_SAMPLE(tex, u, v, out) srpg::devTexSample((const void*) (tex), u, v, out)
+#include "srp/shaderlib_impl.h"
+
+namespace srpg {
+
+/* ----------------------------------------------------------- reset/range */
+
+__global__ void k_reset(const __grid_constant__ DrawParams P)
+{
+	if (threadIdx.x == 0) {
+		/* per-draw counters start at zero; the fragment total accumulates */
+		DeviceCounters c = {};
+		c.fragments = P.ctr->fragments;
+		*P.ctr = c;
+		P.minmax[0] = ~0ull;
+		P.minmax[1] = 0ull;
+	}
+}
+
+__device__ __forceinline__ unsigned long long fetchIndex(const DrawParams& P, unsigned long long i)
+{
+	switch (P.indexSize) {
+	case 1: return ((const uint8_t*) P.indices)[i];
+	case 2: return ((const uint16_t*) P.indices)[i];
+	case 4: return ((const uint32_t*) P.indices)[i];
+	case 8: return ((const unsigned long long*) P.indices)[i];
+	default: return i;
+	}
+}
+
+/* min/max vertex index over the draw's index range
+ * (src/pipeline/vertex_processing.c:90-112). */
+__global__ void k_index_range(const __grid_constant__ DrawParams P)
+{
+	unsigned long long lo = ~0ull, hi = 0;
+	for (unsigned long long i = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; i < P.count;
+	     i += (unsigned long long) gridDim.x * blockDim.x) {
+		const unsigned long long v = fetchIndex(P, P.start + i);
+		lo = v < lo ? v : lo;
+		hi = v > hi ? v : hi;
+	}
+	for (int o = 16; o; o >>= 1) {
+		const unsigned long long l2 = __shfl_xor_sync(0xFFFFFFFFu, lo, o);
+		const unsigned long long h2 = __shfl_xor_sync(0xFFFFFFFFu, hi, o);
+		lo = l2 < lo ? l2 : lo;
+		hi = h2 > hi ? h2 : hi;
+	}
+	if ((threadIdx.x & 31) == 0) {
+		atomicMin(&P.minmax[0], lo);
+		atomicMax(&P.minmax[1], hi);
+	}
+}
+
+/* --------------------------------------------------------------- vertex */
+
+constexpr int kVertexThreads = 128;
+
+template <int VS>
+__device__ __forceinline__ void runVS(SRPVertexShaderIn* in, SRPVertexShaderOut* out)
+{
+	if (VS == SRP_GPU_VS_TRANSFORM) srpslVsTransform(in, out);
+	else if (VS == SRP_GPU_VS_WORLD) srpslVsWorld(in, out);
+}
+
+/* One thread per vertex of [lo, hi]: the block's vertex records (a
+ * contiguous byte range of the user's AoS buffer) are staged through shared
+ * memory with coalesced word loads, each thread runs the vertex shader on its
+ * record, and writes the clip position and varying words. Running every
+ * vertex of the referenced range exactly once gives the same outputs as the
+ * reference's post-VS cache (the shader is a pure function of its inputs). */
+template <int VS>
+__global__ void __launch_bounds__(kVertexThreads) k_vertex(const __grid_constant__ DrawParams P,
+                                                             unsigned long long first, unsigned long long n)
+{
+	extern __shared__ uint32_t stage[];
+	unsigned long long lo, hi;
+	if (P.indexSize) { lo = P.minmax[0]; hi = P.minmax[1]; }
+	else { lo = P.start; hi = P.start + P.count - 1; }
+	if (hi >= P.nVertices) {
+		if (threadIdx.x == 0 && blockIdx.x == 0 && P.indexSize) atomicOr(&P.ctr->errors, kErrBadIndex);
+		hi = P.nVertices ? P.nVertices - 1 : 0;
+	}
+	const unsigned long long vb = first + (unsigned long long) blockIdx.x * kVertexThreads;
+	if (vb > hi || vb + kVertexThreads <= lo || P.nVertices == 0) return;
+	const unsigned long long vend = (vb + kVertexThreads < first + n) ? vb + kVertexThreads : first + n;
+	const int stride = P.stride;
+	const unsigned long long bytes = (vend - vb) * (unsigned long long) stride;
+	const unsigned char* src = P.vertices + vb * (unsigned long long) stride;
+	if ((stride & 3) == 0) {
+		const uint32_t* w = (const uint32_t*) src;
+		for (unsigned long long i = threadIdx.x; i < bytes / 4; i += kVertexThreads) stage[i] = __ldg(w + i);
+	} else {
+		unsigned char* sb = (unsigned char*) stage;
+		for (unsigned long long i = threadIdx.x; i < bytes; i += kVertexThreads) sb[i] = __ldg(src + i);
+	}
+	__syncthreads();
+	const unsigned long long v = vb + threadIdx.x;
+	if (v >= vend || v < lo || v > hi) return;
+	uint32_t vtx[kMaxVertexWords];
+	const unsigned char* rec = (const unsigned char*) stage + (unsigned long long) threadIdx.x * stride;
+	const int words = (stride + 3) / 4 < kMaxVertexWords ? (stride + 3) / 4 : kMaxVertexWords;
+#pragma unroll
+	for (int k = 0; k < kMaxVertexWords; ++k) vtx[k] = 0;
+	if ((stride & 3) == 0) {
+#pragma unroll
+		for (int k = 0; k < kMaxVertexWords; ++k)
+			if (k < words) vtx[k] = ((const uint32_t*) rec)[k];
+	} else {
+		memcpy(vtx, rec, stride < 4 * kMaxVertexWords ? stride : 4 * kMaxVertexWords);
+	}
+	uint32_t out[kMaxVaryingWords];
+#pragma unroll
+	for (int k = 0; k < kMaxVaryingWords; ++k) out[k] = 0;
+	SRPVertexShaderIn in;
+	in.uniform = (SRPUniform*) P.uniform;
+	in.vertex = (SRPVertex*) vtx;
+	in.vertexID = (size_t) v;
+	SRPVertexShaderOut o;
+	o.clipPosition[0] = o.clipPosition[1] = o.clipPosition[2] = o.clipPosition[3] = 0.0f;
+	o.varyings = (SRPVarying*) out;
+	runVS<VS>(&in, &o);
+	P.clip[v] = make_float4(o.clipPosition[0], o.clipPosition[1], o.clipPosition[2], o.clipPosition[3]);
+	const int nw = P.L.nWords;
+	uint32_t* dst = P.vary + v * (unsigned long long) nw;
+#pragma unroll
+	for (int k = 0; k < kMaxVaryingWords; ++k)
+		if (k < nw) dst[k] = out[k];
+}
+
+/* ----------------------------------------------------------------- setup */
+
+struct PV { float4 p; uint32_t ref; };
+
+enum SetupMode { kTriFill = 0, kTriLine = 1, kTriPoint = 2, kLines = 3, kPoints = 4 };
+
+__device__ __forceinline__ float planeDist(const float4& c, int p)
+{
+	/* src/pipeline/clipping.c:260-277 */
+	switch (p) {
+	case 0: return __fadd_rn(c.x, c.w);
+	case 1: return __fsub_rn(c.w, c.x);
+	case 2: return __fadd_rn(c.y, c.w);
+	case 3: return __fsub_rn(c.w, c.y);
+	case 4: return __fadd_rn(c.z, c.w);
+	default: return __fsub_rn(c.w, c.z);
+	}
+}
+
+__device__ __forceinline__ uint32_t outcode(const float4& c)
+{
+	/* src/pipeline/clipping.c:121-137 */
+	uint32_t code = 0;
+#pragma unroll
+	for (int p = 0; p < 6; ++p) code |= (uint32_t) (planeDist(c, p) < 0.0f) << p;
+	return code;
+}
+
+/* New vertex a*(1-t) + b*t with affinely interpolated varyings, stored as a
+ * clip-generated row (src/pipeline/clipping.c:244-258). */
+__device__ PV lerpVertex(const DrawParams& P, const PV& a, const PV& b, float t)
+{
+	PV o;
+	const float s = __fsub_rn(1.0f, t);
+	o.p.x = __fadd_rn(__fmul_rn(a.p.x, s), __fmul_rn(b.p.x, t));
+	o.p.y = __fadd_rn(__fmul_rn(a.p.y, s), __fmul_rn(b.p.y, t));
+	o.p.z = __fadd_rn(__fmul_rn(a.p.z, s), __fmul_rn(b.p.z, t));
+	o.p.w = __fadd_rn(__fmul_rn(a.p.w, s), __fmul_rn(b.p.w, t));
+	const unsigned long long slot = atomicAdd(&P.ctr->clipVerts, 1ull);
+	if (slot >= P.clipCap) {
+		atomicOr(&P.ctr->errors, kErrCapacity);
+		o.ref = a.ref;
+		return o;
+	}
+	o.ref = P.clipBase + (uint32_t) slot;
+	const uint32_t refs[2] = { a.ref, b.ref };
+	const float w[2] = { s, t };
+	const float iw[2] = { 1.0f, 1.0f };
+	uint32_t words[kMaxVaryingWords];
+	interpolate<2>(P.L, P.vary, refs, w, iw, 0.0f, P.st.provokingFirst, true, words);
+	const int nw = P.L.nWords;
+	P.clip[o.ref] = o.p;
+	for (int k = 0; k < nw; ++k) P.vary[(size_t) o.ref * nw + k] = words[k];
+	return o;
+}
+
+/* Sutherland-Hodgman against L, R, B, T, N, F (src/pipeline/clipping.c:68-119,
+ * 199-242). Returns the polygon size; out has room for kMaxPoly vertices. */
+__device__ __noinline__ int clipPolygon(const DrawParams& P, const PV in[3], PV out[kMaxPoly])
+{
+	PV a[kMaxPoly], b[kMaxPoly];
+	int n = 3;
+	for (int i = 0; i < 3; ++i) a[i] = in[i];
+	PV* src = a;
+	PV* dst = b;
+	for (int p = 0; p < 6; ++p) {
+		int m = 0;
+		for (int i = 0; i < n; ++i) {
+			const PV& cur = src[i];
+			const PV& nxt = src[(i + 1) % n];
+			const float da = planeDist(cur.p, p), db = planeDist(nxt.p, p);
+			const bool cin = da >= 0.0f, nin = db >= 0.0f;
+			if (cin && nin) {
+				if (m < kMaxPoly) dst[m++] = nxt;
+			} else if (cin || nin) {
+				const float diff = __fsub_rn(da, db);
+				if (roughlyZero(diff)) continue;
+				const float t = __fdiv_rn(da, diff);
+				if (m < kMaxPoly) dst[m++] = lerpVertex(P, cur, nxt, t);
+				if (!cin && nin && m < kMaxPoly) dst[m++] = nxt;
+			}
+		}
+		n = m;
+		if (n == 0) return 0;
+		PV* tmp = src; src = dst; dst = tmp;
+	}
+	if (n > 6) atomicAdd(&P.ctr->clipOverflow, 1ull);
+	for (int i = 0; i < n; ++i) out[i] = src[i];
+	return n;
+}
+
+/* Liang-Barsky (src/pipeline/clipping.c:139-183); returns true if rejected. */
+__device__ bool clipLine(const DrawParams& P, PV& v0, PV& v1)
+{
+	const uint32_t c0 = outcode(v0.p), c1 = outcode(v1.p);
+	if ((c0 | c1) == 0) return false;
+	if (c0 & c1) return true;
+	float t0 = 0.0f, t1 = 1.0f;
+	for (int p = 0; p < 6; ++p) {
+		const float da = planeDist(v0.p, p), db = planeDist(v1.p, p);
+		if (da < 0.0f && db < 0.0f) return true;
+		if (da < 0.0f || db < 0.0f) {
+			const float diff = __fsub_rn(da, db);
+			if (roughlyZero(diff)) continue;
+			const float t = __fdiv_rn(da, diff);
+			if (da < 0.0f) t0 = t0 > t ? t0 : t;
+			else t1 = t1 > t ? t : t1;
+			if (t0 > t1) return true;
+		}
+	}
+	const PV a = v0, b = v1;
+	if (t0 > 0.0f) v0 = lerpVertex(P, a, b, t0);
+	if (t1 < 1.0f) v1 = lerpVertex(P, a, b, t1);
+	return false;
+}
+
+__device__ __forceinline__ uint32_t tileCount(int minX, int minY, int maxXex, int maxYex)
+{
+	if (maxXex <= minX || maxYex <= minY) return 0;
+	return (uint32_t) ((maxXex - 1) / kTile - minX / kTile + 1) * (uint32_t) ((maxYex - 1) / kTile - minY / kTile + 1);
+}
+
+/* Triangle setup (src/raster/triangle.c:113-238). Returns false if the
+ * triangle is culled or degenerate. */
+__device__ bool setupTriangle(const DrawState& st, PV v0, PV v1, PV v2, TriRaster& R, TriAttr& A)
+{
+	float iw[3], nx[3], ny[3], nz[3];
+	uint32_t ref[3] = { v0.ref, v1.ref, v2.ref };
+	const float4 c[3] = { v0.p, v1.p, v2.p };
+#pragma unroll
+	for (int i = 0; i < 3; ++i) {
+		iw[i] = invW(c[i].w);
+		nx[i] = __fmul_rn(c[i].x, iw[i]);
+		ny[i] = __fmul_rn(c[i].y, iw[i]);
+		nz[i] = __fmul_rn(c[i].z, iw[i]);
+	}
+	/* NDC cull (triangle.c:162-182) */
+	const float e0x = __fsub_rn(nx[1], nx[0]), e0y = __fsub_rn(ny[1], ny[0]);
+	const float e1x = __fsub_rn(nx[2], nx[0]), e1y = __fsub_rn(ny[2], ny[0]);
+	const float area = __fsub_rn(__fmul_rn(e0x, e1y), __fmul_rn(e0y, e1x));
+	const bool front = ((area > 0.0f) && !st.frontFaceCW) || ((area < 0.0f) && st.frontFaceCW);
+	if ((front && st.cullFace == SRP_FACE_FRONT) || (!front && st.cullFace == SRP_FACE_BACK)) return false;
+	if (!(area > 0.0f)) {
+		/* winding fix: swap vertices 1 and 2 (triangle.c:184-195) */
+		float t;
+		t = iw[1]; iw[1] = iw[2]; iw[2] = t;
+		t = nx[1]; nx[1] = nx[2]; nx[2] = t;
+		t = ny[1]; ny[1] = ny[2]; ny[2] = t;
+		t = nz[1]; nz[1] = nz[2]; nz[2] = t;
+		uint32_t r = ref[1]; ref[1] = ref[2]; ref[2] = r;
+	}
+	float sx[3], sy[3];
+#pragma unroll
+	for (int i = 0; i < 3; ++i) ndcToScreen(st.W, st.H, nx[i], ny[i], sx[i], sy[i]);
+	float ex[3], ey[3];
+#pragma unroll
+	for (int i = 0; i < 3; ++i) {
+		ex[i] = __fsub_rn(sx[(i + 1) % 3], sx[i]);
+		ey[i] = __fsub_rn(sy[(i + 1) % 3], sy[i]);
+	}
+	const float areaX2 = fabsf(__fsub_rn(__fmul_rn(ex[0], ey[2]), __fmul_rn(ey[0], ex[2])));
+	if (roughlyZero(areaX2)) return false;
+	/* bbox with the reference's MIN/MAX macro semantics (triangle.c:142-149) */
+	float m;
+	m = sx[1] > sx[2] ? sx[2] : sx[1]; const float mnx = sx[0] > m ? m : sx[0];
+	m = sy[1] > sy[2] ? sy[2] : sy[1]; const float mny = sy[0] > m ? m : sy[0];
+	m = sx[1] > sx[2] ? sx[1] : sx[2]; const float mxx = sx[0] > m ? sx[0] : m;
+	m = sy[1] > sy[2] ? sy[1] : sy[2]; const float mxy = sy[0] > m ? sy[0] : m;
+	float fx = floorf(mnx), fy = floorf(mny), cx = ceilf(mxx), cy = ceilf(mxy);
+	fx = fx > 0.0f ? fx : 0.0f;
+	fy = fy > 0.0f ? fy : 0.0f;
+	cx = cx > (float) st.W ? (float) st.W : cx;
+	cy = cy > (float) st.H ? (float) st.H : cy;
+	/* NaN coordinates compare false everywhere; the reference then walks an
+	 * empty range, which clamping to an empty box reproduces. */
+	if (!(fx <= (float) st.W)) fx = (float) st.W;
+	if (!(fy <= (float) st.H)) fy = (float) st.H;
+	if (!(cx >= 0.0f)) cx = 0.0f;
+	if (!(cy >= 0.0f)) cy = 0.0f;
+	R.minX = (uint16_t) fx; R.minY = (uint16_t) fy;
+	R.maxX = (uint16_t) cx; R.maxY = (uint16_t) cy;
+	/* barycentrics at the first pixel centre (triangle.c:197-226) */
+	const float px = __fadd_rn(fx, 0.5f), py = __fadd_rn(fy, 0.5f);
+	const float ax = __fsub_rn(px, sx[0]), ay = __fsub_rn(py, sy[0]);
+	const float bx = __fsub_rn(px, sx[1]), by = __fsub_rn(py, sy[1]);
+	const float qx = __fsub_rn(px, sx[2]), qy = __fsub_rn(py, sy[2]);
+	R.l0[0] = __fdiv_rn(__fsub_rn(__fmul_rn(bx, ey[1]), __fmul_rn(by, ex[1])), areaX2);
+	R.l0[1] = __fdiv_rn(__fsub_rn(__fmul_rn(qx, ey[2]), __fmul_rn(qy, ex[2])), areaX2);
+	R.l0[2] = __fdiv_rn(__fsub_rn(__fmul_rn(ax, ey[0]), __fmul_rn(ay, ex[0])), areaX2);
+	R.dx[0] = __fdiv_rn(ey[1], areaX2);
+	R.dx[1] = __fdiv_rn(ey[2], areaX2);
+	R.dx[2] = __fdiv_rn(ey[0], areaX2);
+	R.dy[0] = __fdiv_rn(-ex[1], areaX2);
+	R.dy[1] = __fdiv_rn(-ex[2], areaX2);
+	R.dy[2] = __fdiv_rn(-ex[0], areaX2);
+	uint32_t flags = front ? 1u : 0u;
+#pragma unroll
+	for (int i = 0; i < 3; ++i) {
+		const bool tl = (ex[i] > 0.0f && roughlyZero(ey[i])) || (ey[i] < 0.0f);
+		flags |= (tl ? 1u : 0u) << (1 + i);
+		R.c[i] = __fmul_rn(nz[i], iw[i]);
+		A.invW[i] = iw[i];
+		A.vref[i] = ref[i];
+	}
+	R.flags = flags;
+	R.pad = 0;
+	A.pad = 0;
+	return true;
+}
+
+/* Line setup: divide, screen space, DDA parameters
+ * (src/raster/line.c:34-56, 79-86). */
+__device__ void setupLine(const DrawState& st, const PV& a, const PV& b, LineRec& L)
+{
+	const float4 c[2] = { a.p, b.p };
+	float sx[2], sy[2];
+#pragma unroll
+	for (int i = 0; i < 2; ++i) {
+		const float w = invW(c[i].w);
+		const float nx = __fmul_rn(c[i].x, w), ny = __fmul_rn(c[i].y, w), nz = __fmul_rn(c[i].z, w);
+		ndcToScreen(st.W, st.H, nx, ny, sx[i], sy[i]);
+		L.invW[i] = w;
+		L.c[i] = __fmul_rn(nz, w);
+	}
+	const float dx = __fsub_rn(sx[1], sx[0]), dy = __fsub_rn(sy[1], sy[0]);
+	float mx = fmaxf(fabsf(dx), fabsf(dy));
+	int steps = (int) ceilf(mx);
+	/* guard against non-finite or absurd coordinates (the reference would
+	 * loop for billions of steps) */
+	if (!(mx == mx) || mx > 1.0e6f) steps = 0;
+	if (steps == 0) steps = 1;
+	L.x0 = sx[0]; L.y0 = sy[0];
+	L.xInc = __fdiv_rn(dx, (float) steps);
+	L.yInc = __fdiv_rn(dy, (float) steps);
+	L.tInc = __fdiv_rn(1.0f, (float) steps);
+	L.steps = steps;
+	L.vref[0] = a.ref; L.vref[1] = b.ref;
+}
+
+/* Point setup: divide, screen space, coverage square and raster bounds
+ * (src/raster/point.c:32-79, 121-163). */
+__device__ void setupPoint(const DrawState& st, const PV& v, PointRec& R)
+{
+	const float w = invW(v.p.w);
+	const float nx = __fmul_rn(v.p.x, w), ny = __fmul_rn(v.p.y, w), nz = __fmul_rn(v.p.z, w);
+	float sx, sy;
+	ndcToScreen(st.W, st.H, nx, ny, sx, sy);
+	const float half = __fmul_rn(st.pointSize, 0.5f);
+	R.mnx = __fsub_rn(sx, half); R.mny = __fsub_rn(sy, half);
+	R.mxx = __fadd_rn(sx, half); R.mxy = __fadd_rn(sy, half);
+	R.z = nz;
+	R.vref = v.ref;
+	const float fx0 = floorf(R.mnx), fx1 = floorf(R.mxx), fy0 = floorf(R.mny), fy1 = floorf(R.mxy);
+	/* the reference converts with (int); out-of-range values make the point
+	 * fully off-screen there as well */
+	int x0 = fx0 > -1.0e9f ? (fx0 < 1.0e9f ? (int) fx0 : 1000000000) : -1000000000;
+	int x1 = fx1 > -1.0e9f ? (fx1 < 1.0e9f ? (int) fx1 : 1000000000) : -1000000000;
+	int y0 = fy0 > -1.0e9f ? (fy0 < 1.0e9f ? (int) fy0 : 1000000000) : -1000000000;
+	int y1 = fy1 > -1.0e9f ? (fy1 < 1.0e9f ? (int) fy1 : 1000000000) : -1000000000;
+	if (x1 < 0 || y1 < 0 || x0 >= st.W || y0 >= st.H) { x0 = 1; x1 = 0; y0 = 1; y1 = 0; }
+	else {
+		if (x0 < 0) x0 = 0;
+		if (y0 < 0) y0 = 0;
+		if (x1 >= st.W) x1 = st.W - 1;
+		if (y1 >= st.H) y1 = st.H - 1;
+	}
+	R.x0 = (int16_t) x0; R.x1 = (int16_t) x1; R.y0 = (int16_t) y0; R.y1 = (int16_t) y1;
+}
+
+/* Emit the (tile, item) pairs of an item whose pixels lie in the inclusive
+ * pixel box [x0, x1] x [y0, y1]. Few tiles are written inline; the rest is
+ * queued for k_big_entries. */
+__device__ void emitEntries(const DrawParams& P, int kind, uint32_t item, uint32_t base, int x0, int y0, int x1, int y1)
+{
+	const uint32_t n = tileCount(x0, y0, x1 + 1, y1 + 1);
+	if (n == 0) return;
+	if (n <= (uint32_t) kSmallEntries) {
+		uint32_t e = base;
+		for (int ty = y0 / kTile; ty <= y1 / kTile; ++ty)
+			for (int tx = x0 / kTile; tx <= x1 / kTile; ++tx, ++e)
+				if (e < P.entryCap) { P.keys[e] = (uint32_t) (ty * P.st.tilesX + tx); P.vals[e] = item; }
+		if (base + n > P.entryCap) atomicOr(&P.ctr->errors, kErrCapacity);
+	} else {
+		const unsigned long long j = atomicAdd(&P.ctr->bigJobs, 1ull);
+		if (j < P.bigCap) P.bigJobs[j] = make_uint4(item, base, (uint32_t) kind, n);
+		else atomicOr(&P.ctr->errors, kErrCapacity);
+	}
+}
+
+/* Per-thread work on one input primitive: count (write == false) or write
+ * the survivors at the given offsets. Clip-generated vertices are created in
+ * the counting pass and kept in `poly` for the writing pass. */
+template <int MODE>
+struct Assembly {
+	int nPoly;
+	bool clipped;
+	PV v[3];
+	PV poly[kMaxPoly];
+};
+
+template <int MODE>
+__device__ __forceinline__ void handleTriangle(const DrawParams& P, const PV& a, const PV& b, const PV& c, bool write,
+                                               uint32_t& prim, uint32_t& entry)
+{
+	if (MODE == kTriFill) {
+		TriRaster R;
+		TriAttr A;
+		if (!setupTriangle(P.st, a, b, c, R, A)) return;
+		const uint32_t nt = tileCount(R.minX, R.minY, R.maxX, R.maxY);
+		if (write) {
+			if (prim < P.primCap) {
+				A.id = prim;
+				P.triR[prim] = R;
+				P.triA[prim] = A;
+				emitEntries(P, kKindTri, prim, entry, R.minX, R.minY, (int) R.maxX - 1, (int) R.maxY - 1);
+			} else atomicOr(&P.ctr->errors, kErrCapacity);
+		}
+		prim += 1;
+		entry += nt;
+	} else if (MODE == kTriLine) {
+		const PV* vv[3] = { &a, &b, &c };
+#pragma unroll
+		for (int j = 0; j < 3; ++j) {
+			LineRec L;
+			setupLine(P.st, *vv[j], *vv[(j + 1) % 3], L);
+			if (write) {
+				if (prim < P.primCap) { L.id = prim; L.fragBase = entry; P.lines[prim] = L; }
+				else atomicOr(&P.ctr->errors, kErrCapacity);
+			}
+			prim += 1;
+			entry += (uint32_t) L.steps + 1u;
+		}
+	} else if (MODE == kTriPoint) {
+		const PV* vv[3] = { &a, &b, &c };
+#pragma unroll
+		for (int j = 0; j < 3; ++j) {
+			PointRec R;
+			setupPoint(P.st, *vv[j], R);
+			const uint32_t nt = tileCount(R.x0, R.y0, R.x1 + 1, R.y1 + 1);
+			if (write) {
+				if (prim < P.primCap) {
+					R.id = prim;
+					P.points[prim] = R;
+					emitEntries(P, kKindPoint, prim, entry, R.x0, R.y0, R.x1, R.y1);
+				} else atomicOr(&P.ctr->errors, kErrCapacity);
+			}
+			prim += 1;
+			entry += nt;
+		}
+	}
+}
+
+__device__ __forceinline__ void triStream(int prim, unsigned long long base, unsigned long long k, unsigned long long s[3])
+{
+	/* src/pipeline/topology.c:24-48 */
+	if (prim == SRP_PRIM_TRIANGLES) { s[0] = base + 3 * k; s[1] = s[0] + 1; s[2] = s[0] + 2; }
+	else if (prim == SRP_PRIM_TRIANGLE_STRIP) {
+		const bool odd = (k & 1ull) != 0;
+		s[0] = base + k + (odd ? 1 : 0);
+		s[1] = base + k + (odd ? 0 : 1);
+		s[2] = base + k + 2;
+	} else { s[0] = base; s[1] = base + k + 1; s[2] = base + k + 2; }
+}
+
+__device__ __forceinline__ void lineStream(int prim, unsigned long long base, unsigned long long k,
+                                           unsigned long long count, unsigned long long s[2])
+{
+	/* src/pipeline/topology.c:62-83 */
+	if (prim == SRP_PRIM_LINES) { s[0] = base + 2 * k; s[1] = s[0] + 1; }
+	else if (prim == SRP_PRIM_LINE_STRIP) { s[0] = base + k; s[1] = base + k + 1; }
+	else { s[0] = base + k; s[1] = base + (k + 1) % count; }
+}
+
+__device__ __forceinline__ bool loadVertex(const DrawParams& P, unsigned long long stream, PV& v)
+{
+	const unsigned long long vi = P.indexSize ? fetchIndex(P, stream) : stream;
+	if (vi >= P.nVertices) { atomicOr(&P.ctr->errors, kErrBadIndex); return false; }
+	v.p = P.clip[vi];
+	v.ref = (uint32_t) vi;
+	return true;
+}
+
+/* Status word of the decoupled look-back: flag (2 bits) | prims (30) | entries (32). */
+__device__ __forceinline__ unsigned long long packStatus(unsigned long long flag, uint32_t prims, uint32_t entries)
+{
+	return (flag << 62) | ((unsigned long long) (prims & 0x3FFFFFFFu) << 32) | entries;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__ DrawParams P)
+{
+	__shared__ uint32_t sBlock;
+	__shared__ unsigned long long sWarp[kSetupThreads / 32];
+	__shared__ unsigned long long sPrefix;
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	if (tid == 0) sBlock = atomicAdd(&P.ctr->lookbackTicket, 1u);
+	__syncthreads();
+	const uint32_t bid = sBlock;
+	const long long k = (long long) bid * kSetupThreads + tid;
+
+	/* ---- phase A: assemble, clip, count */
+	Assembly<MODE> as;
+	as.nPoly = 0;
+	as.clipped = false;
+	bool live = k < P.nIn;
+	if (live) {
+		if (MODE == kPoints) {
+			const unsigned long long s = P.start + (unsigned long long) k;
+			live = loadVertex(P, s, as.v[0]);
+			if (live) {
+				/* whole-point reject (src/pipeline/clipping.c:185-197) */
+				const float4 c = as.v[0].p;
+				const float nw = -c.w;
+				if ((c.x < nw || c.x > c.w) || (c.y < nw || c.y > c.w) || (c.z < nw || c.z > c.w)) live = false;
+			}
+		} else if (MODE == kLines) {
+			unsigned long long s[2];
+			lineStream(P.prim, P.start, (unsigned long long) k, P.count, s);
+			live = loadVertex(P, s[0], as.v[0]) && loadVertex(P, s[1], as.v[1]);
+			if (live) live = !clipLine(P, as.v[0], as.v[1]);
+		} else {
+			unsigned long long s[3];
+			triStream(P.prim, P.start, (unsigned long long) k, s);
+			live = loadVertex(P, s[0], as.v[0]) && loadVertex(P, s[1], as.v[1]) && loadVertex(P, s[2], as.v[2]);
+			if (live) {
+				const uint32_t c0 = outcode(as.v[0].p), c1 = outcode(as.v[1].p), c2 = outcode(as.v[2].p);
+				if (c0 & c1 & c2) live = false;
+				else if (c0 | c1 | c2) {
+					as.clipped = true;
+					as.nPoly = clipPolygon(P, as.v, as.poly);
+					if (as.nPoly < 3) live = false;
+				}
+			}
+		}
+	}
+	uint32_t nPrim = 0, nEnt = 0;
+	if (live) {
+		if (MODE == kPoints) {
+			PointRec R;
+			setupPoint(P.st, as.v[0], R);
+			nPrim = 1;
+			nEnt = tileCount(R.x0, R.y0, R.x1 + 1, R.y1 + 1);
+		} else if (MODE == kLines) {
+			LineRec L;
+			setupLine(P.st, as.v[0], as.v[1], L);
+			nPrim = 1;
+			nEnt = (uint32_t) L.steps + 1u;
+		} else if (!as.clipped) {
+			handleTriangle<MODE>(P, as.v[0], as.v[1], as.v[2], false, nPrim, nEnt);
+		} else {
+			for (int f = 1; f + 1 < as.nPoly; ++f)
+				handleTriangle<MODE>(P, as.poly[0], as.poly[f], as.poly[f + 1], false, nPrim, nEnt);
+		}
+	}
+
+	/* ---- block scan of (prims, entries) packed as one 64-bit sum */
+	unsigned long long mine = ((unsigned long long) nPrim << 32) | nEnt;
+	unsigned long long incl = mine;
+#pragma unroll
+	for (int o = 1; o < 32; o <<= 1) {
+		const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+		if (lane >= o) incl += y;
+	}
+	if (lane == 31) sWarp[warp] = incl;
+	__syncthreads();
+	if (warp == 0) {
+		unsigned long long w = lane < kSetupThreads / 32 ? sWarp[lane] : 0ull;
+#pragma unroll
+		for (int o = 1; o < 32; o <<= 1) {
+			const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+			if (lane >= o) w += y;
+		}
+		if (lane < kSetupThreads / 32) sWarp[lane] = w;  /* inclusive over warps */
+	}
+	__syncthreads();
+	const unsigned long long warpExcl = warp ? sWarp[warp - 1] : 0ull;
+	const unsigned long long blockTotal = sWarp[kSetupThreads / 32 - 1];
+
+	/* ---- decoupled look-back for the block's global offset */
+	if (tid == 0) {
+		const uint32_t aggP = (uint32_t) (blockTotal >> 32), aggE = (uint32_t) blockTotal;
+		unsigned long long prefix = 0;
+		if (bid == 0) {
+			atomicExch(&P.lookback[0], packStatus(2, aggP, aggE));
+		} else {
+			atomicExch(&P.lookback[bid], packStatus(1, aggP, aggE));
+			long long j = (long long) bid - 1;
+			unsigned spins = 0;
+			unsigned long long accP = 0, accE = 0;
+			while (j >= 0) {
+				const unsigned long long s = *((volatile unsigned long long*) &P.lookback[j]);
+				const unsigned long long flag = s >> 62;
+				if (flag == 0) {
+					if (++spins > kSpinLimit) { atomicOr(&P.ctr->errors, kErrSpin); break; }
+					__nanosleep(32);
+					continue;
+				}
+				accP += (s >> 32) & 0x3FFFFFFFull;
+				accE += s & 0xFFFFFFFFull;
+				if (flag == 2) break;
+				--j;
+			}
+			if (accE + aggE > 0xFFFFFFFFull || accP + aggP > 0x3FFFFFFFull) atomicOr(&P.ctr->errors, kErrCapacity);
+			atomicExch(&P.lookback[bid], packStatus(2, (uint32_t) (accP + aggP), (uint32_t) (accE + aggE)));
+			prefix = (accP << 32) | (accE & 0xFFFFFFFFull);
+		}
+		sPrefix = prefix;
+		if (bid == gridDim.x - 1) {
+			P.ctr->prims = (prefix >> 32) + aggP;
+			P.ctr->entries = (prefix & 0xFFFFFFFFull) + aggE;
+		}
+	}
+	__syncthreads();
+	const unsigned long long base = sPrefix + warpExcl + (incl - mine);
+	uint32_t primBase = (uint32_t) (base >> 32), entBase = (uint32_t) base;
+
+	/* ---- phase C: write the survivors */
+	if (!live) return;
+	if (MODE == kPoints) {
+		PointRec R;
+		setupPoint(P.st, as.v[0], R);
+		if (primBase < P.primCap) {
+			R.id = primBase;
+			P.points[primBase] = R;
+			emitEntries(P, kKindPoint, primBase, entBase, R.x0, R.y0, R.x1, R.y1);
+		} else atomicOr(&P.ctr->errors, kErrCapacity);
+	} else if (MODE == kLines) {
+		LineRec L;
+		setupLine(P.st, as.v[0], as.v[1], L);
+		if (primBase < P.primCap) {
+			L.id = primBase;
+			L.fragBase = entBase;
+			P.lines[primBase] = L;
+		} else atomicOr(&P.ctr->errors, kErrCapacity);
+	} else if (!as.clipped) {
+		handleTriangle<MODE>(P, as.v[0], as.v[1], as.v[2], true, primBase, entBase);
+	} else {
+		for (int f = 1; f + 1 < as.nPoly; ++f)
+			handleTriangle<MODE>(P, as.poly[0], as.poly[f], as.poly[f + 1], true, primBase, entBase);
+	}
+}
+
+/* Entries of primitives covering more than kSmallEntries tiles: one block per
+ * primitive writes its tiles row by row. */
+__global__ void k_big_entries(const __grid_constant__ DrawParams P, uint32_t nJobs)
+{
+	for (uint32_t j = blockIdx.x; j < nJobs; j += gridDim.x) {
+		const uint4 job = P.bigJobs[j];
+		int x0, y0, x1, y1;
+		if (job.z == kKindTri) {
+			const TriRaster& R = P.triR[job.x];
+			x0 = R.minX; y0 = R.minY; x1 = (int) R.maxX - 1; y1 = (int) R.maxY - 1;
+		} else {
+			const PointRec& R = P.points[job.x];
+			x0 = R.x0; y0 = R.y0; x1 = R.x1; y1 = R.y1;
+		}
+		const int tx0 = x0 / kTile, ty0 = y0 / kTile, ntx = x1 / kTile - tx0 + 1;
+		for (uint32_t i = threadIdx.x; i < job.w; i += blockDim.x) {
+			const uint32_t e = job.y + i;
+			if (e >= P.entryCap) break;
+			const int tx = tx0 + (int) (i % (uint32_t) ntx), ty = ty0 + (int) (i / (uint32_t) ntx);
+			P.keys[e] = (uint32_t) (ty * P.st.tilesX + tx);
+			P.vals[e] = job.x;
+		}
+	}
+}
+
+/* One thread per line walks the reference's DDA exactly (fp32 accumulators,
+ * round half away from zero) and writes one record and one (tile, fragment)
+ * pair per step; steps whose pixel fails the scissor test or falls outside
+ * the framebuffer get the key one past the last tile, which sorts them out
+ * (src/raster/line.c:34-77, src/raster/fragment.c:63-75). */
+__global__ void k_line_frags(const __grid_constant__ DrawParams P, uint32_t nLines)
+{
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	unsigned long long passed = 0;
+	if (i < nLines) {
+		const LineRec L = P.lines[i];
+		const uint32_t invalid = (uint32_t) (P.st.tilesX * P.st.tilesY);
+		float x = L.x0, y = L.y0, t = 0.0f;
+		const unsigned long long size = (unsigned long long) P.st.W * (unsigned long long) P.st.H;
+		for (int s = 0; s <= L.steps; ++s) {
+			const int px = (int) roundf(x), py = (int) roundf(y);
+			const float w0 = __fsub_rn(1.0f, t);
+			const float depth = __fadd_rn(__fmul_rn(L.c[0], w0), __fmul_rn(L.c[1], t));
+			const uint32_t e = L.fragBase + (uint32_t) s;
+			uint32_t key = invalid;
+			if (scissorPass(P.st, px, py)) {
+				++passed;
+				const unsigned long long idx = (unsigned long long) (long long) py * (unsigned long long) P.st.W
+				                             + (unsigned long long) (long long) px;
+				if (idx < size) {
+					const uint32_t gx = (uint32_t) (idx % (unsigned long long) P.st.W);
+					const uint32_t gy = (uint32_t) (idx / (unsigned long long) P.st.W);
+					key = (gy / kTile) * (uint32_t) P.st.tilesX + gx / kTile;
+				}
+			}
+			if (e < P.fragCap && e < P.entryCap) {
+				LineFrag F;
+				F.depth = depth; F.t = t; F.line = i; F.px = (int16_t) px; F.py = (int16_t) py;
+				P.frags[e] = F;
+				P.keys[e] = key;
+				P.vals[e] = e;
+			}
+			x = __fadd_rn(x, L.xInc);
+			y = __fadd_rn(y, L.yInc);
+			t = __fadd_rn(t, L.tInc);
+		}
+	}
+	for (int o = 16; o; o >>= 1) passed += __shfl_xor_sync(0xFFFFFFFFu, passed, o);
+	if ((threadIdx.x & 31) == 0 && passed) atomicAdd(&P.ctr->fragments, passed);
+}
+
+/* ------------------------------------------------------------ launchers */
+
+void launchReset(const DrawParams& P, cudaStream_t s) { k_reset<<<1, 32, 0, s>>>(P); }
+
+void launchIndexRange(const DrawParams& P, cudaStream_t s)
+{
+	unsigned long long blocks = (P.count + 255) / 256;
+	if (blocks > 152 * 8) blocks = 152 * 8;
+	if (blocks < 1) blocks = 1;
+	k_index_range<<<(unsigned) blocks, 256, 0, s>>>(P);
+}
+
+void launchVertex(const DrawParams& P, unsigned long long first, unsigned long long n, cudaStream_t s)
+{
+	const unsigned blocks = (unsigned) ((n + kVertexThreads - 1) / kVertexThreads);
+	if (!blocks) return;
+	const size_t smem = (size_t) kVertexThreads * P.stride + 16;
+	switch (P.vsId) {
+	case SRP_GPU_VS_WORLD:
+		cudaFuncSetAttribute(k_vertex<SRP_GPU_VS_WORLD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+		k_vertex<SRP_GPU_VS_WORLD><<<blocks, kVertexThreads, smem, s>>>(P, first, n);
+		break;
+	default:
+		cudaFuncSetAttribute(k_vertex<SRP_GPU_VS_TRANSFORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+		k_vertex<SRP_GPU_VS_TRANSFORM><<<blocks, kVertexThreads, smem, s>>>(P, first, n);
+		break;
+	}
+}
+
+void launchSetup(const DrawParams& P, cudaStream_t s)
+{
+	const unsigned blocks = (unsigned) ((P.nIn + kSetupThreads - 1) / kSetupThreads);
+	if (!blocks) return;
+	const bool tri = P.prim == SRP_PRIM_TRIANGLES || P.prim == SRP_PRIM_TRIANGLE_STRIP || P.prim == SRP_PRIM_TRIANGLE_FAN;
+	if (tri && P.st.polygonMode == SRP_POLYGON_MODE_LINE) k_setup<kTriLine><<<blocks, kSetupThreads, 0, s>>>(P);
+	else if (tri && P.st.polygonMode == SRP_POLYGON_MODE_POINT) k_setup<kTriPoint><<<blocks, kSetupThreads, 0, s>>>(P);
+	else if (tri) k_setup<kTriFill><<<blocks, kSetupThreads, 0, s>>>(P);
+	else if (P.prim == SRP_PRIM_POINTS) k_setup<kPoints><<<blocks, kSetupThreads, 0, s>>>(P);
+	else k_setup<kLines><<<blocks, kSetupThreads, 0, s>>>(P);
+}
+
+void launchBigEntries(const DrawParams& P, uint32_t nJobs, cudaStream_t s)
+{
+	if (!nJobs) return;
+	k_big_entries<<<nJobs < 152u * 16u ? nJobs : 152u * 16u, 256, 0, s>>>(P, nJobs);
+}
+
+void launchLineFrags(const DrawParams& P, uint32_t nLines, cudaStream_t s)
+{
+	if (!nLines) return;
+	k_line_frags<<<(nLines + 127) / 128, 128, 0, s>>>(P, nLines);
+}
+
+}  // namespace srpg

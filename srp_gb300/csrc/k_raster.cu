@@ -1,0 +1,346 @@
+/* Per-tile rasterisation: visibility resolve and deferred shading.
+ *
+ * One warp owns one 8x8 tile; lane l owns pixels l and l + 32 of it. The
+ * tile's items (triangles, points or line fragments, already in submission
+ * order) are taken 32 at a time:
+ *   phase 1  lane j evaluates item j over the tile -- for a triangle the
+ *            reference's incremental barycentrics (exact chain, see chain.h)
+ *            and the top-left test -- leaving a 64-bit coverage mask and the
+ *            per-pixel depths in shared memory;
+ *   phase 2  each lane walks, for its own pixels, the covering items in order
+ *            and applies the stencil test, the depth test and the stencil
+ *            operations exactly as the reference's emitFragment does
+ *            (src/raster/fragment.c:63-125), remembering the last item that
+ *            reached the colour write.
+ * Because srp has no blending and a shader that does not write fragDepth
+ * cannot influence depth or stencil, the colour of a pixel is the shader
+ * output of that last item; k_shade evaluates it once per pixel afterwards.
+ * Shaders that write fragDepth take the in-order path (k_resolve with
+ * LATE_FS), which shades every fragment in phase 2. */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "device_common.cuh"
+#include "kernels.h"
+#include "srp/buffer.h"
+
+namespace srpg {
+__device__ __forceinline__ void rasterTexSample(const void* tex, float u, float v, float out[4])
+{
+	textureSample((const TextureDesc*) tex, u, v, out);
+}
+}  // namespace srpg
+#define SRP_DEVICE_TEXTURE_SAMPLE(tex, u, v, out) srpg::rasterTexSample((const void*) (tex), u, v, out)
+#include "srp/shaderlib_impl.h"
+
+namespace srpg {
+
+constexpr int kResolveWarps = 4;
+
+template <int FS>
+__device__ __forceinline__ void runFS(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out)
+{
+	switch (FS) {
+	case SRP_GPU_FS_VARYING_COLOR: srpslFsVaryingColor(in, out); break;
+	case SRP_GPU_FS_SOLID: srpslFsSolid(in, out); break;
+	case SRP_GPU_FS_PRIMITIVE_ID: srpslFsPrimitiveId(in, out); break;
+	case SRP_GPU_FS_TEXTURE: srpslFsTexture(in, out); break;
+	case SRP_GPU_FS_TEXTURE_MODULATE: srpslFsTextureModulate(in, out); break;
+	case SRP_GPU_FS_BLINN_PHONG: srpslFsBlinnPhong(in, out); break;
+	case SRP_GPU_FS_MARBLE: srpslFsMarble(in, out); break;
+	case SRP_GPU_FS_DEPTH_OVERWRITE: srpslFsDepthOverwrite(in, out); break;
+	case SRP_GPU_FS_FRAGCOORD: srpslFsFragCoord(in, out); break;
+	case SRP_GPU_FS_FLAT_INT: srpslFsFlatInt(in, out); break;
+	default: break;
+	}
+}
+
+/* Shader inputs of `item` at pixel (gx, gy) and the shader call
+ * (fragCoord and varyings as built by src/raster/triangle.c:89-99,
+ * line.c:62-75, point.c:107-116). */
+template <int KIND, int FS>
+__device__ __forceinline__ void shadeItem(const DrawParams& P, uint32_t item, int gx, int gy, SRPFragmentShaderOut& out)
+{
+	uint32_t words[kMaxVaryingWords];
+	SRPFragmentShaderIn in;
+	in.uniform = (SRPUniform*) P.uniform;
+	in.varyings = (SRPInterpolated*) words;
+	if (KIND == kKindTri) {
+		const TriRaster R = P.triR[item];
+		const TriAttr A = P.triA[item];
+		float l[3];
+		lambdaAt(R, gx, gy, l);
+		const float depth = triDepth(R.c, l);
+		const float recip = triRecip(A.invW, l);
+		interpolate<3>(P.L, P.vary, A.vref, l, A.invW, recip, P.st.provokingFirst, false, words);
+		in.fragCoord[0] = __fadd_rn((float) gx, 0.5f);
+		in.fragCoord[1] = __fadd_rn((float) gy, 0.5f);
+		in.fragCoord[2] = depth;
+		in.fragCoord[3] = recip;
+		in.frontFacing = (R.flags & 1u) != 0;
+		in.primitiveID = A.id;
+	} else if (KIND == kKindLineFrag) {
+		const LineFrag F = P.frags[item];
+		const LineRec L = P.lines[F.line];
+		const float w[2] = { __fsub_rn(1.0f, F.t), F.t };
+		const float recip = __fdiv_rn(1.0f, __fadd_rn(__fmul_rn(L.invW[0], w[0]), __fmul_rn(L.invW[1], w[1])));
+		interpolate<2>(P.L, P.vary, L.vref, w, L.invW, recip, P.st.provokingFirst, false, words);
+		in.fragCoord[0] = __fadd_rn((float) F.px, 0.5f);
+		in.fragCoord[1] = __fadd_rn((float) F.py, 0.5f);
+		in.fragCoord[2] = F.depth;
+		in.fragCoord[3] = recip;
+		in.frontFacing = true;
+		in.primitiveID = L.id;
+	} else {
+		const PointRec R = P.points[item];
+		const int nw = P.L.nWords;
+#pragma unroll
+		for (int k = 0; k < kMaxVaryingWords; ++k)
+			if (k < nw) words[k] = P.vary[(size_t) R.vref * nw + k];
+		in.fragCoord[0] = __fadd_rn((float) gx, 0.5f);
+		in.fragCoord[1] = __fadd_rn((float) gy, 0.5f);
+		in.fragCoord[2] = R.z;
+		in.fragCoord[3] = 1.0f;
+		in.frontFacing = true;
+		in.primitiveID = R.id;
+	}
+	out.color[0] = out.color[1] = out.color[2] = out.color[3] = 0.0f;
+	out.fragDepth = __int_as_float(0x7FC00000);
+	runFS<FS>(&in, &out);
+}
+
+/* Phase 1: coverage of one item over the tile at (x0, y0). */
+template <int KIND>
+__device__ __forceinline__ void coverage(const DrawParams& P, uint32_t item, int x0, int y0,
+                                         unsigned long long& mask, float* dep, uint32_t& flags)
+{
+	mask = 0;
+	if (KIND == kKindTri) {
+		const TriRaster R = P.triR[item];
+		flags = R.flags;
+		const int xs = max(x0, (int) R.minX), xe = min(x0 + kTile, (int) R.maxX);
+		const int ys = max(y0, (int) R.minY), ye = min(y0 + kTile, (int) R.maxY);
+		if (xs >= xe || ys >= ye) return;
+		float lr[3];
+#pragma unroll
+		for (int i = 0; i < 3; ++i) lr[i] = srpChainAdd(R.l0[i], R.dy[i], (uint32_t) (ys - R.minY));
+		for (int y = ys; y < ye; ++y) {
+			float l[3];
+#pragma unroll
+			for (int i = 0; i < 3; ++i) l[i] = srpChainAdd(lr[i], R.dx[i], (uint32_t) (xs - R.minX));
+			for (int x = xs; x < xe; ++x) {
+				if (insideTri(l, R.flags)) {
+					const int q = (y - y0) * kTile + (x - x0);
+					mask |= 1ull << q;
+					dep[q] = triDepth(R.c, l);
+				}
+#pragma unroll
+				for (int i = 0; i < 3; ++i) l[i] = __fadd_rn(l[i], R.dx[i]);
+			}
+#pragma unroll
+			for (int i = 0; i < 3; ++i) lr[i] = __fadd_rn(lr[i], R.dy[i]);
+		}
+	} else if (KIND == kKindPoint) {
+		const PointRec R = P.points[item];
+		flags = 1u;
+		const int xs = max(x0, (int) R.x0), xe = min(x0 + kTile - 1, (int) R.x1);
+		const int ys = max(y0, (int) R.y0), ye = min(y0 + kTile - 1, (int) R.y1);
+		for (int y = ys; y <= ye; ++y)
+			for (int x = xs; x <= xe; ++x) {
+				const float cx = __fadd_rn((float) x, 0.5f), cy = __fadd_rn((float) y, 0.5f);
+				if (cx < R.mnx || cx >= R.mxx || cy < R.mny || cy >= R.mxy) continue;
+				const int q = (y - y0) * kTile + (x - x0);
+				mask |= 1ull << q;
+				dep[q] = R.z;
+			}
+	} else {
+		const LineFrag F = P.frags[item];
+		flags = 1u;
+		const unsigned long long idx = (unsigned long long) (long long) F.py * (unsigned long long) P.st.W
+		                             + (unsigned long long) (long long) F.px;
+		const int gx = (int) (idx % (unsigned long long) P.st.W), gy = (int) (idx / (unsigned long long) P.st.W);
+		const int q = (gy - y0) * kTile + (gx - x0);
+		if (q >= 0 && q < 64) { mask = 1ull << q; dep[q] = F.depth; }
+	}
+}
+
+/* LATE_FS = 0: early depth test, colour deferred to k_shade.
+ * LATE_FS = a fragment shader id: the shader runs per fragment in order and
+ * may replace the depth (src/raster/fragment.c:97-111). */
+template <int KIND, int LATE_FS>
+__global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(const __grid_constant__ DrawParams P,
+                                                               const uint32_t* vals, uint32_t numTiles)
+{
+	__shared__ unsigned long long sMask[kResolveWarps][32];
+	__shared__ uint32_t sItem[kResolveWarps][32];
+	__shared__ uint32_t sFlag[kResolveWarps][32];
+	__shared__ float sDep[kResolveWarps][32][64];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const uint32_t tile = blockIdx.x * kResolveWarps + warp;
+	if (tile >= numTiles) return;
+	const uint32_t s = P.tileStart[tile], e = P.tileEnd[tile];
+	if (s >= e) return;
+	const DrawState& st = P.st;
+	const int x0 = (int) (tile % (uint32_t) st.tilesX) * kTile, y0 = (int) (tile / (uint32_t) st.tilesX) * kTile;
+
+	float depth[2];
+	uint32_t sten[2], col[2];
+	int32_t win[2];
+	bool ok[2];
+	size_t idx[2];
+	int gx[2], gy[2];
+#pragma unroll
+	for (int p = 0; p < 2; ++p) {
+		const int q = lane + 32 * p;
+		gx[p] = x0 + (q & 7);
+		gy[p] = y0 + (q >> 3);
+		const bool valid = gx[p] < st.W && gy[p] < st.H;
+		idx[p] = valid ? (size_t) gy[p] * st.W + gx[p] : 0;
+		depth[p] = valid ? P.depth[idx[p]] : 0.0f;
+		sten[p] = valid ? P.stencil[idx[p]] : 0u;
+		col[p] = 0;
+		win[p] = -1;
+		/* line fragments were scissor-tested on their logical coordinates */
+		ok[p] = valid && (KIND == kKindLineFrag || scissorPass(st, gx[p], gy[p]));
+	}
+	unsigned long long frags = 0;
+	for (uint32_t b = s; b < e; b += 32) {
+		const uint32_t n = min(32u, e - b);
+		unsigned long long mask = 0;
+		uint32_t item = 0, flags = 0;
+		if ((uint32_t) lane < n) {
+			item = vals[b + lane];
+			coverage<KIND>(P, item, x0, y0, mask, sDep[warp][lane], flags);
+		}
+		sMask[warp][lane] = mask;
+		sItem[warp][lane] = item;
+		sFlag[warp][lane] = flags;
+		__syncwarp();
+#pragma unroll
+		for (int p = 0; p < 2; ++p) {
+			if (!ok[p]) continue;
+			const int q = lane + 32 * p;
+			uint32_t m = 0;
+			for (uint32_t j = 0; j < n; ++j) m |= (uint32_t) ((sMask[warp][j] >> q) & 1ull) << j;
+			frags += __popc(m);
+			while (m) {
+				const int j = __ffs(m) - 1;
+				m &= m - 1;
+				const bool front = (sFlag[warp][j] & 1u) != 0;
+				const StencilFace& sf = front ? st.front : st.back;
+				float d = sDep[warp][j][q];
+				if (st.stencilEnabled && !stencilCompare(sf.ref, sten[p], sf.mask, sf.func)) {
+					sten[p] = stencilApply(sf.sfail, sten[p], sf.ref, sf.writeMask);
+					continue;
+				}
+				if (LATE_FS == 0) {
+					if (st.depthTest && !depthCompare(st.depthOp, d, depth[p])) {
+						if (st.stencilEnabled) sten[p] = stencilApply(sf.dfail, sten[p], sf.ref, sf.writeMask);
+						continue;
+					}
+				} else {
+					SRPFragmentShaderOut out;
+					shadeItem<KIND, LATE_FS>(P, sItem[warp][j], gx[p], gy[p], out);
+					if (!isnan(out.fragDepth)) d = out.fragDepth;
+					if (st.depthTest && !depthCompare(st.depthOp, d, depth[p])) {
+						if (st.stencilEnabled) sten[p] = stencilApply(sf.dfail, sten[p], sf.ref, sf.writeMask);
+						continue;
+					}
+					col[p] = packColor(out.color);
+				}
+				if (st.stencilEnabled) sten[p] = stencilApply(sf.pass, sten[p], sf.ref, sf.writeMask);
+				win[p] = (int32_t) sItem[warp][j];
+				if (st.depthTest && st.depthWrite) depth[p] = d;
+			}
+		}
+		__syncwarp();
+	}
+#pragma unroll
+	for (int p = 0; p < 2; ++p) {
+		if (!(gx[p] < st.W && gy[p] < st.H)) continue;
+		P.depth[idx[p]] = depth[p];
+		P.stencil[idx[p]] = (uint8_t) sten[p];
+		if (LATE_FS == 0) P.winner[idx[p]] = win[p];
+		else if (win[p] >= 0) P.color[idx[p]] = col[p];
+	}
+	if (KIND != kKindLineFrag) {
+		for (int o = 16; o; o >>= 1) frags += __shfl_xor_sync(0xFFFFFFFFu, frags, o);
+		if (lane == 0 && frags) atomicAdd(&P.ctr->fragments, frags);
+	}
+}
+
+/* Deferred shading: one shader invocation per pixel whose colour was written
+ * by the resolve pass. */
+template <int KIND, int FS>
+__global__ void __launch_bounds__(kResolveWarps * 32) k_shade(const __grid_constant__ DrawParams P, uint32_t numTiles)
+{
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const uint32_t tile = blockIdx.x * kResolveWarps + warp;
+	if (tile >= numTiles) return;
+	if (P.tileStart[tile] >= P.tileEnd[tile]) return;
+	const DrawState& st = P.st;
+	const int x0 = (int) (tile % (uint32_t) st.tilesX) * kTile, y0 = (int) (tile / (uint32_t) st.tilesX) * kTile;
+#pragma unroll
+	for (int p = 0; p < 2; ++p) {
+		const int q = lane + 32 * p;
+		const int gx = x0 + (q & 7), gy = y0 + (q >> 3);
+		if (gx >= st.W || gy >= st.H) continue;
+		const size_t idx = (size_t) gy * st.W + gx;
+		const int32_t w = P.winner[idx];
+		if (w < 0) continue;
+		SRPFragmentShaderOut out;
+		shadeItem<KIND, FS>(P, (uint32_t) w, gx, gy, out);
+		P.color[idx] = packColor(out.color);
+	}
+}
+
+/* ------------------------------------------------------------ launchers */
+
+static unsigned tileBlocks(uint32_t numTiles) { return (numTiles + kResolveWarps - 1) / kResolveWarps; }
+
+void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, cudaStream_t s)
+{
+	const unsigned b = tileBlocks(numTiles);
+	if (kind == kKindTri) k_resolve<kKindTri, 0><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+	else if (kind == kKindPoint) k_resolve<kKindPoint, 0><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+	else k_resolve<kKindLineFrag, 0><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+}
+
+bool shadeSupportsLateDepth(int fsId) { return fsId == SRP_GPU_FS_DEPTH_OVERWRITE; }
+
+void launchResolveLate(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, cudaStream_t s)
+{
+	const unsigned b = tileBlocks(numTiles);
+	if (kind == kKindTri) k_resolve<kKindTri, SRP_GPU_FS_DEPTH_OVERWRITE><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+	else if (kind == kKindPoint) k_resolve<kKindPoint, SRP_GPU_FS_DEPTH_OVERWRITE><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+	else k_resolve<kKindLineFrag, SRP_GPU_FS_DEPTH_OVERWRITE><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+}
+
+template <int KIND>
+static void shadeKind(const DrawParams& P, uint32_t numTiles, cudaStream_t s)
+{
+	const unsigned b = tileBlocks(numTiles);
+	const unsigned t = kResolveWarps * 32;
+	switch (P.fsId) {
+	case SRP_GPU_FS_VARYING_COLOR: k_shade<KIND, SRP_GPU_FS_VARYING_COLOR><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_SOLID: k_shade<KIND, SRP_GPU_FS_SOLID><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_PRIMITIVE_ID: k_shade<KIND, SRP_GPU_FS_PRIMITIVE_ID><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_TEXTURE: k_shade<KIND, SRP_GPU_FS_TEXTURE><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_TEXTURE_MODULATE: k_shade<KIND, SRP_GPU_FS_TEXTURE_MODULATE><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_BLINN_PHONG: k_shade<KIND, SRP_GPU_FS_BLINN_PHONG><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_MARBLE: k_shade<KIND, SRP_GPU_FS_MARBLE><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_DEPTH_OVERWRITE: k_shade<KIND, SRP_GPU_FS_DEPTH_OVERWRITE><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_FRAGCOORD: k_shade<KIND, SRP_GPU_FS_FRAGCOORD><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_FLAT_INT: k_shade<KIND, SRP_GPU_FS_FLAT_INT><<<b, t, 0, s>>>(P, numTiles); break;
+	default: break;
+	}
+}
+
+void launchShade(const DrawParams& P, int kind, uint32_t numTiles, cudaStream_t s)
+{
+	if (kind == kKindTri) shadeKind<kKindTri>(P, numTiles, s);
+	else if (kind == kKindPoint) shadeKind<kKindPoint>(P, numTiles, s);
+	else shadeKind<kKindLineFrag>(P, numTiles, s);
+}
+
+}  // namespace srpg

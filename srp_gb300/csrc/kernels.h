@@ -1,0 +1,79 @@
+/* Draw parameters passed to every kernel (as a __grid_constant__ parameter,
+ * so the user uniform inside it is read straight from the constant bank) and
+ * the host-side launch wrappers of each kernel translation unit. */
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "gpu_types.h"
+
+namespace srpg {
+
+struct DrawParams {
+	DrawState st;
+	VaryingLayout L;
+	int vsId, fsId;
+	int prim;                      /* SRPPrimitive of the draw */
+	int indexSize;                 /* 0: non-indexed, else 1/2/4/8 bytes */
+	const void* indices;           /* device copy of the index buffer */
+	unsigned long long start, count;
+	const unsigned char* vertices; /* device copy of the vertex buffer (user AoS) */
+	unsigned long long nVertices;
+	int stride;                    /* bytes per vertex */
+	int nIn;                       /* input primitives of this draw */
+	/* post-VS vertices: rows [0, nVertices) from the vertex shader, rows
+	 * [clipBase, clipBase + clipCap) created by clipping */
+	float4* clip;
+	uint32_t* vary;
+	uint32_t clipBase, clipCap;
+	unsigned long long* minmax;    /* [0] min, [1] max vertex index referenced */
+	/* primitives in submission order */
+	TriRaster* triR;
+	TriAttr* triA;
+	LineRec* lines;
+	PointRec* points;
+	LineFrag* frags;
+	uint32_t primCap, fragCap;
+	/* (tile, item) pairs */
+	uint32_t* keys;
+	uint32_t* vals;
+	uint32_t entryCap;
+	uint4* bigJobs;                /* primitives covering many tiles */
+	uint32_t bigCap;
+	unsigned long long* lookback;  /* decoupled look-back status, one per block */
+	/* framebuffer planes */
+	uint32_t* color;
+	float* depth;
+	uint8_t* stencil;
+	int32_t* winner;               /* last item that reached the colour write */
+	uint32_t* tileStart;
+	uint32_t* tileEnd;
+	DeviceCounters* ctr;
+	unsigned char uniform[kMaxUniformBytes];
+};
+
+constexpr int kTile = 8;              /* tile edge in pixels */
+constexpr int kSetupThreads = 256;
+constexpr int kSmallEntries = 16;     /* tiles a primitive may write inline */
+
+/* k_front.cu */
+void launchReset(const DrawParams& P, cudaStream_t s);
+void launchIndexRange(const DrawParams& P, cudaStream_t s);
+void launchVertex(const DrawParams& P, unsigned long long first, unsigned long long n, cudaStream_t s);
+void launchSetup(const DrawParams& P, cudaStream_t s);
+void launchBigEntries(const DrawParams& P, uint32_t nJobs, cudaStream_t s);
+void launchLineFrags(const DrawParams& P, uint32_t nLines, cudaStream_t s);
+/* k_bin.cu */
+void sortEntries(const DrawParams& P, uint32_t n, uint32_t keyBits, uint32_t* keysAlt, uint32_t* valsAlt,
+                 uint32_t* hist, uint32_t* partials, uint32_t** keysOut, uint32_t** valsOut, cudaStream_t s);
+void launchTileRanges(const DrawParams& P, const uint32_t* keys, uint32_t n, uint32_t numTiles, cudaStream_t s);
+size_t sortHistWords(uint32_t n);
+size_t sortPartialWords(uint32_t n);
+/* k_raster.cu */
+void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, cudaStream_t s);
+/* k_shade.cu */
+void launchShade(const DrawParams& P, int kind, uint32_t numTiles, cudaStream_t s);
+bool shadeSupportsLateDepth(int fsId);
+void launchResolveLate(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, cudaStream_t s);
+
+}  // namespace srpg

@@ -1,0 +1,972 @@
+/* Host side of the GPU library: the srp public API (include/srp/*.h) on top
+ * of device-resident buffers, plus the additions in srp/gpu.h.
+ *
+ * Behaviour kept from kitrofimov/srp:
+ *   state setters and defaults          src/core/context.c:15-180
+ *   error reporting through the callback src/utils/message_callback.c:18-35
+ *   draw validation and dispatch        src/pipeline/draw.c:63-208
+ *   excess-vertex warnings              src/pipeline/primitive_assembly.c:137-153
+ *   buffers (copy on CopyData)          src/core/buffer.c:20-136
+ *   framebuffer clear semantics         src/core/framebuffer.c:17-62
+ *   textures (3 channels, nearest)      src/core/texture.c:21-139
+ * Every draw is executed by the CUDA pipeline in k_front.cu, k_bin.cu and
+ * k_raster.cu; nothing is rendered on the host. */
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "srp/srp.h"
+#include "srp/gpu.h"
+#include "srp/mat.h"
+#include "srp/shaderlib.h"
+#include "gpu_types.h"
+#include "imageio.h"
+#include "kernels.h"
+
+/* The reference requires the user program to define `SRPContext srpContext`.
+ * A weak default lets the library also be used from programs (and language
+ * bindings) that do not; a user definition takes precedence. */
+extern "C" {
+__attribute__((weak)) SRPContext srpContext;
+}
+
+using namespace srpg;
+
+/* ------------------------------------------------------------- messages */
+
+static void message(SRPMessageType type, SRPMessageSeverity sev, const char* fn, const char* fmt, ...)
+{
+	if (!srpContext.messageCallback.func) return;
+	char buf[1024];
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(buf, sizeof buf, fmt, ap);
+	va_end(ap);
+	srpContext.messageCallback.func(type, sev, fn, buf, srpContext.messageCallback.userParameter);
+}
+
+#define SRP_ERROR(fn, ...) message(SRP_MESSAGE_ERROR, SRP_MESSAGE_SEVERITY_HIGH, fn, __VA_ARGS__)
+
+static bool cudaOk(cudaError_t e, const char* fn, const char* what)
+{
+	if (e == cudaSuccess) return true;
+	SRP_ERROR(fn, "CUDA error in %s: %s", what, cudaGetErrorString(e));
+	return false;
+}
+
+/* --------------------------------------------------------- library state */
+
+namespace {
+
+struct DeviceBuffer {
+	void* ptr = nullptr;
+	size_t bytes = 0;
+	bool reserve(size_t need, const char* fn)
+	{
+		if (need <= bytes) return true;
+		size_t nb = std::max(need, bytes + bytes / 2);
+		if (ptr) cudaFree(ptr);
+		ptr = nullptr;
+		bytes = 0;
+		if (!cudaOk(cudaMalloc(&ptr, nb), fn, "cudaMalloc")) return false;
+		bytes = nb;
+		return true;
+	}
+	template <class T> T* as() const { return (T*) ptr; }
+};
+
+struct Registry {
+	std::vector<std::pair<void*, int>> vs, fs;
+};
+
+struct Lib {
+	bool init = false;
+	cudaStream_t stream = nullptr;
+	cudaStream_t ownStream = nullptr;
+	SRPGpuFramebufferMode fbMode = SRP_GPU_FB_COHERENT;
+	Registry reg;
+	/* scratch pools, grown on demand */
+	DeviceBuffer clip, vary, triR, triA, lines, points, frags, keys, vals, keys2, vals2, big, lookback;
+	DeviceBuffer hist, partials, tileStart, tileEnd, winner, minmax, ctr;
+	DeviceCounters* hostCtr = nullptr;
+	SRPGpuStats stats = {};
+	unsigned long long launches = 0;
+	uint32_t clipRows = 4096;
+	uint32_t bigCap = 1 << 16;
+	double entryRatio = 4.0;
+};
+
+Lib g;
+
+bool ensureInit(const char* fn)
+{
+	if (g.init) return true;
+	if (!cudaOk(cudaStreamCreateWithFlags(&g.ownStream, cudaStreamNonBlocking), fn, "cudaStreamCreate")) return false;
+	g.stream = g.ownStream;
+	if (!cudaOk(cudaMallocHost((void**) &g.hostCtr, sizeof(DeviceCounters)), fn, "cudaMallocHost")) return false;
+	if (!g.ctr.reserve(sizeof(DeviceCounters), fn) || !g.minmax.reserve(16, fn)) return false;
+	cudaMemset(g.ctr.ptr, 0, sizeof(DeviceCounters));
+	g.init = true;
+	return true;
+}
+
+}  // namespace
+
+/* ---------------------------------------------------------------- context */
+
+extern "C" {
+
+void srpNewContext(SRPContext* c)
+{
+	c->messageCallback.func = NULL;
+	c->messageCallback.userParameter = NULL;
+	c->provokingVertexMode = SRP_PROVOKING_VERTEX_LAST;
+	c->raster.frontFace = SRP_WINDING_CCW;
+	c->raster.cullFace = SRP_FACE_NONE;
+	c->raster.polygonMode = SRP_POLYGON_MODE_FILL;
+	c->raster.pointSize = 1.f;
+	memset(&c->scissor, 0, sizeof c->scissor);
+	c->depth.testEnable = false;
+	c->depth.writeEnable = true;
+	c->depth.compareOp = SRP_COMPARE_GREATER;
+	SRPStencilFaceState f = { SRP_COMPARE_ALWAYS, 0, 0xFF, 0xFF, SRP_STENCIL_KEEP, SRP_STENCIL_KEEP, SRP_STENCIL_KEEP };
+	c->stencil.enabled = false;
+	c->stencil.front = f;
+	c->stencil.back = f;
+	c->arena = NULL;
+}
+
+void srpSetMessageCallback(SRPMessageCallback cb) { srpContext.messageCallback = cb; }
+void srpProvokingVertexMode(SRPProvokingVertexMode m) { srpContext.provokingVertexMode = m; }
+void srpRasterCullFace(SRPFace f) { srpContext.raster.cullFace = f; }
+void srpRasterFrontFace(SRPWinding w) { srpContext.raster.frontFace = w; }
+void srpRasterPolygonMode(SRPPolygonMode m) { srpContext.raster.polygonMode = m; }
+void srpRasterPointSize(float s) { srpContext.raster.pointSize = s; }
+void srpScissorTest(bool e) { srpContext.scissor.enabled = e; }
+void srpScissorOptions(size_t x, size_t y, size_t w, size_t h)
+{
+	srpContext.scissor.x = x; srpContext.scissor.y = y;
+	srpContext.scissor.width = w; srpContext.scissor.height = h;
+}
+/* enables the test whatever the argument, as the reference does */
+void srpStencilTest(bool) { srpContext.stencil.enabled = true; }
+void srpStencilFunc(SRPCompareOp func, uint8_t ref, uint8_t mask)
+{
+	SRPStencilFaceState* s[2] = { &srpContext.stencil.front, &srpContext.stencil.back };
+	for (auto* f : s) { f->func = func; f->ref = ref; f->mask = mask; }
+}
+static SRPStencilFaceState* faceState(SRPFace face)
+{
+	return face == SRP_FACE_FRONT ? &srpContext.stencil.front : &srpContext.stencil.back;
+}
+void srpStencilFuncSeparate(SRPFace face, SRPCompareOp func, uint8_t ref, uint8_t mask)
+{
+	if (face == SRP_FACE_NONE) return;
+	if (face == SRP_FACE_FRONT_AND_BACK) srpStencilFunc(func, ref, mask);
+	SRPStencilFaceState* s = faceState(face);
+	s->func = func; s->ref = ref; s->mask = mask;
+}
+void srpStencilOp(SRPStencilOp sfail, SRPStencilOp dfail, SRPStencilOp pass)
+{
+	SRPStencilFaceState* s[2] = { &srpContext.stencil.front, &srpContext.stencil.back };
+	for (auto* f : s) { f->sfailOp = sfail; f->dfailOp = dfail; f->passOp = pass; }
+}
+void srpStencilOpSeparate(SRPFace face, SRPStencilOp sfail, SRPStencilOp dfail, SRPStencilOp pass)
+{
+	if (face == SRP_FACE_NONE) return;
+	if (face == SRP_FACE_FRONT_AND_BACK) srpStencilOp(sfail, dfail, pass);
+	SRPStencilFaceState* s = faceState(face);
+	s->sfailOp = sfail; s->dfailOp = dfail; s->passOp = pass;
+}
+void srpStencilWriteMask(uint8_t mask)
+{
+	srpContext.stencil.front.writeMask = mask;
+	srpContext.stencil.back.writeMask = mask;
+}
+void srpStencilWriteMaskSeparate(SRPFace face, uint8_t mask)
+{
+	if (face == SRP_FACE_NONE) return;
+	if (face == SRP_FACE_FRONT_AND_BACK) srpStencilWriteMask(mask);
+	faceState(face)->writeMask = mask;
+}
+void srpDepthTest(bool e) { srpContext.depth.testEnable = e; }
+void srpDepthWrite(bool e) { srpContext.depth.writeEnable = e; }
+void srpDepthCompareOp(SRPCompareOp op) { srpContext.depth.compareOp = op; }
+
+}  // extern "C"
+
+/* ---------------------------------------------------------------- buffers */
+
+struct SRPVertexBuffer {
+	size_t stride = 0, nVertices = 0, nBytes = 0, cap = 0;
+	unsigned char* host = nullptr;    /* staging copy made by CopyData */
+	DeviceBuffer dev;
+	bool dirty = false;
+};
+
+struct SRPIndexBuffer {
+	SRPType type = SRP_UINT8;
+	size_t elemSize = 1, nIndices = 0, nBytes = 0, cap = 0;
+	unsigned char* host = nullptr;
+	DeviceBuffer dev;
+	bool dirty = false;
+};
+
+static size_t indexTypeSize(SRPType t)
+{
+	/* srpSizeofType (src/utils/type.c:15-40) */
+	switch (t) {
+	case SRP_UINT8: return 1;
+	case SRP_UINT16: return 2;
+	case SRP_UINT32: case SRP_FLOAT: return 4;
+	case SRP_UINT64: case SRP_DOUBLE: return 8;
+	default:
+		SRP_ERROR("srpSizeofType", "Unknown type (%i)", (int) t);
+		return 0;
+	}
+}
+
+static void* pinnedRealloc(void* old, size_t n)
+{
+	if (old) cudaFreeHost(old);
+	void* p = nullptr;
+	if (cudaMallocHost(&p, n ? n : 1) != cudaSuccess) {
+		p = malloc(n ? n : 1);
+		if (!p) { fprintf(stderr, "srp-gb300: out of host memory\n"); abort(); }
+	}
+	return p;
+}
+
+extern "C" {
+
+SRPVertexBuffer* srpNewVertexBuffer(void) { return new SRPVertexBuffer(); }
+
+void srpFreeVertexBuffer(SRPVertexBuffer* b)
+{
+	if (!b) return;
+	if (b->host) cudaFreeHost(b->host);
+	if (b->dev.ptr) cudaFree(b->dev.ptr);
+	delete b;
+}
+
+void srpVertexBufferCopyData(SRPVertexBuffer* b, size_t stride, size_t nBytes, const void* data)
+{
+	if (nBytes > b->cap) { b->host = (unsigned char*) pinnedRealloc(b->host, nBytes); b->cap = nBytes; }
+	b->stride = stride;
+	b->nVertices = stride ? nBytes / stride : 0;
+	b->nBytes = nBytes;
+	if (nBytes) memcpy(b->host, data, nBytes);
+	b->dirty = true;
+}
+
+SRPIndexBuffer* srpNewIndexBuffer(void) { return new SRPIndexBuffer(); }
+
+void srpFreeIndexBuffer(SRPIndexBuffer* b)
+{
+	if (!b) return;
+	if (b->host) cudaFreeHost(b->host);
+	if (b->dev.ptr) cudaFree(b->dev.ptr);
+	delete b;
+}
+
+void srpIndexBufferCopyData(SRPIndexBuffer* b, SRPType type, size_t nBytes, const void* data)
+{
+	if (nBytes > b->cap) { b->host = (unsigned char*) pinnedRealloc(b->host, nBytes); b->cap = nBytes; }
+	b->type = type;
+	b->elemSize = indexTypeSize(type);
+	/* the reference divides by zero for a type without a size; report instead */
+	b->nIndices = b->elemSize ? nBytes / b->elemSize : 0;
+	b->nBytes = nBytes;
+	if (nBytes) memcpy(b->host, data, nBytes);
+	b->dirty = true;
+}
+
+}  // extern "C"
+
+/* ------------------------------------------------------------ framebuffer */
+
+namespace {
+struct FbExtra {
+	uint32_t* color = nullptr;
+	float* depth = nullptr;
+	uint8_t* stencil = nullptr;
+};
+/* The public struct has no room for device pointers; they live in a side
+ * table keyed by the framebuffer address. */
+std::vector<std::pair<const SRPFramebuffer*, FbExtra>> fbTable;
+
+FbExtra* fbFind(const SRPFramebuffer* fb)
+{
+	for (auto& e : fbTable) if (e.first == fb) return &e.second;
+	return nullptr;
+}
+}  // namespace
+
+__global__ void k_fill32(uint32_t* p, uint32_t v, size_t n)
+{
+	for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n; i += (size_t) gridDim.x * blockDim.x) p[i] = v;
+}
+
+static void fill32(uint32_t* p, uint32_t v, size_t n)
+{
+	if (!n) return;
+	size_t blocks = std::min<size_t>((n + 255) / 256, 152 * 16);
+	k_fill32<<<(unsigned) blocks, 256, 0, g.stream>>>(p, v, n);
+	++g.launches;
+}
+
+static void fbUpload(const SRPFramebuffer* fb, FbExtra* x)
+{
+	cudaMemcpyAsync(x->color, fb->color, 4 * fb->size, cudaMemcpyHostToDevice, g.stream);
+	cudaMemcpyAsync(x->depth, fb->depth, 4 * fb->size, cudaMemcpyHostToDevice, g.stream);
+	cudaMemcpyAsync(x->stencil, fb->stencil, fb->size, cudaMemcpyHostToDevice, g.stream);
+}
+
+static void fbDownload(const SRPFramebuffer* fb, FbExtra* x)
+{
+	cudaMemcpyAsync(fb->color, x->color, 4 * fb->size, cudaMemcpyDeviceToHost, g.stream);
+	cudaMemcpyAsync(fb->depth, x->depth, 4 * fb->size, cudaMemcpyDeviceToHost, g.stream);
+	cudaMemcpyAsync(fb->stencil, x->stencil, fb->size, cudaMemcpyDeviceToHost, g.stream);
+	cudaStreamSynchronize(g.stream);
+}
+
+extern "C" {
+
+SRPFramebuffer* srpNewFramebuffer(size_t w, size_t h)
+{
+	if (!ensureInit("srpNewFramebuffer")) return nullptr;
+	if (w > 32767 || h > 32767) {
+		SRP_ERROR("srpNewFramebuffer", "Framebuffer %zux%zu exceeds the GPU limit of 32767 per side", w, h);
+		return nullptr;
+	}
+	SRPFramebuffer* fb = (SRPFramebuffer*) calloc(1, sizeof(SRPFramebuffer));
+	fb->width = w; fb->height = h; fb->size = w * h;
+	fb->color = (uint32_t*) pinnedRealloc(nullptr, 4 * fb->size);
+	fb->depth = (float*) pinnedRealloc(nullptr, 4 * fb->size);
+	fb->stencil = (uint8_t*) pinnedRealloc(nullptr, fb->size);
+	memset(fb->color, 0, 4 * fb->size);
+	memset(fb->depth, 0, 4 * fb->size);
+	memset(fb->stencil, 0, fb->size);
+	FbExtra x;
+	const size_t n = fb->size ? fb->size : 1;
+	if (!cudaOk(cudaMalloc(&x.color, 4 * n), "srpNewFramebuffer", "cudaMalloc") ||
+	    !cudaOk(cudaMalloc(&x.depth, 4 * n), "srpNewFramebuffer", "cudaMalloc") ||
+	    !cudaOk(cudaMalloc(&x.stencil, n), "srpNewFramebuffer", "cudaMalloc")) return fb;
+	cudaMemsetAsync(x.color, 0, 4 * n, g.stream);
+	cudaMemsetAsync(x.depth, 0, 4 * n, g.stream);
+	cudaMemsetAsync(x.stencil, 0, n, g.stream);
+	fbTable.push_back({ fb, x });
+	return fb;
+}
+
+void srpFreeFramebuffer(SRPFramebuffer* fb)
+{
+	if (!fb) return;
+	cudaStreamSynchronize(g.stream);
+	for (size_t i = 0; i < fbTable.size(); ++i)
+		if (fbTable[i].first == fb) {
+			cudaFree(fbTable[i].second.color);
+			cudaFree(fbTable[i].second.depth);
+			cudaFree(fbTable[i].second.stencil);
+			fbTable.erase(fbTable.begin() + (long) i);
+			break;
+		}
+	cudaFreeHost(fb->color);
+	cudaFreeHost(fb->depth);
+	cudaFreeHost(fb->stencil);
+	free(fb);
+}
+
+void srpFramebufferClear(const SRPFramebuffer* fb)
+{
+	FbExtra* x = fbFind(fb);
+	if (!x) return;
+	cudaMemsetAsync(x->color, 0, 4 * fb->size, g.stream);
+	fill32((uint32_t*) x->depth, 0xBF800000u /* -1.0f */, fb->size);
+	if (g.fbMode == SRP_GPU_FB_COHERENT) {
+		memset(fb->color, 0, 4 * fb->size);
+		for (size_t i = 0; i < fb->size; ++i) fb->depth[i] = -1.0f;
+	}
+}
+
+void srpGpuSetFramebufferMode(SRPGpuFramebufferMode mode) { g.fbMode = mode; }
+SRPGpuFramebufferMode srpGpuGetFramebufferMode(void) { return g.fbMode; }
+
+void srpGpuFramebufferSync(const SRPFramebuffer* fb)
+{
+	FbExtra* x = fbFind(fb);
+	if (x) fbDownload(fb, x);
+}
+
+void srpGpuFramebufferUpload(const SRPFramebuffer* fb)
+{
+	FbExtra* x = fbFind(fb);
+	if (x) fbUpload(fb, x);
+}
+
+void srpGpuFramebufferFill(const SRPFramebuffer* fb, uint32_t color, float depth, uint8_t stencil, unsigned planes)
+{
+	FbExtra* x = fbFind(fb);
+	if (!x) return;
+	uint32_t dbits;
+	memcpy(&dbits, &depth, 4);
+	if (planes & SRP_GPU_FILL_COLOR) fill32(x->color, color, fb->size);
+	if (planes & SRP_GPU_FILL_DEPTH) fill32((uint32_t*) x->depth, dbits, fb->size);
+	if (planes & SRP_GPU_FILL_STENCIL) cudaMemsetAsync(x->stencil, stencil, fb->size, g.stream);
+	if (g.fbMode == SRP_GPU_FB_COHERENT) {
+		for (size_t i = 0; i < fb->size; ++i) {
+			if (planes & SRP_GPU_FILL_COLOR) fb->color[i] = color;
+			if (planes & SRP_GPU_FILL_DEPTH) fb->depth[i] = depth;
+			if (planes & SRP_GPU_FILL_STENCIL) fb->stencil[i] = stencil;
+		}
+	}
+}
+
+}  // extern "C"
+
+/* ---------------------------------------------------------------- texture */
+
+struct SRPTexture {
+	uint8_t* rgb = nullptr;   /* host copy, 3 channels */
+	int width = 0, height = 0, wm1 = 0, hm1 = 0;
+	SRPTextureWrappingMode wx = TW_REPEAT, wy = TW_REPEAT;
+	uint32_t* texels = nullptr;      /* device RGBA8 */
+	TextureDesc* desc = nullptr;     /* device descriptor */
+	bool dirty = true;
+};
+
+static bool textureSync(SRPTexture* t)
+{
+	if (!t->texels) {
+		if (!cudaOk(cudaMalloc(&t->texels, (size_t) t->width * t->height * 4), "srpNewTexture", "cudaMalloc")) return false;
+		if (!cudaOk(cudaMalloc(&t->desc, sizeof(TextureDesc)), "srpNewTexture", "cudaMalloc")) return false;
+		std::vector<uint32_t> rgba((size_t) t->width * t->height);
+		for (size_t i = 0; i < rgba.size(); ++i)
+			rgba[i] = (uint32_t) t->rgb[3 * i] | (uint32_t) t->rgb[3 * i + 1] << 8 | (uint32_t) t->rgb[3 * i + 2] << 16;
+		cudaMemcpy(t->texels, rgba.data(), rgba.size() * 4, cudaMemcpyHostToDevice);
+	}
+	if (t->dirty) {
+		TextureDesc d;
+		d.texels = t->texels;
+		d.width = t->width; d.height = t->height; d.wm1 = t->wm1; d.hm1 = t->hm1;
+		d.wrapX = t->wx; d.wrapY = t->wy;
+		cudaMemcpyAsync(t->desc, &d, sizeof d, cudaMemcpyHostToDevice, g.stream);
+		cudaStreamSynchronize(g.stream);
+		t->dirty = false;
+	}
+	return true;
+}
+
+extern "C" {
+
+SRPTexture* srpNewTextureFromMemory(const uint8_t* texels, int w, int h, int ch,
+                                    SRPTextureWrappingMode wx, SRPTextureWrappingMode wy)
+{
+	if (!texels || w <= 0 || h <= 0 || (ch != 3 && ch != 4)) {
+		SRP_ERROR("srpNewTextureFromMemory", "Invalid texture arguments");
+		return nullptr;
+	}
+	if (!ensureInit("srpNewTextureFromMemory")) return nullptr;
+	SRPTexture* t = new SRPTexture();
+	t->rgb = (uint8_t*) malloc((size_t) w * h * 3);
+	for (size_t i = 0; i < (size_t) w * h; ++i) memcpy(t->rgb + 3 * i, texels + (size_t) ch * i, 3);
+	t->width = w; t->height = h; t->wm1 = w - 1; t->hm1 = h - 1; t->wx = wx; t->wy = wy;
+	if (!textureSync(t)) { free(t->rgb); delete t; return nullptr; }
+	return t;
+}
+
+SRPTexture* srpNewTexture(const char* path, SRPTextureWrappingMode wx, SRPTextureWrappingMode wy)
+{
+	SRPImage img;
+	const char* err = "";
+	if (!srpImageLoad(path, &img, &err)) {
+		SRP_ERROR("srpNewTexture", "Failed to load image `%s`: %s", path, err);
+		return nullptr;
+	}
+	SRPTexture* t = srpNewTextureFromMemory(img.rgb, img.width, img.height, 3, wx, wy);
+	free(img.rgb);
+	return t;
+}
+
+void srpFreeTexture(SRPTexture* t)
+{
+	if (!t) return;
+	cudaStreamSynchronize(g.stream);
+	if (t->texels) cudaFree(t->texels);
+	if (t->desc) cudaFree(t->desc);
+	free(t->rgb);
+	delete t;
+}
+
+void srpTextureGetFilteredColor(const SRPTexture* t, float u, float v, float out[4])
+{
+	/* host lookup, same arithmetic as the device sampler (texture.c:56-81) */
+	if (u < 0 || u > 1) u = (float) (t->wx == TW_REPEAT ? (double) u - floor(u) : fmax(0.0, fmin(1.0, u)));
+	if (v < 0 || v > 1) v = (float) (t->wy == TW_REPEAT ? (double) v - floor(v) : fmax(0.0, fmin(1.0, v)));
+	float x = (float) t->wm1 * u;
+	float y = (float) t->hm1 * (1 - v);
+	size_t xi = (size_t) ((double) x + 0.5), yi = (size_t) ((double) y + 0.5);
+	const uint8_t* p = t->rgb + 3 * (xi + yi * (size_t) t->width);
+	const float inv255 = (float) (1. / 255.);
+	out[0] = p[0] * inv255; out[1] = p[1] * inv255; out[2] = p[2] * inv255; out[3] = 1.f;
+}
+
+int srpTextureGet(SRPTexture* t, SRPTextureParameter p)
+{
+	switch (p) {
+	case SRP_TEXTURE_WRAPPING_MODE_X: return t->wx;
+	case SRP_TEXTURE_WRAPPING_MODE_Y: return t->wy;
+	}
+	SRP_ERROR("srpTextureGet", "Unknown texture parameter (%i)", (int) p);
+	return -1;
+}
+
+void srpTextureSet(SRPTexture* t, SRPTextureParameter p, int data)
+{
+	if (p != SRP_TEXTURE_WRAPPING_MODE_X && p != SRP_TEXTURE_WRAPPING_MODE_Y) {
+		SRP_ERROR("srpTextureSet", "Unknown texture parameter (%i)", (int) p);
+		return;
+	}
+	if (p == SRP_TEXTURE_WRAPPING_MODE_X) t->wx = (SRPTextureWrappingMode) data;
+	else t->wy = (SRPTextureWrappingMode) data;
+	t->dirty = true;
+	if (data != TW_REPEAT && data != TW_CLAMP_TO_EDGE)
+		SRP_ERROR("srpTextureSet", "Unknown texture wrapping mode (%i). Falling back to TW_REPEAT", data);
+}
+
+/* ---------------------------------------------------------------- shaders */
+
+void srpGpuRegisterVertexShader(void (*fn)(SRPVertexShaderIn*, SRPVertexShaderOut*), SRPGpuVertexShaderId id)
+{
+	for (auto& e : g.reg.vs) if (e.first == (void*) fn) { e.second = id; return; }
+	g.reg.vs.push_back({ (void*) fn, (int) id });
+}
+
+void srpGpuRegisterFragmentShader(void (*fn)(SRPFragmentShaderIn*, SRPFragmentShaderOut*), SRPGpuFragmentShaderId id)
+{
+	for (auto& e : g.reg.fs) if (e.first == (void*) fn) { e.second = id; return; }
+	g.reg.fs.push_back({ (void*) fn, (int) id });
+}
+
+}  // extern "C"
+
+/* the library's own host copies of the shared shaders */
+#define SRP_SHADERLIB_HOST_ONLY
+extern "C" {
+#include "srp/shaderlib_host.inc"
+}
+
+static int lookupVS(void* fn)
+{
+	if (fn == (void*) srpVsTransform) return SRP_GPU_VS_TRANSFORM;
+	if (fn == (void*) srpVsWorld) return SRP_GPU_VS_WORLD;
+	for (auto& e : g.reg.vs) if (e.first == fn) return e.second;
+	return 0;
+}
+
+static int lookupFS(void* fn)
+{
+	static const struct { void* f; int id; } builtin[] = {
+		{ (void*) srpFsVaryingColor, SRP_GPU_FS_VARYING_COLOR }, { (void*) srpFsSolid, SRP_GPU_FS_SOLID },
+		{ (void*) srpFsPrimitiveId, SRP_GPU_FS_PRIMITIVE_ID }, { (void*) srpFsTexture, SRP_GPU_FS_TEXTURE },
+		{ (void*) srpFsTextureModulate, SRP_GPU_FS_TEXTURE_MODULATE }, { (void*) srpFsBlinnPhong, SRP_GPU_FS_BLINN_PHONG },
+		{ (void*) srpFsMarble, SRP_GPU_FS_MARBLE }, { (void*) srpFsDepthOverwrite, SRP_GPU_FS_DEPTH_OVERWRITE },
+		{ (void*) srpFsFragCoord, SRP_GPU_FS_FRAGCOORD }, { (void*) srpFsFlatInt, SRP_GPU_FS_FLAT_INT },
+	};
+	for (auto& b : builtin) if (b.f == fn) return b.id;
+	for (auto& e : g.reg.fs) if (e.first == fn) return e.second;
+	return 0;
+}
+
+/* ------------------------------------------------------------------- draw */
+
+static size_t varyingElemSize(SRPType t)
+{
+	switch (t) {
+	case SRP_INT8: case SRP_UINT8: return 1;
+	case SRP_INT16: case SRP_UINT16: return 2;
+	case SRP_INT32: case SRP_UINT32: case SRP_FLOAT: return 4;
+	case SRP_INT64: case SRP_UINT64: case SRP_DOUBLE: return 8;
+	}
+	return 0;
+}
+
+static bool buildLayout(const SRPVertexShader* vs, VaryingLayout& L)
+{
+	memset(&L, 0, sizeof L);
+	if (vs->nVaryings > (size_t) kMaxVaryings) {
+		SRP_ERROR("srpDraw", "GPU path supports at most %d varyings (got %zu)", kMaxVaryings, vs->nVaryings);
+		return false;
+	}
+	size_t off = 0;
+	bool floatOnly = true;
+	for (size_t a = 0; a < vs->nVaryings; ++a) {
+		const SRPVaryingInfo& in = vs->varyingsInfo[a];
+		const size_t es = varyingElemSize(in.type);
+		if (!es) SRP_ERROR("interpolateAttributes", "Unexpected type (%i)", (int) in.type);
+		VaryingAttr& at = L.attr[a];
+		at.offset = (uint16_t) off;
+		at.nItems = (uint16_t) in.nItems;
+		at.type = (uint8_t) in.type;
+		at.mode = (uint8_t) (in.interpolationMode == SRP_INTERPOLATION_MODE_PERSPECTIVE ? kPerspective
+		                   : in.interpolationMode == SRP_INTERPOLATION_MODE_AFFINE ? kAffine : kFlat);
+		at.elemSize = (uint8_t) es;
+		if (es != 4 || (off & 3)) floatOnly = false;
+		for (size_t e = 0; e < in.nItems && es == 4 && !(off & 3); ++e) {
+			const size_t w = off / 4 + e;
+			if (w < (size_t) kMaxVaryingWords) {
+				L.wordMode[w] = at.mode;
+				L.wordIsFloat[w] = in.type == SRP_FLOAT;
+			}
+		}
+		off += es * in.nItems;
+	}
+	const size_t bytes = std::max(off, vs->varyingsSize);
+	if (bytes > (size_t) 4 * kMaxVaryingWords) {
+		SRP_ERROR("srpDraw", "GPU path supports varying blocks up to %d bytes (got %zu)", 4 * kMaxVaryingWords, bytes);
+		return false;
+	}
+	L.nAttr = (int) vs->nVaryings;
+	L.sizeBytes = (int) bytes;
+	L.nWords = (int) ((bytes + 3) / 4);
+	/* words outside any attribute are copied from the provoking vertex */
+	for (int w = (int) ((off + 3) / 4); w < L.nWords; ++w) { L.wordMode[w] = kFlat; L.wordIsFloat[w] = 0; }
+	L.floatOnly = floatOnly ? 1 : 0;
+	return true;
+}
+
+static bool isTri(SRPPrimitive p) { return p == SRP_PRIM_TRIANGLES || p == SRP_PRIM_TRIANGLE_STRIP || p == SRP_PRIM_TRIANGLE_FAN; }
+static bool isLine(SRPPrimitive p) { return p == SRP_PRIM_LINES || p == SRP_PRIM_LINE_STRIP || p == SRP_PRIM_LINE_LOOP; }
+
+static bool uploadVB(SRPVertexBuffer* vb)
+{
+	if (!vb->dirty && vb->dev.ptr) return true;
+	if (!vb->dev.reserve(vb->nBytes + 16, "srpDraw")) return false;
+	if (vb->nBytes) cudaMemcpyAsync(vb->dev.ptr, vb->host, vb->nBytes, cudaMemcpyHostToDevice, g.stream);
+	vb->dirty = false;
+	return true;
+}
+
+static bool uploadIB(SRPIndexBuffer* ib)
+{
+	if (!ib->dirty && ib->dev.ptr) return true;
+	if (!ib->dev.reserve(ib->nBytes + 16, "srpDraw")) return false;
+	if (ib->nBytes) cudaMemcpyAsync(ib->dev.ptr, ib->host, ib->nBytes, cudaMemcpyHostToDevice, g.stream);
+	ib->dirty = false;
+	return true;
+}
+
+static uint32_t bitsFor(uint32_t n)
+{
+	uint32_t b = 0;
+	while ((1ull << b) < (unsigned long long) n + 1ull) ++b;
+	return (b + 7) / 8 * 8;
+}
+
+static bool readCounters()
+{
+	cudaMemcpyAsync(g.hostCtr, g.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, g.stream);
+	return cudaOk(cudaStreamSynchronize(g.stream), "srpDraw", "kernel execution");
+}
+
+/* The GPU pipeline for one draw call. */
+static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const SRPFramebuffer* fb,
+                    const SRPShaderProgram* sp, SRPPrimitive prim, size_t start, size_t count, size_t nIn)
+{
+	const char* FN = "srpDraw";
+	SRPIndexBuffer* ib = (SRPIndexBuffer*) ibc;
+	SRPVertexBuffer* vb = (SRPVertexBuffer*) vbc;
+	FbExtra* fx = fbFind(fb);
+	if (!fx) { SRP_ERROR(FN, "Framebuffer was not created by srpNewFramebuffer"); return; }
+	const int vsId = lookupVS((void*) sp->vs->shader);
+	const int fsId = lookupFS((void*) sp->fs->shader);
+	if (!vsId || !fsId) {
+		SRP_ERROR(FN, "Shader has no GPU implementation; map it with srpGpuRegisterVertexShader/FragmentShader");
+		return;
+	}
+	if (vb->stride == 0 || vb->stride > 1024) {
+		SRP_ERROR(FN, "GPU path supports vertex strides of 1..1024 bytes (got %zu)", vb->stride);
+		return;
+	}
+	static DrawParams P;
+	memset(&P, 0, sizeof P);
+	if (!buildLayout(sp->vs, P.L)) return;
+	/* state snapshot */
+	DrawState& st = P.st;
+	st.W = (int) fb->width; st.H = (int) fb->height;
+	st.frontFaceCW = srpContext.raster.frontFace == SRP_WINDING_CW;
+	st.cullFace = srpContext.raster.cullFace;
+	st.polygonMode = srpContext.raster.polygonMode;
+	st.pointSize = srpContext.raster.pointSize;
+	st.provokingFirst = srpContext.provokingVertexMode == SRP_PROVOKING_VERTEX_FIRST;
+	st.scissorEnabled = srpContext.scissor.enabled;
+	st.sx0 = srpContext.scissor.x; st.sx1 = srpContext.scissor.x + srpContext.scissor.width;
+	st.sy0 = srpContext.scissor.y; st.sy1 = srpContext.scissor.y + srpContext.scissor.height;
+	st.stencilEnabled = srpContext.stencil.enabled;
+	const SRPStencilFaceState* fsrc[2] = { &srpContext.stencil.front, &srpContext.stencil.back };
+	StencilFace* fdst[2] = { &st.front, &st.back };
+	for (int i = 0; i < 2; ++i) {
+		fdst[i]->func = fsrc[i]->func; fdst[i]->sfail = fsrc[i]->sfailOp; fdst[i]->dfail = fsrc[i]->dfailOp;
+		fdst[i]->pass = fsrc[i]->passOp; fdst[i]->ref = fsrc[i]->ref; fdst[i]->mask = fsrc[i]->mask;
+		fdst[i]->writeMask = fsrc[i]->writeMask;
+	}
+	st.depthTest = srpContext.depth.testEnable;
+	st.depthWrite = srpContext.depth.writeEnable;
+	st.depthOp = srpContext.depth.compareOp;
+	st.earlyZ = !sp->fs->mayOverwriteDepth;
+	st.tile = kTile;
+	st.tilesX = (st.W + kTile - 1) / kTile;
+	st.tilesY = (st.H + kTile - 1) / kTile;
+	const uint32_t numTiles = (uint32_t) st.tilesX * (uint32_t) st.tilesY;
+	/* uniform: the built-in shaders read SRPStdUniform; its texture pointer
+	 * is replaced by the texture's device descriptor */
+	if (sp->uniform) {
+		SRPStdUniform u;
+		memcpy(&u, sp->uniform, sizeof u);
+		if (u.texture) {
+			SRPTexture* t = u.texture;
+			if (!textureSync(t)) return;
+			u.texture = (SRPTexture*) t->desc;
+		}
+		memcpy(P.uniform, &u, sizeof u);
+	}
+	static_assert(sizeof(SRPStdUniform) <= kMaxUniformBytes, "uniform too large");
+	P.vsId = vsId;
+	P.fsId = fsId;
+	P.prim = prim;
+	P.start = start;
+	P.count = count;
+	P.nIn = (int) nIn;
+	if (!uploadVB(vb)) return;
+	P.vertices = vb->dev.as<unsigned char>();
+	P.nVertices = vb->nVertices;
+	P.stride = (int) vb->stride;
+	if (ib) {
+		if (!uploadIB(ib)) return;
+		P.indices = ib->dev.ptr;
+		P.indexSize = (int) ib->elemSize;
+		if (ib->type != SRP_UINT8 && ib->type != SRP_UINT16 && ib->type != SRP_UINT32 && ib->type != SRP_UINT64) {
+			SRP_ERROR("indexIndexBuffer", "Unexpected type (%i)", (int) ib->type);
+			return;
+		}
+	}
+	P.minmax = g.minmax.as<unsigned long long>();
+	P.ctr = g.ctr.as<DeviceCounters>();
+	P.color = fx->color;
+	P.depth = fx->depth;
+	P.stencil = fx->stencil;
+	const int mode = isTri(prim) ? st.polygonMode : (isLine(prim) ? SRP_POLYGON_MODE_LINE : SRP_POLYGON_MODE_POINT);
+	const int kind = mode == SRP_POLYGON_MODE_FILL ? kKindTri : mode == SRP_POLYGON_MODE_LINE ? kKindLineFrag : kKindPoint;
+	const size_t outPer = isTri(prim) && mode != SRP_POLYGON_MODE_FILL ? 3 : 1;
+	if (g.fbMode == SRP_GPU_FB_COHERENT) fbUpload(fb, fx);
+
+	uint32_t primCap = (uint32_t) std::min<size_t>(nIn * outPer + 4096, 0x3FFFFFFFu);
+	uint32_t entryCap = (uint32_t) std::min<double>(primCap * g.entryRatio + 4096, 4.0e9);
+	for (int attempt = 0; attempt < 4; ++attempt) {
+		const uint32_t rows = (uint32_t) vb->nVertices + g.clipRows;
+		const size_t nw = (size_t) std::max(P.L.nWords, 1);
+		const uint32_t blocks = (uint32_t) ((nIn + kSetupThreads - 1) / kSetupThreads);
+		bool ok = g.clip.reserve((size_t) rows * 16, FN) && g.vary.reserve((size_t) rows * nw * 4, FN) &&
+		          g.lookback.reserve((size_t) std::max(blocks, 1u) * 8, FN) &&
+		          g.keys.reserve((size_t) entryCap * 4, FN) && g.vals.reserve((size_t) entryCap * 4, FN) &&
+		          g.big.reserve((size_t) g.bigCap * 16, FN);
+		if (kind == kKindTri) ok = ok && g.triR.reserve((size_t) primCap * sizeof(TriRaster), FN) &&
+		                           g.triA.reserve((size_t) primCap * sizeof(TriAttr), FN);
+		else if (kind == kKindPoint) ok = ok && g.points.reserve((size_t) primCap * sizeof(PointRec), FN);
+		else ok = ok && g.lines.reserve((size_t) primCap * sizeof(LineRec), FN) &&
+		          g.frags.reserve((size_t) entryCap * sizeof(LineFrag), FN);
+		if (!ok) return;
+		P.clip = g.clip.as<float4>();
+		P.vary = g.vary.as<uint32_t>();
+		P.clipBase = (uint32_t) vb->nVertices;
+		P.clipCap = g.clipRows;
+		P.triR = g.triR.as<TriRaster>();
+		P.triA = g.triA.as<TriAttr>();
+		P.lines = g.lines.as<LineRec>();
+		P.points = g.points.as<PointRec>();
+		P.frags = g.frags.as<LineFrag>();
+		P.primCap = primCap;
+		P.fragCap = kind == kKindLineFrag ? entryCap : 0;
+		P.keys = g.keys.as<uint32_t>();
+		P.vals = g.vals.as<uint32_t>();
+		P.entryCap = entryCap;
+		P.bigJobs = g.big.as<uint4>();
+		P.bigCap = g.bigCap;
+		P.lookback = g.lookback.as<unsigned long long>();
+
+		launchReset(P, g.stream);
+		if (ib) launchIndexRange(P, g.stream);
+		if (ib) launchVertex(P, 0, vb->nVertices, g.stream);
+		else launchVertex(P, start, count, g.stream);
+		cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, g.stream);
+		launchSetup(P, g.stream);
+		g.launches += 3 + (ib ? 1 : 0);
+		if (!cudaOk(cudaGetLastError(), FN, "launch") || !readCounters()) return;
+		const DeviceCounters c = *g.hostCtr;
+		if (c.errors & kErrBadIndex) {
+			SRP_ERROR(FN, "Vertex index out of range of the vertex buffer (%zu vertices)", vb->nVertices);
+			return;
+		}
+		if (c.errors & kErrSpin) { SRP_ERROR(FN, "Ordered-compaction wait timed out"); return; }
+		if (c.errors & kErrCapacity) {
+			bool grew = false;
+			if (c.clipVerts > g.clipRows) { g.clipRows = (uint32_t) std::min<unsigned long long>(c.clipVerts * 2, 0x7FFFFFFF); grew = true; }
+			if (c.prims > primCap) { primCap = (uint32_t) std::min<unsigned long long>(c.prims + 1024, 0x3FFFFFFF); grew = true; }
+			if (c.entries > entryCap) { entryCap = (uint32_t) std::min<double>(c.entries * 1.25 + 1024, 4.0e9); grew = true; }
+			if (c.bigJobs > g.bigCap) { g.bigCap = (uint32_t) std::min<unsigned long long>(c.bigJobs * 2, 1u << 30); grew = true; }
+			if (!grew) { SRP_ERROR(FN, "Scratch capacity exceeded"); return; }
+			continue;
+		}
+		if (c.prims) g.entryRatio = std::max(1.0, std::min(64.0, (double) c.entries / (double) c.prims * 1.25));
+		g.stats.primitives += c.prims;
+		g.stats.binEntries += c.entries;
+		g.stats.clipOverflows += c.clipOverflow;
+		const uint32_t E = (uint32_t) c.entries;
+		if (kind == kKindLineFrag) { launchLineFrags(P, (uint32_t) c.prims, g.stream); ++g.launches; }
+		else if (c.bigJobs) { launchBigEntries(P, (uint32_t) c.bigJobs, g.stream); ++g.launches; }
+		if (E == 0) break;
+		/* sort (tile, item) pairs by tile, keeping item order */
+		const uint32_t keyBits = bitsFor(numTiles);
+		if (!g.keys2.reserve((size_t) E * 4, FN) || !g.vals2.reserve((size_t) E * 4, FN) ||
+		    !g.hist.reserve(sortHistWords(E) * 4, FN) || !g.partials.reserve(sortPartialWords(E) * 4 + 64, FN) ||
+		    !g.tileStart.reserve((size_t) (numTiles + 1) * 4, FN) || !g.tileEnd.reserve((size_t) (numTiles + 1) * 4, FN) ||
+		    !g.winner.reserve(fb->size * 4 + 4, FN)) return;
+		uint32_t* sk;
+		uint32_t* sv;
+		sortEntries(P, E, keyBits, g.keys2.as<uint32_t>(), g.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
+		            g.partials.as<uint32_t>(), &sk, &sv, g.stream);
+		g.launches += (keyBits / 8) * 5;
+		P.tileStart = g.tileStart.as<uint32_t>();
+		P.tileEnd = g.tileEnd.as<uint32_t>();
+		P.winner = g.winner.as<int32_t>();
+		cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, g.stream);
+		cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, g.stream);
+		launchTileRanges(P, sk, E, numTiles, g.stream);
+		const bool late = sp->fs->mayOverwriteDepth && shadeSupportsLateDepth(fsId);
+		if (late) {
+			launchResolveLate(P, kind, sv, numTiles, g.stream);
+			g.launches += 2;
+		} else {
+			launchResolve(P, kind, sv, numTiles, g.stream);
+			launchShade(P, kind, numTiles, g.stream);
+			g.launches += 3;
+		}
+		cudaOk(cudaGetLastError(), FN, "launch");
+		break;
+	}
+	++g.stats.draws;
+	if (g.fbMode == SRP_GPU_FB_COHERENT) fbDownload(fb, fx);
+}
+
+static void warnExcess(SRPPrimitive p, size_t n)
+{
+	if (p == SRP_PRIM_LINES && n % 2 != 0)
+		message(SRP_MESSAGE_WARNING, SRP_MESSAGE_SEVERITY_LOW, "warnOnExcessVertexCount",
+		        "Odd vertex count when drawing SRP_PRIM_LINES. The last vertex will be ignored\n");
+	if (p == SRP_PRIM_TRIANGLES && n % 3 != 0)
+		message(SRP_MESSAGE_WARNING, SRP_MESSAGE_SEVERITY_LOW, "warnOnExcessVertexCount",
+		        "Vertex count not divisible by 3 when drawing SRP_PRIM_TRIANGLES. The last %i vertex/vertices will be ignored\n",
+		        (int) (n % 3));
+}
+
+/* drawBuffer (src/pipeline/draw.c:63-82): range check, primitive class,
+ * early returns, then the GPU pipeline. */
+static void drawBuffer(const SRPIndexBuffer* ib, const SRPVertexBuffer* vb, const SRPFramebuffer* fb,
+                       const SRPShaderProgram* sp, SRPPrimitive prim, size_t start, size_t count)
+{
+	if (count == 0) return;
+	const size_t end = start + count - 1;
+	const size_t size = ib ? ib->nIndices : vb->nVertices;
+	if (end >= size) {
+		SRP_ERROR("checkOOB", ib ? "Attempt to OOB access index buffer (read) at indices %zu-%zu (size: %zu)\n"
+		                         : "Attempt to OOB access vertex buffer (read) at indices %zu-%zu (size: %zu)\n",
+		          start, end, size);
+		return;
+	}
+	size_t nIn = 0;
+	if (isTri(prim)) {
+		if (srpContext.raster.cullFace == SRP_FACE_FRONT_AND_BACK) return;
+		warnExcess(prim, count);
+		nIn = prim == SRP_PRIM_TRIANGLES ? count / 3 : (count >= 3 ? count - 2 : 0);
+		if (srpContext.raster.polygonMode != SRP_POLYGON_MODE_FILL && srpContext.raster.polygonMode != SRP_POLYGON_MODE_LINE &&
+		    srpContext.raster.polygonMode != SRP_POLYGON_MODE_POINT) {
+			SRP_ERROR("assembleTrianglesGeneric", "Unexpected srpContext.raster.polygonMode (%i)", (int) srpContext.raster.polygonMode);
+			return;
+		}
+	} else if (isLine(prim)) {
+		warnExcess(prim, count);
+		nIn = prim == SRP_PRIM_LINES ? count / 2 : (count != 1 ? (prim == SRP_PRIM_LINE_STRIP ? count - 1 : count) : 0);
+	} else if (prim == SRP_PRIM_POINTS) {
+		if (srpContext.raster.pointSize <= 0.) return;
+		nIn = count;
+	} else {
+		SRP_ERROR("drawBuffer", "Unknown primitive type: %i", (int) prim);
+		return;
+	}
+	if (nIn == 0) return;
+	if (nIn > 0x7FFFFFFFull) { SRP_ERROR("drawBuffer", "Draw too large for the GPU path (%zu primitives)", nIn); return; }
+	if (!ensureInit("drawBuffer")) return;
+	runDraw(ib, vb, fb, sp, prim, start, count, nIn);
+}
+
+extern "C" {
+
+void srpDrawVertexBuffer(const SRPVertexBuffer* vb, const SRPFramebuffer* fb, const SRPShaderProgram* sp,
+                         SRPPrimitive prim, size_t start, size_t count)
+{
+	drawBuffer(nullptr, vb, fb, sp, prim, start, count);
+}
+
+void srpDrawIndexBuffer(const SRPIndexBuffer* ib, const SRPVertexBuffer* vb, const SRPFramebuffer* fb,
+                        const SRPShaderProgram* sp, SRPPrimitive prim, size_t start, size_t count)
+{
+	drawBuffer(ib, vb, fb, sp, prim, start, count);
+}
+
+/* ------------------------------------------------------- stream and stats */
+
+void srpGpuSetStream(void* stream)
+{
+	if (!ensureInit("srpGpuSetStream")) return;
+	cudaStreamSynchronize(g.stream);
+	g.stream = stream ? (cudaStream_t) stream : g.ownStream;
+}
+
+void* srpGpuGetStream(void) { return ensureInit("srpGpuGetStream") ? (void*) g.stream : nullptr; }
+
+int srpGpuSynchronize(void)
+{
+	if (!g.init) return 0;
+	return cudaOk(cudaStreamSynchronize(g.stream), "srpGpuSynchronize", "kernel execution") ? 0 : 1;
+}
+
+void srpGpuGetStats(SRPGpuStats* s)
+{
+	if (!g.init) { memset(s, 0, sizeof *s); return; }
+	readCounters();
+	*s = g.stats;
+	s->fragments = g.hostCtr->fragments;
+	s->kernelLaunches = g.launches;
+}
+
+void srpGpuResetStats(void)
+{
+	if (!g.init) return;
+	cudaStreamSynchronize(g.stream);
+	cudaMemset(g.ctr.ptr, 0, sizeof(DeviceCounters));
+	g.stats = SRPGpuStats();
+	g.launches = 0;
+}
+
+void srpGpuSetTileSize(int tileSize)
+{
+	if (tileSize != kTile) SRP_ERROR("srpGpuSetTileSize", "Only %d-pixel tiles are built into this library", kTile);
+}
+
+}  // extern "C"

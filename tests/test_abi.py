@@ -1,0 +1,81 @@
+"""The C-ABI library: it loads, exports every function the public headers
+declare, and its host-side validation reports through the message callback
+the way the reference does. No GPU work is issued here."""
+import ctypes
+import os
+import re
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in ("context.h", "buffer.h", "framebuffer.h", "texture.h", "vec.h", "mat.h", "gpu.h", "shaderlib.h"):
+        src = open(os.path.join(ROOT, "include", "srp", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b((?:srp|vec[234]|mat4)\w*)\s*\(", src, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_headers_declare_the_reference_api():
+    names = declared_functions()
+    for n in ("srpNewContext", "srpDrawIndexBuffer", "srpDrawVertexBuffer", "srpFramebufferClear",
+              "srpStencilOpSeparate", "srpTextureGetFilteredColor", "mat4ConstructPerspectiveProjection",
+              "vec3Normalize", "srpGpuFramebufferSync", "srpVsTransform"):
+        assert n in names
+    assert len(names) > 60
+
+
+def test_library_exports_every_declared_symbol(built_library):
+    out = subprocess.check_output(["nm", "-D", "--defined-only", built_library]).decode()
+    exported = {line.split()[-1] for line in out.splitlines() if line.strip()}
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, missing
+    assert "srpContext" in exported
+
+
+HOST_SCRIPT = r"""
+import ctypes, sys
+sys.path.insert(0, sys.argv[1])
+import srp_gb300 as s
+L = s.lib()
+msgs = []
+@s.MESSAGE_CALLBACK
+def cb(t, sev, fn, msg, user):
+    msgs.append((t, sev, fn.decode(), msg.decode()))
+ctx = ctypes.c_void_p.in_dll(L, "srpContext")
+L.srpNewContext.argtypes = [ctypes.c_void_p]
+L.srpNewContext(ctypes.addressof(ctx))
+L.srpNewVertexBuffer.restype = ctypes.c_void_p
+L.srpNewIndexBuffer.restype = ctypes.c_void_p
+L.srpSetMessageCallback(s.SRPMessageCallback(cb, None))
+vb = ctypes.c_void_p(L.srpNewVertexBuffer())
+data = (ctypes.c_float * 30)()
+L.srpVertexBufferCopyData.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_void_p]
+L.srpVertexBufferCopyData(vb, 12, 120, data)
+L.srpDrawVertexBuffer.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, ctypes.c_size_t]
+L.srpDrawVertexBuffer(vb, None, None, 4, 8, 3)   # 8..10 of 10 vertices: out of range
+L.srpDrawVertexBuffer(vb, None, None, 42, 0, 3)  # unknown primitive
+L.srpDrawVertexBuffer(vb, None, None, 4, 0, 0)   # empty draw: nothing
+L.srpRasterCullFace(3)                           # FRONT_AND_BACK: triangle draws are no-ops
+L.srpDrawVertexBuffer(vb, None, None, 4, 0, 9)
+ib = ctypes.c_void_p(L.srpNewIndexBuffer())
+L.srpIndexBufferCopyData.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p]
+L.srpIndexBufferCopyData(ib, 4, 16, data)        # SRP_INT32 has no index size
+for m in msgs:
+    print("MSG", m)
+"""
+
+
+def test_host_validation_reports_like_the_reference(built_library):
+    out = subprocess.check_output([sys.executable, "-c", HOST_SCRIPT, ROOT], cwd=ROOT).decode()
+    msgs = [l for l in out.splitlines() if l.startswith("MSG")]
+    assert any("checkOOB" in m and "indices 8-10 (size: 10)" in m for m in msgs), msgs
+    assert any("drawBuffer" in m and "Unknown primitive type: 42" in m for m in msgs), msgs
+    assert any("srpSizeofType" in m for m in msgs), msgs
+    assert len(msgs) == 3, msgs
