@@ -49,7 +49,7 @@ struct DrawParams {
 	uint32_t* tileStart;
 	uint32_t* tileEnd;
 	DeviceCounters* ctr;
-	unsigned char uniform[kMaxUniformBytes];
+	alignas(16) unsigned char uniform[kMaxUniformBytes];
 };
 
 constexpr int kTile = 8;              /* tile edge in pixels */
