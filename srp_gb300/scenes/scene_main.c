@@ -51,7 +51,9 @@ int main(int argc, char** argv)
 	SceneInfo info;
 	sceneGetInfo(s, &info);
 	SRPFramebuffer* fb = srpNewFramebuffer((size_t) info.width, (size_t) info.height);
-	if (!strcmp(argv[1], "render")) {
+	if (!strcmp(argv[1], "inputs")) {
+		sceneDumpInputs(s, argv[5]);
+	} else if (!strcmp(argv[1], "render")) {
 		scenePrepareFramebuffer(s, fb);
 		uint64_t f0 = fragments();
 		sceneRender(s, fb);

@@ -1167,6 +1167,17 @@ void sceneGetInfo(const Scene* s, SceneInfo* info)
 
 uint64_t sceneInputHash(const Scene* s) { return s->hash; }
 
+int sceneDumpInputs(const Scene* s, const char* path)
+{
+	FILE* f = fopen(path, "wb");
+	if (!f) return 1;
+	for (int k = 0; k < s->nvb; ++k) fwrite(s->vdata[k], 1, s->vbytes[k], f);
+	for (int k = 0; k < s->nib; ++k) fwrite(s->idata[k], 1, s->ibytes[k], f);
+	for (int k = 0; k < s->nprog; ++k) fwrite(&s->uni[k], 1, offsetof(SRPStdUniform, texture), f);
+	fclose(f);
+	return 0;
+}
+
 void sceneUpload(Scene* s)
 {
 	for (int k = 0; k < s->nvb; ++k) srpVertexBufferCopyData(s->vb[k], s->vstride[k], s->vbytes[k], s->vdata[k]);

@@ -47,6 +47,10 @@ void scenePrepareFramebuffer(Scene* s, SRPFramebuffer* fb);
 /* Set the pipeline state and issue the scene's draw calls. */
 void sceneRender(Scene* s, SRPFramebuffer* fb);
 
+/* Write the scene's generated inputs (vertex, index, texture and uniform
+ * bytes, pointer fields excluded) to `path`; used to compare machines. */
+int sceneDumpInputs(const Scene* s, const char* path);
+
 /* Convenience: create a framebuffer of the scene's size, prepare, render, copy
  * the planes out (color W*H u32, depth W*H f32, stencil W*H u8). Returns 0 on
  * success. */
