@@ -84,17 +84,22 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_chunks(uint32_t* data, ui
 	if (threadIdx.x == 0) partials[blockIdx.x] = total;
 }
 
-/* Pass 2: one block scans the chunk totals (up to kScanChunk of them). */
+/* Pass 2: one block scans the chunk totals, kScanChunk at a time with a
+ * running carry. */
 __global__ void __launch_bounds__(kScanThreads) k_scan_partials(uint32_t* partials, uint32_t n)
 {
 	__shared__ uint32_t sWarp[kScanThreads / 32];
-	const uint32_t base = threadIdx.x * kScanItems;
-	uint32_t v[kScanItems];
+	uint32_t carry = 0;
+	for (uint32_t off = 0; off < n; off += kScanChunk) {
+		const uint32_t base = off + threadIdx.x * kScanItems;
+		uint32_t v[kScanItems];
 #pragma unroll
-	for (int k = 0; k < kScanItems; ++k) v[k] = base + k < n ? partials[base + k] : 0u;
-	blockScanExclusive(v, sWarp);
+		for (int k = 0; k < kScanItems; ++k) v[k] = base + k < n ? partials[base + k] : 0u;
+		const uint32_t total = blockScanExclusive(v, sWarp);
 #pragma unroll
-	for (int k = 0; k < kScanItems; ++k) if (base + k < n) partials[base + k] = v[k];
+		for (int k = 0; k < kScanItems; ++k) if (base + k < n) partials[base + k] = v[k] + carry;
+		carry += total;
+	}
 }
 
 /* Pass 3: add each chunk's offset. */
@@ -176,7 +181,6 @@ static void scanExclusive(uint32_t* data, uint32_t n, uint32_t* partials, cudaSt
 	const uint32_t chunks = (n + kScanChunk - 1) / kScanChunk;
 	k_scan_chunks<<<chunks, kScanThreads, 0, s>>>(data, n, partials);
 	if (chunks > 1) {
-		/* partials fit one block: chunks <= kScanChunk holds for n < 16M */
 		k_scan_partials<<<1, kScanThreads, 0, s>>>(partials, chunks);
 		k_scan_apply<<<chunks, kScanThreads, 0, s>>>(data, n, partials);
 	}

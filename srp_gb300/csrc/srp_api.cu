@@ -814,7 +814,11 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			return;
 		}
 		if (c.errors & kErrSpin) { SRP_ERROR(FN, "Ordered-compaction wait timed out"); return; }
-		if (c.errors & kErrCapacity) {
+		/* capacities are decided from the counters themselves: every
+		 * overflow, whichever kernel met it, shows up as a count above the
+		 * buffer it was meant for */
+		const bool over = c.clipVerts > g.clipRows || c.prims > primCap || c.entries > entryCap || c.bigJobs > g.bigCap;
+		if ((c.errors & kErrCapacity) || over) {
 			bool grew = false;
 			if (c.clipVerts > g.clipRows) { g.clipRows = (uint32_t) std::min<unsigned long long>(c.clipVerts * 2, 0x7FFFFFFF); grew = true; }
 			if (c.prims > primCap) { primCap = (uint32_t) std::min<unsigned long long>(c.prims + 1024, 0x3FFFFFFF); grew = true; }

@@ -326,7 +326,10 @@ static void appendGeodesic(float** verts, size_t* nv, size_t* capv, uint32_t** i
 	size_t addV = (size_t) 20 * (f + 1) * (f + 2) / 2, addI = (size_t) 20 * f * f * 3;
 	while (*nv + addV > *capv) { *capv = *capv ? *capv * 2 : 1 << 16; *verts = (float*) realloc(*verts, *capv * stride * sizeof(float)); }
 	while (*ni + addI > *capi) { *capi = *capi ? *capi * 2 : 1 << 16; *idx = (uint32_t*) realloc(*idx, *capi * sizeof(uint32_t)); }
-	float tint[3] = { (float) rngRange(rng, 0.4, 1), (float) rngRange(rng, 0.4, 1), (float) rngRange(rng, 0.4, 1) };
+	/* one draw per statement: C leaves the order of evaluation of function
+	 * arguments and initialiser-list elements unspecified */
+	float tint[3];
+	for (int k = 0; k < 3; ++k) tint[k] = (float) rngRange(rng, 0.4, 1);
 	for (int fc = 0; fc < 20; ++fc) {
 		double A[3], B[3], C[3];
 		icoVertex(ICO_F[fc][0], A); icoVertex(ICO_F[fc][1], B); icoVertex(ICO_F[fc][2], C);
@@ -393,7 +396,9 @@ static void buildSphere(Scene* s, Rng* rng)
 	freeMesh(&m);
 	SRPStdUniform* u = &s->uni[0];
 	baseUniform(u);
-	u->model = rotation(rngRange(rng, 0, 2 * PI_D), rngRange(rng, 0, 2 * PI_D), rngRange(rng, 0, 2 * PI_D));
+	double ang[3];
+	for (int k = 0; k < 3; ++k) ang[k] = rngRange(rng, 0, 2 * PI_D);
+	u->model = rotation(ang[0], ang[1], ang[2]);
 	u->view = mat4ConstructTranslate(0, 0, 3);
 	u->projection = perspective60((float) s->W / (float) s->H, 0.1f, 100.f);
 	u->passOffset = 8; u->passCount = 3;  /* Gouraud rgb */
@@ -470,8 +475,9 @@ static void buildSoup(Scene* s, Rng* rng)
 	float* lv = (float*) malloc((2 * s->nLines + 1) * 6 * sizeof(float));
 	for (size_t i = 0; i < s->nLines; ++i) {
 		float* a = lv + 12 * i;
-		double p[3] = { rngRange(rng, -10, 10), rngRange(rng, -10, 10), rngRange(rng, 0.2, 20.5) };
-		double d[3] = { rngRange(rng, -1, 1), rngRange(rng, -1, 1), rngRange(rng, -1, 1) };
+		double p[3], d[3];
+		p[0] = rngRange(rng, -10, 10); p[1] = rngRange(rng, -10, 10); p[2] = rngRange(rng, 0.2, 20.5);
+		for (int k = 0; k < 3; ++k) d[k] = rngRange(rng, -1, 1);
 		double len = rngRange(rng, 0.05, 1.0);
 		for (int k = 0; k < 3; ++k) { a[k] = (float) p[k]; a[6 + k] = (float) (p[k] + len * d[k]); }
 		for (int k = 0; k < 3; ++k) { a[3 + k] = (float) rngU(rng); a[9 + k] = (float) rngU(rng); }
@@ -516,7 +522,8 @@ static void featureSize(Scene* s) { s->W = 256; s->H = 192; }
 static void randomTris(Rng* rng, float* v, size_t n, double spread, double zmin, double zmax, int words)
 {
 	for (size_t t = 0; t < n; ++t) {
-		double c[3] = { rngRange(rng, -spread, spread), rngRange(rng, -spread, spread), rngRange(rng, zmin, zmax) };
+		double c[3];
+		c[0] = rngRange(rng, -spread, spread); c[1] = rngRange(rng, -spread, spread); c[2] = rngRange(rng, zmin, zmax);
 		double size = rngRange(rng, 0.05, 1.5);
 		for (int k = 0; k < 3; ++k) {
 			float* p = v + (t * 3 + k) * words;
