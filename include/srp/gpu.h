@@ -82,6 +82,32 @@ void srpGpuResetStats(void);
 /** Tile edge in pixels used by the binning and raster stages (8 or 16). */
 void srpGpuSetTileSize(int tileSize);
 
+/* ---------------------------------------------------------- profiling */
+
+typedef enum SRPGpuStage
+{
+	SRP_GPU_STAGE_VERTEX = 0,   /* index range + vertex shading */
+	SRP_GPU_STAGE_SETUP,        /* assembly, clipping, setup, ordered compaction */
+	SRP_GPU_STAGE_BIN,          /* big-primitive pairs, lambda tables, line DDA, sort */
+	SRP_GPU_STAGE_RESOLVE,      /* per-tile coverage, stencil and depth */
+	SRP_GPU_STAGE_SHADE,        /* deferred fragment shading */
+	SRP_GPU_STAGE_COUNT
+} SRPGpuStage;
+
+typedef struct SRPGpuProfile
+{
+	double ms[SRP_GPU_STAGE_COUNT];        /* device time per stage (CUDA events) */
+	uint64_t launches[SRP_GPU_STAGE_COUNT];
+	uint64_t resolveTiles;                 /* tiles handled by the resolve stage */
+	uint64_t resolveItems;                 /* (tile, item) pairs it consumed */
+} SRPGpuProfile;
+
+/** Record CUDA events around every stage of every draw (off by default). */
+void srpGpuSetProfiling(int enable);
+/** Sum of the recorded stage times since the last reset (waits for the GPU). */
+void srpGpuGetProfile(SRPGpuProfile* profile);
+void srpGpuResetProfile(void);
+
 #ifdef __cplusplus
 }
 #endif

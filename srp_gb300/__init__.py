@@ -34,6 +34,14 @@ class SceneInfo(ctypes.Structure):
                 ("draws", ctypes.c_int), ("usesStencil", ctypes.c_int)]
 
 
+STAGES = ("vertex", "setup", "bin", "resolve", "shade")
+
+
+class SRPGpuProfile(ctypes.Structure):
+    _fields_ = [("ms", ctypes.c_double * 5), ("launches", ctypes.c_uint64 * 5),
+                ("resolveTiles", ctypes.c_uint64), ("resolveItems", ctypes.c_uint64)]
+
+
 MESSAGE_CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p,
                                     ctypes.c_void_p)
 
@@ -60,6 +68,8 @@ def lib():
         L.srpGpuGetStream.restype = ctypes.c_void_p
         L.srpGpuSynchronize.restype = ctypes.c_int
         L.srpSetMessageCallback.argtypes = [SRPMessageCallback]
+        L.srpGpuGetProfile.argtypes = [ctypes.POINTER(SRPGpuProfile)]
+        L.srpGpuSetProfiling.argtypes = [ctypes.c_int]
         _lib = L
     return _lib
 

@@ -78,8 +78,10 @@ struct __align__(16) TriRaster {
 	float c[3];          /* z_ndc * invW per vertex (depth = sum c_i * lambda_i) */
 	uint16_t minX, minY, maxX, maxY;   /* bbox, max exclusive */
 	uint32_t flags;      /* bit0 front facing, bits1..3 top-left flags */
-	uint32_t pad;
+	uint32_t table;      /* big triangles: offset of their lambda table, else kNoTable */
 };
+
+constexpr uint32_t kNoTable = 0xFFFFFFFFu;
 
 /* Triangle data needed only for shading (32 bytes). */
 struct __align__(16) TriAttr {
@@ -130,6 +132,7 @@ struct DeviceCounters {
 	unsigned long long clipVerts;    /* clip-generated vertices */
 	unsigned long long lineFrags;
 	unsigned long long clipOverflow;
+	unsigned long long tableWords;   /* floats of lambda tables requested */
 	unsigned int errors;             /* bit mask, see kErr* */
 	unsigned int lookbackTicket;
 	unsigned int nonEmptyTiles;

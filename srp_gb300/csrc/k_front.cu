@@ -360,7 +360,7 @@ __device__ bool setupTriangle(const DrawState& st, PV v0, PV v1, PV v2, TriRaste
 		A.vref[i] = ref[i];
 	}
 	R.flags = flags;
-	R.pad = 0;
+	R.table = kNoTable;
 	A.pad = 0;
 	return true;
 }
@@ -455,6 +455,25 @@ struct Assembly {
 	PV poly[kMaxPoly];
 };
 
+/* Write a set-up triangle as primitive `prim` with its pairs at `entry`. */
+__device__ __forceinline__ void writeTri(const DrawParams& P, TriRaster& R, TriAttr& A, uint32_t nt, uint32_t prim,
+                                         uint32_t entry)
+{
+			if (nt > (uint32_t) kSmallEntries) {
+				/* big triangle: room for its lambda table */
+				const int cols = ((int) R.maxX - 1) / kTile - (int) R.minX / kTile + 1;
+				const unsigned long long words = 3ull * (unsigned long long) (R.maxY - R.minY) * (unsigned long long) cols;
+				const unsigned long long off = atomicAdd(&P.ctr->tableWords, words);
+				if (off + words <= P.tableCap && off < 0xFFFFFFFFull) R.table = (uint32_t) off;
+			}
+			if (prim < P.primCap) {
+				A.id = prim;
+				P.triR[prim] = R;
+				P.triA[prim] = A;
+				emitEntries(P, kKindTri, prim, entry, R.minX, R.minY, (int) R.maxX - 1, (int) R.maxY - 1);
+			} else atomicOr(&P.ctr->errors, kErrCapacity);
+}
+
 template <int MODE>
 __device__ __forceinline__ void handleTriangle(const DrawParams& P, const PV& a, const PV& b, const PV& c, bool write,
                                                uint32_t& prim, uint32_t& entry)
@@ -464,14 +483,7 @@ __device__ __forceinline__ void handleTriangle(const DrawParams& P, const PV& a,
 		TriAttr A;
 		if (!setupTriangle(P.st, a, b, c, R, A)) return;
 		const uint32_t nt = tileCount(R.minX, R.minY, R.maxX, R.maxY);
-		if (write) {
-			if (prim < P.primCap) {
-				A.id = prim;
-				P.triR[prim] = R;
-				P.triA[prim] = A;
-				emitEntries(P, kKindTri, prim, entry, R.minX, R.minY, (int) R.maxX - 1, (int) R.maxY - 1);
-			} else atomicOr(&P.ctr->errors, kErrCapacity);
-		}
+		if (write) writeTri(P, R, A, nt, prim, entry);
 		prim += 1;
 		entry += nt;
 	} else if (MODE == kTriLine) {
@@ -591,6 +603,10 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
 		}
 	}
 	uint32_t nPrim = 0, nEnt = 0;
+	/* unclipped filled triangle: set up once, kept in registers across the scan */
+	TriRaster fR;
+	TriAttr fA;
+	bool fOk = false;
 	if (live) {
 		if (MODE == kPoints) {
 			PointRec R;
@@ -603,7 +619,12 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
 			nPrim = 1;
 			nEnt = (uint32_t) L.steps + 1u;
 		} else if (!as.clipped) {
-			handleTriangle<MODE>(P, as.v[0], as.v[1], as.v[2], false, nPrim, nEnt);
+			if (MODE == kTriFill) {
+				fOk = setupTriangle(P.st, as.v[0], as.v[1], as.v[2], fR, fA);
+				if (fOk) { nPrim = 1; nEnt = tileCount(fR.minX, fR.minY, fR.maxX, fR.maxY); }
+			} else {
+				handleTriangle<MODE>(P, as.v[0], as.v[1], as.v[2], false, nPrim, nEnt);
+			}
 		} else {
 			for (int f = 1; f + 1 < as.nPoly; ++f)
 				handleTriangle<MODE>(P, as.poly[0], as.poly[f], as.poly[f + 1], false, nPrim, nEnt);
@@ -690,26 +711,62 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
 			P.lines[primBase] = L;
 		} else atomicOr(&P.ctr->errors, kErrCapacity);
 	} else if (!as.clipped) {
-		handleTriangle<MODE>(P, as.v[0], as.v[1], as.v[2], true, primBase, entBase);
+		if (MODE == kTriFill) {
+			if (fOk) writeTri(P, fR, fA, nEnt, primBase, entBase);
+		} else {
+			handleTriangle<MODE>(P, as.v[0], as.v[1], as.v[2], true, primBase, entBase);
+		}
 	} else {
 		for (int f = 1; f + 1 < as.nPoly; ++f)
 			handleTriangle<MODE>(P, as.poly[0], as.poly[f], as.poly[f + 1], true, primBase, entBase);
 	}
 }
 
+/* Lambda table of a big triangle: for every bbox row and every tile column,
+ * the barycentrics the reference holds when its row walk reaches
+ * max(minX, 8 * column) -- i.e. the exact serial chain. Each thread takes one
+ * row and a run of up to 8 tile columns: it enters the run with the exact
+ * jump-ahead (chain.h) and then adds dldx pixel by pixel, as the reference
+ * does, storing the value at each column start. */
+__device__ void fillLambdaTable(const DrawParams& P, const TriRaster& R, int first, int stride)
+{
+	if (R.table == kNoTable) return;
+	const int rows = (int) R.maxY - (int) R.minY;
+	const int c0 = (int) R.minX / kTile, c1 = ((int) R.maxX - 1) / kTile, ncols = c1 - c0 + 1;
+	const int nseg = (ncols + 7) / 8;
+	float* T = P.table + R.table;
+	for (int idx = first; idx < rows * nseg; idx += stride) {
+		const int r = idx / nseg, sg = idx % nseg;
+		const int cs = c0 + sg * 8, ce = min(cs + 8, c1 + 1);
+		int x = max((int) R.minX, cs * kTile);
+		float l[3];
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+			l[i] = srpChainAdd(srpChainAdd(R.l0[i], R.dy[i], (uint32_t) r), R.dx[i], (uint32_t) (x - R.minX));
+		for (int c = cs; c < ce; ++c) {
+			const int xt = max((int) R.minX, c * kTile);
+			for (; x < xt; ++x)
+#pragma unroll
+				for (int i = 0; i < 3; ++i) l[i] = __fadd_rn(l[i], R.dx[i]);
+			float* t = T + 3 * ((size_t) r * ncols + (c - c0));
+			t[0] = l[0]; t[1] = l[1]; t[2] = l[2];
+		}
+	}
+}
+
 /* Entries of primitives covering more than kSmallEntries tiles: one block per
- * primitive writes its tiles row by row. */
+ * primitive writes its tiles row by row (and a triangle's lambda table). */
 __global__ void k_big_entries(const __grid_constant__ DrawParams P, uint32_t nJobs)
 {
 	for (uint32_t j = blockIdx.x; j < nJobs; j += gridDim.x) {
 		const uint4 job = P.bigJobs[j];
-		int x0, y0, x1, y1;
+		int x0, y0, x1;
 		if (job.z == kKindTri) {
 			const TriRaster& R = P.triR[job.x];
-			x0 = R.minX; y0 = R.minY; x1 = (int) R.maxX - 1; y1 = (int) R.maxY - 1;
+			x0 = R.minX; y0 = R.minY; x1 = (int) R.maxX - 1;
 		} else {
 			const PointRec& R = P.points[job.x];
-			x0 = R.x0; y0 = R.y0; x1 = R.x1; y1 = R.y1;
+			x0 = R.x0; y0 = R.y0; x1 = R.x1;
 		}
 		const int tx0 = x0 / kTile, ty0 = y0 / kTile, ntx = x1 / kTile - tx0 + 1;
 		for (uint32_t i = threadIdx.x; i < job.w; i += blockDim.x) {
@@ -722,21 +779,39 @@ __global__ void k_big_entries(const __grid_constant__ DrawParams P, uint32_t nJo
 	}
 }
 
-/* One thread per line walks the reference's DDA exactly (fp32 accumulators,
- * round half away from zero) and writes one record and one (tile, fragment)
- * pair per step; steps whose pixel fails the scissor test or falls outside
- * the framebuffer get the key one past the last tile, which sorts them out
+/* Lambda tables of all big triangles: blockIdx.y walks the jobs, the
+ * blockIdx.x blocks of a job share its (row, column-run) work items. */
+__global__ void k_lambda_tables(const __grid_constant__ DrawParams P, uint32_t nJobs)
+{
+	for (uint32_t j = blockIdx.y; j < nJobs; j += gridDim.y) {
+		const uint4 job = P.bigJobs[j];
+		if (job.z != kKindTri) continue;
+		fillLambdaTable(P, P.triR[job.x], blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+	}
+}
+
+/* One warp per line walks the reference's DDA exactly (fp32 accumulators,
+ * round half away from zero): lane l takes a contiguous run of steps, enters
+ * it with the exact jump-ahead of the x, y and t accumulators (chain.h) and
+ * then steps serially. Each step writes one record and one (tile, fragment)
+ * pair; steps whose pixel fails the scissor test or falls outside the
+ * framebuffer get the key one past the last tile, which sorts them out
  * (src/raster/line.c:34-77, src/raster/fragment.c:63-75). */
 __global__ void k_line_frags(const __grid_constant__ DrawParams P, uint32_t nLines)
 {
-	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	const uint32_t i = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+	const uint32_t lane = threadIdx.x & 31;
 	unsigned long long passed = 0;
 	if (i < nLines) {
 		const LineRec L = P.lines[i];
 		const uint32_t invalid = (uint32_t) (P.st.tilesX * P.st.tilesY);
-		float x = L.x0, y = L.y0, t = 0.0f;
+		const uint32_t total = (uint32_t) L.steps + 1u;
+		const uint32_t seg = (total + 31u) / 32u;
+		const uint32_t s0 = min(lane * seg, total), s1 = min(s0 + seg, total);
+		float x = srpChainAdd(L.x0, L.xInc, s0), y = srpChainAdd(L.y0, L.yInc, s0);
+		float t = srpChainAdd(0.0f, L.tInc, s0);
 		const unsigned long long size = (unsigned long long) P.st.W * (unsigned long long) P.st.H;
-		for (int s = 0; s <= L.steps; ++s) {
+		for (uint32_t s = s0; s < s1; ++s) {
 			const int px = (int) roundf(x), py = (int) roundf(y);
 			const float w0 = __fsub_rn(1.0f, t);
 			const float depth = __fadd_rn(__fmul_rn(L.c[0], w0), __fmul_rn(L.c[1], t));
@@ -813,12 +888,13 @@ void launchBigEntries(const DrawParams& P, uint32_t nJobs, cudaStream_t s)
 {
 	if (!nJobs) return;
 	k_big_entries<<<nJobs < 152u * 16u ? nJobs : 152u * 16u, 256, 0, s>>>(P, nJobs);
+	k_lambda_tables<<<dim3(8, nJobs < 65535u ? nJobs : 65535u), 256, 0, s>>>(P, nJobs);
 }
 
 void launchLineFrags(const DrawParams& P, uint32_t nLines, cudaStream_t s)
 {
 	if (!nLines) return;
-	k_line_frags<<<(nLines + 127) / 128, 128, 0, s>>>(P, nLines);
+	k_line_frags<<<(nLines + 3) / 4, 128, 0, s>>>(P, nLines);
 }
 
 }  // namespace srpg

@@ -69,7 +69,21 @@ __device__ __forceinline__ void shadeItem(const DrawParams& P, uint32_t item, in
 		const TriRaster R = P.triR[item];
 		const TriAttr A = P.triA[item];
 		float l[3];
-		lambdaAt(R, gx, gy, l);
+		if (R.table != kNoTable) {
+			/* table entry of this row and tile column, then the remaining steps */
+			const int ncols = ((int) R.maxX - 1) / kTile - (int) R.minX / kTile + 1;
+			const int col = gx / kTile;
+			const float* T = P.table + R.table + 3 * ((size_t) (gy - R.minY) * ncols + (col - (int) R.minX / kTile));
+			const int xs = max((int) R.minX, col * kTile);
+#pragma unroll
+			for (int i = 0; i < 3; ++i) {
+				float v = T[i];
+				for (int x = xs; x < gx; ++x) v = __fadd_rn(v, R.dx[i]);
+				l[i] = v;
+			}
+		} else {
+			lambdaAt(R, gx, gy, l);
+		}
 		const float depth = triDepth(R.c, l);
 		const float recip = triRecip(A.invW, l);
 		interpolate<3>(P.L, P.vary, A.vref, l, A.invW, recip, P.st.provokingFirst, false, words);
@@ -121,13 +135,28 @@ __device__ __forceinline__ void coverage(const DrawParams& P, uint32_t item, int
 		const int xs = max(x0, (int) R.minX), xe = min(x0 + kTile, (int) R.maxX);
 		const int ys = max(y0, (int) R.minY), ye = min(y0 + kTile, (int) R.maxY);
 		if (xs >= xe || ys >= ye) return;
+		/* row starts: the big-triangle table, or the exact chain */
+		const float* T = nullptr;
+		int ncols = 0;
+		if (R.table != kNoTable) {
+			ncols = ((int) R.maxX - 1) / kTile - (int) R.minX / kTile + 1;
+			T = P.table + R.table + 3 * ((size_t) (ys - R.minY) * ncols + (x0 / kTile - (int) R.minX / kTile));
+		}
 		float lr[3];
+		if (!T) {
 #pragma unroll
-		for (int i = 0; i < 3; ++i) lr[i] = srpChainAdd(R.l0[i], R.dy[i], (uint32_t) (ys - R.minY));
+			for (int i = 0; i < 3; ++i) lr[i] = srpChainAdd(R.l0[i], R.dy[i], (uint32_t) (ys - R.minY));
+		}
 		for (int y = ys; y < ye; ++y) {
 			float l[3];
+			if (T) {
 #pragma unroll
-			for (int i = 0; i < 3; ++i) l[i] = srpChainAdd(lr[i], R.dx[i], (uint32_t) (xs - R.minX));
+				for (int i = 0; i < 3; ++i) l[i] = T[i];
+				T += 3 * ncols;
+			} else {
+#pragma unroll
+				for (int i = 0; i < 3; ++i) l[i] = srpChainAdd(lr[i], R.dx[i], (uint32_t) (xs - R.minX));
+			}
 			for (int x = xs; x < xe; ++x) {
 				if (insideTri(l, R.flags)) {
 					const int q = (y - y0) * kTile + (x - x0);
@@ -137,8 +166,10 @@ __device__ __forceinline__ void coverage(const DrawParams& P, uint32_t item, int
 #pragma unroll
 				for (int i = 0; i < 3; ++i) l[i] = __fadd_rn(l[i], R.dx[i]);
 			}
+			if (!T) {
 #pragma unroll
-			for (int i = 0; i < 3; ++i) lr[i] = __fadd_rn(lr[i], R.dy[i]);
+				for (int i = 0; i < 3; ++i) lr[i] = __fadd_rn(lr[i], R.dy[i]);
+			}
 		}
 	} else if (KIND == kKindPoint) {
 		const PointRec R = P.points[item];

@@ -40,6 +40,10 @@ struct DrawParams {
 	uint32_t entryCap;
 	uint4* bigJobs;                /* primitives covering many tiles */
 	uint32_t bigCap;
+	/* exact barycentrics of big triangles at every (row, tile column) start:
+	 * rows x columns x 3 floats per triangle */
+	float* table;
+	unsigned long long tableCap;
 	unsigned long long* lookback;  /* decoupled look-back status, one per block */
 	/* framebuffer planes */
 	uint32_t* color;

@@ -93,12 +93,19 @@ struct Lib {
 	Registry reg;
 	/* scratch pools, grown on demand */
 	DeviceBuffer clip, vary, triR, triA, lines, points, frags, keys, vals, keys2, vals2, big, lookback;
-	DeviceBuffer hist, partials, tileStart, tileEnd, winner, minmax, ctr;
+	DeviceBuffer hist, partials, tileStart, tileEnd, winner, minmax, ctr, table;
 	DeviceCounters* hostCtr = nullptr;
 	SRPGpuStats stats = {};
 	unsigned long long launches = 0;
 	uint32_t clipRows = 4096;
 	uint32_t bigCap = 1 << 16;
+	/* stage profiling */
+	bool profiling = false;
+	std::vector<cudaEvent_t> eventPool;
+	std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+	SRPGpuProfile profile = {};
+	cudaEvent_t openEvent = nullptr;
+	unsigned long long tableCap = 1ull << 22;  /* floats */
 	double entryRatio = 4.0;
 };
 
@@ -114,6 +121,32 @@ bool ensureInit(const char* fn)
 	cudaMemset(g.ctr.ptr, 0, sizeof(DeviceCounters));
 	g.init = true;
 	return true;
+}
+
+cudaEvent_t takeEvent()
+{
+	if (!g.eventPool.empty()) { cudaEvent_t e = g.eventPool.back(); g.eventPool.pop_back(); return e; }
+	cudaEvent_t e = nullptr;
+	cudaEventCreate(&e);
+	return e;
+}
+
+/* Marks the start of a stage; stageEnd records the matching event. */
+void stageBegin()
+{
+	if (!g.profiling) return;
+	g.openEvent = takeEvent();
+	cudaEventRecord(g.openEvent, g.stream);
+}
+
+void stageEnd(int stage, int launches)
+{
+	if (!g.profiling || !g.openEvent) return;
+	cudaEvent_t e = takeEvent();
+	cudaEventRecord(e, g.stream);
+	g.pending.push_back({ stage, { g.openEvent, e } });
+	g.profile.launches[stage] += (uint64_t) launches;
+	g.openEvent = nullptr;
 }
 
 }  // namespace
@@ -775,7 +808,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		bool ok = g.clip.reserve((size_t) rows * 16, FN) && g.vary.reserve((size_t) rows * nw * 4, FN) &&
 		          g.lookback.reserve((size_t) std::max(blocks, 1u) * 8, FN) &&
 		          g.keys.reserve((size_t) entryCap * 4, FN) && g.vals.reserve((size_t) entryCap * 4, FN) &&
-		          g.big.reserve((size_t) g.bigCap * 16, FN);
+		          g.big.reserve((size_t) g.bigCap * 16, FN) && g.table.reserve((size_t) g.tableCap * 4, FN);
 		if (kind == kKindTri) ok = ok && g.triR.reserve((size_t) primCap * sizeof(TriRaster), FN) &&
 		                           g.triA.reserve((size_t) primCap * sizeof(TriAttr), FN);
 		else if (kind == kKindPoint) ok = ok && g.points.reserve((size_t) primCap * sizeof(PointRec), FN);
@@ -798,14 +831,20 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		P.entryCap = entryCap;
 		P.bigJobs = g.big.as<uint4>();
 		P.bigCap = g.bigCap;
+		P.table = g.table.as<float>();
+		P.tableCap = g.tableCap;
 		P.lookback = g.lookback.as<unsigned long long>();
 
+		stageBegin();
 		launchReset(P, g.stream);
 		if (ib) launchIndexRange(P, g.stream);
 		if (ib) launchVertex(P, 0, vb->nVertices, g.stream);
 		else launchVertex(P, start, count, g.stream);
+		stageEnd(SRP_GPU_STAGE_VERTEX, ib ? 3 : 2);
+		stageBegin();
 		cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, g.stream);
 		launchSetup(P, g.stream);
+		stageEnd(SRP_GPU_STAGE_SETUP, 1);
 		g.launches += 3 + (ib ? 1 : 0);
 		if (!cudaOk(cudaGetLastError(), FN, "launch") || !readCounters()) return;
 		const DeviceCounters c = *g.hostCtr;
@@ -817,13 +856,15 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		/* capacities are decided from the counters themselves: every
 		 * overflow, whichever kernel met it, shows up as a count above the
 		 * buffer it was meant for */
-		const bool over = c.clipVerts > g.clipRows || c.prims > primCap || c.entries > entryCap || c.bigJobs > g.bigCap;
+		const bool over = c.clipVerts > g.clipRows || c.prims > primCap || c.entries > entryCap || c.bigJobs > g.bigCap ||
+		                  c.tableWords > g.tableCap;
 		if ((c.errors & kErrCapacity) || over) {
 			bool grew = false;
 			if (c.clipVerts > g.clipRows) { g.clipRows = (uint32_t) std::min<unsigned long long>(c.clipVerts * 2, 0x7FFFFFFF); grew = true; }
 			if (c.prims > primCap) { primCap = (uint32_t) std::min<unsigned long long>(c.prims + 1024, 0x3FFFFFFF); grew = true; }
 			if (c.entries > entryCap) { entryCap = (uint32_t) std::min<double>(c.entries * 1.25 + 1024, 4.0e9); grew = true; }
 			if (c.bigJobs > g.bigCap) { g.bigCap = (uint32_t) std::min<unsigned long long>(c.bigJobs * 2, 1u << 30); grew = true; }
+			if (c.tableWords > g.tableCap) { g.tableCap = std::min<unsigned long long>(c.tableWords * 5 / 4 + 1024, 0xFFFFFFFFull); grew = true; }
 			if (!grew) { SRP_ERROR(FN, "Scratch capacity exceeded"); return; }
 			continue;
 		}
@@ -832,9 +873,12 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		g.stats.binEntries += c.entries;
 		g.stats.clipOverflows += c.clipOverflow;
 		const uint32_t E = (uint32_t) c.entries;
-		if (kind == kKindLineFrag) { launchLineFrags(P, (uint32_t) c.prims, g.stream); ++g.launches; }
-		else if (c.bigJobs) { launchBigEntries(P, (uint32_t) c.bigJobs, g.stream); ++g.launches; }
-		if (E == 0) break;
+		stageBegin();
+		int binLaunches = 0;
+		if (kind == kKindLineFrag) { launchLineFrags(P, (uint32_t) c.prims, g.stream); binLaunches += 1; }
+		else if (c.bigJobs) { launchBigEntries(P, (uint32_t) c.bigJobs, g.stream); binLaunches += 2; }
+		g.launches += binLaunches;
+		if (E == 0) { stageEnd(SRP_GPU_STAGE_BIN, binLaunches); break; }
 		/* sort (tile, item) pairs by tile, keeping item order */
 		const uint32_t keyBits = bitsFor(numTiles);
 		if (!g.keys2.reserve((size_t) E * 4, FN) || !g.vals2.reserve((size_t) E * 4, FN) ||
@@ -852,13 +896,22 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, g.stream);
 		cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, g.stream);
 		launchTileRanges(P, sk, E, numTiles, g.stream);
+		stageEnd(SRP_GPU_STAGE_BIN, binLaunches + (int) (keyBits / 8) * 5 + 1);
 		const bool late = sp->fs->mayOverwriteDepth && shadeSupportsLateDepth(fsId);
+		g.profile.resolveTiles += numTiles;
+		g.profile.resolveItems += E;
 		if (late) {
+			stageBegin();
 			launchResolveLate(P, kind, sv, numTiles, g.stream);
+			stageEnd(SRP_GPU_STAGE_RESOLVE, 1);
 			g.launches += 2;
 		} else {
+			stageBegin();
 			launchResolve(P, kind, sv, numTiles, g.stream);
+			stageEnd(SRP_GPU_STAGE_RESOLVE, 1);
+			stageBegin();
 			launchShade(P, kind, numTiles, g.stream);
+			stageEnd(SRP_GPU_STAGE_SHADE, 1);
 			g.launches += 3;
 		}
 		cudaOk(cudaGetLastError(), FN, "launch");
@@ -966,6 +1019,30 @@ void srpGpuResetStats(void)
 	cudaMemset(g.ctr.ptr, 0, sizeof(DeviceCounters));
 	g.stats = SRPGpuStats();
 	g.launches = 0;
+}
+
+void srpGpuSetProfiling(int enable) { g.profiling = enable != 0; }
+
+void srpGpuGetProfile(SRPGpuProfile* out)
+{
+	if (g.init) {
+		cudaStreamSynchronize(g.stream);
+		for (auto& p : g.pending) {
+			float ms = 0.f;
+			if (cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess) g.profile.ms[p.first] += ms;
+			g.eventPool.push_back(p.second.first);
+			g.eventPool.push_back(p.second.second);
+		}
+		g.pending.clear();
+	}
+	*out = g.profile;
+}
+
+void srpGpuResetProfile(void)
+{
+	SRPGpuProfile tmp;
+	srpGpuGetProfile(&tmp);
+	g.profile = SRPGpuProfile();
 }
 
 void srpGpuSetTileSize(int tileSize)
