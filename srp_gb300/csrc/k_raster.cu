@@ -36,6 +36,12 @@ __device__ __forceinline__ void rasterTexSample(const void* tex, float u, float 
 namespace srpg {
 
 constexpr int kResolveWarps = 4;
+/* row pitch of the per-item depth rows in shared memory: 65 keeps lanes that
+ * write the same pixel of different items in different banks */
+constexpr int kDepRow = 65;
+/* tiles with more items than this are resolved by a whole CTA */
+constexpr uint32_t kHeavyItems = 96;
+constexpr int kHeavyThreads = 256;
 
 template <int FS>
 __device__ __forceinline__ void runFS(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out)
@@ -205,12 +211,13 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(const __grid_con
 	__shared__ unsigned long long sMask[kResolveWarps][32];
 	__shared__ uint32_t sItem[kResolveWarps][32];
 	__shared__ uint32_t sFlag[kResolveWarps][32];
-	__shared__ float sDep[kResolveWarps][32][64];
+	__shared__ float sDep[kResolveWarps][32][kDepRow];
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const uint32_t tile = blockIdx.x * kResolveWarps + warp;
 	if (tile >= numTiles) return;
 	const uint32_t s = P.tileStart[tile], e = P.tileEnd[tile];
 	if (s >= e) return;
+	if (LATE_FS == 0 && e - s > kHeavyItems) return;  /* k_resolve_heavy's */
 	const DrawState& st = P.st;
 	const int x0 = (int) (tile % (uint32_t) st.tilesX) * kTile, y0 = (int) (tile / (uint32_t) st.tilesX) * kTile;
 
@@ -300,6 +307,110 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(const __grid_con
 	}
 }
 
+/* Applies one fragment to a pixel's depth/stencil state (early depth test;
+ * src/raster/fragment.c:63-125). Returns true if it reached the colour write. */
+__device__ __forceinline__ bool applyFragment(const DrawState& st, bool front, float d, float& depth, uint32_t& sten)
+{
+	const StencilFace& sf = front ? st.front : st.back;
+	if (st.stencilEnabled && !stencilCompare(sf.ref, sten, sf.mask, sf.func)) {
+		sten = stencilApply(sf.sfail, sten, sf.ref, sf.writeMask);
+		return false;
+	}
+	if (st.depthTest && !depthCompare(st.depthOp, d, depth)) {
+		if (st.stencilEnabled) sten = stencilApply(sf.dfail, sten, sf.ref, sf.writeMask);
+		return false;
+	}
+	if (st.stencilEnabled) sten = stencilApply(sf.pass, sten, sf.ref, sf.writeMask);
+	if (st.depthTest && st.depthWrite) depth = d;
+	return true;
+}
+
+/* Tiles with many items (typically far-away meshes whose thousands of tiny
+ * triangles land in a handful of tiles): a CTA takes 256 consecutive items
+ * at a time, every thread evaluates one item's coverage and depths, warp
+ * ballots transpose the coverage into per-pixel item masks, and 64 pixel
+ * owners then apply just the covering fragments, in item order. Work per
+ * chunk is parallel over items; per pixel only real fragments are walked.
+ * Heavy tiles come from a list built by k_tile_classify and are pulled by a
+ * fixed grid of CTAs. */
+template <int KIND>
+__global__ void __launch_bounds__(kHeavyThreads) k_resolve_heavy(const __grid_constant__ DrawParams P,
+                                                                const uint32_t* vals, const uint32_t* heavy)
+{
+	extern __shared__ float hDep[];                 /* [kHeavyThreads][kDepRow] */
+	__shared__ uint32_t ballots[kHeavyThreads / 32][64];
+	__shared__ uint32_t hFlag[kHeavyThreads], hItem[kHeavyThreads];
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const DrawState& st = P.st;
+	const uint32_t nHeavy = P.ctr->nonEmptyTiles;
+	for (uint32_t h = blockIdx.x; h < nHeavy; h += gridDim.x) {
+		const uint32_t tile = heavy[h];
+		const uint32_t s = P.tileStart[tile], e = P.tileEnd[tile];
+		const int x0 = (int) (tile % (uint32_t) st.tilesX) * kTile, y0 = (int) (tile / (uint32_t) st.tilesX) * kTile;
+		const int gx = x0 + (tid & 7), gy = y0 + ((tid >> 3) & 7);
+		const bool owner = tid < 64;
+		const bool valid = owner && gx < st.W && gy < st.H;
+		const size_t idx = valid ? (size_t) gy * st.W + gx : 0;
+		float depth = valid ? P.depth[idx] : 0.0f;
+		uint32_t sten = valid ? P.stencil[idx] : 0u;
+		int32_t win = -1;
+		const bool ok = valid && (KIND == kKindLineFrag || scissorPass(st, gx, gy));
+		unsigned long long frags = 0;
+		for (uint32_t b = s; b < e; b += kHeavyThreads) {
+			const uint32_t n = min((uint32_t) kHeavyThreads, e - b);
+			unsigned long long mask = 0;
+			uint32_t item = 0, flags = 0;
+			if ((uint32_t) tid < n) {
+				item = vals[b + tid];
+				coverage<KIND>(P, item, x0, y0, mask, hDep + tid * kDepRow, flags);
+			}
+			hFlag[tid] = flags;
+			hItem[tid] = item;
+			uint32_t lo = 0, hi = 0;
+#pragma unroll
+			for (int q = 0; q < 64; ++q) {
+				const uint32_t bq = __ballot_sync(0xFFFFFFFFu, (mask >> q) & 1ull);
+				if (lane == (q & 31)) { if (q < 32) lo = bq; else hi = bq; }
+			}
+			ballots[warp][lane] = lo;
+			ballots[warp][32 + lane] = hi;
+			__syncthreads();
+			if (ok) {
+				const int q = tid;
+				for (int w = 0; w < kHeavyThreads / 32; ++w) {
+					uint32_t m = ballots[w][q];
+					frags += __popc(m);
+					while (m) {
+						const int j = w * 32 + __ffs(m) - 1;
+						m &= m - 1;
+						if (applyFragment(st, (hFlag[j] & 1u) != 0, hDep[j * kDepRow + q], depth, sten))
+							win = (int32_t) hItem[j];
+					}
+				}
+			}
+			__syncthreads();
+		}
+		if (valid) {
+			P.depth[idx] = depth;
+			P.stencil[idx] = (uint8_t) sten;
+			P.winner[idx] = win;
+		}
+		if (KIND != kKindLineFrag && warp < 2) {
+			for (int o = 16; o; o >>= 1) frags += __shfl_xor_sync(0xFFFFFFFFu, frags, o);
+			if (lane == 0 && frags) atomicAdd(&P.ctr->fragments, frags);
+		}
+	}
+}
+
+/* Lists the tiles with more than kHeavyItems items for k_resolve_heavy. */
+__global__ void k_tile_classify(const __grid_constant__ DrawParams P, uint32_t numTiles, uint32_t* heavy)
+{
+	const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= numTiles) return;
+	const uint32_t n = P.tileEnd[t] - P.tileStart[t];
+	if (P.tileEnd[t] > P.tileStart[t] && n > kHeavyItems) heavy[atomicAdd(&P.ctr->nonEmptyTiles, 1u)] = t;
+}
+
 /* Deferred shading: one shader invocation per pixel whose colour was written
  * by the resolve pass. */
 template <int KIND, int FS>
@@ -329,12 +440,28 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_shade(const __grid_const
 
 static unsigned tileBlocks(uint32_t numTiles) { return (numTiles + kResolveWarps - 1) / kResolveWarps; }
 
-void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, cudaStream_t s)
+template <int KIND>
+static void launchHeavy(const DrawParams& P, const uint32_t* vals, uint32_t* heavy, cudaStream_t s)
+{
+	const int smem = kHeavyThreads * kDepRow * 4;
+	cudaFuncSetAttribute(k_resolve_heavy<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+	k_resolve_heavy<KIND><<<152 * 3, kHeavyThreads, smem, s>>>(P, vals, heavy);
+}
+
+void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, uint32_t* heavy, cudaStream_t s)
 {
 	const unsigned b = tileBlocks(numTiles);
-	if (kind == kKindTri) k_resolve<kKindTri, 0><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
-	else if (kind == kKindPoint) k_resolve<kKindPoint, 0><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
-	else k_resolve<kKindLineFrag, 0><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+	k_tile_classify<<<(numTiles + 255) / 256, 256, 0, s>>>(P, numTiles, heavy);
+	if (kind == kKindTri) {
+		launchHeavy<kKindTri>(P, vals, heavy, s);
+		k_resolve<kKindTri, 0><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+	} else if (kind == kKindPoint) {
+		launchHeavy<kKindPoint>(P, vals, heavy, s);
+		k_resolve<kKindPoint, 0><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+	} else {
+		launchHeavy<kKindLineFrag>(P, vals, heavy, s);
+		k_resolve<kKindLineFrag, 0><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+	}
 }
 
 bool shadeSupportsLateDepth(int fsId) { return fsId == SRP_GPU_FS_DEPTH_OVERWRITE; }

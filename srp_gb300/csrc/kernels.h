@@ -74,7 +74,8 @@ void launchTileRanges(const DrawParams& P, const uint32_t* keys, uint32_t n, uin
 size_t sortHistWords(uint32_t n);
 size_t sortPartialWords(uint32_t n);
 /* k_raster.cu */
-void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, cudaStream_t s);
+void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, uint32_t* heavy,
+                   cudaStream_t s);
 /* k_shade.cu */
 void launchShade(const DrawParams& P, int kind, uint32_t numTiles, cudaStream_t s);
 bool shadeSupportsLateDepth(int fsId);

@@ -93,7 +93,7 @@ struct Lib {
 	Registry reg;
 	/* scratch pools, grown on demand */
 	DeviceBuffer clip, vary, triR, triA, lines, points, frags, keys, vals, keys2, vals2, big, lookback;
-	DeviceBuffer hist, partials, tileStart, tileEnd, winner, minmax, ctr, table;
+	DeviceBuffer hist, partials, tileStart, tileEnd, winner, minmax, ctr, table, heavy;
 	DeviceCounters* hostCtr = nullptr;
 	SRPGpuStats stats = {};
 	unsigned long long launches = 0;
@@ -884,7 +884,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		if (!g.keys2.reserve((size_t) E * 4, FN) || !g.vals2.reserve((size_t) E * 4, FN) ||
 		    !g.hist.reserve(sortHistWords(E) * 4, FN) || !g.partials.reserve(sortPartialWords(E) * 4 + 64, FN) ||
 		    !g.tileStart.reserve((size_t) (numTiles + 1) * 4, FN) || !g.tileEnd.reserve((size_t) (numTiles + 1) * 4, FN) ||
-		    !g.winner.reserve(fb->size * 4 + 4, FN)) return;
+		    !g.winner.reserve(fb->size * 4 + 4, FN) || !g.heavy.reserve((size_t) (numTiles + 1) * 4, FN)) return;
 		uint32_t* sk;
 		uint32_t* sv;
 		sortEntries(P, E, keyBits, g.keys2.as<uint32_t>(), g.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
@@ -907,12 +907,12 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			g.launches += 2;
 		} else {
 			stageBegin();
-			launchResolve(P, kind, sv, numTiles, g.stream);
-			stageEnd(SRP_GPU_STAGE_RESOLVE, 1);
+			launchResolve(P, kind, sv, numTiles, g.heavy.as<uint32_t>(), g.stream);
+			stageEnd(SRP_GPU_STAGE_RESOLVE, 3);
 			stageBegin();
 			launchShade(P, kind, numTiles, g.stream);
 			stageEnd(SRP_GPU_STAGE_SHADE, 1);
-			g.launches += 3;
+			g.launches += 5;
 		}
 		cudaOk(cudaGetLastError(), FN, "launch");
 		break;
