@@ -265,6 +265,34 @@ static size_t indexTypeSize(SRPType t)
 	}
 }
 
+/* True when a CUDA device is usable (probed once, silently). */
+static bool gpuPresent()
+{
+	static int present = -1;
+	if (present < 0) {
+		int n = 0;
+		present = cudaGetDeviceCount(&n) == cudaSuccess && n > 0;
+	}
+	return present == 1;
+}
+
+/* CopyData on a machine with a GPU: the bytes go straight to HBM. From
+ * pageable memory cudaMemcpyAsync returns once the source has been read; from
+ * page-locked memory the copy is asynchronous, so it is waited for before
+ * returning (the caller may reuse its buffer at once, as with the
+ * reference's memcpy). */
+static bool copyToDevice(DeviceBuffer& dev, const void* data, size_t nBytes, const char* fn)
+{
+	if (!ensureInit(fn) || !dev.reserve(nBytes + 16, fn)) return false;
+	if (!nBytes) return true;
+	if (!cudaOk(cudaMemcpyAsync(dev.ptr, data, nBytes, cudaMemcpyHostToDevice, g.stream), fn, "cudaMemcpyAsync"))
+		return false;
+	cudaPointerAttributes attr;
+	if (cudaPointerGetAttributes(&attr, data) != cudaSuccess) { cudaGetLastError(); attr.type = cudaMemoryTypeUnregistered; }
+	if (attr.type != cudaMemoryTypeUnregistered) cudaStreamSynchronize(g.stream);
+	return true;
+}
+
 static void* pinnedRealloc(void* old, size_t n)
 {
 	if (old) cudaFreeHost(old);
@@ -290,10 +318,15 @@ void srpFreeVertexBuffer(SRPVertexBuffer* b)
 
 void srpVertexBufferCopyData(SRPVertexBuffer* b, size_t stride, size_t nBytes, const void* data)
 {
-	if (nBytes > b->cap) { b->host = (unsigned char*) pinnedRealloc(b->host, nBytes); b->cap = nBytes; }
 	b->stride = stride;
 	b->nVertices = stride ? nBytes / stride : 0;
 	b->nBytes = nBytes;
+	if (gpuPresent()) {
+		b->dirty = !copyToDevice(b->dev, data, nBytes, "srpVertexBufferCopyData");
+		if (!b->dirty) return;
+	}
+	/* no device: keep a host copy, uploaded by the first draw */
+	if (nBytes > b->cap) { b->host = (unsigned char*) pinnedRealloc(b->host, nBytes); b->cap = nBytes; }
 	if (nBytes) memcpy(b->host, data, nBytes);
 	b->dirty = true;
 }
@@ -310,12 +343,16 @@ void srpFreeIndexBuffer(SRPIndexBuffer* b)
 
 void srpIndexBufferCopyData(SRPIndexBuffer* b, SRPType type, size_t nBytes, const void* data)
 {
-	if (nBytes > b->cap) { b->host = (unsigned char*) pinnedRealloc(b->host, nBytes); b->cap = nBytes; }
 	b->type = type;
 	b->elemSize = indexTypeSize(type);
 	/* the reference divides by zero for a type without a size; report instead */
 	b->nIndices = b->elemSize ? nBytes / b->elemSize : 0;
 	b->nBytes = nBytes;
+	if (gpuPresent()) {
+		b->dirty = !copyToDevice(b->dev, data, nBytes, "srpIndexBufferCopyData");
+		if (!b->dirty) return;
+	}
+	if (nBytes > b->cap) { b->host = (unsigned char*) pinnedRealloc(b->host, nBytes); b->cap = nBytes; }
 	if (nBytes) memcpy(b->host, data, nBytes);
 	b->dirty = true;
 }
