@@ -61,7 +61,7 @@ SRP_HD float srpFAdd(float a, float b)
 }
 
 /* Number of serial steps below which the plain loop is used. */
-#define SRP_CHAIN_SERIAL 12
+#define SRP_CHAIN_SERIAL 32
 
 SRP_HD float srpChainAdd(float s, float d, uint32_t n)
 {

@@ -2,14 +2,15 @@
  * sorted by tile so that each tile's list keeps primitive order (the
  * reference rasterises primitives strictly one after another,
  * src/pipeline/draw.c:101-122). LSD radix sort with 8-bit digits:
- *   k_radix_hist    per-block digit histograms, stored digit-major
- *   k_scan_*        exclusive scan of the histograms (global digit offsets)
- *   k_radix_scatter stable ranks inside each block from warp match_any /
- *                   popc prefix counts, then the scatter
+ *   k_radix_global_hist  digit totals of every pass in one read
+ *   k_radix_onesweep     one kernel per pass: stable ranks inside each block
+ *                        from warp match_any / popc prefix counts, block
+ *                        offsets per digit from a decoupled look-back
  * followed by k_tile_ranges, which records each tile's [start, end). */
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "device_common.cuh"
 #include "kernels.h"
 
 namespace srpg {
@@ -18,108 +19,55 @@ constexpr int kSortThreads = 256;
 constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kSortItems = 8;                       /* per thread */
 constexpr int kSortTileItems = kSortThreads * kSortItems;
-constexpr int kScanThreads = 512;
-constexpr int kScanItems = 8;
-constexpr int kScanChunk = kScanThreads * kScanItems;
+constexpr int kMaxPasses = 3;                       /* keys up to 24 bits */
 
-__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint32_t* keys, uint32_t n, uint32_t shift,
-                                                            uint32_t* hist, uint32_t nBlocks)
+/* Digit counts of every pass in one read of the keys (the totals do not
+ * depend on the order the passes leave the keys in). */
+__global__ void __launch_bounds__(kSortThreads) k_radix_global_hist(const uint32_t* keys, uint32_t n, uint32_t passes,
+                                                                   uint32_t* ghist)
 {
-	__shared__ uint32_t h[256];
-	h[threadIdx.x] = 0;
+	__shared__ uint32_t h[kMaxPasses][256];
+	for (int i = threadIdx.x; i < kMaxPasses * 256; i += kSortThreads) (&h[0][0])[i] = 0;
 	__syncthreads();
-	const uint32_t base = blockIdx.x * kSortTileItems;
-	for (int r = 0; r < kSortItems; ++r) {
-		const uint32_t i = base + r * kSortThreads + threadIdx.x;
-		if (i < n) atomicAdd(&h[(keys[i] >> shift) & 0xFFu], 1u);
+	for (uint32_t i = blockIdx.x * kSortThreads + threadIdx.x; i < n; i += gridDim.x * kSortThreads) {
+		const uint32_t k = keys[i];
+		for (uint32_t p = 0; p < passes; ++p) atomicAdd(&h[p][(k >> (8 * p)) & 0xFFu], 1u);
 	}
 	__syncthreads();
-	hist[threadIdx.x * nBlocks + blockIdx.x] = h[threadIdx.x];
-}
-
-/* Block-wide exclusive scan of kScanItems values per thread (in order). */
-__device__ __forceinline__ uint32_t blockScanExclusive(uint32_t v[kScanItems], uint32_t* sWarp)
-{
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	uint32_t local = 0;
-#pragma unroll
-	for (int k = 0; k < kScanItems; ++k) { const uint32_t t = v[k]; v[k] = local; local += t; }
-	uint32_t incl = local;
-#pragma unroll
-	for (int o = 1; o < 32; o <<= 1) {
-		const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-		if (lane >= o) incl += y;
-	}
-	if (lane == 31) sWarp[warp] = incl;
-	__syncthreads();
-	if (warp == 0) {
-		uint32_t w = lane < kScanThreads / 32 ? sWarp[lane] : 0u;
-#pragma unroll
-		for (int o = 1; o < 32; o <<= 1) {
-			const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
-			if (lane >= o) w += y;
-		}
-		if (lane < kScanThreads / 32) sWarp[lane] = w;
-	}
-	__syncthreads();
-	const uint32_t off = (warp ? sWarp[warp - 1] : 0u) + incl - local;
-	const uint32_t total = sWarp[kScanThreads / 32 - 1];
-#pragma unroll
-	for (int k = 0; k < kScanItems; ++k) v[k] += off;
-	__syncthreads();
-	return total;
-}
-
-/* Pass 1: scan each chunk in place, record the chunk total. */
-__global__ void __launch_bounds__(kScanThreads) k_scan_chunks(uint32_t* data, uint32_t n, uint32_t* partials)
-{
-	__shared__ uint32_t sWarp[kScanThreads / 32];
-	const uint32_t base = blockIdx.x * kScanChunk + threadIdx.x * kScanItems;
-	uint32_t v[kScanItems];
-#pragma unroll
-	for (int k = 0; k < kScanItems; ++k) v[k] = base + k < n ? data[base + k] : 0u;
-	const uint32_t total = blockScanExclusive(v, sWarp);
-#pragma unroll
-	for (int k = 0; k < kScanItems; ++k) if (base + k < n) data[base + k] = v[k];
-	if (threadIdx.x == 0) partials[blockIdx.x] = total;
-}
-
-/* Pass 2: one block scans the chunk totals, kScanChunk at a time with a
- * running carry. */
-__global__ void __launch_bounds__(kScanThreads) k_scan_partials(uint32_t* partials, uint32_t n)
-{
-	__shared__ uint32_t sWarp[kScanThreads / 32];
-	uint32_t carry = 0;
-	for (uint32_t off = 0; off < n; off += kScanChunk) {
-		const uint32_t base = off + threadIdx.x * kScanItems;
-		uint32_t v[kScanItems];
-#pragma unroll
-		for (int k = 0; k < kScanItems; ++k) v[k] = base + k < n ? partials[base + k] : 0u;
-		const uint32_t total = blockScanExclusive(v, sWarp);
-#pragma unroll
-		for (int k = 0; k < kScanItems; ++k) if (base + k < n) partials[base + k] = v[k] + carry;
-		carry += total;
+	for (int i = threadIdx.x; i < (int) passes * 256; i += kSortThreads) {
+		const uint32_t v = (&h[0][0])[i];
+		if (v) atomicAdd(&ghist[i], v);
 	}
 }
 
-/* Pass 3: add each chunk's offset. */
-__global__ void __launch_bounds__(kScanThreads) k_scan_apply(uint32_t* data, uint32_t n, const uint32_t* partials)
-{
-	const uint32_t off = partials[blockIdx.x];
-	const uint32_t base = blockIdx.x * kScanChunk;
-	for (int k = threadIdx.x; k < kScanChunk; k += kScanThreads)
-		if (base + k < n) data[base + k] += off;
-}
-
-__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t* keysIn, const uint32_t* valsIn, uint32_t n,
-                                                               uint32_t shift, const uint32_t* offsets, uint32_t nBlocks,
-                                                               uint32_t* keysOut, uint32_t* valsOut)
+/* One stable LSD pass (OneSweep style). Blocks take 2048 consecutive keys in
+ * ticket order; ranks inside the block come from warp match_any / popc prefix
+ * counts over rounds that follow input order; each block publishes its 256
+ * digit counts and walks back over its predecessors' (decoupled look-back,
+ * one thread per digit) to find where its run of each digit starts. */
+__global__ void __launch_bounds__(kSortThreads) k_radix_onesweep(const uint32_t* keysIn, const uint32_t* valsIn, uint32_t n,
+                                                                uint32_t shift, const uint32_t* ghistPass,
+                                                                uint32_t* status, uint32_t* ticket, uint32_t* errors,
+                                                                uint32_t* keysOut, uint32_t* valsOut)
 {
 	__shared__ uint32_t cnt[kSortWarps][256];
+	__shared__ uint32_t digitBase[256];
+	__shared__ uint32_t digitStart[256];
+	__shared__ uint32_t sBlock;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	if (threadIdx.x == 0) sBlock = atomicAdd(ticket, 1u);
 	for (int i = threadIdx.x; i < kSortWarps * 256; i += kSortThreads) (&cnt[0][0])[i] = 0;
+	/* exclusive scan of the pass's digit totals (Hillis-Steele in shared memory) */
+	digitStart[threadIdx.x] = ghistPass[threadIdx.x];
 	__syncthreads();
-	const uint32_t base = blockIdx.x * kSortTileItems + warp * (32 * kSortItems);
+	for (int o = 1; o < 256; o <<= 1) {
+		const uint32_t v = threadIdx.x >= o ? digitStart[threadIdx.x - o] : 0u;
+		__syncthreads();
+		digitStart[threadIdx.x] += v;
+		__syncthreads();
+	}
+	const uint32_t blk = sBlock;
+	const uint32_t base = blk * kSortTileItems + warp * (32 * kSortItems);
 	const uint32_t ltMask = (1u << lane) - 1u;
 	uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
 #pragma unroll
@@ -129,7 +77,6 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t* 
 		key[r] = valid ? keysIn[i] : 0u;
 		val[r] = valid ? valsIn[i] : 0u;
 		const uint32_t d = (key[r] >> shift) & 0xFFu;
-		/* lanes holding the same digit in this round, in lane (= input) order */
 		const uint32_t peers = __match_any_sync(0xFFFFFFFFu, valid ? d : 256u + lane);
 		const uint32_t before = valid ? cnt[warp][d] : 0u;
 		__syncwarp();
@@ -138,19 +85,43 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t* 
 		rank[r] = valid ? before + __popc(peers & ltMask) : 0xFFFFFFFFu;
 	}
 	__syncthreads();
-	/* per digit, exclusive prefix over warps: earlier warps hold earlier items */
 	{
+		/* thread d: exclusive prefix over warps, block total, look-back */
 		const int d = threadIdx.x;
 		uint32_t run = 0;
 #pragma unroll
 		for (int w = 0; w < kSortWarps; ++w) { const uint32_t t = cnt[w][d]; cnt[w][d] = run; run += t; }
+		uint32_t* st = status + (size_t) blk * 256 + d;
+		uint32_t prefix = 0;
+		if (blk == 0) {
+			atomicExch(st, (2u << 30) | run);
+		} else {
+			atomicExch(st, (1u << 30) | run);
+			long long j = (long long) blk - 1;
+			unsigned spins = 0;
+			while (j >= 0) {
+				const uint32_t v = *((volatile uint32_t*) (status + (size_t) j * 256 + d));
+				const uint32_t flag = v >> 30;
+				if (flag == 0) {
+					if (++spins > kSpinLimit) { atomicOr(errors, kErrSpin); break; }
+					__nanosleep(32);
+					continue;
+				}
+				prefix += v & 0x3FFFFFFFu;
+				if (flag == 2) break;
+				--j;
+			}
+			atomicExch(st, (2u << 30) | (prefix + run));
+		}
+		/* start of digit d in the output: all smaller digits, then earlier blocks */
+		digitBase[d] = digitStart[d] - ghistPass[d] + prefix;
 	}
 	__syncthreads();
 #pragma unroll
 	for (int r = 0; r < kSortItems; ++r) {
 		if (rank[r] == 0xFFFFFFFFu) continue;
 		const uint32_t d = (key[r] >> shift) & 0xFFu;
-		const uint32_t pos = offsets[d * nBlocks + blockIdx.x] + cnt[warp][d] + rank[r];
+		const uint32_t pos = digitBase[d] + cnt[warp][d] + rank[r];
 		keysOut[pos] = key[r];
 		valsOut[pos] = val[r];
 	}
@@ -168,37 +139,31 @@ __global__ void k_tile_ranges(const uint32_t* keys, uint32_t n, uint32_t numTile
 
 static uint32_t sortBlocks(uint32_t n) { return (n + kSortTileItems - 1) / kSortTileItems; }
 
-size_t sortHistWords(uint32_t n) { return (size_t) 256 * (sortBlocks(n) ? sortBlocks(n) : 1); }
+/* scratch words: global histograms, per-pass look-back status, tickets */
+size_t sortHistWords(uint32_t n) { return (size_t) kMaxPasses * 256 + (size_t) kMaxPasses * 256 * (sortBlocks(n) + 1) + 8; }
 
-size_t sortPartialWords(uint32_t n)
-{
-	const size_t m = sortHistWords(n);
-	return (m + kScanChunk - 1) / kScanChunk + 1;
-}
-
-static void scanExclusive(uint32_t* data, uint32_t n, uint32_t* partials, cudaStream_t s)
-{
-	const uint32_t chunks = (n + kScanChunk - 1) / kScanChunk;
-	k_scan_chunks<<<chunks, kScanThreads, 0, s>>>(data, n, partials);
-	if (chunks > 1) {
-		k_scan_partials<<<1, kScanThreads, 0, s>>>(partials, chunks);
-		k_scan_apply<<<chunks, kScanThreads, 0, s>>>(data, n, partials);
-	}
-}
+size_t sortPartialWords(uint32_t) { return 8; }
 
 void sortEntries(const DrawParams& P, uint32_t n, uint32_t keyBits, uint32_t* keysAlt, uint32_t* valsAlt,
-                 uint32_t* hist, uint32_t* partials, uint32_t** keysOut, uint32_t** valsOut, cudaStream_t s)
+                 uint32_t* hist, uint32_t*, uint32_t** keysOut, uint32_t** valsOut, cudaStream_t s)
 {
 	uint32_t* kin = P.keys;
 	uint32_t* vin = P.vals;
 	uint32_t* kout = keysAlt;
 	uint32_t* vout = valsAlt;
 	const uint32_t nb = sortBlocks(n);
-	if (n > 1) {
-		for (uint32_t shift = 0; shift < keyBits; shift += 8) {
-			k_radix_hist<<<nb, kSortThreads, 0, s>>>(kin, n, shift, hist, nb);
-			scanExclusive(hist, 256 * nb, partials, s);
-			k_radix_scatter<<<nb, kSortThreads, 0, s>>>(kin, vin, n, shift, hist, nb, kout, vout);
+	const uint32_t passes = (keyBits + 7) / 8;
+	if (n > 1 && passes) {
+		uint32_t* ghist = hist;
+		uint32_t* tickets = hist + kMaxPasses * 256;
+		uint32_t* status = tickets + 8;
+		cudaMemsetAsync(hist, 0, sortHistWords(n) * 4, s);
+		const uint32_t hb = nb < 152u * 4u ? nb : 152u * 4u;
+		k_radix_global_hist<<<hb, kSortThreads, 0, s>>>(kin, n, passes, ghist);
+		for (uint32_t p = 0; p < passes; ++p) {
+			k_radix_onesweep<<<nb, kSortThreads, 0, s>>>(kin, vin, n, 8 * p, ghist + 256 * p,
+			                                            status + (size_t) p * 256 * nb, tickets + p, &P.ctr->errors,
+			                                            kout, vout);
 			uint32_t* t = kin; kin = kout; kout = t;
 			t = vin; vin = vout; vout = t;
 		}

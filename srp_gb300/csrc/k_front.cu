@@ -79,6 +79,64 @@ __global__ void k_index_range(const __grid_constant__ DrawParams P)
 	}
 }
 
+/* ------------------------------------------------- per-vertex setup data */
+
+struct PV { float4 p; uint32_t ref; };
+
+/* Per-vertex results of the reference's perspective divide and viewport
+ * transform (src/pipeline/vertex_processing.c:76-88,
+ * src/core/framebuffer.c:48-55). The reference recomputes them for every
+ * primitive corner from the same clip position, so they are a pure function
+ * of the vertex and are computed once per vertex by k_vertex; clipping
+ * creates new vertices, whose values are computed on the spot. */
+struct VSet { float nx, ny, nz, sx, sy, c, iw; };
+struct SV { VSet s; uint32_t ref; };
+
+__device__ __forceinline__ VSet vertexSetup(const DrawState& st, const float4& clip)
+{
+	VSet v;
+	v.iw = invW(clip.w);
+	v.nx = __fmul_rn(clip.x, v.iw);
+	v.ny = __fmul_rn(clip.y, v.iw);
+	v.nz = __fmul_rn(clip.z, v.iw);
+	ndcToScreen(st.W, st.H, v.nx, v.ny, v.sx, v.sy);
+	v.c = __fmul_rn(v.nz, v.iw);
+	return v;
+}
+
+__device__ __forceinline__ SV fromClip(const DrawState& st, const PV& p)
+{
+	SV v;
+	v.s = vertexSetup(st, p.p);
+	v.ref = p.ref;
+	return v;
+}
+
+enum SetupMode { kTriFill = 0, kTriLine = 1, kTriPoint = 2, kLines = 3, kPoints = 4 };
+
+__device__ __forceinline__ float planeDist(const float4& c, int p)
+{
+	/* src/pipeline/clipping.c:260-277 */
+	switch (p) {
+	case 0: return __fadd_rn(c.x, c.w);
+	case 1: return __fsub_rn(c.w, c.x);
+	case 2: return __fadd_rn(c.y, c.w);
+	case 3: return __fsub_rn(c.w, c.y);
+	case 4: return __fadd_rn(c.z, c.w);
+	default: return __fsub_rn(c.w, c.z);
+	}
+}
+
+__device__ __forceinline__ uint32_t outcode(const float4& c)
+{
+	/* src/pipeline/clipping.c:121-137 */
+	uint32_t code = 0;
+#pragma unroll
+	for (int p = 0; p < 6; ++p) code |= (uint32_t) (planeDist(c, p) < 0.0f) << p;
+	return code;
+}
+
+
 /* --------------------------------------------------------------- vertex */
 
 constexpr int kVertexThreads = 128;
@@ -147,7 +205,11 @@ __global__ void __launch_bounds__(kVertexThreads) k_vertex(const __grid_constant
 	o.clipPosition[0] = o.clipPosition[1] = o.clipPosition[2] = o.clipPosition[3] = 0.0f;
 	o.varyings = (SRPVarying*) out;
 	runVS<VS>(&in, &o);
-	P.clip[v] = make_float4(o.clipPosition[0], o.clipPosition[1], o.clipPosition[2], o.clipPosition[3]);
+	const float4 clip = make_float4(o.clipPosition[0], o.clipPosition[1], o.clipPosition[2], o.clipPosition[3]);
+	P.clip[v] = clip;
+	const VSet vs = vertexSetup(P.st, clip);
+	P.vset0[v] = make_float4(vs.nx, vs.ny, vs.sx, vs.sy);
+	P.vset1[v] = make_float4(vs.c, vs.iw, vs.nz, __uint_as_float(outcode(clip)));
 	const int nw = P.L.nWords;
 	uint32_t* dst = P.vary + v * (unsigned long long) nw;
 #pragma unroll
@@ -156,32 +218,6 @@ __global__ void __launch_bounds__(kVertexThreads) k_vertex(const __grid_constant
 }
 
 /* ----------------------------------------------------------------- setup */
-
-struct PV { float4 p; uint32_t ref; };
-
-enum SetupMode { kTriFill = 0, kTriLine = 1, kTriPoint = 2, kLines = 3, kPoints = 4 };
-
-__device__ __forceinline__ float planeDist(const float4& c, int p)
-{
-	/* src/pipeline/clipping.c:260-277 */
-	switch (p) {
-	case 0: return __fadd_rn(c.x, c.w);
-	case 1: return __fsub_rn(c.w, c.x);
-	case 2: return __fadd_rn(c.y, c.w);
-	case 3: return __fsub_rn(c.w, c.y);
-	case 4: return __fadd_rn(c.z, c.w);
-	default: return __fsub_rn(c.w, c.z);
-	}
-}
-
-__device__ __forceinline__ uint32_t outcode(const float4& c)
-{
-	/* src/pipeline/clipping.c:121-137 */
-	uint32_t code = 0;
-#pragma unroll
-	for (int p = 0; p < 6; ++p) code |= (uint32_t) (planeDist(c, p) < 0.0f) << p;
-	return code;
-}
 
 /* New vertex a*(1-t) + b*t with affinely interpolated varyings, stored as a
  * clip-generated row (src/pipeline/clipping.c:244-258). */
@@ -279,18 +315,15 @@ __device__ __forceinline__ uint32_t tileCount(int minX, int minY, int maxXex, in
 
 /* Triangle setup (src/raster/triangle.c:113-238). Returns false if the
  * triangle is culled or degenerate. */
-__device__ bool setupTriangle(const DrawState& st, PV v0, PV v1, PV v2, TriRaster& R, TriAttr& A)
+__device__ bool setupTriangle(const DrawState& st, const SV& v0, const SV& v1, const SV& v2, TriRaster& R, TriAttr& A)
 {
-	float iw[3], nx[3], ny[3], nz[3];
+	float iw[3] = { v0.s.iw, v1.s.iw, v2.s.iw };
+	float nx[3] = { v0.s.nx, v1.s.nx, v2.s.nx };
+	float ny[3] = { v0.s.ny, v1.s.ny, v2.s.ny };
+	float cz[3] = { v0.s.c, v1.s.c, v2.s.c };
+	float sx[3] = { v0.s.sx, v1.s.sx, v2.s.sx };
+	float sy[3] = { v0.s.sy, v1.s.sy, v2.s.sy };
 	uint32_t ref[3] = { v0.ref, v1.ref, v2.ref };
-	const float4 c[3] = { v0.p, v1.p, v2.p };
-#pragma unroll
-	for (int i = 0; i < 3; ++i) {
-		iw[i] = invW(c[i].w);
-		nx[i] = __fmul_rn(c[i].x, iw[i]);
-		ny[i] = __fmul_rn(c[i].y, iw[i]);
-		nz[i] = __fmul_rn(c[i].z, iw[i]);
-	}
 	/* NDC cull (triangle.c:162-182) */
 	const float e0x = __fsub_rn(nx[1], nx[0]), e0y = __fsub_rn(ny[1], ny[0]);
 	const float e1x = __fsub_rn(nx[2], nx[0]), e1y = __fsub_rn(ny[2], ny[0]);
@@ -301,14 +334,11 @@ __device__ bool setupTriangle(const DrawState& st, PV v0, PV v1, PV v2, TriRaste
 		/* winding fix: swap vertices 1 and 2 (triangle.c:184-195) */
 		float t;
 		t = iw[1]; iw[1] = iw[2]; iw[2] = t;
-		t = nx[1]; nx[1] = nx[2]; nx[2] = t;
-		t = ny[1]; ny[1] = ny[2]; ny[2] = t;
-		t = nz[1]; nz[1] = nz[2]; nz[2] = t;
+		t = cz[1]; cz[1] = cz[2]; cz[2] = t;
+		t = sx[1]; sx[1] = sx[2]; sx[2] = t;
+		t = sy[1]; sy[1] = sy[2]; sy[2] = t;
 		uint32_t r = ref[1]; ref[1] = ref[2]; ref[2] = r;
 	}
-	float sx[3], sy[3];
-#pragma unroll
-	for (int i = 0; i < 3; ++i) ndcToScreen(st.W, st.H, nx[i], ny[i], sx[i], sy[i]);
 	float ex[3], ey[3];
 #pragma unroll
 	for (int i = 0; i < 3; ++i) {
@@ -355,7 +385,7 @@ __device__ bool setupTriangle(const DrawState& st, PV v0, PV v1, PV v2, TriRaste
 	for (int i = 0; i < 3; ++i) {
 		const bool tl = (ex[i] > 0.0f && roughlyZero(ey[i])) || (ey[i] < 0.0f);
 		flags |= (tl ? 1u : 0u) << (1 + i);
-		R.c[i] = __fmul_rn(nz[i], iw[i]);
+		R.c[i] = cz[i];
 		A.invW[i] = iw[i];
 		A.vref[i] = ref[i];
 	}
@@ -367,18 +397,11 @@ __device__ bool setupTriangle(const DrawState& st, PV v0, PV v1, PV v2, TriRaste
 
 /* Line setup: divide, screen space, DDA parameters
  * (src/raster/line.c:34-56, 79-86). */
-__device__ void setupLine(const DrawState& st, const PV& a, const PV& b, LineRec& L)
+__device__ void setupLine(const DrawState& st, const SV& a, const SV& b, LineRec& L)
 {
-	const float4 c[2] = { a.p, b.p };
-	float sx[2], sy[2];
-#pragma unroll
-	for (int i = 0; i < 2; ++i) {
-		const float w = invW(c[i].w);
-		const float nx = __fmul_rn(c[i].x, w), ny = __fmul_rn(c[i].y, w), nz = __fmul_rn(c[i].z, w);
-		ndcToScreen(st.W, st.H, nx, ny, sx[i], sy[i]);
-		L.invW[i] = w;
-		L.c[i] = __fmul_rn(nz, w);
-	}
+	const float sx[2] = { a.s.sx, b.s.sx }, sy[2] = { a.s.sy, b.s.sy };
+	L.invW[0] = a.s.iw; L.invW[1] = b.s.iw;
+	L.c[0] = a.s.c; L.c[1] = b.s.c;
 	const float dx = __fsub_rn(sx[1], sx[0]), dy = __fsub_rn(sy[1], sy[0]);
 	float mx = fmaxf(fabsf(dx), fabsf(dy));
 	int steps = (int) ceilf(mx);
@@ -396,12 +419,9 @@ __device__ void setupLine(const DrawState& st, const PV& a, const PV& b, LineRec
 
 /* Point setup: divide, screen space, coverage square and raster bounds
  * (src/raster/point.c:32-79, 121-163). */
-__device__ void setupPoint(const DrawState& st, const PV& v, PointRec& R)
+__device__ void setupPoint(const DrawState& st, const SV& v, PointRec& R)
 {
-	const float w = invW(v.p.w);
-	const float nx = __fmul_rn(v.p.x, w), ny = __fmul_rn(v.p.y, w), nz = __fmul_rn(v.p.z, w);
-	float sx, sy;
-	ndcToScreen(st.W, st.H, nx, ny, sx, sy);
+	const float sx = v.s.sx, sy = v.s.sy, nz = v.s.nz;
 	const float half = __fmul_rn(st.pointSize, 0.5f);
 	R.mnx = __fsub_rn(sx, half); R.mny = __fsub_rn(sy, half);
 	R.mxx = __fadd_rn(sx, half); R.mxy = __fadd_rn(sy, half);
@@ -451,8 +471,8 @@ template <int MODE>
 struct Assembly {
 	int nPoly;
 	bool clipped;
-	PV v[3];
-	PV poly[kMaxPoly];
+	SV sv[3];            /* unclipped: per-vertex setup data from k_vertex */
+	PV poly[kMaxPoly];   /* clipped: polygon in clip space */
 };
 
 /* Write a set-up triangle as primitive `prim` with its pairs at `entry`. */
@@ -475,7 +495,7 @@ __device__ __forceinline__ void writeTri(const DrawParams& P, TriRaster& R, TriA
 }
 
 template <int MODE>
-__device__ __forceinline__ void handleTriangle(const DrawParams& P, const PV& a, const PV& b, const PV& c, bool write,
+__device__ __forceinline__ void handleTriangle(const DrawParams& P, const SV& a, const SV& b, const SV& c, bool write,
                                                uint32_t& prim, uint32_t& entry)
 {
 	if (MODE == kTriFill) {
@@ -487,7 +507,7 @@ __device__ __forceinline__ void handleTriangle(const DrawParams& P, const PV& a,
 		prim += 1;
 		entry += nt;
 	} else if (MODE == kTriLine) {
-		const PV* vv[3] = { &a, &b, &c };
+		const SV* vv[3] = { &a, &b, &c };
 #pragma unroll
 		for (int j = 0; j < 3; ++j) {
 			LineRec L;
@@ -500,7 +520,7 @@ __device__ __forceinline__ void handleTriangle(const DrawParams& P, const PV& a,
 			entry += (uint32_t) L.steps + 1u;
 		}
 	} else if (MODE == kTriPoint) {
-		const PV* vv[3] = { &a, &b, &c };
+		const SV* vv[3] = { &a, &b, &c };
 #pragma unroll
 		for (int j = 0; j < 3; ++j) {
 			PointRec R;
@@ -540,13 +560,35 @@ __device__ __forceinline__ void lineStream(int prim, unsigned long long base, un
 	else { s[0] = base + k; s[1] = base + (k + 1) % count; }
 }
 
-__device__ __forceinline__ bool loadVertex(const DrawParams& P, unsigned long long stream, PV& v)
+__device__ __forceinline__ bool vertexIndex(const DrawParams& P, unsigned long long stream, uint32_t& vi)
 {
-	const unsigned long long vi = P.indexSize ? fetchIndex(P, stream) : stream;
-	if (vi >= P.nVertices) { atomicOr(&P.ctr->errors, kErrBadIndex); return false; }
-	v.p = P.clip[vi];
-	v.ref = (uint32_t) vi;
+	const unsigned long long v = P.indexSize ? fetchIndex(P, stream) : stream;
+	if (v >= P.nVertices) { atomicOr(&P.ctr->errors, kErrBadIndex); return false; }
+	vi = (uint32_t) v;
 	return true;
+}
+
+__device__ __forceinline__ uint32_t vertexCode(const DrawParams& P, uint32_t vi)
+{
+	return __float_as_uint(P.vset1[vi].w);
+}
+
+__device__ __forceinline__ SV loadSV(const DrawParams& P, uint32_t vi)
+{
+	const float4 a = P.vset0[vi], b = P.vset1[vi];
+	SV v;
+	v.s.nx = a.x; v.s.ny = a.y; v.s.sx = a.z; v.s.sy = a.w;
+	v.s.c = b.x; v.s.iw = b.y; v.s.nz = b.z;
+	v.ref = vi;
+	return v;
+}
+
+__device__ __forceinline__ PV loadPV(const DrawParams& P, uint32_t vi)
+{
+	PV v;
+	v.p = P.clip[vi];
+	v.ref = vi;
+	return v;
 }
 
 /* Status word of the decoupled look-back: flag (2 bits) | prims (30) | entries (32). */
@@ -574,29 +616,45 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
 	bool live = k < P.nIn;
 	if (live) {
 		if (MODE == kPoints) {
-			const unsigned long long s = P.start + (unsigned long long) k;
-			live = loadVertex(P, s, as.v[0]);
-			if (live) {
-				/* whole-point reject (src/pipeline/clipping.c:185-197) */
-				const float4 c = as.v[0].p;
-				const float nw = -c.w;
-				if ((c.x < nw || c.x > c.w) || (c.y < nw || c.y > c.w) || (c.z < nw || c.z > c.w)) live = false;
-			}
+			uint32_t vi;
+			live = vertexIndex(P, P.start + (unsigned long long) k, vi);
+			/* whole-point reject (src/pipeline/clipping.c:185-197): x < -w and
+			 * x + w < 0 are the same test in fp32, so any outcode bit rejects */
+			if (live) live = vertexCode(P, vi) == 0;
+			if (live) as.sv[0] = loadSV(P, vi);
 		} else if (MODE == kLines) {
 			unsigned long long s[2];
+			uint32_t vi[2];
 			lineStream(P.prim, P.start, (unsigned long long) k, P.count, s);
-			live = loadVertex(P, s[0], as.v[0]) && loadVertex(P, s[1], as.v[1]);
-			if (live) live = !clipLine(P, as.v[0], as.v[1]);
+			live = vertexIndex(P, s[0], vi[0]) && vertexIndex(P, s[1], vi[1]);
+			if (live) {
+				const uint32_t c0 = vertexCode(P, vi[0]), c1 = vertexCode(P, vi[1]);
+				if ((c0 | c1) == 0) {
+					as.sv[0] = loadSV(P, vi[0]);
+					as.sv[1] = loadSV(P, vi[1]);
+				} else if (c0 & c1) {
+					live = false;
+				} else {
+					PV a = loadPV(P, vi[0]), b = loadPV(P, vi[1]);
+					live = !clipLine(P, a, b);
+					if (live) { as.sv[0] = fromClip(P.st, a); as.sv[1] = fromClip(P.st, b); }
+				}
+			}
 		} else {
 			unsigned long long s[3];
+			uint32_t vi[3];
 			triStream(P.prim, P.start, (unsigned long long) k, s);
-			live = loadVertex(P, s[0], as.v[0]) && loadVertex(P, s[1], as.v[1]) && loadVertex(P, s[2], as.v[2]);
+			live = vertexIndex(P, s[0], vi[0]) && vertexIndex(P, s[1], vi[1]) && vertexIndex(P, s[2], vi[2]);
 			if (live) {
-				const uint32_t c0 = outcode(as.v[0].p), c1 = outcode(as.v[1].p), c2 = outcode(as.v[2].p);
+				const uint32_t c0 = vertexCode(P, vi[0]), c1 = vertexCode(P, vi[1]), c2 = vertexCode(P, vi[2]);
 				if (c0 & c1 & c2) live = false;
-				else if (c0 | c1 | c2) {
+				else if ((c0 | c1 | c2) == 0) {
+#pragma unroll
+					for (int i = 0; i < 3; ++i) as.sv[i] = loadSV(P, vi[i]);
+				} else {
 					as.clipped = true;
-					as.nPoly = clipPolygon(P, as.v, as.poly);
+					PV in[3] = { loadPV(P, vi[0]), loadPV(P, vi[1]), loadPV(P, vi[2]) };
+					as.nPoly = clipPolygon(P, in, as.poly);
 					if (as.nPoly < 3) live = false;
 				}
 			}
@@ -610,24 +668,25 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
 	if (live) {
 		if (MODE == kPoints) {
 			PointRec R;
-			setupPoint(P.st, as.v[0], R);
+			setupPoint(P.st, as.sv[0], R);
 			nPrim = 1;
 			nEnt = tileCount(R.x0, R.y0, R.x1 + 1, R.y1 + 1);
 		} else if (MODE == kLines) {
 			LineRec L;
-			setupLine(P.st, as.v[0], as.v[1], L);
+			setupLine(P.st, as.sv[0], as.sv[1], L);
 			nPrim = 1;
 			nEnt = (uint32_t) L.steps + 1u;
 		} else if (!as.clipped) {
 			if (MODE == kTriFill) {
-				fOk = setupTriangle(P.st, as.v[0], as.v[1], as.v[2], fR, fA);
+				fOk = setupTriangle(P.st, as.sv[0], as.sv[1], as.sv[2], fR, fA);
 				if (fOk) { nPrim = 1; nEnt = tileCount(fR.minX, fR.minY, fR.maxX, fR.maxY); }
 			} else {
-				handleTriangle<MODE>(P, as.v[0], as.v[1], as.v[2], false, nPrim, nEnt);
+				handleTriangle<MODE>(P, as.sv[0], as.sv[1], as.sv[2], false, nPrim, nEnt);
 			}
 		} else {
+			const SV p0 = fromClip(P.st, as.poly[0]);
 			for (int f = 1; f + 1 < as.nPoly; ++f)
-				handleTriangle<MODE>(P, as.poly[0], as.poly[f], as.poly[f + 1], false, nPrim, nEnt);
+				handleTriangle<MODE>(P, p0, fromClip(P.st, as.poly[f]), fromClip(P.st, as.poly[f + 1]), false, nPrim, nEnt);
 		}
 	}
 
@@ -696,7 +755,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
 	if (!live) return;
 	if (MODE == kPoints) {
 		PointRec R;
-		setupPoint(P.st, as.v[0], R);
+		setupPoint(P.st, as.sv[0], R);
 		if (primBase < P.primCap) {
 			R.id = primBase;
 			P.points[primBase] = R;
@@ -704,7 +763,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
 		} else atomicOr(&P.ctr->errors, kErrCapacity);
 	} else if (MODE == kLines) {
 		LineRec L;
-		setupLine(P.st, as.v[0], as.v[1], L);
+		setupLine(P.st, as.sv[0], as.sv[1], L);
 		if (primBase < P.primCap) {
 			L.id = primBase;
 			L.fragBase = entBase;
@@ -714,11 +773,12 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
 		if (MODE == kTriFill) {
 			if (fOk) writeTri(P, fR, fA, nEnt, primBase, entBase);
 		} else {
-			handleTriangle<MODE>(P, as.v[0], as.v[1], as.v[2], true, primBase, entBase);
+			handleTriangle<MODE>(P, as.sv[0], as.sv[1], as.sv[2], true, primBase, entBase);
 		}
 	} else {
+		const SV p0 = fromClip(P.st, as.poly[0]);
 		for (int f = 1; f + 1 < as.nPoly; ++f)
-			handleTriangle<MODE>(P, as.poly[0], as.poly[f], as.poly[f + 1], true, primBase, entBase);
+			handleTriangle<MODE>(P, p0, fromClip(P.st, as.poly[f]), fromClip(P.st, as.poly[f + 1]), true, primBase, entBase);
 	}
 }
 
@@ -790,57 +850,88 @@ __global__ void k_lambda_tables(const __grid_constant__ DrawParams P, uint32_t n
 	}
 }
 
-/* One warp per line walks the reference's DDA exactly (fp32 accumulators,
- * round half away from zero): lane l takes a contiguous run of steps, enters
- * it with the exact jump-ahead of the x, y and t accumulators (chain.h) and
- * then steps serially. Each step writes one record and one (tile, fragment)
- * pair; steps whose pixel fails the scissor test or falls outside the
- * framebuffer get the key one past the last tile, which sorts them out
- * (src/raster/line.c:34-77, src/raster/fragment.c:63-75). */
+/* Steps [s0, s1) of line i's DDA, exactly as the reference walks them
+ * (fp32 accumulators, round half away from zero; src/raster/line.c:34-77):
+ * the accumulators are entered at s0 with the exact jump-ahead (chain.h),
+ * then stepped serially. Each step writes one record and one (tile,
+ * fragment) pair; steps whose pixel fails the scissor test or falls outside
+ * the framebuffer get the key one past the last tile, which sorts them out
+ * (src/raster/fragment.c:63-75). Returns the steps that passed the scissor. */
+__device__ unsigned long long walkLine(const DrawParams& P, const LineRec& L, uint32_t i, uint32_t s0, uint32_t s1)
+{
+	unsigned long long passed = 0;
+	const uint32_t invalid = (uint32_t) (P.st.tilesX * P.st.tilesY);
+	float x = srpChainAdd(L.x0, L.xInc, s0), y = srpChainAdd(L.y0, L.yInc, s0);
+	float t = srpChainAdd(0.0f, L.tInc, s0);
+	const unsigned long long size = (unsigned long long) P.st.W * (unsigned long long) P.st.H;
+	for (uint32_t s = s0; s < s1; ++s) {
+		const int px = (int) roundf(x), py = (int) roundf(y);
+		const float w0 = __fsub_rn(1.0f, t);
+		const float depth = __fadd_rn(__fmul_rn(L.c[0], w0), __fmul_rn(L.c[1], t));
+		const uint32_t e = L.fragBase + s;
+		uint32_t key = invalid;
+		if (scissorPass(P.st, px, py)) {
+			++passed;
+			const unsigned long long idx = (unsigned long long) (long long) py * (unsigned long long) P.st.W
+			                             + (unsigned long long) (long long) px;
+			if (idx < size) {
+				const uint32_t gx = (uint32_t) (idx % (unsigned long long) P.st.W);
+				const uint32_t gy = (uint32_t) (idx / (unsigned long long) P.st.W);
+				key = (gy / kTile) * (uint32_t) P.st.tilesX + gx / kTile;
+			}
+		}
+		if (e < P.fragCap && e < P.entryCap) {
+			LineFrag F;
+			F.depth = depth; F.t = t; F.line = i; F.px = (int16_t) px; F.py = (int16_t) py;
+			P.frags[e] = F;
+			P.keys[e] = key;
+			P.vals[e] = e;
+		}
+		x = __fadd_rn(x, L.xInc);
+		y = __fadd_rn(y, L.yInc);
+		t = __fadd_rn(t, L.tInc);
+	}
+	return passed;
+}
+
+constexpr uint32_t kShortLine = 48;   /* steps one thread walks on its own */
+
+/* One thread per line; lines longer than kShortLine steps are queued for
+ * k_line_frags_long. */
 __global__ void k_line_frags(const __grid_constant__ DrawParams P, uint32_t nLines)
 {
-	const uint32_t i = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	unsigned long long passed = 0;
 	if (i < nLines) {
 		const LineRec L = P.lines[i];
-		const uint32_t invalid = (uint32_t) (P.st.tilesX * P.st.tilesY);
 		const uint32_t total = (uint32_t) L.steps + 1u;
-		const uint32_t seg = (total + 31u) / 32u;
-		const uint32_t s0 = min(lane * seg, total), s1 = min(s0 + seg, total);
-		float x = srpChainAdd(L.x0, L.xInc, s0), y = srpChainAdd(L.y0, L.yInc, s0);
-		float t = srpChainAdd(0.0f, L.tInc, s0);
-		const unsigned long long size = (unsigned long long) P.st.W * (unsigned long long) P.st.H;
-		for (uint32_t s = s0; s < s1; ++s) {
-			const int px = (int) roundf(x), py = (int) roundf(y);
-			const float w0 = __fsub_rn(1.0f, t);
-			const float depth = __fadd_rn(__fmul_rn(L.c[0], w0), __fmul_rn(L.c[1], t));
-			const uint32_t e = L.fragBase + (uint32_t) s;
-			uint32_t key = invalid;
-			if (scissorPass(P.st, px, py)) {
-				++passed;
-				const unsigned long long idx = (unsigned long long) (long long) py * (unsigned long long) P.st.W
-				                             + (unsigned long long) (long long) px;
-				if (idx < size) {
-					const uint32_t gx = (uint32_t) (idx % (unsigned long long) P.st.W);
-					const uint32_t gy = (uint32_t) (idx / (unsigned long long) P.st.W);
-					key = (gy / kTile) * (uint32_t) P.st.tilesX + gx / kTile;
-				}
-			}
-			if (e < P.fragCap && e < P.entryCap) {
-				LineFrag F;
-				F.depth = depth; F.t = t; F.line = i; F.px = (int16_t) px; F.py = (int16_t) py;
-				P.frags[e] = F;
-				P.keys[e] = key;
-				P.vals[e] = e;
-			}
-			x = __fadd_rn(x, L.xInc);
-			y = __fadd_rn(y, L.yInc);
-			t = __fadd_rn(t, L.tInc);
+		if (total > kShortLine) {
+			const unsigned long long j = atomicAdd(&P.ctr->lineFrags, 1ull);
+			if (j < P.bigCap) P.bigJobs[j].x = i;
+		} else {
+			passed = walkLine(P, L, i, 0, total);
 		}
 	}
 	for (int o = 16; o; o >>= 1) passed += __shfl_xor_sync(0xFFFFFFFFu, passed, o);
 	if ((threadIdx.x & 31) == 0 && passed) atomicAdd(&P.ctr->fragments, passed);
+}
+
+/* Long lines: one warp per line, lane l walks a contiguous run of steps. */
+__global__ void k_line_frags_long(const __grid_constant__ DrawParams P)
+{
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t nLong = (uint32_t) min(P.ctr->lineFrags, (unsigned long long) P.bigCap);
+	const uint32_t warps = gridDim.x * (blockDim.x / 32);
+	for (uint32_t q = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); q < nLong; q += warps) {
+		const uint32_t i = P.bigJobs[q].x;
+		const LineRec L = P.lines[i];
+		const uint32_t total = (uint32_t) L.steps + 1u;
+		const uint32_t seg = (total + 31u) / 32u;
+		const uint32_t s0 = min(lane * seg, total), s1 = min(s0 + seg, total);
+		unsigned long long passed = walkLine(P, L, i, s0, s1);
+		for (int o = 16; o; o >>= 1) passed += __shfl_xor_sync(0xFFFFFFFFu, passed, o);
+		if (lane == 0 && passed) atomicAdd(&P.ctr->fragments, passed);
+	}
 }
 
 /* ------------------------------------------------------------ launchers */
@@ -894,7 +985,8 @@ void launchBigEntries(const DrawParams& P, uint32_t nJobs, cudaStream_t s)
 void launchLineFrags(const DrawParams& P, uint32_t nLines, cudaStream_t s)
 {
 	if (!nLines) return;
-	k_line_frags<<<(nLines + 3) / 4, 128, 0, s>>>(P, nLines);
+	k_line_frags<<<(nLines + 127) / 128, 128, 0, s>>>(P, nLines);
+	k_line_frags_long<<<152 * 8, 128, 0, s>>>(P);
 }
 
 }  // namespace srpg

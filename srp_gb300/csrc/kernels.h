@@ -24,6 +24,8 @@ struct DrawParams {
 	/* post-VS vertices: rows [0, nVertices) from the vertex shader, rows
 	 * [clipBase, clipBase + clipCap) created by clipping */
 	float4* clip;
+	float4* vset0;                 /* per vertex: ndc x, ndc y, screen x, screen y */
+	float4* vset1;                 /* per vertex: z_ndc/w, 1/w, z_ndc, outcode bits */
 	uint32_t* vary;
 	uint32_t clipBase, clipCap;
 	unsigned long long* minmax;    /* [0] min, [1] max vertex index referenced */

@@ -92,7 +92,7 @@ struct Lib {
 	SRPGpuFramebufferMode fbMode = SRP_GPU_FB_COHERENT;
 	Registry reg;
 	/* scratch pools, grown on demand */
-	DeviceBuffer clip, vary, triR, triA, lines, points, frags, keys, vals, keys2, vals2, big, lookback;
+	DeviceBuffer clip, vset0, vset1, vary, triR, triA, lines, points, frags, keys, vals, keys2, vals2, big, lookback;
 	DeviceBuffer hist, partials, tileStart, tileEnd, winner, minmax, ctr, table, heavy;
 	DeviceCounters* hostCtr = nullptr;
 	SRPGpuStats stats = {};
@@ -843,6 +843,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		const size_t nw = (size_t) std::max(P.L.nWords, 1);
 		const uint32_t blocks = (uint32_t) ((nIn + kSetupThreads - 1) / kSetupThreads);
 		bool ok = g.clip.reserve((size_t) rows * 16, FN) && g.vary.reserve((size_t) rows * nw * 4, FN) &&
+		          g.vset0.reserve((size_t) vb->nVertices * 16 + 16, FN) && g.vset1.reserve((size_t) vb->nVertices * 16 + 16, FN) &&
 		          g.lookback.reserve((size_t) std::max(blocks, 1u) * 8, FN) &&
 		          g.keys.reserve((size_t) entryCap * 4, FN) && g.vals.reserve((size_t) entryCap * 4, FN) &&
 		          g.big.reserve((size_t) g.bigCap * 16, FN) && g.table.reserve((size_t) g.tableCap * 4, FN);
@@ -853,6 +854,8 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		          g.frags.reserve((size_t) entryCap * sizeof(LineFrag), FN);
 		if (!ok) return;
 		P.clip = g.clip.as<float4>();
+		P.vset0 = g.vset0.as<float4>();
+		P.vset1 = g.vset1.as<float4>();
 		P.vary = g.vary.as<uint32_t>();
 		P.clipBase = (uint32_t) vb->nVertices;
 		P.clipCap = g.clipRows;
@@ -912,7 +915,17 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		const uint32_t E = (uint32_t) c.entries;
 		stageBegin();
 		int binLaunches = 0;
-		if (kind == kKindLineFrag) { launchLineFrags(P, (uint32_t) c.prims, g.stream); binLaunches += 1; }
+		if (kind == kKindLineFrag) {
+			/* the long-line queue reuses the big-job buffer: room for every line */
+			if (c.prims > g.bigCap) {
+				g.bigCap = (uint32_t) c.prims;
+				if (!g.big.reserve((size_t) g.bigCap * 16, FN)) return;
+				P.bigJobs = g.big.as<uint4>();
+				P.bigCap = g.bigCap;
+			}
+			launchLineFrags(P, (uint32_t) c.prims, g.stream);
+			binLaunches += 2;
+		}
 		else if (c.bigJobs) { launchBigEntries(P, (uint32_t) c.bigJobs, g.stream); binLaunches += 2; }
 		g.launches += binLaunches;
 		if (E == 0) { stageEnd(SRP_GPU_STAGE_BIN, binLaunches); break; }
@@ -926,14 +939,14 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		uint32_t* sv;
 		sortEntries(P, E, keyBits, g.keys2.as<uint32_t>(), g.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
 		            g.partials.as<uint32_t>(), &sk, &sv, g.stream);
-		g.launches += (keyBits / 8) * 5;
+		g.launches += 1 + keyBits / 8;
 		P.tileStart = g.tileStart.as<uint32_t>();
 		P.tileEnd = g.tileEnd.as<uint32_t>();
 		P.winner = g.winner.as<int32_t>();
 		cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, g.stream);
 		cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, g.stream);
 		launchTileRanges(P, sk, E, numTiles, g.stream);
-		stageEnd(SRP_GPU_STAGE_BIN, binLaunches + (int) (keyBits / 8) * 5 + 1);
+		stageEnd(SRP_GPU_STAGE_BIN, binLaunches + 1 + (int) (keyBits / 8) + 1);
 		const bool late = sp->fs->mayOverwriteDepth && shadeSupportsLateDepth(fsId);
 		g.profile.resolveTiles += numTiles;
 		g.profile.resolveItems += E;
