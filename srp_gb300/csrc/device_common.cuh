@@ -257,4 +257,37 @@ __device__ __forceinline__ float triRecip(const float iw[3], const float l[3])
 /* Bounded spin budget for waits on other blocks. */
 constexpr unsigned kSpinLimit = 1u << 24;
 
+/* Decoupled look-back over a status array whose words hold a 2-bit flag in
+ * the top bits (0 not yet published, 1 block aggregate, 2 inclusive prefix)
+ * and a value below. Starting at predecessor j, returns the sum of values up
+ * to and including the nearest inclusive prefix. W predecessors are loaded
+ * per step with independent loads, so a block that has to walk far back (all
+ * blocks of a wave finish their local work together) waits W times fewer
+ * load latencies. A predecessor that has not published yet is re-read with
+ * a bounded spin; on timeout the error bit is set and the walk ends. */
+template <typename T, int W>
+__device__ __forceinline__ T lookBack(const T* status, long long j, int flagShift, T valueMask, unsigned* errors)
+{
+	T acc = 0;
+	unsigned spins = 0;
+	while (j >= 0) {
+		T v[W];
+#pragma unroll
+		for (int k = 0; k < W; ++k)
+			v[k] = (j - k >= 0) ? *((volatile const T*) (status + (j - k))) : ((T) 2 << flagShift);
+#pragma unroll
+		for (int k = 0; k < W; ++k) {
+			while ((v[k] >> flagShift) == 0) {
+				if (++spins > kSpinLimit) { atomicOr(errors, kErrSpin); return acc; }
+				__nanosleep(32);
+				v[k] = *((volatile const T*) (status + (j - k)));
+			}
+			acc += v[k] & valueMask;
+			if ((v[k] >> flagShift) == 2) return acc;
+		}
+		j -= W;
+	}
+	return acc;
+}
+
 }  // namespace srpg

@@ -40,6 +40,31 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_global_hist(const uint32
 	}
 }
 
+/* Per-digit look-back: predecessor j's word for this digit is at j * 256. */
+__device__ __forceinline__ uint32_t lookBackStrided(const uint32_t* status, long long j, uint32_t* errors)
+{
+	constexpr int W = 8;
+	uint32_t acc = 0;
+	unsigned spins = 0;
+	while (j >= 0) {
+		uint32_t v[W];
+#pragma unroll
+		for (int k = 0; k < W; ++k) v[k] = (j - k >= 0) ? *((volatile const uint32_t*) (status + (j - k) * 256)) : (2u << 30);
+#pragma unroll
+		for (int k = 0; k < W; ++k) {
+			while ((v[k] >> 30) == 0) {
+				if (++spins > kSpinLimit) { atomicOr(errors, kErrSpin); return acc; }
+				__nanosleep(32);
+				v[k] = *((volatile const uint32_t*) (status + (j - k) * 256));
+			}
+			acc += v[k] & 0x3FFFFFFFu;
+			if ((v[k] >> 30) == 2) return acc;
+		}
+		j -= W;
+	}
+	return acc;
+}
+
 /* One stable LSD pass (OneSweep style). Blocks take 2048 consecutive keys in
  * ticket order; ranks inside the block come from warp match_any / popc prefix
  * counts over rounds that follow input order; each block publishes its 256
@@ -97,20 +122,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_onesweep(const uint32_t*
 			atomicExch(st, (2u << 30) | run);
 		} else {
 			atomicExch(st, (1u << 30) | run);
-			long long j = (long long) blk - 1;
-			unsigned spins = 0;
-			while (j >= 0) {
-				const uint32_t v = *((volatile uint32_t*) (status + (size_t) j * 256 + d));
-				const uint32_t flag = v >> 30;
-				if (flag == 0) {
-					if (++spins > kSpinLimit) { atomicOr(errors, kErrSpin); break; }
-					__nanosleep(32);
-					continue;
-				}
-				prefix += v & 0x3FFFFFFFu;
-				if (flag == 2) break;
-				--j;
-			}
+			prefix = lookBackStrided(status + d, (long long) blk - 1, errors);
 			atomicExch(st, (2u << 30) | (prefix + run));
 		}
 		/* start of digit d in the output: all smaller digits, then earlier blocks */

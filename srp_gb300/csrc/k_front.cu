@@ -721,22 +721,11 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
 			atomicExch(&P.lookback[0], packStatus(2, aggP, aggE));
 		} else {
 			atomicExch(&P.lookback[bid], packStatus(1, aggP, aggE));
-			long long j = (long long) bid - 1;
-			unsigned spins = 0;
-			unsigned long long accP = 0, accE = 0;
-			while (j >= 0) {
-				const unsigned long long s = *((volatile unsigned long long*) &P.lookback[j]);
-				const unsigned long long flag = s >> 62;
-				if (flag == 0) {
-					if (++spins > kSpinLimit) { atomicOr(&P.ctr->errors, kErrSpin); break; }
-					__nanosleep(32);
-					continue;
-				}
-				accP += (s >> 32) & 0x3FFFFFFFull;
-				accE += s & 0xFFFFFFFFull;
-				if (flag == 2) break;
-				--j;
-			}
+			/* prims (bits 32..61) and entries (bits 0..31) summed as one word:
+			 * the entry total stays below 2^32 (checked by the host) */
+			const unsigned long long acc = lookBack<unsigned long long, 16>(
+				P.lookback, (long long) bid - 1, 62, 0x3FFFFFFFFFFFFFFFull, &P.ctr->errors);
+			const unsigned long long accP = acc >> 32, accE = acc & 0xFFFFFFFFull;
 			if (accE + aggE > 0xFFFFFFFFull || accP + aggP > 0x3FFFFFFFull) atomicOr(&P.ctr->errors, kErrCapacity);
 			atomicExch(&P.lookback[bid], packStatus(2, (uint32_t) (accP + aggP), (uint32_t) (accE + aggE)));
 			prefix = (accP << 32) | (accE & 0xFFFFFFFFull);
