@@ -133,6 +133,7 @@ struct DeviceCounters {
 	unsigned long long lineFrags;
 	unsigned long long clipOverflow;
 	unsigned long long tableWords;   /* floats of lambda tables requested */
+	unsigned long long clipTris;     /* triangles clipped by the pre-pass */
 	unsigned int errors;             /* bit mask, see kErr* */
 	unsigned int lookbackTicket;
 	unsigned int nonEmptyTiles;

@@ -652,10 +652,16 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
 #pragma unroll
 					for (int i = 0; i < 3; ++i) as.sv[i] = loadSV(P, vi[i]);
 				} else {
+					/* clipped by k_clip_prepass: read back its polygon */
 					as.clipped = true;
-					PV in[3] = { loadPV(P, vi[0]), loadPV(P, vi[1]), loadPV(P, vi[2]) };
-					as.nPoly = clipPolygon(P, in, as.poly);
-					if (as.nPoly < 3) live = false;
+					const uint32_t slot = P.clipSlot[k];
+					if (slot >= P.clipPolyCap) { live = false; }
+					else {
+						const uint32_t* poly = P.clipPolys + (size_t) slot * (1 + kMaxPoly);
+						as.nPoly = (int) poly[0];
+						for (int i = 0; i < as.nPoly && i < kMaxPoly; ++i) as.poly[i] = loadPV(P, poly[1 + i]);
+						if (as.nPoly < 3) live = false;
+					}
 				}
 			}
 		}
@@ -769,6 +775,32 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
 		for (int f = 1; f + 1 < as.nPoly; ++f)
 			handleTriangle<MODE>(P, p0, fromClip(P.st, as.poly[f]), fromClip(P.st, as.poly[f + 1]), true, primBase, entBase);
 	}
+}
+
+/* Clipping of the triangles that straddle a frustum plane, ahead of the
+ * ordered setup: no ordering is needed to clip, so the long, divergent
+ * Sutherland-Hodgman path runs here instead of inside the scan-coupled setup
+ * blocks. The polygon (vertex count and vertex rows, new vertices included)
+ * goes to a slot that k_setup reads back. */
+__global__ void __launch_bounds__(kSetupThreads) k_clip_prepass(const __grid_constant__ DrawParams P)
+{
+	const long long k = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= P.nIn) return;
+	unsigned long long s[3];
+	uint32_t vi[3];
+	triStream(P.prim, P.start, (unsigned long long) k, s);
+	if (!(vertexIndex(P, s[0], vi[0]) && vertexIndex(P, s[1], vi[1]) && vertexIndex(P, s[2], vi[2]))) return;
+	const uint32_t c0 = vertexCode(P, vi[0]), c1 = vertexCode(P, vi[1]), c2 = vertexCode(P, vi[2]);
+	if ((c0 & c1 & c2) || (c0 | c1 | c2) == 0) return;
+	PV in[3] = { loadPV(P, vi[0]), loadPV(P, vi[1]), loadPV(P, vi[2]) };
+	PV poly[kMaxPoly];
+	const int n = clipPolygon(P, in, poly);
+	const unsigned long long slot = atomicAdd(&P.ctr->clipTris, 1ull);
+	if (slot >= P.clipPolyCap) { atomicOr(&P.ctr->errors, kErrCapacity); P.clipSlot[k] = 0xFFFFFFFFu; return; }
+	uint32_t* out = P.clipPolys + (size_t) slot * (1 + kMaxPoly);
+	out[0] = (uint32_t) n;
+	for (int i = 0; i < n; ++i) out[1 + i] = poly[i].ref;
+	P.clipSlot[k] = (uint32_t) slot;
 }
 
 /* Lambda table of a big triangle: for every bbox row and every tile column,
@@ -962,6 +994,12 @@ void launchSetup(const DrawParams& P, cudaStream_t s)
 	else if (tri) k_setup<kTriFill><<<blocks, kSetupThreads, 0, s>>>(P);
 	else if (P.prim == SRP_PRIM_POINTS) k_setup<kPoints><<<blocks, kSetupThreads, 0, s>>>(P);
 	else k_setup<kLines><<<blocks, kSetupThreads, 0, s>>>(P);
+}
+
+void launchClipPrepass(const DrawParams& P, cudaStream_t s)
+{
+	const unsigned blocks = (unsigned) ((P.nIn + kSetupThreads - 1) / kSetupThreads);
+	if (blocks) k_clip_prepass<<<blocks, kSetupThreads, 0, s>>>(P);
 }
 
 void launchBigEntries(const DrawParams& P, uint32_t nJobs, cudaStream_t s)

@@ -40,6 +40,11 @@ struct DrawParams {
 	uint32_t* keys;
 	uint32_t* vals;
 	uint32_t entryCap;
+	/* triangles that need clipping: the pre-pass stores their polygon
+	 * (count + vertex rows) and, per input triangle, its polygon slot */
+	uint32_t* clipSlot;            /* [nIn], written only for clipped triangles */
+	uint32_t* clipPolys;           /* [clipPolyCap][1 + kMaxPoly] */
+	uint32_t clipPolyCap;
 	uint4* bigJobs;                /* primitives covering many tiles */
 	uint32_t bigCap;
 	/* exact barycentrics of big triangles at every (row, tile column) start:
@@ -67,6 +72,7 @@ void launchReset(const DrawParams& P, cudaStream_t s);
 void launchIndexRange(const DrawParams& P, cudaStream_t s);
 void launchVertex(const DrawParams& P, unsigned long long first, unsigned long long n, cudaStream_t s);
 void launchSetup(const DrawParams& P, cudaStream_t s);
+void launchClipPrepass(const DrawParams& P, cudaStream_t s);
 void launchBigEntries(const DrawParams& P, uint32_t nJobs, cudaStream_t s);
 void launchLineFrags(const DrawParams& P, uint32_t nLines, cudaStream_t s);
 /* k_bin.cu */

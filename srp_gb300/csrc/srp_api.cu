@@ -93,7 +93,7 @@ struct Lib {
 	Registry reg;
 	/* scratch pools, grown on demand */
 	DeviceBuffer clip, vset0, vset1, vary, triR, triA, lines, points, frags, keys, vals, keys2, vals2, big, lookback;
-	DeviceBuffer hist, partials, tileStart, tileEnd, winner, minmax, ctr, table, heavy;
+	DeviceBuffer hist, partials, tileStart, tileEnd, winner, minmax, ctr, table, heavy, clipSlot, clipPolys;
 	DeviceCounters* hostCtr = nullptr;
 	SRPGpuStats stats = {};
 	unsigned long long launches = 0;
@@ -106,6 +106,7 @@ struct Lib {
 	SRPGpuProfile profile = {};
 	cudaEvent_t openEvent = nullptr;
 	unsigned long long tableCap = 1ull << 22;  /* floats */
+	uint32_t clipPolyCap = 1 << 14;
 	double entryRatio = 4.0;
 };
 
@@ -846,7 +847,9 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		          g.vset0.reserve((size_t) vb->nVertices * 16 + 16, FN) && g.vset1.reserve((size_t) vb->nVertices * 16 + 16, FN) &&
 		          g.lookback.reserve((size_t) std::max(blocks, 1u) * 8, FN) &&
 		          g.keys.reserve((size_t) entryCap * 4, FN) && g.vals.reserve((size_t) entryCap * 4, FN) &&
-		          g.big.reserve((size_t) g.bigCap * 16, FN) && g.table.reserve((size_t) g.tableCap * 4, FN);
+		          g.big.reserve((size_t) g.bigCap * 16, FN) && g.table.reserve((size_t) g.tableCap * 4, FN) &&
+		          g.clipSlot.reserve((size_t) nIn * 4 + 4, FN) &&
+		          g.clipPolys.reserve((size_t) g.clipPolyCap * (1 + kMaxPoly) * 4, FN);
 		if (kind == kKindTri) ok = ok && g.triR.reserve((size_t) primCap * sizeof(TriRaster), FN) &&
 		                           g.triA.reserve((size_t) primCap * sizeof(TriAttr), FN);
 		else if (kind == kKindPoint) ok = ok && g.points.reserve((size_t) primCap * sizeof(PointRec), FN);
@@ -872,6 +875,9 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		P.bigJobs = g.big.as<uint4>();
 		P.bigCap = g.bigCap;
 		P.table = g.table.as<float>();
+		P.clipSlot = g.clipSlot.as<uint32_t>();
+		P.clipPolys = g.clipPolys.as<uint32_t>();
+		P.clipPolyCap = g.clipPolyCap;
 		P.tableCap = g.tableCap;
 		P.lookback = g.lookback.as<unsigned long long>();
 
@@ -883,9 +889,10 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		stageEnd(SRP_GPU_STAGE_VERTEX, ib ? 3 : 2);
 		stageBegin();
 		cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, g.stream);
+		if (isTri(prim)) launchClipPrepass(P, g.stream);
 		launchSetup(P, g.stream);
-		stageEnd(SRP_GPU_STAGE_SETUP, 1);
-		g.launches += 3 + (ib ? 1 : 0);
+		stageEnd(SRP_GPU_STAGE_SETUP, isTri(prim) ? 2 : 1);
+		g.launches += 3 + (ib ? 1 : 0) + (isTri(prim) ? 1 : 0);
 		if (!cudaOk(cudaGetLastError(), FN, "launch") || !readCounters()) return;
 		const DeviceCounters c = *g.hostCtr;
 		if (c.errors & kErrBadIndex) {
@@ -897,13 +904,14 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		 * overflow, whichever kernel met it, shows up as a count above the
 		 * buffer it was meant for */
 		const bool over = c.clipVerts > g.clipRows || c.prims > primCap || c.entries > entryCap || c.bigJobs > g.bigCap ||
-		                  c.tableWords > g.tableCap;
+		                  c.tableWords > g.tableCap || c.clipTris > g.clipPolyCap;
 		if ((c.errors & kErrCapacity) || over) {
 			bool grew = false;
 			if (c.clipVerts > g.clipRows) { g.clipRows = (uint32_t) std::min<unsigned long long>(c.clipVerts * 2, 0x7FFFFFFF); grew = true; }
 			if (c.prims > primCap) { primCap = (uint32_t) std::min<unsigned long long>(c.prims + 1024, 0x3FFFFFFF); grew = true; }
 			if (c.entries > entryCap) { entryCap = (uint32_t) std::min<double>(c.entries * 1.25 + 1024, 4.0e9); grew = true; }
 			if (c.bigJobs > g.bigCap) { g.bigCap = (uint32_t) std::min<unsigned long long>(c.bigJobs * 2, 1u << 30); grew = true; }
+			if (c.clipTris > g.clipPolyCap) { g.clipPolyCap = (uint32_t) std::min<unsigned long long>(c.clipTris * 2, 1u << 30); grew = true; }
 			if (c.tableWords > g.tableCap) { g.tableCap = std::min<unsigned long long>(c.tableWords * 5 / 4 + 1024, 0xFFFFFFFFull); grew = true; }
 			if (!grew) { SRP_ERROR(FN, "Scratch capacity exceeded"); return; }
 			continue;
