@@ -207,9 +207,18 @@ __global__ void __launch_bounds__(kVertexThreads) k_vertex(const __grid_constant
 	runVS<VS>(&in, &o);
 	const float4 clip = make_float4(o.clipPosition[0], o.clipPosition[1], o.clipPosition[2], o.clipPosition[3]);
 	P.clip[v] = clip;
-	const VSet vs = vertexSetup(P.st, clip);
-	P.vset0[v] = make_float4(vs.nx, vs.ny, vs.sx, vs.sy);
-	P.vset1[v] = make_float4(vs.c, vs.iw, vs.nz, __uint_as_float(outcode(clip)));
+	/* setup data is read only for vertices inside the frustum (outcode 0):
+	 * every primitive with an outside vertex is rejected or re-derived from
+	 * clip coordinates, so the divide and the double-precision viewport step
+	 * are skipped for outside vertices */
+	const uint32_t code = outcode(clip);
+	if (code == 0) {
+		const VSet vs = vertexSetup(P.st, clip);
+		P.vset0[v] = make_float4(vs.nx, vs.ny, vs.sx, vs.sy);
+		P.vset1[v] = make_float4(vs.c, vs.iw, vs.nz, __uint_as_float(0u));
+	} else {
+		P.vset1[v] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(code));
+	}
 	const int nw = P.L.nWords;
 	uint32_t* dst = P.vary + v * (unsigned long long) nw;
 #pragma unroll

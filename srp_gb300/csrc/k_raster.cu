@@ -201,6 +201,60 @@ __device__ __forceinline__ void coverage(const DrawParams& P, uint32_t item, int
 	}
 }
 
+/* Tile-relative span of triangle R over the tile at (x0, y0): columns
+ * [xs, xe), first row ys, packed 4 bits each; returns the number of rows. */
+__device__ __forceinline__ uint32_t triSpan(const TriRaster& R, int x0, int y0, uint32_t& span)
+{
+	const int xs = max(x0, (int) R.minX), xe = min(x0 + kTile, (int) R.maxX);
+	const int ys = max(y0, (int) R.minY), ye = min(y0 + kTile, (int) R.maxY);
+	span = 0;
+	if (xs >= xe || ys >= ye) return 0;
+	span = (uint32_t) (xs - x0) | (uint32_t) (xe - x0) << 4 | (uint32_t) (ys - y0) << 8;
+	return (uint32_t) (ye - ys);
+}
+
+/* One row of a triangle inside a tile: barycentrics at the first column
+ * (big-triangle table, or the exact chain l0 -> row -> column), then the
+ * reference's per-pixel steps. Sets the covered bits and stores the depths. */
+__device__ __forceinline__ unsigned long long triRow(const DrawParams& P, const TriRaster& R, int x0, int y0, int xs,
+                                                     int xe, int y, float* dep)
+{
+	float l[3];
+	if (R.table != kNoTable) {
+		const int ncols = ((int) R.maxX - 1) / kTile - (int) R.minX / kTile + 1;
+		const float* T = P.table + R.table + 3 * ((size_t) (y - R.minY) * ncols + (x0 / kTile - (int) R.minX / kTile));
+		l[0] = T[0]; l[1] = T[1]; l[2] = T[2];
+	} else {
+#pragma unroll
+		for (int i = 0; i < 3; ++i)
+			l[i] = srpChainAdd(srpChainAdd(R.l0[i], R.dy[i], (uint32_t) (y - R.minY)), R.dx[i], (uint32_t) (xs - R.minX));
+	}
+	unsigned long long bits = 0;
+	for (int x = xs; x < xe; ++x) {
+		if (insideTri(l, R.flags)) {
+			const int q = (y - y0) * kTile + (x - x0);
+			bits |= 1ull << q;
+			dep[q] = triDepth(R.c, l);
+		}
+#pragma unroll
+		for (int i = 0; i < 3; ++i) l[i] = __fadd_rn(l[i], R.dx[i]);
+	}
+	return bits;
+}
+
+/* Index of the item owning flattened row p: the last j with off[j] <= p
+ * (items without rows share their successor's offset and are skipped). */
+template <int N>
+__device__ __forceinline__ int findOwner(const uint32_t* off, uint32_t p)
+{
+	int lo = 0, hi = N;
+	while (hi - lo > 1) {
+		const int mid = (lo + hi) >> 1;
+		if (off[mid] <= p) lo = mid; else hi = mid;
+	}
+	return lo;
+}
+
 /* LATE_FS = 0: early depth test, colour deferred to k_shade.
  * LATE_FS = a fragment shader id: the shader runs per fragment in order and
  * may replace the depth (src/raster/fragment.c:97-111). */
@@ -212,6 +266,9 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(const __grid_con
 	__shared__ uint32_t sItem[kResolveWarps][32];
 	__shared__ uint32_t sFlag[kResolveWarps][32];
 	__shared__ float sDep[kResolveWarps][32][kDepRow];
+	__shared__ TriRaster sRec[KIND == kKindTri ? kResolveWarps : 1][32];
+	__shared__ uint32_t sOff[kResolveWarps][32];
+	__shared__ uint32_t sSpan[kResolveWarps][32];
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const uint32_t tile = blockIdx.x * kResolveWarps + warp;
 	if (tile >= numTiles) return;
@@ -246,11 +303,44 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(const __grid_con
 		const uint32_t n = min(32u, e - b);
 		unsigned long long mask = 0;
 		uint32_t item = 0, flags = 0;
-		if ((uint32_t) lane < n) {
-			item = vals[b + lane];
-			coverage<KIND>(P, item, x0, y0, mask, sDep[warp][lane], flags);
+		if (KIND == kKindTri) {
+			/* triangles: coverage over flattened (item, row) pairs so that the
+			 * lanes share the work whatever the items' sizes */
+			uint32_t rows = 0, span = 0;
+			if ((uint32_t) lane < n) {
+				item = vals[b + lane];
+				const TriRaster R = P.triR[item];
+				sRec[warp][lane] = R;
+				flags = R.flags;
+				rows = triSpan(R, x0, y0, span);
+			}
+			uint32_t incl = rows;
+#pragma unroll
+			for (int o = 1; o < 32; o <<= 1) {
+				const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+				if (lane >= o) incl += y;
+			}
+			const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+			sOff[warp][lane] = incl - rows;
+			sSpan[warp][lane] = span;
+			sMask[warp][lane] = 0;
+			__syncwarp();
+			for (uint32_t pr = lane; pr < total; pr += 32) {
+				const int j = findOwner<32>(sOff[warp], pr);
+				const uint32_t sp = sSpan[warp][j];
+				const int xs = x0 + (int) (sp & 15u), xe = x0 + (int) ((sp >> 4) & 15u);
+				const int y = y0 + (int) ((sp >> 8) & 15u) + (int) (pr - sOff[warp][j]);
+				const unsigned long long bits = triRow(P, sRec[warp][j], x0, y0, xs, xe, y, sDep[warp][j]);
+				if (bits) atomicOr(&sMask[warp][j], bits);
+			}
+			__syncwarp();
+		} else {
+			if ((uint32_t) lane < n) {
+				item = vals[b + lane];
+				coverage<KIND>(P, item, x0, y0, mask, sDep[warp][lane], flags);
+			}
+			sMask[warp][lane] = mask;
 		}
-		sMask[warp][lane] = mask;
 		sItem[warp][lane] = item;
 		sFlag[warp][lane] = flags;
 		__syncwarp();
@@ -340,6 +430,9 @@ __global__ void __launch_bounds__(kHeavyThreads) k_resolve_heavy(const __grid_co
 	extern __shared__ float hDep[];                 /* [kHeavyThreads][kDepRow] */
 	__shared__ uint32_t ballots[kHeavyThreads / 32][64];
 	__shared__ uint32_t hFlag[kHeavyThreads], hItem[kHeavyThreads];
+	__shared__ unsigned long long hMask[kHeavyThreads];
+	__shared__ uint32_t hOff[kHeavyThreads], hSpan[kHeavyThreads], hWarpSum[kHeavyThreads / 32 + 1];
+	__shared__ TriRaster hRec[KIND == kKindTri ? kHeavyThreads : 1];
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	const DrawState& st = P.st;
 	const uint32_t nHeavy = P.ctr->nonEmptyTiles;
@@ -360,7 +453,46 @@ __global__ void __launch_bounds__(kHeavyThreads) k_resolve_heavy(const __grid_co
 			const uint32_t n = min((uint32_t) kHeavyThreads, e - b);
 			unsigned long long mask = 0;
 			uint32_t item = 0, flags = 0;
-			if ((uint32_t) tid < n) {
+			if (KIND == kKindTri) {
+				/* flattened (item, row) pairs over the whole block */
+				uint32_t rows = 0, span = 0;
+				if ((uint32_t) tid < n) {
+					item = vals[b + tid];
+					const TriRaster R = P.triR[item];
+					hRec[tid] = R;
+					flags = R.flags;
+					rows = triSpan(R, x0, y0, span);
+				}
+				uint32_t incl = rows;
+#pragma unroll
+				for (int o = 1; o < 32; o <<= 1) {
+					const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+					if (lane >= o) incl += y;
+				}
+				if (lane == 31) hWarpSum[warp] = incl;
+				hMask[tid] = 0;
+				hSpan[tid] = span;
+				__syncthreads();
+				if (tid == 0) {
+					uint32_t run = 0;
+					for (int w = 0; w < kHeavyThreads / 32; ++w) { const uint32_t t = hWarpSum[w]; hWarpSum[w] = run; run += t; }
+					hWarpSum[kHeavyThreads / 32] = run;
+				}
+				__syncthreads();
+				hOff[tid] = hWarpSum[warp] + incl - rows;
+				const uint32_t total = hWarpSum[kHeavyThreads / 32];
+				__syncthreads();
+				for (uint32_t pr = tid; pr < total; pr += kHeavyThreads) {
+					const int j = findOwner<kHeavyThreads>(hOff, pr);
+					const uint32_t sp = hSpan[j];
+					const int xs = x0 + (int) (sp & 15u), xe = x0 + (int) ((sp >> 4) & 15u);
+					const int y = y0 + (int) ((sp >> 8) & 15u) + (int) (pr - hOff[j]);
+					const unsigned long long bits = triRow(P, hRec[j], x0, y0, xs, xe, y, hDep + j * kDepRow);
+					if (bits) atomicOr(&hMask[j], bits);
+				}
+				__syncthreads();
+				mask = hMask[tid];
+			} else if ((uint32_t) tid < n) {
 				item = vals[b + tid];
 				coverage<KIND>(P, item, x0, y0, mask, hDep + tid * kDepRow, flags);
 			}
@@ -445,7 +577,7 @@ static void launchHeavy(const DrawParams& P, const uint32_t* vals, uint32_t* hea
 {
 	const int smem = kHeavyThreads * kDepRow * 4;
 	cudaFuncSetAttribute(k_resolve_heavy<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-	k_resolve_heavy<KIND><<<152 * 3, kHeavyThreads, smem, s>>>(P, vals, heavy);
+	k_resolve_heavy<KIND><<<152 * 2, kHeavyThreads, smem, s>>>(P, vals, heavy);
 }
 
 void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, uint32_t* heavy, cudaStream_t s)
