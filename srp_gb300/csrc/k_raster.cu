@@ -129,14 +129,27 @@ __device__ __forceinline__ void shadeItem(const DrawParams& P, uint32_t item, in
 	runFS<FS>(&in, &out);
 }
 
-/* Phase 1: coverage of one item over the tile at (x0, y0). */
+/* Record of an item, by kind (loaded ahead of use by k_resolve_heavy). */
+template <int KIND> struct RecOf { typedef TriRaster T; };
+template <> struct RecOf<kKindPoint> { typedef PointRec T; };
+template <> struct RecOf<kKindLineFrag> { typedef LineFrag T; };
+
 template <int KIND>
-__device__ __forceinline__ void coverage(const DrawParams& P, uint32_t item, int x0, int y0,
-                                         unsigned long long& mask, float* dep, uint32_t& flags)
+__device__ __forceinline__ typename RecOf<KIND>::T loadRec(const DrawParams& P, uint32_t item)
+{
+	if constexpr (KIND == kKindTri) return P.triR[item];
+	else if constexpr (KIND == kKindPoint) return P.points[item];
+	else return P.frags[item];
+}
+
+/* Phase 1: coverage of one item (its record) over the tile at (x0, y0). */
+template <int KIND>
+__device__ __forceinline__ void coverageRec(const DrawParams& P, const typename RecOf<KIND>::T& Rec, int x0, int y0,
+                                            unsigned long long& mask, float* dep, uint32_t& flags)
 {
 	mask = 0;
-	if (KIND == kKindTri) {
-		const TriRaster R = P.triR[item];
+	if constexpr (KIND == kKindTri) {
+		const TriRaster& R = Rec;
 		flags = R.flags;
 		const int xs = max(x0, (int) R.minX), xe = min(x0 + kTile, (int) R.maxX);
 		const int ys = max(y0, (int) R.minY), ye = min(y0 + kTile, (int) R.maxY);
@@ -177,8 +190,8 @@ __device__ __forceinline__ void coverage(const DrawParams& P, uint32_t item, int
 				for (int i = 0; i < 3; ++i) lr[i] = __fadd_rn(lr[i], R.dy[i]);
 			}
 		}
-	} else if (KIND == kKindPoint) {
-		const PointRec R = P.points[item];
+	} else if constexpr (KIND == kKindPoint) {
+		const PointRec& R = Rec;
 		flags = 1u;
 		const int xs = max(x0, (int) R.x0), xe = min(x0 + kTile - 1, (int) R.x1);
 		const int ys = max(y0, (int) R.y0), ye = min(y0 + kTile - 1, (int) R.y1);
@@ -191,7 +204,7 @@ __device__ __forceinline__ void coverage(const DrawParams& P, uint32_t item, int
 				dep[q] = R.z;
 			}
 	} else {
-		const LineFrag F = P.frags[item];
+		const LineFrag& F = Rec;
 		flags = 1u;
 		const unsigned long long idx = (unsigned long long) (long long) F.py * (unsigned long long) P.st.W
 		                             + (unsigned long long) (long long) F.px;
@@ -199,6 +212,13 @@ __device__ __forceinline__ void coverage(const DrawParams& P, uint32_t item, int
 		const int q = (gy - y0) * kTile + (gx - x0);
 		if (q >= 0 && q < 64) { mask = 1ull << q; dep[q] = F.depth; }
 	}
+}
+
+template <int KIND>
+__device__ __forceinline__ void coverage(const DrawParams& P, uint32_t item, int x0, int y0,
+                                         unsigned long long& mask, float* dep, uint32_t& flags)
+{
+	coverageRec<KIND>(P, loadRec<KIND>(P, item), x0, y0, mask, dep, flags);
 }
 
 /* Tile-relative span of triangle R over the tile at (x0, y0): columns
@@ -430,9 +450,7 @@ __global__ void __launch_bounds__(kHeavyThreads) k_resolve_heavy(const __grid_co
 	extern __shared__ float hDep[];                 /* [kHeavyThreads][kDepRow] */
 	__shared__ uint32_t ballots[kHeavyThreads / 32][64];
 	__shared__ uint32_t hFlag[kHeavyThreads], hItem[kHeavyThreads];
-	__shared__ unsigned long long hMask[kHeavyThreads];
-	__shared__ uint32_t hOff[kHeavyThreads], hSpan[kHeavyThreads], hWarpSum[kHeavyThreads / 32 + 1];
-	__shared__ TriRaster hRec[KIND == kKindTri ? kHeavyThreads : 1];
+
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	const DrawState& st = P.st;
 	const uint32_t nHeavy = P.ctr->nonEmptyTiles;
@@ -449,52 +467,21 @@ __global__ void __launch_bounds__(kHeavyThreads) k_resolve_heavy(const __grid_co
 		int32_t win = -1;
 		const bool ok = valid && (KIND == kKindLineFrag || scissorPass(st, gx, gy));
 		unsigned long long frags = 0;
+		uint32_t curItem = 0;
+		typename RecOf<KIND>::T cur = {};
+		if (s + tid < e) { curItem = vals[s + tid]; cur = loadRec<KIND>(P, curItem); }
 		for (uint32_t b = s; b < e; b += kHeavyThreads) {
 			const uint32_t n = min((uint32_t) kHeavyThreads, e - b);
 			unsigned long long mask = 0;
 			uint32_t item = 0, flags = 0;
-			if (KIND == kKindTri) {
-				/* flattened (item, row) pairs over the whole block */
-				uint32_t rows = 0, span = 0;
-				if ((uint32_t) tid < n) {
-					item = vals[b + tid];
-					const TriRaster R = P.triR[item];
-					hRec[tid] = R;
-					flags = R.flags;
-					rows = triSpan(R, x0, y0, span);
-				}
-				uint32_t incl = rows;
-#pragma unroll
-				for (int o = 1; o < 32; o <<= 1) {
-					const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-					if (lane >= o) incl += y;
-				}
-				if (lane == 31) hWarpSum[warp] = incl;
-				hMask[tid] = 0;
-				hSpan[tid] = span;
-				__syncthreads();
-				if (tid == 0) {
-					uint32_t run = 0;
-					for (int w = 0; w < kHeavyThreads / 32; ++w) { const uint32_t t = hWarpSum[w]; hWarpSum[w] = run; run += t; }
-					hWarpSum[kHeavyThreads / 32] = run;
-				}
-				__syncthreads();
-				hOff[tid] = hWarpSum[warp] + incl - rows;
-				const uint32_t total = hWarpSum[kHeavyThreads / 32];
-				__syncthreads();
-				for (uint32_t pr = tid; pr < total; pr += kHeavyThreads) {
-					const int j = findOwner<kHeavyThreads>(hOff, pr);
-					const uint32_t sp = hSpan[j];
-					const int xs = x0 + (int) (sp & 15u), xe = x0 + (int) ((sp >> 4) & 15u);
-					const int y = y0 + (int) ((sp >> 8) & 15u) + (int) (pr - hOff[j]);
-					const unsigned long long bits = triRow(P, hRec[j], x0, y0, xs, xe, y, hDep + j * kDepRow);
-					if (bits) atomicOr(&hMask[j], bits);
-				}
-				__syncthreads();
-				mask = hMask[tid];
-			} else if ((uint32_t) tid < n) {
-				item = vals[b + tid];
-				coverage<KIND>(P, item, x0, y0, mask, hDep + tid * kDepRow, flags);
+			if ((uint32_t) tid < n) {
+				item = curItem;
+				coverageRec<KIND>(P, cur, x0, y0, mask, hDep + tid * kDepRow, flags);
+			}
+			/* prefetch the next chunk's item while this one is resolved */
+			if (b + kHeavyThreads + tid < e) {
+				curItem = vals[b + kHeavyThreads + tid];
+				cur = loadRec<KIND>(P, curItem);
 			}
 			hFlag[tid] = flags;
 			hItem[tid] = item;
@@ -577,7 +564,7 @@ static void launchHeavy(const DrawParams& P, const uint32_t* vals, uint32_t* hea
 {
 	const int smem = kHeavyThreads * kDepRow * 4;
 	cudaFuncSetAttribute(k_resolve_heavy<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-	k_resolve_heavy<KIND><<<152 * 2, kHeavyThreads, smem, s>>>(P, vals, heavy);
+	k_resolve_heavy<KIND><<<152 * 3, kHeavyThreads, smem, s>>>(P, vals, heavy);
 }
 
 void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, uint32_t* heavy, cudaStream_t s)
