@@ -55,6 +55,57 @@ void srpGpuFramebufferUpload(const SRPFramebuffer* fb);
 void srpGpuFramebufferFill(const SRPFramebuffer* fb, uint32_t color, float depth, uint8_t stencil,
                            unsigned planes);
 
+/* ------------------------------------------------- fixed-scratch draw */
+
+/** Size of the device array that srpGpuDrawFixedScratch takes its scratch
+ *  from (64 MiB). */
+#define SRP_GPU_FIXED_SCRATCH_BYTES (64u << 20)
+
+/** A draw that allocates nothing. It has no counterpart in kitrofimov/srp.
+ *
+ *  Arguments and result are those of srpDrawIndexBuffer (ib not NULL) or
+ *  srpDrawVertexBuffer (ib NULL), computed by the same kernels. The ordinary
+ *  draws grow their scratch buffers with cudaMalloc and cudaFree whenever a
+ *  draw needs more than the draws before it. This one takes every scratch
+ *  buffer from one array of SRP_GPU_FIXED_SCRATCH_BYTES in device memory
+ *  that belongs to the library's device image, and calls no allocating
+ *  routine. It is meant for callers that cannot have device memory allocated
+ *  or freed in the middle of a frame: cudaFree waits for all work on the
+ *  device, which stalls a renderer whose other streams must keep running,
+ *  and a program that has given the rest of device memory to a caching
+ *  allocator or to other processes may see a mid-frame allocation fail.
+ *
+ *  The first call on a device looks up the array's address (with that device
+ *  current; the lookup loads the part of the library's device image that
+ *  holds the array) and keeps it for later calls. Make that first call before
+ *  any stream capture begins. Vertex and index buffers must already be in
+ *  device memory, as srpVertexBufferCopyData / srpIndexBufferCopyData leave
+ *  them when a GPU is present.
+ *
+ *  Limits. The parts of the scratch sized by the vertex buffer (about 64
+ *  bytes and 4 per varying word per vertex), by the primitives (up to 96
+ *  bytes each) and by the framebuffer (about 4 bytes per pixel) must leave at
+ *  least 4 MiB of the array free; this is checked before anything runs. What
+ *  the draw produces is checked once the setup stage has counted it: tile
+ *  entries (about 16 bytes each, 32 for lines) in three quarters of what is
+ *  left, barycentric tables of large triangles in the other quarter, at most
+ *  16384 vertices created by clipping and 4096 triangles that need clipping.
+ *  A draw beyond a limit is rejected: it returns -1, says which size was too
+ *  large through the message callback and leaves the framebuffer unchanged.
+ *
+ *  Every call uses the same array. Each call clears, on the library's
+ *  stream, the parts that must start at zero (counters, look-back flags,
+ *  tile ranges, sort histograms) before using them, so calls in sequence on
+ *  one stream are independent. Calls that overlap on the GPU (issued on
+ *  different streams, or from several host threads) race on the array and
+ *  give wrong images. Fragments of these draws are not added to the
+ *  srpGpuGetStats fragment count, and stage profiling does not time them.
+ *
+ *  Returns 0 when the draw ran or had nothing to draw, -1 when it was
+ *  rejected or a CUDA call failed. */
+int srpGpuDrawFixedScratch(const SRPIndexBuffer* ib, const SRPVertexBuffer* vb, const SRPFramebuffer* fb,
+                           const SRPShaderProgram* sp, SRPPrimitive prim, size_t startIndex, size_t count);
+
 /* ------------------------------------------------------ stream, stats */
 
 /** Launch all work on `stream` (a cudaStream_t; NULL = the library's own

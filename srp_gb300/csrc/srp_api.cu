@@ -1109,3 +1109,173 @@ void srpGpuSetTileSize(int tileSize)
 }
 
 }  // extern "C"
+
+/* ------------------------------------------- for the fixed-scratch draw */
+
+#include "draw_internal.h"
+
+namespace srpg {
+
+int fixedDrawPrepare(DrawParams& P, const SRPIndexBuffer* ib, const SRPVertexBuffer* vb, const SRPFramebuffer* fb,
+                     const SRPShaderProgram* sp, SRPPrimitive prim, size_t start, size_t count, FixedDrawInfo& info)
+{
+	const char* FN = "srpGpuDrawFixedScratch";
+	/* validation and early returns of drawBuffer (src/pipeline/draw.c:63-82) */
+	if (count == 0) return 1;
+	const size_t end = start + count - 1;
+	const size_t size = ib ? ib->nIndices : vb->nVertices;
+	if (end >= size) {
+		SRP_ERROR("checkOOB", ib ? "Attempt to OOB access index buffer (read) at indices %zu-%zu (size: %zu)\n"
+		                         : "Attempt to OOB access vertex buffer (read) at indices %zu-%zu (size: %zu)\n",
+		          start, end, size);
+		return -1;
+	}
+	size_t nIn = 0;
+	if (isTri(prim)) {
+		if (srpContext.raster.cullFace == SRP_FACE_FRONT_AND_BACK) return 1;
+		warnExcess(prim, count);
+		nIn = prim == SRP_PRIM_TRIANGLES ? count / 3 : (count >= 3 ? count - 2 : 0);
+		if (srpContext.raster.polygonMode != SRP_POLYGON_MODE_FILL && srpContext.raster.polygonMode != SRP_POLYGON_MODE_LINE &&
+		    srpContext.raster.polygonMode != SRP_POLYGON_MODE_POINT) {
+			SRP_ERROR("assembleTrianglesGeneric", "Unexpected srpContext.raster.polygonMode (%i)", (int) srpContext.raster.polygonMode);
+			return -1;
+		}
+	} else if (isLine(prim)) {
+		warnExcess(prim, count);
+		nIn = prim == SRP_PRIM_LINES ? count / 2 : (count != 1 ? (prim == SRP_PRIM_LINE_STRIP ? count - 1 : count) : 0);
+	} else if (prim == SRP_PRIM_POINTS) {
+		if (srpContext.raster.pointSize <= 0.) return 1;
+		nIn = count;
+	} else {
+		SRP_ERROR("drawBuffer", "Unknown primitive type: %i", (int) prim);
+		return -1;
+	}
+	if (nIn == 0) return 1;
+	if (nIn > 0x7FFFFFFFull) { SRP_ERROR(FN, "Draw too large for the GPU path (%zu primitives)", nIn); return -1; }
+	/* what the ordinary draw would set up by allocating */
+	if (!g.init) { SRP_ERROR(FN, "The library is not initialised: create the framebuffer with srpNewFramebuffer first"); return -1; }
+	FbExtra* fx = fbFind(fb);
+	if (!fx) { SRP_ERROR(FN, "Framebuffer was not created by srpNewFramebuffer"); return -1; }
+	if (vb->dirty || (!vb->dev.ptr && vb->nBytes)) {
+		SRP_ERROR(FN, "Vertex buffer is not in device memory (its data was copied while no GPU was usable)");
+		return -1;
+	}
+	if (ib && (ib->dirty || (!ib->dev.ptr && ib->nBytes))) {
+		SRP_ERROR(FN, "Index buffer is not in device memory (its data was copied while no GPU was usable)");
+		return -1;
+	}
+	const int vsId = lookupVS((void*) sp->vs->shader);
+	const int fsId = lookupFS((void*) sp->fs->shader);
+	if (!vsId || !fsId) {
+		SRP_ERROR(FN, "Shader has no GPU implementation; map it with srpGpuRegisterVertexShader/FragmentShader");
+		return -1;
+	}
+	if (vb->stride == 0 || vb->stride > 1024) {
+		SRP_ERROR(FN, "GPU path supports vertex strides of 1..1024 bytes (got %zu)", vb->stride);
+		return -1;
+	}
+	memset(&P, 0, sizeof P);
+	if (!buildLayout(sp->vs, P.L)) return -1;
+	/* state snapshot, as in runDraw */
+	DrawState& st = P.st;
+	st.W = (int) fb->width; st.H = (int) fb->height;
+	st.frontFaceCW = srpContext.raster.frontFace == SRP_WINDING_CW;
+	st.cullFace = srpContext.raster.cullFace;
+	st.polygonMode = srpContext.raster.polygonMode;
+	st.pointSize = srpContext.raster.pointSize;
+	st.provokingFirst = srpContext.provokingVertexMode == SRP_PROVOKING_VERTEX_FIRST;
+	st.scissorEnabled = srpContext.scissor.enabled;
+	st.sx0 = srpContext.scissor.x; st.sx1 = srpContext.scissor.x + srpContext.scissor.width;
+	st.sy0 = srpContext.scissor.y; st.sy1 = srpContext.scissor.y + srpContext.scissor.height;
+	st.stencilEnabled = srpContext.stencil.enabled;
+	const SRPStencilFaceState* fsrc[2] = { &srpContext.stencil.front, &srpContext.stencil.back };
+	StencilFace* fdst[2] = { &st.front, &st.back };
+	for (int i = 0; i < 2; ++i) {
+		fdst[i]->func = fsrc[i]->func; fdst[i]->sfail = fsrc[i]->sfailOp; fdst[i]->dfail = fsrc[i]->dfailOp;
+		fdst[i]->pass = fsrc[i]->passOp; fdst[i]->ref = fsrc[i]->ref; fdst[i]->mask = fsrc[i]->mask;
+		fdst[i]->writeMask = fsrc[i]->writeMask;
+	}
+	st.depthTest = srpContext.depth.testEnable;
+	st.depthWrite = srpContext.depth.writeEnable;
+	st.depthOp = srpContext.depth.compareOp;
+	st.earlyZ = !sp->fs->mayOverwriteDepth;
+	st.tile = kTile;
+	st.tilesX = (st.W + kTile - 1) / kTile;
+	st.tilesY = (st.H + kTile - 1) / kTile;
+	if (sp->uniform) {
+		SRPStdUniform u;
+		memcpy(&u, sp->uniform, sizeof u);
+		if (u.texture) {
+			SRPTexture* t = u.texture;
+			/* textures get their device texels when they are created */
+			if (!t->texels || !t->desc) { SRP_ERROR(FN, "Texture has no device texels"); return -1; }
+			if (!textureSync(t)) return -1;
+			u.texture = (SRPTexture*) t->desc;
+		}
+		memcpy(P.uniform, &u, sizeof u);
+	}
+	P.vsId = vsId;
+	P.fsId = fsId;
+	P.prim = prim;
+	P.start = start;
+	P.count = count;
+	P.nIn = (int) nIn;
+	P.vertices = vb->dev.as<unsigned char>();
+	P.nVertices = vb->nVertices;
+	P.stride = (int) vb->stride;
+	if (ib) {
+		if (ib->type != SRP_UINT8 && ib->type != SRP_UINT16 && ib->type != SRP_UINT32 && ib->type != SRP_UINT64) {
+			SRP_ERROR("indexIndexBuffer", "Unexpected type (%i)", (int) ib->type);
+			return -1;
+		}
+		P.indices = ib->dev.ptr;
+		P.indexSize = (int) ib->elemSize;
+	}
+	P.color = fx->color;
+	P.depth = fx->depth;
+	P.stencil = fx->stencil;
+	const int mode = isTri(prim) ? st.polygonMode : (isLine(prim) ? SRP_POLYGON_MODE_LINE : SRP_POLYGON_MODE_POINT);
+	info.stream = g.stream;
+	info.nIn = nIn;
+	info.outPer = isTri(prim) && mode != SRP_POLYGON_MODE_FILL ? 3 : 1;
+	info.numTiles = (uint32_t) st.tilesX * (uint32_t) st.tilesY;
+	info.pixels = fb->size;
+	info.kind = mode == SRP_POLYGON_MODE_FILL ? kKindTri : mode == SRP_POLYGON_MODE_LINE ? kKindLineFrag : kKindPoint;
+	info.triangles = isTri(prim);
+	info.late = sp->fs->mayOverwriteDepth && shadeSupportsLateDepth(fsId);
+	info.coherent = g.fbMode == SRP_GPU_FB_COHERENT;
+	return 0;
+}
+
+void fixedDrawError(const char* fn, const char* fmt, ...)
+{
+	if (!srpContext.messageCallback.func) return;
+	char buf[1024];
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(buf, sizeof buf, fmt, ap);
+	va_end(ap);
+	srpContext.messageCallback.func(SRP_MESSAGE_ERROR, SRP_MESSAGE_SEVERITY_HIGH, fn, buf,
+	                                srpContext.messageCallback.userParameter);
+}
+
+void fixedDrawUpload(const SRPFramebuffer* fb)
+{
+	if (FbExtra* x = fbFind(fb)) fbUpload(fb, x);
+}
+
+void fixedDrawDownload(const SRPFramebuffer* fb)
+{
+	if (FbExtra* x = fbFind(fb)) fbDownload(fb, x);
+}
+
+void fixedDrawAccount(const DeviceCounters& c, unsigned launches)
+{
+	g.stats.primitives += c.prims;
+	g.stats.binEntries += c.entries;
+	g.stats.clipOverflows += c.clipOverflow;
+	++g.stats.draws;
+	g.launches += launches;
+}
+
+}  // namespace srpg

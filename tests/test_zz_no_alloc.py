@@ -1,0 +1,243 @@
+"""srpGpuDrawFixedScratch, the draw that takes all of its scratch from one
+fixed array in device memory, against the ordinary draw of the same inputs,
+through the C ABI of libsrp_gb300.so.
+
+The file is named so that pytest collects it last: it has to pass both on its
+own in a fresh process (the first call then does the per-device set-up) and
+after every other GPU test in the same process. Images must be bit-identical
+to those of srpDrawIndexBuffer / srpDrawVertexBuffer."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+SRP_FLOAT, SRP_UINT32 = 0, 8
+SRP_INTERPOLATION_MODE_PERSPECTIVE = 0
+SRP_PRIM_LINE_STRIP, SRP_PRIM_TRIANGLES = 2, 4
+
+
+class VaryingInfo(ctypes.Structure):
+    _fields_ = [("nItems", ctypes.c_size_t), ("type", ctypes.c_int), ("interpolationMode", ctypes.c_int)]
+
+
+class VertexShader(ctypes.Structure):
+    _fields_ = [("shader", ctypes.c_void_p), ("nVaryings", ctypes.c_size_t),
+                ("varyingsInfo", ctypes.POINTER(VaryingInfo)), ("varyingsSize", ctypes.c_size_t)]
+
+
+class FragmentShader(ctypes.Structure):
+    _fields_ = [("shader", ctypes.c_void_p), ("mayOverwriteDepth", ctypes.c_bool)]
+
+
+class ShaderProgram(ctypes.Structure):
+    _fields_ = [("uniform", ctypes.c_void_p), ("vs", ctypes.POINTER(VertexShader)),
+                ("fs", ctypes.POINTER(FragmentShader))]
+
+
+class StdUniform(ctypes.Structure):
+    """SRPStdUniform of srp/shaderlib.h."""
+    _fields_ = [("model", ctypes.c_float * 16), ("view", ctypes.c_float * 16), ("projection", ctypes.c_float * 16),
+                ("color", ctypes.c_float * 4), ("cameraPos", ctypes.c_float * 4),
+                ("lightPos", ctypes.c_float * 64), ("lightColor", ctypes.c_float * 64), ("ambient", ctypes.c_float * 4),
+                ("shininess", ctypes.c_float), ("marbleFrequency", ctypes.c_float), ("marbleGain", ctypes.c_float),
+                ("depthScale", ctypes.c_float), ("depthBias", ctypes.c_float)] + \
+               [(n, ctypes.c_uint32) for n in ("nLights", "marbleOctaves", "passOffset", "passCount", "normalOffset",
+                                               "uvOffset", "extraOffset", "extraCount", "varyingOffset", "pad0")] + \
+               [("texture", ctypes.c_void_p)]
+
+
+class Api:
+    """The calls of this test, typed, plus a message log and a colour-varying
+    shader program (srpVsTransform with identity matrices, srpFsVaryingColor)."""
+
+    def __init__(self):
+        import srp_gb300
+        self.srp = srp_gb300
+        L = srp_gb300.lib()
+        vp = ctypes.c_void_p
+        for name, res, args in [
+            ("srpNewFramebuffer", vp, [ctypes.c_size_t, ctypes.c_size_t]),
+            ("srpFreeFramebuffer", None, [vp]),
+            ("srpFramebufferClear", None, [vp]),
+            ("srpGpuFramebufferSync", None, [vp]),
+            ("srpNewVertexBuffer", vp, []),
+            ("srpFreeVertexBuffer", None, [vp]),
+            ("srpVertexBufferCopyData", None, [vp, ctypes.c_size_t, ctypes.c_size_t, vp]),
+            ("srpNewIndexBuffer", vp, []),
+            ("srpFreeIndexBuffer", None, [vp]),
+            ("srpIndexBufferCopyData", None, [vp, ctypes.c_int, ctypes.c_size_t, vp]),
+            ("srpDrawVertexBuffer", None, [vp, vp, vp, ctypes.c_int, ctypes.c_size_t, ctypes.c_size_t]),
+            ("srpDrawIndexBuffer", None, [vp, vp, vp, vp, ctypes.c_int, ctypes.c_size_t, ctypes.c_size_t]),
+            ("srpGpuDrawFixedScratch", ctypes.c_int, [vp, vp, vp, vp, ctypes.c_int, ctypes.c_size_t, ctypes.c_size_t]),
+            ("srpNewContext", None, [vp]),
+            ("srpDepthTest", None, [ctypes.c_bool]),
+        ]:
+            f = getattr(L, name)
+            f.restype, f.argtypes = res, args
+        self.L = L
+        ctx = ctypes.c_char.in_dll(L, "srpContext")
+        L.srpNewContext(ctypes.addressof(ctx))
+        self.messages = []
+        self._cb = srp_gb300.MESSAGE_CALLBACK(
+            lambda t, sev, fn, msg, user: self.messages.append((t, fn.decode(), msg.decode())))
+        L.srpSetMessageCallback(srp_gb300.SRPMessageCallback(self._cb, None))
+        L.srpDepthTest(True)
+        u = StdUniform()
+        for m in (u.model, u.view, u.projection):
+            for i in range(4):
+                m[5 * i] = 1.0
+        u.passOffset, u.passCount = 3, 3
+        self.uniform = u
+        self.vinfo = (VaryingInfo * 1)(VaryingInfo(3, SRP_FLOAT, SRP_INTERPOLATION_MODE_PERSPECTIVE))
+        self.vs = VertexShader(ctypes.cast(L.srpVsTransform, ctypes.c_void_p).value, 1, self.vinfo, 12)
+        self.fs = FragmentShader(ctypes.cast(L.srpFsVaryingColor, ctypes.c_void_p).value, False)
+        self.prog = ShaderProgram(ctypes.addressof(u), ctypes.pointer(self.vs), ctypes.pointer(self.fs))
+        self.owned = []
+
+    def errors(self):
+        return [m for m in self.messages if m[0] == 0]  # SRP_MESSAGE_ERROR
+
+    def framebuffer(self, w, h):
+        fb = self.L.srpNewFramebuffer(w, h)
+        assert fb, "srpNewFramebuffer failed"
+        self.owned.append((self.L.srpFreeFramebuffer, fb))
+        self.L.srpFramebufferClear(fb)
+        return fb
+
+    def vertex_buffer(self, verts):
+        verts = np.ascontiguousarray(verts, dtype=np.float32)
+        vb = self.L.srpNewVertexBuffer()
+        self.owned.append((self.L.srpFreeVertexBuffer, vb))
+        self.L.srpVertexBufferCopyData(vb, verts.shape[1] * 4, verts.nbytes, verts.ctypes.data)
+        return vb
+
+    def index_buffer(self, idx):
+        idx = np.ascontiguousarray(idx, dtype=np.uint32)
+        ib = self.L.srpNewIndexBuffer()
+        self.owned.append((self.L.srpFreeIndexBuffer, ib))
+        self.L.srpIndexBufferCopyData(ib, SRP_UINT32, idx.nbytes, idx.ctypes.data)
+        return ib
+
+    def planes(self, fb):
+        self.L.srpGpuFramebufferSync(fb)
+        c, d, s = self.srp.framebuffer_arrays(fb)
+        return c, d.view(np.uint32), s
+
+    def close(self):
+        self.L.srpGpuSynchronize()
+        for free, p in reversed(self.owned):
+            free(p)
+        self.owned = []
+
+
+@pytest.fixture()
+def api(built_library):
+    a = Api()
+    yield a
+    a.close()
+
+
+def triangle_soup(rng, n):
+    """n small triangles, x/y in [-1.1, 1.1], z in [-1.1, 1.1] so that some
+    are clipped; xyz then rgb per vertex."""
+    centre = rng.uniform(-1.1, 1.1, size=(n, 1, 3))
+    offs = rng.uniform(-0.06, 0.06, size=(n, 3, 3))
+    pos = (centre + offs).reshape(-1, 3)
+    rgb = rng.uniform(0.0, 1.0, size=(3 * n, 3))
+    return np.concatenate([pos, rgb], axis=1)
+
+
+def random_walk(rng, n):
+    pos = np.cumsum(rng.uniform(-0.04, 0.04, size=(n, 3)), axis=0)
+    pos = np.clip(pos, -0.95, 0.95)
+    rgb = rng.uniform(0.0, 1.0, size=(n, 3))
+    return np.concatenate([pos, rgb], axis=1)
+
+
+def assert_same(a, b, what):
+    for name, x, y in zip(("color", "depth", "stencil"), a, b):
+        bad = np.flatnonzero(x != y)
+        assert bad.size == 0, f"{what}: {name} differs at {bad.size} pixels (first {bad[:5]})"
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["coherent", "device"])
+def test_fixed_scratch_matches_ordinary_draw(api, mode):
+    """Two fixed-scratch draws in a row (indexed triangles, then a line strip
+    over the first image) give exactly the images of the ordinary draws."""
+    L = api.L
+    L.srpGpuSetFramebufferMode(mode)
+    rng = np.random.default_rng(20261204)
+    W, H = 512, 384
+    tris = triangle_soup(rng, 6000)
+    perm = rng.permutation(tris.shape[0]).astype(np.uint32)
+    tri_vb = api.vertex_buffer(tris[perm])
+    tri_ib = api.index_buffer(np.argsort(perm).astype(np.uint32))
+    walk = random_walk(rng, 3000)
+    line_vb = api.vertex_buffer(walk)
+    n_tri_idx, n_walk = tris.shape[0], walk.shape[0]
+
+    ordinary = api.framebuffer(W, H)
+    L.srpDrawIndexBuffer(tri_ib, tri_vb, ordinary, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, n_tri_idx)
+    want1 = api.planes(ordinary)
+    L.srpDrawVertexBuffer(line_vb, ordinary, ctypes.byref(api.prog), SRP_PRIM_LINE_STRIP, 0, n_walk)
+    want2 = api.planes(ordinary)
+    assert not api.errors(), api.errors()
+
+    fixed = api.framebuffer(W, H)
+    rc1 = L.srpGpuDrawFixedScratch(tri_ib, tri_vb, fixed, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, n_tri_idx)
+    got1 = api.planes(fixed)
+    rc2 = L.srpGpuDrawFixedScratch(None, line_vb, fixed, ctypes.byref(api.prog), SRP_PRIM_LINE_STRIP, 0, n_walk)
+    got2 = api.planes(fixed)
+    assert (rc1, rc2) == (0, 0), api.errors()
+    assert not api.errors(), api.errors()
+    assert L.srpGpuSynchronize() == 0
+
+    drawn1 = int(np.count_nonzero(want1[1] != np.float32(-1.0).view(np.uint32)))
+    assert drawn1 > 10000, "the triangle soup should cover a good part of the framebuffer"
+    assert int(np.count_nonzero(want2[0] != want1[0])) > 1000, "the line strip should change the image"
+    assert_same(got1, want1, "first call (indexed triangles)")
+    assert_same(got2, want2, "second call (line strip)")
+
+
+def test_fixed_scratch_rejects_oversized_draws(api):
+    """Draws beyond the array are refused with a message and leave the
+    framebuffer as it was; the next draw that fits is still exact."""
+    L = api.L
+    L.srpGpuSetFramebufferMode(1)
+    rng = np.random.default_rng(7)
+    W, H = 512, 384
+    fb = api.framebuffer(W, H)
+    before = api.planes(fb)
+
+    # known before anything runs: per-vertex scratch for 1.2M vertices
+    big_vb = api.vertex_buffer(np.zeros((1_200_000, 6), dtype=np.float32))
+    rc = L.srpGpuDrawFixedScratch(None, big_vb, fb, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, 3)
+    errs = api.errors()
+    assert rc == -1 and errs and "fixed scratch" in errs[-1][2], errs
+    assert_same(api.planes(fb), before, "rejected draw (vertices)")
+
+    # known after setup: 3000 half-screen triangles need ~5M tile entries
+    half = np.array([[-1, -1], [1, -1], [-1, 1]], dtype=np.float32)
+    n = 3000
+    pos = np.tile(half, (n, 1))
+    z = np.repeat(rng.uniform(-0.5, 0.5, size=n), 3)[:, None]
+    verts = np.concatenate([pos, z, rng.uniform(0, 1, size=(3 * n, 3))], axis=1)
+    vb = api.vertex_buffer(verts)
+    api.messages.clear()
+    rc = L.srpGpuDrawFixedScratch(None, vb, fb, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, 3 * n)
+    errs = api.errors()
+    assert rc == -1 and errs and "tile entries" in errs[-1][2], errs
+    assert_same(api.planes(fb), before, "rejected draw (tile entries)")
+
+    # a draw that fits, after the rejected ones, matches the ordinary draw
+    small = triangle_soup(rng, 2000)
+    svb = api.vertex_buffer(small)
+    ordinary = api.framebuffer(W, H)
+    L.srpDrawVertexBuffer(svb, ordinary, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, small.shape[0])
+    api.messages.clear()
+    rc = L.srpGpuDrawFixedScratch(None, svb, fb, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, small.shape[0])
+    assert rc == 0 and not api.errors(), api.errors()
+    assert_same(api.planes(fb), api.planes(ordinary), "draw after rejections")
+    assert L.srpGpuSynchronize() == 0
