@@ -48,6 +48,24 @@ def peaks():
         return 6800.0, "fallback"
 
 
+TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "resolve_soup_1080p.md")
+
+
+def resolve_traffic(scale):
+    """DRAM bytes (read + write) of the resolve stage per full-size frame, from
+    the committed ncu capture; None for any other size."""
+    if scale != 1.0:
+        return None
+    try:
+        with open(TRAFFIC_PROFILE) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_frame:"):
+                    return int(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
 class ClockSampler:
     """Samples SM clocks and throttle reasons with nvidia-smi while running."""
 
@@ -258,7 +276,9 @@ def main():
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": round(resolve_gbs, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(resolve_gbs / peak, 5), "traffic": None,
+                     "frac": round(resolve_gbs / peak, 5), "traffic": resolve_traffic(args.scale),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
+                                       "profiles/resolve_soup_1080p.md",
                      "kernel": "k_resolve (all three draws of the frame)",
                      "algorithmic_bytes_per_frame": int(resolve_bytes),
                      "ms_per_frame": round(stage_ms["resolve"], 4),
