@@ -91,8 +91,11 @@ def build(verbose=False, ptxas_info=False):
     scenes = os.path.join(LIB, "libsrp_scenes_gpu.so")
     ssrc = [os.path.join(PKG, "scenes", "scenes.c")]
     if _stale(scenes, ssrc + [so] + hdrs):
+        cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
         _run(["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-DSCENES_GPU", "-I", INC,
-              *ssrc, "-o", scenes, "-L", LIB, "-lsrp_gb300", "-Wl,-rpath,$ORIGIN", "-lm"])
+              "-I", os.path.join(cuda, "include"), *ssrc, "-o", scenes, "-L", LIB, "-lsrp_gb300",
+              "-Wl,-rpath,$ORIGIN", "-L", os.path.join(cuda, "lib64"), "-lcudart",
+              "-Wl,-rpath," + os.path.join(cuda, "lib64"), "-lm"])
     return so
 
 

@@ -567,19 +567,31 @@ static void launchHeavy(const DrawParams& P, const uint32_t* vals, uint32_t* hea
 	k_resolve_heavy<KIND><<<152 * 3, kHeavyThreads, smem, s>>>(P, vals, heavy);
 }
 
-void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, uint32_t* heavy, cudaStream_t s)
+void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, uint32_t* heavy, cudaStream_t s,
+                   cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join)
 {
 	const unsigned b = tileBlocks(numTiles);
 	k_tile_classify<<<(numTiles + 255) / 256, 256, 0, s>>>(P, numTiles, heavy);
+	const bool split = aux && fork && join;
+	cudaStream_t hs = s;
+	if (split) {
+		cudaEventRecord(fork, s);
+		cudaStreamWaitEvent(aux, fork, 0);
+		hs = aux;
+	}
 	if (kind == kKindTri) {
-		launchHeavy<kKindTri>(P, vals, heavy, s);
+		launchHeavy<kKindTri>(P, vals, heavy, hs);
 		k_resolve<kKindTri, 0><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
 	} else if (kind == kKindPoint) {
-		launchHeavy<kKindPoint>(P, vals, heavy, s);
+		launchHeavy<kKindPoint>(P, vals, heavy, hs);
 		k_resolve<kKindPoint, 0><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
 	} else {
-		launchHeavy<kKindLineFrag>(P, vals, heavy, s);
+		launchHeavy<kKindLineFrag>(P, vals, heavy, hs);
 		k_resolve<kKindLineFrag, 0><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+	}
+	if (split) {
+		cudaEventRecord(join, aux);
+		cudaStreamWaitEvent(s, join, 0);
 	}
 }
 

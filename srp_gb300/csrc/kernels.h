@@ -82,8 +82,13 @@ void launchTileRanges(const DrawParams& P, const uint32_t* keys, uint32_t n, uin
 size_t sortHistWords(uint32_t n);
 size_t sortPartialWords(uint32_t n);
 /* k_raster.cu */
+/* Heavy tiles (k_resolve_heavy) and light tiles (k_resolve) are disjoint: with
+ * an auxiliary stream and two events the heavy kernel runs on `aux` beside
+ * the light one, joined back into `s` before the function's work ends;
+ * without them both run on `s` in turn. */
 void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, uint32_t* heavy,
-                   cudaStream_t s);
+                   cudaStream_t s, cudaStream_t aux = nullptr, cudaEvent_t fork = nullptr,
+                   cudaEvent_t join = nullptr);
 /* k_shade.cu */
 void launchShade(const DrawParams& P, int kind, uint32_t numTiles, cudaStream_t s);
 bool shadeSupportsLateDepth(int fsId);

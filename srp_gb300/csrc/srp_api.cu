@@ -89,6 +89,9 @@ struct Lib {
 	bool init = false;
 	cudaStream_t stream = nullptr;
 	cudaStream_t ownStream = nullptr;
+	/* heavy-tile resolve runs here, beside the light tiles on `stream` */
+	cudaStream_t auxStream = nullptr;
+	cudaEvent_t forkEvent = nullptr, joinEvent = nullptr;
 	SRPGpuFramebufferMode fbMode = SRP_GPU_FB_COHERENT;
 	Registry reg;
 	/* scratch pools, grown on demand */
@@ -117,6 +120,11 @@ bool ensureInit(const char* fn)
 	if (g.init) return true;
 	if (!cudaOk(cudaStreamCreateWithFlags(&g.ownStream, cudaStreamNonBlocking), fn, "cudaStreamCreate")) return false;
 	g.stream = g.ownStream;
+	int loPri = 0, hiPri = 0;
+	cudaDeviceGetStreamPriorityRange(&loPri, &hiPri);
+	if (!cudaOk(cudaStreamCreateWithPriority(&g.auxStream, cudaStreamNonBlocking, hiPri), fn, "cudaStreamCreate") ||
+	    !cudaOk(cudaEventCreateWithFlags(&g.forkEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
+	    !cudaOk(cudaEventCreateWithFlags(&g.joinEvent, cudaEventDisableTiming), fn, "cudaEventCreate")) return false;
 	if (!cudaOk(cudaMallocHost((void**) &g.hostCtr, sizeof(DeviceCounters)), fn, "cudaMallocHost")) return false;
 	if (!g.ctr.reserve(sizeof(DeviceCounters), fn) || !g.minmax.reserve(16, fn)) return false;
 	cudaMemset(g.ctr.ptr, 0, sizeof(DeviceCounters));
@@ -965,7 +973,8 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			g.launches += 2;
 		} else {
 			stageBegin();
-			launchResolve(P, kind, sv, numTiles, g.heavy.as<uint32_t>(), g.stream);
+			launchResolve(P, kind, sv, numTiles, g.heavy.as<uint32_t>(), g.stream, g.auxStream, g.forkEvent,
+			              g.joinEvent);
 			stageEnd(SRP_GPU_STAGE_RESOLVE, 3);
 			stageBegin();
 			launchShade(P, kind, numTiles, g.stream);

@@ -24,6 +24,7 @@
 #include "srp/mat.h"
 #include "srp/shaderlib.h"
 #ifdef SCENES_GPU
+#include <cuda_runtime_api.h>
 #include "srp/gpu.h"
 #endif
 #ifdef SCENES_REF
@@ -152,10 +153,34 @@ struct Scene {
 	uint64_t hash;
 };
 
+/* Host copies of the scene's buffers. With a GPU they are page-locked, so
+ * that the per-frame upload of the end-to-end measurement runs at the host
+ * link's speed, as it would for a program that keeps its geometry pinned. */
+static void* hostAlloc(size_t nbytes)
+{
+#ifdef SCENES_GPU
+	void* p = NULL;
+	if (cudaMallocHost(&p, nbytes ? nbytes : 1) == cudaSuccess) return p;
+	fprintf(stderr, "scenes: cudaMallocHost of %zu bytes failed\n", nbytes);
+	abort();
+#else
+	return malloc(nbytes ? nbytes : 1);
+#endif
+}
+
+static void hostFree(void* p)
+{
+#ifdef SCENES_GPU
+	cudaFreeHost(p);
+#else
+	free(p);
+#endif
+}
+
 static int addVB(Scene* s, const void* data, size_t stride, size_t nbytes)
 {
 	int k = s->nvb++;
-	s->vdata[k] = malloc(nbytes ? nbytes : 1);
+	s->vdata[k] = hostAlloc(nbytes);
 	memcpy(s->vdata[k], data, nbytes);
 	s->vbytes[k] = nbytes;
 	s->vstride[k] = stride;
@@ -168,7 +193,7 @@ static int addVB(Scene* s, const void* data, size_t stride, size_t nbytes)
 static int addIB(Scene* s, SRPType type, const void* data, size_t nbytes)
 {
 	int k = s->nib++;
-	s->idata[k] = malloc(nbytes ? nbytes : 1);
+	s->idata[k] = hostAlloc(nbytes);
 	memcpy(s->idata[k], data, nbytes);
 	s->ibytes[k] = nbytes;
 	s->itype[k] = type;
@@ -1154,8 +1179,8 @@ Scene* sceneCreate(const char* name, uint64_t seed, double scale)
 void sceneDestroy(Scene* s)
 {
 	if (!s) return;
-	for (int k = 0; k < s->nvb; ++k) { srpFreeVertexBuffer(s->vb[k]); free(s->vdata[k]); }
-	for (int k = 0; k < s->nib; ++k) { srpFreeIndexBuffer(s->ib[k]); free(s->idata[k]); }
+	for (int k = 0; k < s->nvb; ++k) { srpFreeVertexBuffer(s->vb[k]); hostFree(s->vdata[k]); }
+	for (int k = 0; k < s->nib; ++k) { srpFreeIndexBuffer(s->ib[k]); hostFree(s->idata[k]); }
 	if (s->tex) srpFreeTexture(s->tex);
 	free(s);
 }
