@@ -55,6 +55,33 @@ void srpGpuFramebufferUpload(const SRPFramebuffer* fb);
 void srpGpuFramebufferFill(const SRPFramebuffer* fb, uint32_t color, float depth, uint8_t stencil,
                            unsigned planes);
 
+/* ----------------------------------------------------- batched draws */
+
+/** One draw of srpGpuDrawBatch: the arguments of srpDrawIndexBuffer
+ *  (indexBuffer not NULL) or srpDrawVertexBuffer (indexBuffer NULL). */
+typedef struct SRPGpuDraw
+{
+	const SRPIndexBuffer* indexBuffer;
+	const SRPVertexBuffer* vertexBuffer;
+	const SRPFramebuffer* framebuffer;
+	const SRPShaderProgram* program;
+	SRPPrimitive primitive;
+	size_t startIndex;
+	size_t count;
+} SRPGpuDraw;
+
+/** Issue n draws in one call. It has no counterpart in kitrofimov/srp; the
+ *  result is exactly that of calling srpDrawIndexBuffer / srpDrawVertexBuffer
+ *  for draws[0], draws[1], ... in order, with the context state of the call.
+ *
+ *  Runs of consecutive draws that are filled triangles with an early-depth
+ *  device shader, share the vertex shader, fragment shader and varying
+ *  layout, and target different framebuffers are rendered as one multi-draw
+ *  pass: one set of kernel launches for all of them, whatever their sizes.
+ *  Every other draw, including any draw the ordinary path would reject with
+ *  a message, is issued through the ordinary path at its place in the order. */
+void srpGpuDrawBatch(const SRPGpuDraw* draws, size_t n);
+
 /* ------------------------------------------------- fixed-scratch draw */
 
 /** Size of the device array that srpGpuDrawFixedScratch takes its scratch

@@ -26,6 +26,12 @@ class SRPGpuStats(ctypes.Structure):
                 ("fragments", "primitives", "binEntries", "clipOverflows", "draws", "kernelLaunches")]
 
 
+class SRPGpuDraw(ctypes.Structure):
+    _fields_ = [("indexBuffer", ctypes.c_void_p), ("vertexBuffer", ctypes.c_void_p),
+                ("framebuffer", ctypes.c_void_p), ("program", ctypes.c_void_p), ("primitive", ctypes.c_int),
+                ("startIndex", ctypes.c_size_t), ("count", ctypes.c_size_t)]
+
+
 class SceneInfo(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int), ("height", ctypes.c_int),
                 ("inputTriangles", ctypes.c_size_t), ("inputLines", ctypes.c_size_t),
@@ -97,6 +103,9 @@ def scenes():
         S.srpNewFramebuffer.argtypes = [ctypes.c_size_t, ctypes.c_size_t]
         S.srpFreeFramebuffer.argtypes = [ctypes.c_void_p]
         S.srpGpuFramebufferSync.argtypes = [ctypes.c_void_p]
+        S.sceneDrawDesc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(SRPGpuDraw)]
+        S.sceneBatchRender.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t,
+                                       ctypes.POINTER(SRPGpuDraw)]
         _scenes = S
     return _scenes
 
@@ -175,6 +184,24 @@ class Scene:
             self.close()
         except Exception:
             pass
+
+
+def batch_seed(base, i):
+    """Seed of scene i of a batch: the scene generator's streams of seeds that
+    differ by d are the same stream shifted by d draws, so batch scenes are
+    spaced 2^32 draws apart."""
+    return ((i + 1) << 32) + base
+
+
+def render_batch(batch, fbs):
+    """Render batch[i] (Scene objects of the batched workload, one draw each)
+    into fbs[i] with one srpGpuDrawBatch call; fbs may repeat a framebuffer."""
+    S = scenes()
+    n = len(batch)
+    sp = (ctypes.c_void_p * n)(*[sc.ptr for sc in batch])
+    fp = (ctypes.c_void_p * n)(*fbs)
+    scratch = (SRPGpuDraw * n)()
+    S.sceneBatchRender(sp, fp, n, scratch)
 
 
 def render_scene(name, seed=1, scale=1.0):

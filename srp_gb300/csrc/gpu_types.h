@@ -123,6 +123,24 @@ struct __align__(16) PointRec {
 
 enum PrimKind { kKindTri = 0, kKindLineFrag = 1, kKindPoint = 2 };
 
+/* One draw of a multi-draw pass (srpGpuDrawBatch): the fields in which the
+ * draws of one pass differ. State, shaders and varying layout are shared by
+ * the pass and stay in DrawParams. */
+struct alignas(16) DrawDesc {
+	const unsigned char* vertices;   /* device copy of the draw's vertex buffer */
+	const void* indices;             /* device copy of its index buffer, or null */
+	unsigned long long start, count, nVertices;
+	int indexSize, stride;
+	int prim;                        /* SRPPrimitive (a triangle topology) */
+	int W, H, tilesX, tilesY;
+	int pad;
+	uint32_t* color;                 /* the draw's framebuffer planes */
+	float* depth;
+	uint8_t* stencil;
+	int32_t* winner;                 /* its part of the pass's winner plane */
+	alignas(16) unsigned char uniform[kMaxUniformBytes];
+};
+
 /* Counters written by the kernels, read back by the host. */
 struct DeviceCounters {
 	unsigned long long fragments;

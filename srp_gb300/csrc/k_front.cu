@@ -45,15 +45,20 @@ __global__ void k_reset(const __grid_constant__ DrawParams P)
 	}
 }
 
-__device__ __forceinline__ unsigned long long fetchIndex(const DrawParams& P, unsigned long long i)
+__device__ __forceinline__ unsigned long long fetchIndexRaw(const void* indices, int indexSize, unsigned long long i)
 {
-	switch (P.indexSize) {
-	case 1: return ((const uint8_t*) P.indices)[i];
-	case 2: return ((const uint16_t*) P.indices)[i];
-	case 4: return ((const uint32_t*) P.indices)[i];
-	case 8: return ((const unsigned long long*) P.indices)[i];
+	switch (indexSize) {
+	case 1: return ((const uint8_t*) indices)[i];
+	case 2: return ((const uint16_t*) indices)[i];
+	case 4: return ((const uint32_t*) indices)[i];
+	case 8: return ((const unsigned long long*) indices)[i];
 	default: return i;
 	}
+}
+
+__device__ __forceinline__ unsigned long long fetchIndex(const DrawParams& P, unsigned long long i)
+{
+	return fetchIndexRaw(P.indices, P.indexSize, i);
 }
 
 /* min/max vertex index over the draw's index range
@@ -92,24 +97,34 @@ struct PV { float4 p; uint32_t ref; };
 struct VSet { float nx, ny, nz, sx, sy, c, iw; };
 struct SV { VSet s; uint32_t ref; };
 
-__device__ __forceinline__ VSet vertexSetup(const DrawState& st, const float4& clip)
+__device__ __forceinline__ VSet vertexSetup(int W, int H, const float4& clip)
 {
 	VSet v;
 	v.iw = invW(clip.w);
 	v.nx = __fmul_rn(clip.x, v.iw);
 	v.ny = __fmul_rn(clip.y, v.iw);
 	v.nz = __fmul_rn(clip.z, v.iw);
-	ndcToScreen(st.W, st.H, v.nx, v.ny, v.sx, v.sy);
+	ndcToScreen(W, H, v.nx, v.ny, v.sx, v.sy);
 	v.c = __fmul_rn(v.nz, v.iw);
+	return v;
+}
+
+__device__ __forceinline__ VSet vertexSetup(const DrawState& st, const float4& clip)
+{
+	return vertexSetup(st.W, st.H, clip);
+}
+
+__device__ __forceinline__ SV fromClip(int W, int H, const PV& p)
+{
+	SV v;
+	v.s = vertexSetup(W, H, p.p);
+	v.ref = p.ref;
 	return v;
 }
 
 __device__ __forceinline__ SV fromClip(const DrawState& st, const PV& p)
 {
-	SV v;
-	v.s = vertexSetup(st, p.p);
-	v.ref = p.ref;
-	return v;
+	return fromClip(st.W, st.H, p);
 }
 
 enum SetupMode { kTriFill = 0, kTriLine = 1, kTriPoint = 2, kLines = 3, kPoints = 4 };
@@ -324,7 +339,8 @@ __device__ __forceinline__ uint32_t tileCount(int minX, int minY, int maxXex, in
 
 /* Triangle setup (src/raster/triangle.c:113-238). Returns false if the
  * triangle is culled or degenerate. */
-__device__ bool setupTriangle(const DrawState& st, const SV& v0, const SV& v1, const SV& v2, TriRaster& R, TriAttr& A)
+__device__ bool setupTriangle(const DrawState& st, int W, int H, const SV& v0, const SV& v1, const SV& v2, TriRaster& R,
+                              TriAttr& A)
 {
 	float iw[3] = { v0.s.iw, v1.s.iw, v2.s.iw };
 	float nx[3] = { v0.s.nx, v1.s.nx, v2.s.nx };
@@ -365,12 +381,12 @@ __device__ bool setupTriangle(const DrawState& st, const SV& v0, const SV& v1, c
 	float fx = floorf(mnx), fy = floorf(mny), cx = ceilf(mxx), cy = ceilf(mxy);
 	fx = fx > 0.0f ? fx : 0.0f;
 	fy = fy > 0.0f ? fy : 0.0f;
-	cx = cx > (float) st.W ? (float) st.W : cx;
-	cy = cy > (float) st.H ? (float) st.H : cy;
+	cx = cx > (float) W ? (float) W : cx;
+	cy = cy > (float) H ? (float) H : cy;
 	/* NaN coordinates compare false everywhere; the reference then walks an
 	 * empty range, which clamping to an empty box reproduces. */
-	if (!(fx <= (float) st.W)) fx = (float) st.W;
-	if (!(fy <= (float) st.H)) fy = (float) st.H;
+	if (!(fx <= (float) W)) fx = (float) W;
+	if (!(fy <= (float) H)) fy = (float) H;
 	if (!(cx >= 0.0f)) cx = 0.0f;
 	if (!(cy >= 0.0f)) cy = 0.0f;
 	R.minX = (uint16_t) fx; R.minY = (uint16_t) fy;
@@ -510,7 +526,7 @@ __device__ __forceinline__ void handleTriangle(const DrawParams& P, const SV& a,
 	if (MODE == kTriFill) {
 		TriRaster R;
 		TriAttr A;
-		if (!setupTriangle(P.st, a, b, c, R, A)) return;
+		if (!setupTriangle(P.st, P.st.W, P.st.H, a, b, c, R, A)) return;
 		const uint32_t nt = tileCount(R.minX, R.minY, R.maxX, R.maxY);
 		if (write) writeTri(P, R, A, nt, prim, entry);
 		prim += 1;
@@ -606,6 +622,65 @@ __device__ __forceinline__ unsigned long long packStatus(unsigned long long flag
 	return (flag << 62) | ((unsigned long long) (prims & 0x3FFFFFFFu) << 32) | entries;
 }
 
+/* This thread's exclusive offset, (prims << 32) | entries, over the whole
+ * launch in input order: a block scan, then a decoupled look-back over the
+ * blocks in ticket order. The last block stores the totals in the counters.
+ * Called by all threads of the block. */
+__device__ __forceinline__ unsigned long long orderedOffset(const DrawParams& P, uint32_t bid, uint32_t nPrim,
+                                                            uint32_t nEnt, unsigned long long* sWarp,
+                                                            unsigned long long& sPrefix)
+{
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	/* ---- block scan of (prims, entries) packed as one 64-bit sum */
+	unsigned long long mine = ((unsigned long long) nPrim << 32) | nEnt;
+	unsigned long long incl = mine;
+#pragma unroll
+	for (int o = 1; o < 32; o <<= 1) {
+		const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+		if (lane >= o) incl += y;
+	}
+	if (lane == 31) sWarp[warp] = incl;
+	__syncthreads();
+	if (warp == 0) {
+		unsigned long long w = lane < kSetupThreads / 32 ? sWarp[lane] : 0ull;
+#pragma unroll
+		for (int o = 1; o < 32; o <<= 1) {
+			const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+			if (lane >= o) w += y;
+		}
+		if (lane < kSetupThreads / 32) sWarp[lane] = w;  /* inclusive over warps */
+	}
+	__syncthreads();
+	const unsigned long long warpExcl = warp ? sWarp[warp - 1] : 0ull;
+	const unsigned long long blockTotal = sWarp[kSetupThreads / 32 - 1];
+
+	/* ---- decoupled look-back for the block's global offset */
+	if (tid == 0) {
+		const uint32_t aggP = (uint32_t) (blockTotal >> 32), aggE = (uint32_t) blockTotal;
+		unsigned long long prefix = 0;
+		if (bid == 0) {
+			atomicExch(&P.lookback[0], packStatus(2, aggP, aggE));
+		} else {
+			atomicExch(&P.lookback[bid], packStatus(1, aggP, aggE));
+			/* prims (bits 32..61) and entries (bits 0..31) summed as one word:
+			 * the entry total stays below 2^32 (checked by the host) */
+			const unsigned long long acc = lookBack<unsigned long long, 16>(
+				P.lookback, (long long) bid - 1, 62, 0x3FFFFFFFFFFFFFFFull, &P.ctr->errors);
+			const unsigned long long accP = acc >> 32, accE = acc & 0xFFFFFFFFull;
+			if (accE + aggE > 0xFFFFFFFFull || accP + aggP > 0x3FFFFFFFull) atomicOr(&P.ctr->errors, kErrCapacity);
+			atomicExch(&P.lookback[bid], packStatus(2, (uint32_t) (accP + aggP), (uint32_t) (accE + aggE)));
+			prefix = (accP << 32) | (accE & 0xFFFFFFFFull);
+		}
+		sPrefix = prefix;
+		if (bid == gridDim.x - 1) {
+			P.ctr->prims = (prefix >> 32) + aggP;
+			P.ctr->entries = (prefix & 0xFFFFFFFFull) + aggE;
+		}
+	}
+	__syncthreads();
+	return sPrefix + warpExcl + (incl - mine);
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__ DrawParams P)
 {
@@ -693,7 +768,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
 			nEnt = (uint32_t) L.steps + 1u;
 		} else if (!as.clipped) {
 			if (MODE == kTriFill) {
-				fOk = setupTriangle(P.st, as.sv[0], as.sv[1], as.sv[2], fR, fA);
+				fOk = setupTriangle(P.st, P.st.W, P.st.H, as.sv[0], as.sv[1], as.sv[2], fR, fA);
 				if (fOk) { nPrim = 1; nEnt = tileCount(fR.minX, fR.minY, fR.maxX, fR.maxY); }
 			} else {
 				handleTriangle<MODE>(P, as.sv[0], as.sv[1], as.sv[2], false, nPrim, nEnt);
@@ -705,54 +780,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
 		}
 	}
 
-	/* ---- block scan of (prims, entries) packed as one 64-bit sum */
-	unsigned long long mine = ((unsigned long long) nPrim << 32) | nEnt;
-	unsigned long long incl = mine;
-#pragma unroll
-	for (int o = 1; o < 32; o <<= 1) {
-		const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-		if (lane >= o) incl += y;
-	}
-	if (lane == 31) sWarp[warp] = incl;
-	__syncthreads();
-	if (warp == 0) {
-		unsigned long long w = lane < kSetupThreads / 32 ? sWarp[lane] : 0ull;
-#pragma unroll
-		for (int o = 1; o < 32; o <<= 1) {
-			const unsigned long long y = __shfl_up_sync(0xFFFFFFFFu, w, o);
-			if (lane >= o) w += y;
-		}
-		if (lane < kSetupThreads / 32) sWarp[lane] = w;  /* inclusive over warps */
-	}
-	__syncthreads();
-	const unsigned long long warpExcl = warp ? sWarp[warp - 1] : 0ull;
-	const unsigned long long blockTotal = sWarp[kSetupThreads / 32 - 1];
-
-	/* ---- decoupled look-back for the block's global offset */
-	if (tid == 0) {
-		const uint32_t aggP = (uint32_t) (blockTotal >> 32), aggE = (uint32_t) blockTotal;
-		unsigned long long prefix = 0;
-		if (bid == 0) {
-			atomicExch(&P.lookback[0], packStatus(2, aggP, aggE));
-		} else {
-			atomicExch(&P.lookback[bid], packStatus(1, aggP, aggE));
-			/* prims (bits 32..61) and entries (bits 0..31) summed as one word:
-			 * the entry total stays below 2^32 (checked by the host) */
-			const unsigned long long acc = lookBack<unsigned long long, 16>(
-				P.lookback, (long long) bid - 1, 62, 0x3FFFFFFFFFFFFFFFull, &P.ctr->errors);
-			const unsigned long long accP = acc >> 32, accE = acc & 0xFFFFFFFFull;
-			if (accE + aggE > 0xFFFFFFFFull || accP + aggP > 0x3FFFFFFFull) atomicOr(&P.ctr->errors, kErrCapacity);
-			atomicExch(&P.lookback[bid], packStatus(2, (uint32_t) (accP + aggP), (uint32_t) (accE + aggE)));
-			prefix = (accP << 32) | (accE & 0xFFFFFFFFull);
-		}
-		sPrefix = prefix;
-		if (bid == gridDim.x - 1) {
-			P.ctr->prims = (prefix >> 32) + aggP;
-			P.ctr->entries = (prefix & 0xFFFFFFFFull) + aggE;
-		}
-	}
-	__syncthreads();
-	const unsigned long long base = sPrefix + warpExcl + (incl - mine);
+	const unsigned long long base = orderedOffset(P, bid, nPrim, nEnt, sWarp, sPrefix);
 	uint32_t primBase = (uint32_t) (base >> 32), entBase = (uint32_t) base;
 
 	/* ---- phase C: write the survivors */
@@ -964,6 +992,295 @@ __global__ void k_line_frags_long(const __grid_constant__ DrawParams P)
 	}
 }
 
+/* ============================================================ multi-draw */
+
+/* A multi-draw pass (srpGpuDrawBatch) runs many independent triangle draws,
+ * each into its own framebuffer, through one set of launches. Input
+ * primitives, vertex rows, tiles and (tile, item) pairs are numbered
+ * globally over the pass; each work item finds its draw by a binary search
+ * over the pass's prefix arrays. Within a draw the order is the draw's own
+ * submission order, exactly as for a single draw, so every draw renders as
+ * if it had been issued alone. */
+
+/* The draw d holding position x: prefix[d] <= x < prefix[d + 1]. Empty
+ * draws share their successor's start and are never returned. */
+__device__ __forceinline__ uint32_t drawOf(const uint32_t* prefix, uint32_t n, uint32_t x)
+{
+	uint32_t lo = 0, hi = n;
+	while (hi - lo > 1) {
+		const uint32_t mid = (lo + hi) >> 1;
+		if (__ldg(prefix + mid) <= x) lo = mid; else hi = mid;
+	}
+	return lo;
+}
+
+/* Vertex shading of every vertex of every draw of the pass. Blocks are
+ * handed out per draw (blkPrefix), so a block stages one contiguous run of
+ * one vertex buffer exactly as k_vertex does. */
+template <int VS>
+__global__ void __launch_bounds__(kVertexThreads) k_vertex_multi(const __grid_constant__ DrawParams P)
+{
+	extern __shared__ uint32_t stage[];
+	const uint32_t d = drawOf(P.blkPrefix, P.nDraws, blockIdx.x);
+	const DrawDesc& D = P.draws[d];
+	const unsigned long long vb = (unsigned long long) (blockIdx.x - P.blkPrefix[d]) * kVertexThreads;
+	const unsigned long long nV = D.nVertices;
+	if (vb >= nV) return;
+	const unsigned long long vend = vb + kVertexThreads < nV ? vb + kVertexThreads : nV;
+	const int stride = D.stride;
+	const unsigned long long bytes = (vend - vb) * (unsigned long long) stride;
+	const unsigned char* src = D.vertices + vb * (unsigned long long) stride;
+	if ((stride & 3) == 0) {
+		const uint32_t* w = (const uint32_t*) src;
+		for (unsigned long long i = threadIdx.x; i < bytes / 4; i += kVertexThreads) stage[i] = __ldg(w + i);
+	} else {
+		unsigned char* sb = (unsigned char*) stage;
+		for (unsigned long long i = threadIdx.x; i < bytes; i += kVertexThreads) sb[i] = __ldg(src + i);
+	}
+	__syncthreads();
+	const unsigned long long v = vb + threadIdx.x;
+	if (v >= vend) return;
+	uint32_t vtx[kMaxVertexWords];
+	const unsigned char* rec = (const unsigned char*) stage + (unsigned long long) threadIdx.x * stride;
+	const int words = (stride + 3) / 4 < kMaxVertexWords ? (stride + 3) / 4 : kMaxVertexWords;
+#pragma unroll
+	for (int k = 0; k < kMaxVertexWords; ++k) vtx[k] = 0;
+	if ((stride & 3) == 0) {
+#pragma unroll
+		for (int k = 0; k < kMaxVertexWords; ++k)
+			if (k < words) vtx[k] = ((const uint32_t*) rec)[k];
+	} else {
+		memcpy(vtx, rec, stride < 4 * kMaxVertexWords ? stride : 4 * kMaxVertexWords);
+	}
+	uint32_t out[kMaxVaryingWords];
+#pragma unroll
+	for (int k = 0; k < kMaxVaryingWords; ++k) out[k] = 0;
+	SRPVertexShaderIn in;
+	in.uniform = (SRPUniform*) D.uniform;
+	in.vertex = (SRPVertex*) vtx;
+	in.vertexID = (size_t) v;
+	SRPVertexShaderOut o;
+	o.clipPosition[0] = o.clipPosition[1] = o.clipPosition[2] = o.clipPosition[3] = 0.0f;
+	o.varyings = (SRPVarying*) out;
+	runVS<VS>(&in, &o);
+	const float4 clip = make_float4(o.clipPosition[0], o.clipPosition[1], o.clipPosition[2], o.clipPosition[3]);
+	const unsigned long long row = P.vPrefix[d] + v;
+	P.clip[row] = clip;
+	const uint32_t code = outcode(clip);
+	if (code == 0) {
+		const VSet vs = vertexSetup(D.W, D.H, clip);
+		P.vset0[row] = make_float4(vs.nx, vs.ny, vs.sx, vs.sy);
+		P.vset1[row] = make_float4(vs.c, vs.iw, vs.nz, __uint_as_float(0u));
+	} else {
+		P.vset1[row] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(code));
+	}
+	const int nw = P.L.nWords;
+	uint32_t* dst = P.vary + row * (unsigned long long) nw;
+#pragma unroll
+	for (int k = 0; k < kMaxVaryingWords; ++k)
+		if (k < nw) dst[k] = out[k];
+}
+
+/* Vertex row of stream position `stream` of draw D (rows of the pass start
+ * at rowBase for this draw). */
+__device__ __forceinline__ bool vertexIndexD(const DrawParams& P, const DrawDesc& D, uint32_t rowBase,
+                                             unsigned long long stream, uint32_t& vi)
+{
+	const unsigned long long v = D.indexSize ? fetchIndexRaw(D.indices, D.indexSize, stream) : stream;
+	if (v >= D.nVertices) { atomicOr(&P.ctr->errors, kErrBadIndex); return false; }
+	vi = rowBase + (uint32_t) v;
+	return true;
+}
+
+/* Input triangle k of the pass: its draw and its three vertex rows. */
+__device__ __forceinline__ bool triangleOfPass(const DrawParams& P, uint32_t k, uint32_t& d, uint32_t vi[3],
+                                               unsigned long long& local)
+{
+	d = drawOf(P.inPrefix, P.nDraws, k);
+	const DrawDesc& D = P.draws[d];
+	local = (unsigned long long) (k - P.inPrefix[d]);
+	unsigned long long s[3];
+	triStream(D.prim, D.start, local, s);
+	const uint32_t rb = P.vPrefix[d];
+	return vertexIndexD(P, D, rb, s[0], vi[0]) && vertexIndexD(P, D, rb, s[1], vi[1]) &&
+	       vertexIndexD(P, D, rb, s[2], vi[2]);
+}
+
+/* Clip pre-pass of a pass (see k_clip_prepass). */
+__global__ void __launch_bounds__(kSetupThreads) k_clip_prepass_multi(const __grid_constant__ DrawParams P)
+{
+	const long long k = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= P.nIn) return;
+	uint32_t d, vi[3];
+	unsigned long long local;
+	if (!triangleOfPass(P, (uint32_t) k, d, vi, local)) return;
+	const uint32_t c0 = vertexCode(P, vi[0]), c1 = vertexCode(P, vi[1]), c2 = vertexCode(P, vi[2]);
+	if ((c0 & c1 & c2) || (c0 | c1 | c2) == 0) return;
+	PV in[3] = { loadPV(P, vi[0]), loadPV(P, vi[1]), loadPV(P, vi[2]) };
+	PV poly[kMaxPoly];
+	const int n = clipPolygon(P, in, poly);
+	const unsigned long long slot = atomicAdd(&P.ctr->clipTris, 1ull);
+	if (slot >= P.clipPolyCap) { atomicOr(&P.ctr->errors, kErrCapacity); P.clipSlot[k] = 0xFFFFFFFFu; return; }
+	uint32_t* out = P.clipPolys + (size_t) slot * (1 + kMaxPoly);
+	out[0] = (uint32_t) n;
+	for (int i = 0; i < n; ++i) out[1 + i] = poly[i].ref;
+	P.clipSlot[k] = (uint32_t) slot;
+}
+
+/* Pairs of a triangle of draw d: keys are global tile numbers of the pass;
+ * big triangles are queued with the draw in place of the kind. */
+__device__ void emitEntriesMulti(const DrawParams& P, uint32_t d, int tilesX, uint32_t tileBase, uint32_t item,
+                                 uint32_t base, int x0, int y0, int x1, int y1)
+{
+	const uint32_t n = tileCount(x0, y0, x1 + 1, y1 + 1);
+	if (n == 0) return;
+	if (n <= (uint32_t) kSmallEntries) {
+		uint32_t e = base;
+		for (int ty = y0 / kTile; ty <= y1 / kTile; ++ty)
+			for (int tx = x0 / kTile; tx <= x1 / kTile; ++tx, ++e)
+				if (e < P.entryCap) { P.keys[e] = tileBase + (uint32_t) (ty * tilesX + tx); P.vals[e] = item; }
+		if (base + n > P.entryCap) atomicOr(&P.ctr->errors, kErrCapacity);
+	} else {
+		const unsigned long long j = atomicAdd(&P.ctr->bigJobs, 1ull);
+		if (j < P.bigCap) P.bigJobs[j] = make_uint4(item, base, d, n);
+		else atomicOr(&P.ctr->errors, kErrCapacity);
+	}
+}
+
+__device__ __forceinline__ void writeTriMulti(const DrawParams& P, uint32_t d, int tilesX, uint32_t tileBase,
+                                              TriRaster& R, TriAttr& A, uint32_t nt, uint32_t prim, uint32_t entry)
+{
+	if (nt > (uint32_t) kSmallEntries) {
+		const int cols = ((int) R.maxX - 1) / kTile - (int) R.minX / kTile + 1;
+		const unsigned long long words = 3ull * (unsigned long long) (R.maxY - R.minY) * (unsigned long long) cols;
+		const unsigned long long off = atomicAdd(&P.ctr->tableWords, words);
+		if (off + words <= P.tableCap && off < 0xFFFFFFFFull) R.table = (uint32_t) off;
+	}
+	if (prim < P.primCap) {
+		A.id = prim;
+		P.triR[prim] = R;
+		P.triA[prim] = A;
+		emitEntriesMulti(P, d, tilesX, tileBase, prim, entry, R.minX, R.minY, (int) R.maxX - 1, (int) R.maxY - 1);
+	} else atomicOr(&P.ctr->errors, kErrCapacity);
+}
+
+/* Ordered setup of a pass (filled triangles): as k_setup<kTriFill>, with the
+ * draw's framebuffer size and tile grid. The first input triangle of every
+ * draw records the number of surviving primitives before the draw, from
+ * which primitive ids local to the draw are recovered. */
+__global__ void __launch_bounds__(kSetupThreads) k_setup_multi(const __grid_constant__ DrawParams P)
+{
+	__shared__ uint32_t sBlock;
+	__shared__ unsigned long long sWarp[kSetupThreads / 32];
+	__shared__ unsigned long long sPrefix;
+	const int tid = threadIdx.x;
+	if (tid == 0) sBlock = atomicAdd(&P.ctr->lookbackTicket, 1u);
+	__syncthreads();
+	const uint32_t bid = sBlock;
+	const long long k = (long long) bid * kSetupThreads + tid;
+
+	bool live = k < P.nIn, clipped = false, first = false;
+	uint32_t d = 0;
+	int W = 0, H = 0, tilesX = 0;
+	uint32_t tileBase = 0;
+	SV sv[3];
+	int nPoly = 0;
+	PV poly[kMaxPoly];
+	if (live) {
+		uint32_t vi[3];
+		unsigned long long local;
+		live = triangleOfPass(P, (uint32_t) k, d, vi, local);
+		first = local == 0;
+		const DrawDesc& D = P.draws[d];
+		W = D.W; H = D.H; tilesX = D.tilesX;
+		tileBase = P.tPrefix[d];
+		if (live) {
+			const uint32_t c0 = vertexCode(P, vi[0]), c1 = vertexCode(P, vi[1]), c2 = vertexCode(P, vi[2]);
+			if (c0 & c1 & c2) live = false;
+			else if ((c0 | c1 | c2) == 0) {
+#pragma unroll
+				for (int i = 0; i < 3; ++i) sv[i] = loadSV(P, vi[i]);
+			} else {
+				clipped = true;
+				const uint32_t slot = P.clipSlot[k];
+				if (slot >= P.clipPolyCap) live = false;
+				else {
+					const uint32_t* pp = P.clipPolys + (size_t) slot * (1 + kMaxPoly);
+					nPoly = (int) pp[0];
+					for (int i = 0; i < nPoly && i < kMaxPoly; ++i) poly[i] = loadPV(P, pp[1 + i]);
+					if (nPoly < 3) live = false;
+				}
+			}
+		}
+	}
+	uint32_t nPrim = 0, nEnt = 0;
+	TriRaster fR;
+	TriAttr fA;
+	bool fOk = false;
+	if (live) {
+		if (!clipped) {
+			fOk = setupTriangle(P.st, W, H, sv[0], sv[1], sv[2], fR, fA);
+			if (fOk) { nPrim = 1; nEnt = tileCount(fR.minX, fR.minY, fR.maxX, fR.maxY); }
+		} else {
+			const SV p0 = fromClip(W, H, poly[0]);
+			for (int f = 1; f + 1 < nPoly; ++f) {
+				TriRaster R;
+				TriAttr A;
+				if (!setupTriangle(P.st, W, H, p0, fromClip(W, H, poly[f]), fromClip(W, H, poly[f + 1]), R, A)) continue;
+				nPrim += 1;
+				nEnt += tileCount(R.minX, R.minY, R.maxX, R.maxY);
+			}
+		}
+	}
+	const unsigned long long base = orderedOffset(P, bid, nPrim, nEnt, sWarp, sPrefix);
+	uint32_t primBase = (uint32_t) (base >> 32), entBase = (uint32_t) base;
+	if (first) P.primPrefix[d] = primBase;
+	if (!live) return;
+	if (!clipped) {
+		if (fOk) writeTriMulti(P, d, tilesX, tileBase, fR, fA, nEnt, primBase, entBase);
+	} else {
+		const SV p0 = fromClip(W, H, poly[0]);
+		for (int f = 1; f + 1 < nPoly; ++f) {
+			TriRaster R;
+			TriAttr A;
+			if (!setupTriangle(P.st, W, H, p0, fromClip(W, H, poly[f]), fromClip(W, H, poly[f + 1]), R, A)) continue;
+			const uint32_t nt = tileCount(R.minX, R.minY, R.maxX, R.maxY);
+			writeTriMulti(P, d, tilesX, tileBase, R, A, nt, primBase, entBase);
+			primBase += 1;
+			entBase += nt;
+		}
+	}
+}
+
+/* k_big_entries for a pass: the job's third word is its draw. */
+__global__ void k_big_entries_multi(const __grid_constant__ DrawParams P, uint32_t nJobs)
+{
+	for (uint32_t j = blockIdx.x; j < nJobs; j += gridDim.x) {
+		const uint4 job = P.bigJobs[j];
+		const TriRaster& R = P.triR[job.x];
+		const int x0 = R.minX, y0 = R.minY, x1 = (int) R.maxX - 1;
+		const int tilesX = P.draws[job.z].tilesX;
+		const uint32_t tileBase = P.tPrefix[job.z];
+		const int tx0 = x0 / kTile, ty0 = y0 / kTile, ntx = x1 / kTile - tx0 + 1;
+		for (uint32_t i = threadIdx.x; i < job.w; i += blockDim.x) {
+			const uint32_t e = job.y + i;
+			if (e >= P.entryCap) break;
+			const int tx = tx0 + (int) (i % (uint32_t) ntx), ty = ty0 + (int) (i / (uint32_t) ntx);
+			P.keys[e] = tileBase + (uint32_t) (ty * tilesX + tx);
+			P.vals[e] = job.x;
+		}
+	}
+}
+
+/* Lambda tables of a pass's big triangles (every job is a triangle). */
+__global__ void k_lambda_tables_multi(const __grid_constant__ DrawParams P, uint32_t nJobs)
+{
+	for (uint32_t j = blockIdx.y; j < nJobs; j += gridDim.y) {
+		const uint4 job = P.bigJobs[j];
+		fillLambdaTable(P, P.triR[job.x], blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+	}
+}
+
 /* ------------------------------------------------------------ launchers */
 
 void launchReset(const DrawParams& P, cudaStream_t s) { k_reset<<<1, 32, 0, s>>>(P); }
@@ -1023,6 +1340,41 @@ void launchLineFrags(const DrawParams& P, uint32_t nLines, cudaStream_t s)
 	if (!nLines) return;
 	k_line_frags<<<(nLines + 127) / 128, 128, 0, s>>>(P, nLines);
 	k_line_frags_long<<<152 * 8, 128, 0, s>>>(P);
+}
+
+void launchVertexMulti(const DrawParams& P, uint32_t blocks, int maxStride, cudaStream_t s)
+{
+	if (!blocks) return;
+	const size_t smem = (size_t) kVertexThreads * maxStride + 16;
+	switch (P.vsId) {
+	case SRP_GPU_VS_WORLD:
+		cudaFuncSetAttribute(k_vertex_multi<SRP_GPU_VS_WORLD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+		k_vertex_multi<SRP_GPU_VS_WORLD><<<blocks, kVertexThreads, smem, s>>>(P);
+		break;
+	default:
+		cudaFuncSetAttribute(k_vertex_multi<SRP_GPU_VS_TRANSFORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+		k_vertex_multi<SRP_GPU_VS_TRANSFORM><<<blocks, kVertexThreads, smem, s>>>(P);
+		break;
+	}
+}
+
+void launchClipPrepassMulti(const DrawParams& P, cudaStream_t s)
+{
+	const unsigned blocks = (unsigned) ((P.nIn + kSetupThreads - 1) / kSetupThreads);
+	if (blocks) k_clip_prepass_multi<<<blocks, kSetupThreads, 0, s>>>(P);
+}
+
+void launchSetupMulti(const DrawParams& P, cudaStream_t s)
+{
+	const unsigned blocks = (unsigned) ((P.nIn + kSetupThreads - 1) / kSetupThreads);
+	if (blocks) k_setup_multi<<<blocks, kSetupThreads, 0, s>>>(P);
+}
+
+void launchBigEntriesMulti(const DrawParams& P, uint32_t nJobs, cudaStream_t s)
+{
+	if (!nJobs) return;
+	k_big_entries_multi<<<nJobs < 152u * 16u ? nJobs : 152u * 16u, 256, 0, s>>>(P, nJobs);
+	k_lambda_tables_multi<<<dim3(8, nJobs < 65535u ? nJobs : 65535u), 256, 0, s>>>(P, nJobs);
 }
 
 }  // namespace srpg

@@ -65,11 +65,12 @@ __device__ __forceinline__ void runFS(SRPFragmentShaderIn* in, SRPFragmentShader
  * (fragCoord and varyings as built by src/raster/triangle.c:89-99,
  * line.c:62-75, point.c:107-116). */
 template <int KIND, int FS>
-__device__ __forceinline__ void shadeItem(const DrawParams& P, uint32_t item, int gx, int gy, SRPFragmentShaderOut& out)
+__device__ __forceinline__ void shadeItem(const DrawParams& P, const unsigned char* uniform, uint32_t primBase,
+                                          uint32_t item, int gx, int gy, SRPFragmentShaderOut& out)
 {
 	uint32_t words[kMaxVaryingWords];
 	SRPFragmentShaderIn in;
-	in.uniform = (SRPUniform*) P.uniform;
+	in.uniform = (SRPUniform*) uniform;
 	in.varyings = (SRPInterpolated*) words;
 	if (KIND == kKindTri) {
 		const TriRaster R = P.triR[item];
@@ -98,7 +99,7 @@ __device__ __forceinline__ void shadeItem(const DrawParams& P, uint32_t item, in
 		in.fragCoord[2] = depth;
 		in.fragCoord[3] = recip;
 		in.frontFacing = (R.flags & 1u) != 0;
-		in.primitiveID = A.id;
+		in.primitiveID = A.id - primBase;
 	} else if (KIND == kKindLineFrag) {
 		const LineFrag F = P.frags[item];
 		const LineRec L = P.lines[F.line];
@@ -275,10 +276,59 @@ __device__ __forceinline__ int findOwner(const uint32_t* off, uint32_t p)
 	return lo;
 }
 
+/* Where a tile's pixels live: its origin in its framebuffer, the
+ * framebuffer's size and planes, and the uniform and primitive-id base of
+ * its draw. A single draw takes them from the parameters; a multi-draw pass
+ * (MULTI) from the descriptor of the draw the global tile belongs to. */
+struct TileCtx {
+	int x0, y0, W, H;
+	uint32_t* color;
+	float* depth;
+	uint8_t* stencil;
+	int32_t* winner;
+	const unsigned char* uniform;
+	uint32_t primBase;
+};
+
+__device__ __forceinline__ uint32_t tileDraw(const uint32_t* prefix, uint32_t n, uint32_t x)
+{
+	uint32_t lo = 0, hi = n;
+	while (hi - lo > 1) {
+		const uint32_t mid = (lo + hi) >> 1;
+		if (__ldg(prefix + mid) <= x) lo = mid; else hi = mid;
+	}
+	return lo;
+}
+
+template <bool MULTI>
+__device__ __forceinline__ TileCtx tileCtx(const DrawParams& P, uint32_t tile)
+{
+	TileCtx c;
+	if constexpr (MULTI) {
+		const uint32_t d = tileDraw(P.tPrefix, P.nDraws, tile);
+		const DrawDesc& D = P.draws[d];
+		const uint32_t lt = tile - P.tPrefix[d];
+		c.x0 = (int) (lt % (uint32_t) D.tilesX) * kTile;
+		c.y0 = (int) (lt / (uint32_t) D.tilesX) * kTile;
+		c.W = D.W; c.H = D.H;
+		c.color = D.color; c.depth = D.depth; c.stencil = D.stencil; c.winner = D.winner;
+		c.uniform = D.uniform;
+		c.primBase = P.primPrefix[d];
+	} else {
+		c.x0 = (int) (tile % (uint32_t) P.st.tilesX) * kTile;
+		c.y0 = (int) (tile / (uint32_t) P.st.tilesX) * kTile;
+		c.W = P.st.W; c.H = P.st.H;
+		c.color = P.color; c.depth = P.depth; c.stencil = P.stencil; c.winner = P.winner;
+		c.uniform = P.uniform;
+		c.primBase = 0;
+	}
+	return c;
+}
+
 /* LATE_FS = 0: early depth test, colour deferred to k_shade.
  * LATE_FS = a fragment shader id: the shader runs per fragment in order and
  * may replace the depth (src/raster/fragment.c:97-111). */
-template <int KIND, int LATE_FS>
+template <int KIND, int LATE_FS, bool MULTI = false>
 __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(const __grid_constant__ DrawParams P,
                                                                const uint32_t* vals, uint32_t numTiles)
 {
@@ -296,7 +346,8 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(const __grid_con
 	if (s >= e) return;
 	if (LATE_FS == 0 && e - s > kHeavyItems) return;  /* k_resolve_heavy's */
 	const DrawState& st = P.st;
-	const int x0 = (int) (tile % (uint32_t) st.tilesX) * kTile, y0 = (int) (tile / (uint32_t) st.tilesX) * kTile;
+	const TileCtx c = tileCtx<MULTI>(P, tile);
+	const int x0 = c.x0, y0 = c.y0;
 
 	float depth[2];
 	uint32_t sten[2], col[2];
@@ -309,10 +360,10 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(const __grid_con
 		const int q = lane + 32 * p;
 		gx[p] = x0 + (q & 7);
 		gy[p] = y0 + (q >> 3);
-		const bool valid = gx[p] < st.W && gy[p] < st.H;
-		idx[p] = valid ? (size_t) gy[p] * st.W + gx[p] : 0;
-		depth[p] = valid ? P.depth[idx[p]] : 0.0f;
-		sten[p] = valid ? P.stencil[idx[p]] : 0u;
+		const bool valid = gx[p] < c.W && gy[p] < c.H;
+		idx[p] = valid ? (size_t) gy[p] * c.W + gx[p] : 0;
+		depth[p] = valid ? c.depth[idx[p]] : 0.0f;
+		sten[p] = valid ? c.stencil[idx[p]] : 0u;
 		col[p] = 0;
 		win[p] = -1;
 		/* line fragments were scissor-tested on their logical coordinates */
@@ -388,7 +439,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(const __grid_con
 					}
 				} else {
 					SRPFragmentShaderOut out;
-					shadeItem<KIND, LATE_FS>(P, sItem[warp][j], gx[p], gy[p], out);
+					shadeItem<KIND, LATE_FS>(P, c.uniform, c.primBase, sItem[warp][j], gx[p], gy[p], out);
 					if (!isnan(out.fragDepth)) d = out.fragDepth;
 					if (st.depthTest && !depthCompare(st.depthOp, d, depth[p])) {
 						if (st.stencilEnabled) sten[p] = stencilApply(sf.dfail, sten[p], sf.ref, sf.writeMask);
@@ -405,11 +456,11 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(const __grid_con
 	}
 #pragma unroll
 	for (int p = 0; p < 2; ++p) {
-		if (!(gx[p] < st.W && gy[p] < st.H)) continue;
-		P.depth[idx[p]] = depth[p];
-		P.stencil[idx[p]] = (uint8_t) sten[p];
-		if (LATE_FS == 0) P.winner[idx[p]] = win[p];
-		else if (win[p] >= 0) P.color[idx[p]] = col[p];
+		if (!(gx[p] < c.W && gy[p] < c.H)) continue;
+		c.depth[idx[p]] = depth[p];
+		c.stencil[idx[p]] = (uint8_t) sten[p];
+		if (LATE_FS == 0) c.winner[idx[p]] = win[p];
+		else if (win[p] >= 0) c.color[idx[p]] = col[p];
 	}
 	if (KIND != kKindLineFrag) {
 		for (int o = 16; o; o >>= 1) frags += __shfl_xor_sync(0xFFFFFFFFu, frags, o);
@@ -443,7 +494,7 @@ __device__ __forceinline__ bool applyFragment(const DrawState& st, bool front, f
  * chunk is parallel over items; per pixel only real fragments are walked.
  * Heavy tiles come from a list built by k_tile_classify and are pulled by a
  * fixed grid of CTAs. */
-template <int KIND>
+template <int KIND, bool MULTI = false>
 __global__ void __launch_bounds__(kHeavyThreads) k_resolve_heavy(const __grid_constant__ DrawParams P,
                                                                 const uint32_t* vals, const uint32_t* heavy)
 {
@@ -457,13 +508,14 @@ __global__ void __launch_bounds__(kHeavyThreads) k_resolve_heavy(const __grid_co
 	for (uint32_t h = blockIdx.x; h < nHeavy; h += gridDim.x) {
 		const uint32_t tile = heavy[h];
 		const uint32_t s = P.tileStart[tile], e = P.tileEnd[tile];
-		const int x0 = (int) (tile % (uint32_t) st.tilesX) * kTile, y0 = (int) (tile / (uint32_t) st.tilesX) * kTile;
+		const TileCtx c = tileCtx<MULTI>(P, tile);
+		const int x0 = c.x0, y0 = c.y0;
 		const int gx = x0 + (tid & 7), gy = y0 + ((tid >> 3) & 7);
 		const bool owner = tid < 64;
-		const bool valid = owner && gx < st.W && gy < st.H;
-		const size_t idx = valid ? (size_t) gy * st.W + gx : 0;
-		float depth = valid ? P.depth[idx] : 0.0f;
-		uint32_t sten = valid ? P.stencil[idx] : 0u;
+		const bool valid = owner && gx < c.W && gy < c.H;
+		const size_t idx = valid ? (size_t) gy * c.W + gx : 0;
+		float depth = valid ? c.depth[idx] : 0.0f;
+		uint32_t sten = valid ? c.stencil[idx] : 0u;
 		int32_t win = -1;
 		const bool ok = valid && (KIND == kKindLineFrag || scissorPass(st, gx, gy));
 		unsigned long long frags = 0;
@@ -510,9 +562,9 @@ __global__ void __launch_bounds__(kHeavyThreads) k_resolve_heavy(const __grid_co
 			__syncthreads();
 		}
 		if (valid) {
-			P.depth[idx] = depth;
-			P.stencil[idx] = (uint8_t) sten;
-			P.winner[idx] = win;
+			c.depth[idx] = depth;
+			c.stencil[idx] = (uint8_t) sten;
+			c.winner[idx] = win;
 		}
 		if (KIND != kKindLineFrag && warp < 2) {
 			for (int o = 16; o; o >>= 1) frags += __shfl_xor_sync(0xFFFFFFFFu, frags, o);
@@ -532,26 +584,26 @@ __global__ void k_tile_classify(const __grid_constant__ DrawParams P, uint32_t n
 
 /* Deferred shading: one shader invocation per pixel whose colour was written
  * by the resolve pass. */
-template <int KIND, int FS>
+template <int KIND, int FS, bool MULTI = false>
 __global__ void __launch_bounds__(kResolveWarps * 32) k_shade(const __grid_constant__ DrawParams P, uint32_t numTiles)
 {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const uint32_t tile = blockIdx.x * kResolveWarps + warp;
 	if (tile >= numTiles) return;
 	if (P.tileStart[tile] >= P.tileEnd[tile]) return;
-	const DrawState& st = P.st;
-	const int x0 = (int) (tile % (uint32_t) st.tilesX) * kTile, y0 = (int) (tile / (uint32_t) st.tilesX) * kTile;
+	const TileCtx c = tileCtx<MULTI>(P, tile);
+	const int x0 = c.x0, y0 = c.y0;
 #pragma unroll
 	for (int p = 0; p < 2; ++p) {
 		const int q = lane + 32 * p;
 		const int gx = x0 + (q & 7), gy = y0 + (q >> 3);
-		if (gx >= st.W || gy >= st.H) continue;
-		const size_t idx = (size_t) gy * st.W + gx;
-		const int32_t w = P.winner[idx];
+		if (gx >= c.W || gy >= c.H) continue;
+		const size_t idx = (size_t) gy * c.W + gx;
+		const int32_t w = c.winner[idx];
 		if (w < 0) continue;
 		SRPFragmentShaderOut out;
-		shadeItem<KIND, FS>(P, (uint32_t) w, gx, gy, out);
-		P.color[idx] = packColor(out.color);
+		shadeItem<KIND, FS>(P, c.uniform, c.primBase, (uint32_t) w, gx, gy, out);
+		c.color[idx] = packColor(out.color);
 	}
 }
 
@@ -559,12 +611,12 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_shade(const __grid_const
 
 static unsigned tileBlocks(uint32_t numTiles) { return (numTiles + kResolveWarps - 1) / kResolveWarps; }
 
-template <int KIND>
+template <int KIND, bool MULTI = false>
 static void launchHeavy(const DrawParams& P, const uint32_t* vals, uint32_t* heavy, cudaStream_t s)
 {
 	const int smem = kHeavyThreads * kDepRow * 4;
-	cudaFuncSetAttribute(k_resolve_heavy<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-	k_resolve_heavy<KIND><<<152 * 3, kHeavyThreads, smem, s>>>(P, vals, heavy);
+	cudaFuncSetAttribute(k_resolve_heavy<KIND, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+	k_resolve_heavy<KIND, MULTI><<<152 * 3, kHeavyThreads, smem, s>>>(P, vals, heavy);
 }
 
 void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, uint32_t* heavy, cudaStream_t s,
@@ -605,22 +657,22 @@ void launchResolveLate(const DrawParams& P, int kind, const uint32_t* vals, uint
 	else k_resolve<kKindLineFrag, SRP_GPU_FS_DEPTH_OVERWRITE><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
 }
 
-template <int KIND>
+template <int KIND, bool MULTI = false>
 static void shadeKind(const DrawParams& P, uint32_t numTiles, cudaStream_t s)
 {
 	const unsigned b = tileBlocks(numTiles);
 	const unsigned t = kResolveWarps * 32;
 	switch (P.fsId) {
-	case SRP_GPU_FS_VARYING_COLOR: k_shade<KIND, SRP_GPU_FS_VARYING_COLOR><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_SOLID: k_shade<KIND, SRP_GPU_FS_SOLID><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_PRIMITIVE_ID: k_shade<KIND, SRP_GPU_FS_PRIMITIVE_ID><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_TEXTURE: k_shade<KIND, SRP_GPU_FS_TEXTURE><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_TEXTURE_MODULATE: k_shade<KIND, SRP_GPU_FS_TEXTURE_MODULATE><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_BLINN_PHONG: k_shade<KIND, SRP_GPU_FS_BLINN_PHONG><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_MARBLE: k_shade<KIND, SRP_GPU_FS_MARBLE><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_DEPTH_OVERWRITE: k_shade<KIND, SRP_GPU_FS_DEPTH_OVERWRITE><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_FRAGCOORD: k_shade<KIND, SRP_GPU_FS_FRAGCOORD><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_FLAT_INT: k_shade<KIND, SRP_GPU_FS_FLAT_INT><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_VARYING_COLOR: k_shade<KIND, SRP_GPU_FS_VARYING_COLOR, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_SOLID: k_shade<KIND, SRP_GPU_FS_SOLID, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_PRIMITIVE_ID: k_shade<KIND, SRP_GPU_FS_PRIMITIVE_ID, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_TEXTURE: k_shade<KIND, SRP_GPU_FS_TEXTURE, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_TEXTURE_MODULATE: k_shade<KIND, SRP_GPU_FS_TEXTURE_MODULATE, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_BLINN_PHONG: k_shade<KIND, SRP_GPU_FS_BLINN_PHONG, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_MARBLE: k_shade<KIND, SRP_GPU_FS_MARBLE, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_DEPTH_OVERWRITE: k_shade<KIND, SRP_GPU_FS_DEPTH_OVERWRITE, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_FRAGCOORD: k_shade<KIND, SRP_GPU_FS_FRAGCOORD, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_FLAT_INT: k_shade<KIND, SRP_GPU_FS_FLAT_INT, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
 	default: break;
 	}
 }
@@ -631,5 +683,27 @@ void launchShade(const DrawParams& P, int kind, uint32_t numTiles, cudaStream_t 
 	else if (kind == kKindPoint) shadeKind<kKindPoint>(P, numTiles, s);
 	else shadeKind<kKindLineFrag>(P, numTiles, s);
 }
+
+void launchResolveMulti(const DrawParams& P, const uint32_t* vals, uint32_t numTiles, uint32_t* heavy, cudaStream_t s,
+                        cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join)
+{
+	const unsigned b = tileBlocks(numTiles);
+	k_tile_classify<<<(numTiles + 255) / 256, 256, 0, s>>>(P, numTiles, heavy);
+	const bool split = aux && fork && join;
+	cudaStream_t hs = s;
+	if (split) {
+		cudaEventRecord(fork, s);
+		cudaStreamWaitEvent(aux, fork, 0);
+		hs = aux;
+	}
+	launchHeavy<kKindTri, true>(P, vals, heavy, hs);
+	k_resolve<kKindTri, 0, true><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+	if (split) {
+		cudaEventRecord(join, aux);
+		cudaStreamWaitEvent(s, join, 0);
+	}
+}
+
+void launchShadeMulti(const DrawParams& P, uint32_t numTiles, cudaStream_t s) { shadeKind<kKindTri, true>(P, numTiles, s); }
 
 }  // namespace srpg

@@ -60,6 +60,18 @@ struct DrawParams {
 	uint32_t* tileStart;
 	uint32_t* tileEnd;
 	DeviceCounters* ctr;
+	/* multi-draw pass (nDraws > 0, triangles in fill mode only): the draws'
+	 * descriptors and prefix sums over the draws ([nDraws + 1] each) of input
+	 * primitives, vertex rows, tiles and vertex-kernel blocks. primPrefix
+	 * (surviving primitives before each draw) is written by k_setup_multi.
+	 * Primitive, entry and tile numbers are then global over the pass. */
+	const DrawDesc* draws;
+	uint32_t nDraws;
+	const uint32_t* inPrefix;
+	const uint32_t* vPrefix;
+	const uint32_t* tPrefix;
+	const uint32_t* blkPrefix;
+	uint32_t* primPrefix;
 	alignas(16) unsigned char uniform[kMaxUniformBytes];
 };
 
@@ -75,6 +87,11 @@ void launchSetup(const DrawParams& P, cudaStream_t s);
 void launchClipPrepass(const DrawParams& P, cudaStream_t s);
 void launchBigEntries(const DrawParams& P, uint32_t nJobs, cudaStream_t s);
 void launchLineFrags(const DrawParams& P, uint32_t nLines, cudaStream_t s);
+/* k_front.cu, multi-draw pass */
+void launchVertexMulti(const DrawParams& P, uint32_t blocks, int maxStride, cudaStream_t s);
+void launchClipPrepassMulti(const DrawParams& P, cudaStream_t s);
+void launchSetupMulti(const DrawParams& P, cudaStream_t s);
+void launchBigEntriesMulti(const DrawParams& P, uint32_t nJobs, cudaStream_t s);
 /* k_bin.cu */
 void sortEntries(const DrawParams& P, uint32_t n, uint32_t keyBits, uint32_t* keysAlt, uint32_t* valsAlt,
                  uint32_t* hist, uint32_t* partials, uint32_t** keysOut, uint32_t** valsOut, cudaStream_t s);
@@ -89,7 +106,10 @@ size_t sortPartialWords(uint32_t n);
 void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, uint32_t* heavy,
                    cudaStream_t s, cudaStream_t aux = nullptr, cudaEvent_t fork = nullptr,
                    cudaEvent_t join = nullptr);
-/* k_shade.cu */
+void launchResolveMulti(const DrawParams& P, const uint32_t* vals, uint32_t numTiles, uint32_t* heavy, cudaStream_t s,
+                        cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join);
+void launchShadeMulti(const DrawParams& P, uint32_t numTiles, cudaStream_t s);
+/* k_raster.cu, deferred shading */
 void launchShade(const DrawParams& P, int kind, uint32_t numTiles, cudaStream_t s);
 bool shadeSupportsLateDepth(int fsId);
 void launchResolveLate(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, cudaStream_t s);

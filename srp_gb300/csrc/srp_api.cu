@@ -1039,6 +1039,268 @@ static void drawBuffer(const SRPIndexBuffer* ib, const SRPVertexBuffer* vb, cons
 	runDraw(ib, vb, fb, sp, prim, start, count, nIn);
 }
 
+/* ------------------------------------------------------ multi-draw pass */
+
+namespace {
+
+struct PassLimits {
+	unsigned long long in = 0, rows = 0, tiles = 0, pixels = 0;
+};
+
+/* Number of input primitives of a draw that a multi-draw pass can take, or 0
+ * when the draw must go through drawBuffer (which also reports its errors):
+ * filled triangles with an early-depth shader of the device set, buffers in
+ * a valid range, framebuffer made by srpNewFramebuffer. */
+size_t passInputs(const SRPGpuDraw& d)
+{
+	if (!d.vertexBuffer || !d.framebuffer || !d.program || !d.program->vs || !d.program->fs) return 0;
+	if (!isTri(d.primitive) || d.count == 0) return 0;
+	if (srpContext.raster.cullFace == SRP_FACE_FRONT_AND_BACK || srpContext.raster.polygonMode != SRP_POLYGON_MODE_FILL)
+		return 0;
+	const size_t size = d.indexBuffer ? d.indexBuffer->nIndices : d.vertexBuffer->nVertices;
+	if (d.startIndex + d.count - 1 >= size || d.startIndex + d.count < d.startIndex) return 0;
+	if (d.indexBuffer) {
+		const SRPType t = d.indexBuffer->type;
+		if (t != SRP_UINT8 && t != SRP_UINT16 && t != SRP_UINT32 && t != SRP_UINT64) return 0;
+	}
+	if (d.vertexBuffer->stride == 0 || d.vertexBuffer->stride > 1024) return 0;
+	if (d.program->fs->mayOverwriteDepth) return 0;
+	if (!lookupVS((void*) d.program->vs->shader) || !lookupFS((void*) d.program->fs->shader)) return 0;
+	if (!fbFind(d.framebuffer)) return 0;
+	const size_t n = d.primitive == SRP_PRIM_TRIANGLES ? d.count / 3 : (d.count >= 3 ? d.count - 2 : 0);
+	return n <= 0x7FFFFFFFull ? n : 0;
+}
+
+std::vector<DrawDesc> passDesc;
+std::vector<uint32_t> passPrefix;   /* in, v, t, blk: 4 x (n + 1) */
+DeviceBuffer passDescDev, passPrefixDev, passPrimPrefix, passWinner;
+
+}  // namespace
+
+/* One multi-draw pass over draws[idx[0..]] (all eligible, same shaders and
+ * varying layout, distinct framebuffers). Returns false (after a message)
+ * only on a CUDA failure; draws that hit a bad vertex index are re-run one
+ * by one so that each reports as the ordinary draw does. */
+static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, const std::vector<size_t>& nInOf)
+{
+	const char* FN = "srpGpuDrawBatch";
+	const size_t n = idx.size();
+	const SRPShaderProgram* sp0 = draws[idx[0]].program;
+	static DrawParams P;
+	memset(&P, 0, sizeof P);
+	if (!buildLayout(sp0->vs, P.L)) return true;
+	DrawState& st = P.st;
+	st.frontFaceCW = srpContext.raster.frontFace == SRP_WINDING_CW;
+	st.cullFace = srpContext.raster.cullFace;
+	st.polygonMode = srpContext.raster.polygonMode;
+	st.pointSize = srpContext.raster.pointSize;
+	st.provokingFirst = srpContext.provokingVertexMode == SRP_PROVOKING_VERTEX_FIRST;
+	st.scissorEnabled = srpContext.scissor.enabled;
+	st.sx0 = srpContext.scissor.x; st.sx1 = srpContext.scissor.x + srpContext.scissor.width;
+	st.sy0 = srpContext.scissor.y; st.sy1 = srpContext.scissor.y + srpContext.scissor.height;
+	st.stencilEnabled = srpContext.stencil.enabled;
+	const SRPStencilFaceState* fsrc[2] = { &srpContext.stencil.front, &srpContext.stencil.back };
+	StencilFace* fdst[2] = { &st.front, &st.back };
+	for (int i = 0; i < 2; ++i) {
+		fdst[i]->func = fsrc[i]->func; fdst[i]->sfail = fsrc[i]->sfailOp; fdst[i]->dfail = fsrc[i]->dfailOp;
+		fdst[i]->pass = fsrc[i]->passOp; fdst[i]->ref = fsrc[i]->ref; fdst[i]->mask = fsrc[i]->mask;
+		fdst[i]->writeMask = fsrc[i]->writeMask;
+	}
+	st.depthTest = srpContext.depth.testEnable;
+	st.depthWrite = srpContext.depth.writeEnable;
+	st.depthOp = srpContext.depth.compareOp;
+	st.earlyZ = 1;
+	st.tile = kTile;
+	P.vsId = lookupVS((void*) sp0->vs->shader);
+	P.fsId = lookupFS((void*) sp0->fs->shader);
+	P.prim = SRP_PRIM_TRIANGLES;
+
+	/* descriptors and prefix sums */
+	passDesc.assign(n, DrawDesc());
+	passPrefix.assign(4 * (n + 1), 0u);
+	uint32_t* pIn = passPrefix.data();
+	uint32_t* pV = pIn + (n + 1);
+	uint32_t* pT = pV + (n + 1);
+	uint32_t* pB = pT + (n + 1);
+	unsigned long long pix = 0;
+	int maxStride = 4;
+	std::vector<unsigned long long> pixBase(n);
+	for (size_t k = 0; k < n; ++k) {
+		const SRPGpuDraw& d = draws[idx[k]];
+		SRPVertexBuffer* vb = (SRPVertexBuffer*) d.vertexBuffer;
+		SRPIndexBuffer* ib = (SRPIndexBuffer*) d.indexBuffer;
+		if (!uploadVB(vb) || (ib && !uploadIB(ib))) return false;
+		FbExtra* fx = fbFind(d.framebuffer);
+		DrawDesc& D = passDesc[k];
+		D.vertices = vb->dev.as<unsigned char>();
+		D.indices = ib ? ib->dev.ptr : nullptr;
+		D.indexSize = ib ? (int) ib->elemSize : 0;
+		D.start = d.startIndex;
+		D.count = d.count;
+		D.nVertices = vb->nVertices;
+		D.stride = (int) vb->stride;
+		D.prim = d.primitive;
+		D.W = (int) d.framebuffer->width;
+		D.H = (int) d.framebuffer->height;
+		D.tilesX = (D.W + kTile - 1) / kTile;
+		D.tilesY = (D.H + kTile - 1) / kTile;
+		D.color = fx->color; D.depth = fx->depth; D.stencil = fx->stencil;
+		if (d.program->uniform) {
+			SRPStdUniform u;
+			memcpy(&u, d.program->uniform, sizeof u);
+			if (u.texture) {
+				SRPTexture* t = u.texture;
+				if (!textureSync(t)) return false;
+				u.texture = (SRPTexture*) t->desc;
+			}
+			memcpy(D.uniform, &u, sizeof u);
+		}
+		maxStride = std::max(maxStride, D.stride);
+		pIn[k + 1] = pIn[k] + (uint32_t) nInOf[k];
+		pV[k + 1] = pV[k] + (uint32_t) D.nVertices;
+		pT[k + 1] = pT[k] + (uint32_t) D.tilesX * (uint32_t) D.tilesY;
+		pB[k + 1] = pB[k] + (uint32_t) ((D.nVertices + 127) / 128);
+		pixBase[k] = pix;
+		pix += d.framebuffer->size;
+	}
+	const uint32_t nIn = pIn[n], vRows = pV[n], numTiles = pT[n], vBlocks = pB[n];
+	if (!passDescDev.reserve(n * sizeof(DrawDesc), FN) || !passPrefixDev.reserve(passPrefix.size() * 4, FN) ||
+	    !passPrimPrefix.reserve((n + 1) * 4, FN) || !passWinner.reserve(pix * 4 + 4, FN))
+		return false;
+	for (size_t k = 0; k < n; ++k) passDesc[k].winner = passWinner.as<int32_t>() + pixBase[k];
+	cudaMemcpyAsync(passDescDev.ptr, passDesc.data(), n * sizeof(DrawDesc), cudaMemcpyHostToDevice, g.stream);
+	cudaMemcpyAsync(passPrefixDev.ptr, passPrefix.data(), passPrefix.size() * 4, cudaMemcpyHostToDevice, g.stream);
+	P.draws = passDescDev.as<DrawDesc>();
+	P.nDraws = (uint32_t) n;
+	P.inPrefix = passPrefixDev.as<uint32_t>();
+	P.vPrefix = P.inPrefix + (n + 1);
+	P.tPrefix = P.vPrefix + (n + 1);
+	P.blkPrefix = P.tPrefix + (n + 1);
+	P.primPrefix = passPrimPrefix.as<uint32_t>();
+	P.nIn = (int) nIn;
+	P.nVertices = vRows;
+	P.minmax = g.minmax.as<unsigned long long>();
+	P.ctr = g.ctr.as<DeviceCounters>();
+	if (g.fbMode == SRP_GPU_FB_COHERENT)
+		for (size_t k = 0; k < n; ++k) fbUpload(draws[idx[k]].framebuffer, fbFind(draws[idx[k]].framebuffer));
+
+	uint32_t primCap = (uint32_t) std::min<unsigned long long>((unsigned long long) nIn + 4096, 0x3FFFFFFFu);
+	uint32_t entryCap = (uint32_t) std::min<double>(primCap * g.entryRatio + 4096, 4.0e9);
+	bool drawn = false;
+	for (int attempt = 0; attempt < 4 && !drawn; ++attempt) {
+		const unsigned long long rows = (unsigned long long) vRows + g.clipRows;
+		const size_t nw = (size_t) std::max(P.L.nWords, 1);
+		const uint32_t blocks = (nIn + kSetupThreads - 1) / kSetupThreads;
+		bool ok = g.clip.reserve(rows * 16, FN) && g.vary.reserve(rows * nw * 4, FN) &&
+		          g.vset0.reserve((size_t) vRows * 16 + 16, FN) && g.vset1.reserve((size_t) vRows * 16 + 16, FN) &&
+		          g.lookback.reserve((size_t) std::max(blocks, 1u) * 8, FN) &&
+		          g.keys.reserve((size_t) entryCap * 4, FN) && g.vals.reserve((size_t) entryCap * 4, FN) &&
+		          g.big.reserve((size_t) g.bigCap * 16, FN) && g.table.reserve((size_t) g.tableCap * 4, FN) &&
+		          g.clipSlot.reserve((size_t) nIn * 4 + 4, FN) &&
+		          g.clipPolys.reserve((size_t) g.clipPolyCap * (1 + kMaxPoly) * 4, FN) &&
+		          g.triR.reserve((size_t) primCap * sizeof(TriRaster), FN) &&
+		          g.triA.reserve((size_t) primCap * sizeof(TriAttr), FN);
+		if (!ok) return false;
+		P.clip = g.clip.as<float4>();
+		P.vset0 = g.vset0.as<float4>();
+		P.vset1 = g.vset1.as<float4>();
+		P.vary = g.vary.as<uint32_t>();
+		P.clipBase = vRows;
+		P.clipCap = g.clipRows;
+		P.triR = g.triR.as<TriRaster>();
+		P.triA = g.triA.as<TriAttr>();
+		P.primCap = primCap;
+		P.keys = g.keys.as<uint32_t>();
+		P.vals = g.vals.as<uint32_t>();
+		P.entryCap = entryCap;
+		P.bigJobs = g.big.as<uint4>();
+		P.bigCap = g.bigCap;
+		P.table = g.table.as<float>();
+		P.tableCap = g.tableCap;
+		P.clipSlot = g.clipSlot.as<uint32_t>();
+		P.clipPolys = g.clipPolys.as<uint32_t>();
+		P.clipPolyCap = g.clipPolyCap;
+		P.lookback = g.lookback.as<unsigned long long>();
+
+		stageBegin();
+		launchReset(P, g.stream);
+		launchVertexMulti(P, vBlocks, maxStride, g.stream);
+		stageEnd(SRP_GPU_STAGE_VERTEX, 2);
+		stageBegin();
+		cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, g.stream);
+		launchClipPrepassMulti(P, g.stream);
+		launchSetupMulti(P, g.stream);
+		stageEnd(SRP_GPU_STAGE_SETUP, 2);
+		g.launches += 4;
+		if (!cudaOk(cudaGetLastError(), FN, "launch") || !readCounters()) return false;
+		const DeviceCounters c = *g.hostCtr;
+		if (c.errors & kErrBadIndex) {
+			/* some draw indexes past its vertex buffer: let each report alone */
+			for (size_t k = 0; k < n; ++k) {
+				const SRPGpuDraw& d = draws[idx[k]];
+				drawBuffer(d.indexBuffer, d.vertexBuffer, d.framebuffer, d.program, d.primitive, d.startIndex, d.count);
+			}
+			return true;
+		}
+		if (c.errors & kErrSpin) { SRP_ERROR(FN, "Ordered-compaction wait timed out"); return false; }
+		const bool over = c.clipVerts > g.clipRows || c.prims > primCap || c.entries > entryCap || c.bigJobs > g.bigCap ||
+		                  c.tableWords > g.tableCap || c.clipTris > g.clipPolyCap;
+		if ((c.errors & kErrCapacity) || over) {
+			bool grew = false;
+			if (c.clipVerts > g.clipRows) { g.clipRows = (uint32_t) std::min<unsigned long long>(c.clipVerts * 2, 0x7FFFFFFF); grew = true; }
+			if (c.prims > primCap) { primCap = (uint32_t) std::min<unsigned long long>(c.prims + 1024, 0x3FFFFFFF); grew = true; }
+			if (c.entries > entryCap) { entryCap = (uint32_t) std::min<double>(c.entries * 1.25 + 1024, 4.0e9); grew = true; }
+			if (c.bigJobs > g.bigCap) { g.bigCap = (uint32_t) std::min<unsigned long long>(c.bigJobs * 2, 1u << 30); grew = true; }
+			if (c.clipTris > g.clipPolyCap) { g.clipPolyCap = (uint32_t) std::min<unsigned long long>(c.clipTris * 2, 1u << 30); grew = true; }
+			if (c.tableWords > g.tableCap) { g.tableCap = std::min<unsigned long long>(c.tableWords * 5 / 4 + 1024, 0xFFFFFFFFull); grew = true; }
+			if (!grew) { SRP_ERROR(FN, "Scratch capacity exceeded"); return false; }
+			continue;
+		}
+		if (c.prims) g.entryRatio = std::max(1.0, std::min(64.0, (double) c.entries / (double) c.prims * 1.25));
+		g.stats.primitives += c.prims;
+		g.stats.binEntries += c.entries;
+		g.stats.clipOverflows += c.clipOverflow;
+		const uint32_t E = (uint32_t) c.entries;
+		stageBegin();
+		int binLaunches = 0;
+		if (c.bigJobs) { launchBigEntriesMulti(P, (uint32_t) c.bigJobs, g.stream); binLaunches += 2; }
+		g.launches += binLaunches;
+		drawn = true;
+		if (E == 0) { stageEnd(SRP_GPU_STAGE_BIN, binLaunches); break; }
+		const uint32_t keyBits = bitsFor(numTiles);
+		if (!g.keys2.reserve((size_t) E * 4, FN) || !g.vals2.reserve((size_t) E * 4, FN) ||
+		    !g.hist.reserve(sortHistWords(E) * 4, FN) || !g.partials.reserve(sortPartialWords(E) * 4 + 64, FN) ||
+		    !g.tileStart.reserve((size_t) (numTiles + 1) * 4, FN) || !g.tileEnd.reserve((size_t) (numTiles + 1) * 4, FN) ||
+		    !g.heavy.reserve((size_t) (numTiles + 1) * 4, FN)) return false;
+		uint32_t* sk;
+		uint32_t* sv;
+		sortEntries(P, E, keyBits, g.keys2.as<uint32_t>(), g.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
+		            g.partials.as<uint32_t>(), &sk, &sv, g.stream);
+		g.launches += 1 + keyBits / 8;
+		P.tileStart = g.tileStart.as<uint32_t>();
+		P.tileEnd = g.tileEnd.as<uint32_t>();
+		cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, g.stream);
+		cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, g.stream);
+		launchTileRanges(P, sk, E, numTiles, g.stream);
+		stageEnd(SRP_GPU_STAGE_BIN, binLaunches + 1 + (int) (keyBits / 8) + 1);
+		g.profile.resolveTiles += numTiles;
+		g.profile.resolveItems += E;
+		stageBegin();
+		launchResolveMulti(P, sv, numTiles, g.heavy.as<uint32_t>(), g.stream, g.auxStream, g.forkEvent, g.joinEvent);
+		stageEnd(SRP_GPU_STAGE_RESOLVE, 3);
+		stageBegin();
+		launchShadeMulti(P, numTiles, g.stream);
+		stageEnd(SRP_GPU_STAGE_SHADE, 1);
+		g.launches += 5;
+		cudaOk(cudaGetLastError(), FN, "launch");
+	}
+	if (!drawn) SRP_ERROR(FN, "Scratch capacity could not be sized for the pass");
+	g.stats.draws += n;
+	if (g.fbMode == SRP_GPU_FB_COHERENT)
+		for (size_t k = 0; k < n; ++k) fbDownload(draws[idx[k]].framebuffer, fbFind(draws[idx[k]].framebuffer));
+	return true;
+}
+
 extern "C" {
 
 void srpDrawVertexBuffer(const SRPVertexBuffer* vb, const SRPFramebuffer* fb, const SRPShaderProgram* sp,
@@ -1051,6 +1313,49 @@ void srpDrawIndexBuffer(const SRPIndexBuffer* ib, const SRPVertexBuffer* vb, con
                         const SRPShaderProgram* sp, SRPPrimitive prim, size_t start, size_t count)
 {
 	drawBuffer(ib, vb, fb, sp, prim, start, count);
+}
+
+void srpGpuDrawBatch(const SRPGpuDraw* draws, size_t n)
+{
+	if (!draws || n == 0) return;
+	if (!ensureInit("srpGpuDrawBatch")) return;
+	/* limits of one pass: 32-bit input, row and tile numbers, 24-bit tile keys */
+	const unsigned long long kMaxIn = 0x7FFFFFFFull, kMaxRows = 0x7FFFFFFFull - (1ull << 24), kMaxTiles = 1ull << 24;
+	size_t i = 0;
+	std::vector<size_t> idx, nInOf;
+	std::vector<const SRPFramebuffer*> fbs;
+	while (i < n) {
+		idx.clear(); nInOf.clear(); fbs.clear();
+		unsigned long long in = 0, rows = 0, tiles = 0;
+		VaryingLayout L0;
+		int vs0 = 0, fs0 = 0;
+		size_t j = i;
+		for (; j < n; ++j) {
+			const SRPGpuDraw& d = draws[j];
+			const size_t k = passInputs(d);
+			if (!k) break;
+			const int vs = lookupVS((void*) d.program->vs->shader), fs = lookupFS((void*) d.program->fs->shader);
+			VaryingLayout L;
+			if (!buildLayout(d.program->vs, L)) break;
+			if (idx.empty()) { L0 = L; vs0 = vs; fs0 = fs; }
+			else if (vs != vs0 || fs != fs0 || memcmp(&L, &L0, sizeof L) != 0) break;
+			if (std::find(fbs.begin(), fbs.end(), d.framebuffer) != fbs.end()) break;
+			const unsigned long long t = (unsigned long long) ((d.framebuffer->width + kTile - 1) / kTile) *
+			                             ((d.framebuffer->height + kTile - 1) / kTile);
+			if (in + k > kMaxIn || rows + d.vertexBuffer->nVertices > kMaxRows || tiles + t >= kMaxTiles) break;
+			in += k; rows += d.vertexBuffer->nVertices; tiles += t;
+			idx.push_back(j); nInOf.push_back(k); fbs.push_back(d.framebuffer);
+		}
+		if (idx.size() >= 2) {
+			for (size_t k : idx) warnExcess(draws[k].primitive, draws[k].count);
+			if (!runPass(draws, idx, nInOf)) return;
+			i = j;
+		} else {
+			const SRPGpuDraw& d = draws[i];
+			drawBuffer(d.indexBuffer, d.vertexBuffer, d.framebuffer, d.program, d.primitive, d.startIndex, d.count);
+			++i;
+		}
+	}
 }
 
 /* ------------------------------------------------------- stream and stats */

@@ -1130,6 +1130,104 @@ static void buildLit(Scene* s, Rng* rng)
 	s->draws = 2;
 }
 
+/* One scene of the batched workload: a single mesh of random triangles
+ * (log-uniform 12 to 200k of them) in its own framebuffer (each side
+ * log-uniform 64 to 1024), random camera, textured Blinn-Phong with one
+ * light. The mesh is a randomly displaced grid, so its triangles are small
+ * and connected; its placement makes some scenes cross the near plane.
+ * State: CCW front faces, back-face culling, depth LESS, depth cleared to 1. */
+static void bsceneState(void)
+{
+	srpRasterFrontFace(SRP_WINDING_CCW);
+	srpRasterCullFace(SRP_FACE_BACK);
+	srpDepthTest(true);
+	srpDepthCompareOp(SRP_COMPARE_LESS);
+}
+
+static void renderBScene(Scene* s, SRPFramebuffer* fb)
+{
+	bsceneState();
+	drawI(s, 0, 0, fb, 0, SRP_PRIM_TRIANGLES, 0, s->ibytes[0] / 4);
+}
+
+static void buildBScene(Scene* s, Rng* rng)
+{
+	double w = logUniform(rng, 64, 1024), h = logUniform(rng, 64, 1024);
+	double tris = logUniform(rng, 12, 200000);
+	if (s->scale < 1.0) {
+		const double lin = dexp(0.5 * dlog(s->scale));
+		w *= lin; h *= lin; tris *= s->scale;
+	}
+	s->W = (int) w < 16 ? 16 : (int) w;
+	s->H = (int) h < 16 ? 16 : (int) h;
+	if (tris < 12) tris = 12;
+	/* grid of gx x gy cells, two triangles per cell */
+	const double aspect = rngRange(rng, 0.5, 2.0);
+	int gx = (int) (dexp(0.5 * dlog(tris / 2 * aspect)) + 0.5);
+	if (gx < 2) gx = 2;
+	int gy = (int) (tris / 2 / gx + 0.5);
+	if (gy < 2) gy = 2;
+	const size_t nv = (size_t) (gx + 1) * (gy + 1), words = 8;
+	float* v = (float*) malloc(nv * words * sizeof(float));
+	const double bump = rngRange(rng, 0.0, 0.08);
+	for (int j = 0; j <= gy; ++j)
+		for (int i = 0; i <= gx; ++i) {
+			float* p = v + ((size_t) j * (gx + 1) + i) * words;
+			const double u = (double) i / gx, t = (double) j / gy;
+			const double dz = rngRange(rng, -bump, bump);
+			p[0] = (float) ((u - 0.5) * 2.0 * aspect / (aspect > 1 ? aspect : 1));
+			p[1] = (float) ((t - 0.5) * 2.0 / (aspect > 1 ? aspect : 1));
+			p[2] = (float) dz;
+			const double nx = rngRange(rng, -0.3, 0.3), ny = rngRange(rng, -0.3, 0.3);
+			p[3] = (float) nx; p[4] = (float) ny; p[5] = 1.0f;
+			p[6] = (float) (u * 4.0); p[7] = (float) (t * 4.0);
+		}
+	const size_t ni = (size_t) gx * gy * 6;
+	uint32_t* idx = (uint32_t*) malloc(ni * sizeof(uint32_t));
+	size_t k = 0;
+	for (int j = 0; j < gy; ++j)
+		for (int i = 0; i < gx; ++i) {
+			const uint32_t a = (uint32_t) (j * (gx + 1) + i), b = a + 1, c = a + (uint32_t) (gx + 1), d = c + 1;
+			idx[k++] = a; idx[k++] = b; idx[k++] = d;
+			idx[k++] = a; idx[k++] = d; idx[k++] = c;
+		}
+	addVB(s, v, words * 4, nv * words * 4);
+	addIB(s, SRP_UINT32, idx, ni * 4);
+	s->nTris = ni / 3;
+	free(v);
+	free(idx);
+	uint8_t* tex = (uint8_t*) malloc(64 * 64 * 3);
+	for (int i = 0; i < 64 * 64 * 3; ++i) tex[i] = (uint8_t) (rngNext(rng) >> 56);
+	s->tex = makeTexture(s, tex, 64, 64, TW_REPEAT, TW_REPEAT);
+	free(tex);
+	SRPStdUniform* u = &s->uni[0];
+	baseUniform(u);
+	/* tilted by up to about 70 degrees, so the front side mostly faces the camera */
+	double ang[3];
+	ang[0] = rngRange(rng, -1.2, 1.2);
+	ang[1] = rngRange(rng, -1.2, 1.2);
+	ang[2] = rngRange(rng, 0, 2 * PI_D);
+	u->model = rotation(ang[0], ang[1], ang[2]);
+	const double dist = rngRange(rng, 0.9, 3.5);
+	u->view = mat4ConstructTranslate(0, 0, (float) dist);
+	u->projection = perspective60((float) s->W / (float) s->H, 0.1f, 100.f);
+	u->cameraPos[2] = (float) -dist;
+	u->normalOffset = 3; u->uvOffset = 6;
+	u->texture = s->tex;
+	u->nLights = 1;
+	u->lightPos[0][0] = (float) rngRange(rng, -3, 3);
+	u->lightPos[0][1] = (float) rngRange(rng, -3, 3);
+	u->lightPos[0][2] = (float) rngRange(rng, -4, -1);
+	for (int c = 0; c < 3; ++c) u->lightColor[0][c] = (float) rngRange(rng, 0.5, 1.0);
+	SRPVaryingInfo v0[3] = { vi(3, SRP_FLOAT, SRP_INTERPOLATION_MODE_PERSPECTIVE),
+	                         vi(3, SRP_FLOAT, SRP_INTERPOLATION_MODE_PERSPECTIVE),
+	                         vi(2, SRP_FLOAT, SRP_INTERPOLATION_MODE_PERSPECTIVE) };
+	program(s, 0, srpVsWorld, srpFsBlinnPhong, 0, 3, v0);
+	s->depthInit = 1.0f;
+	s->render = renderBScene;
+	s->draws = 1;
+}
+
 /* ------------------------------------------------------------- registry */
 
 typedef struct SceneDef { const char* name; void (*build)(Scene*, Rng*); } SceneDef;
@@ -1149,6 +1247,7 @@ static const SceneDef DEFS[] = {
 	{ "topologies", buildTopologies },
 	{ "late_z", buildLateZ },
 	{ "lit", buildLit },
+	{ "bscene", buildBScene },
 };
 
 const char* const* sceneNames(void)
@@ -1239,6 +1338,29 @@ void sceneRender(Scene* s, SRPFramebuffer* fb)
 	resetContext();
 	s->render(s, fb);
 }
+
+#ifdef SCENES_GPU
+int sceneDrawDesc(Scene* s, SRPFramebuffer* fb, SRPGpuDraw* out)
+{
+	if (s->render != renderBScene) return 1;
+	out->indexBuffer = s->ib[0];
+	out->vertexBuffer = s->vb[0];
+	out->framebuffer = fb;
+	out->program = &s->sp[0];
+	out->primitive = SRP_PRIM_TRIANGLES;
+	out->startIndex = 0;
+	out->count = s->ibytes[0] / 4;
+	return 0;
+}
+
+void sceneBatchRender(Scene** scenes, SRPFramebuffer** fbs, size_t n, SRPGpuDraw* scratch)
+{
+	resetContext();
+	bsceneState();
+	for (size_t i = 0; i < n; ++i) sceneDrawDesc(scenes[i], fbs[i], &scratch[i]);
+	srpGpuDrawBatch(scratch, n);
+}
+#endif
 
 int sceneRunOnce(const char* name, uint64_t seed, double scale,
                  uint32_t* color, float* depth, uint8_t* stencil, int* width, int* height)

@@ -51,6 +51,15 @@ void sceneRender(Scene* s, SRPFramebuffer* fb);
  * bytes, pointer fields excluded) to `path`; used to compare machines. */
 int sceneDumpInputs(const Scene* s, const char* path);
 
+#ifdef SCENES_GPU
+#include "srp/gpu.h"
+/* Batched workload ("bscene" scenes, one draw each): the scene's draw as an
+ * srpGpuDrawBatch entry (returns nonzero for other scenes), and one batched
+ * render of n scenes into their framebuffers with the scenes' state. */
+int sceneDrawDesc(Scene* s, SRPFramebuffer* fb, SRPGpuDraw* out);
+void sceneBatchRender(Scene** scenes, SRPFramebuffer** fbs, size_t n, SRPGpuDraw* scratch);
+#endif
+
 /* Convenience: create a framebuffer of the scene's size, prepare, render, copy
  * the planes out (color W*H u32, depth W*H f32, stencil W*H u8). Returns 0 on
  * success. */

@@ -1,0 +1,127 @@
+"""srpGpuDrawBatch: scenes of the batched workload (one textured, lit mesh
+each, framebuffers of different sizes) rendered by multi-draw passes must be
+bit-identical to the same scenes drawn one by one with srpDrawIndexBuffer, and
+match the CPU oracle. All calls go through the C API of libsrp_gb300.so."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle_util import oracle_render, compare_planes
+
+pytestmark = pytest.mark.gpu
+
+BASE = 11
+
+
+def make_scenes(n, scale):
+    import srp_gb300
+    return [srp_gb300.Scene("bscene", srp_gb300.batch_seed(BASE, i), scale) for i in range(n)]
+
+
+def sync_planes(srp_gb300, S, fb):
+    S.srpGpuFramebufferSync(fb)
+    c, d, s = srp_gb300.framebuffer_arrays(fb)
+    return c, d.view(np.uint32), s
+
+
+@pytest.mark.parametrize("mode", [1, 0], ids=["device", "coherent"])
+def test_batch_matches_single_draws(built_library, mode):
+    import srp_gb300
+    L = srp_gb300.lib()
+    S = srp_gb300.scenes()
+    L.srpGpuSetFramebufferMode(mode)
+    scenes = make_scenes(40, 0.25)
+    try:
+        want = []
+        for sc in scenes:
+            sc.prepare()
+            sc.render()
+            want.append(sync_planes(srp_gb300, S, sc.fb))
+        fbs = []
+        for sc in scenes:
+            fb = S.srpNewFramebuffer(sc.info.width, sc.info.height)
+            S.scenePrepareFramebuffer(sc.ptr, fb)
+            fbs.append(fb)
+        L.srpGpuResetStats()
+        srp_gb300.render_batch(scenes, fbs)
+        st = srp_gb300.SRPGpuStats()
+        L.srpGpuGetStats(ctypes.byref(st))
+        assert L.srpGpuSynchronize() == 0
+        assert st.draws == len(scenes)
+        drawn = 0
+        for i, (sc, fb) in enumerate(zip(scenes, fbs)):
+            got = sync_planes(srp_gb300, S, fb)
+            for name, a, b in zip(("color", "depth", "stencil"), got, want[i]):
+                bad = np.flatnonzero(a != b)
+                assert bad.size == 0, f"scene {i}: {name} differs at {bad.size} pixels"
+            drawn += int(np.count_nonzero(want[i][1] != np.float32(1.0).view(np.uint32)))
+        assert drawn > 10000, "the batch should cover pixels"
+    finally:
+        for fb in locals().get("fbs", []):
+            S.srpFreeFramebuffer(fb)
+        for sc in scenes:
+            sc.close()
+
+
+def test_batch_shared_framebuffer_and_order(built_library):
+    """Draws that share a framebuffer split the pass and keep their order."""
+    import srp_gb300
+    L = srp_gb300.lib()
+    S = srp_gb300.scenes()
+    L.srpGpuSetFramebufferMode(1)
+    scenes = make_scenes(9, 0.2)
+    try:
+        order = [0, 1, 2, 2, 3, 4, 4, 4, 5]   # framebuffer of each draw
+        fb_sizes = {}
+        for k, sc in zip(order, scenes):
+            fb_sizes.setdefault(k, (sc.info.width, sc.info.height))
+        def fresh():
+            out = {}
+            for k, (w, h) in fb_sizes.items():
+                fb = S.srpNewFramebuffer(w, h)
+                S.scenePrepareFramebuffer(scenes[order.index(k)].ptr, fb)
+                out[k] = fb
+            return out
+        ref = fresh()
+        for k, sc in zip(order, scenes):
+            S.sceneRender(sc.ptr, ref[k])
+        got = fresh()
+        srp_gb300.render_batch(scenes, [got[k] for k in order])
+        assert L.srpGpuSynchronize() == 0
+        for k in fb_sizes:
+            a = sync_planes(srp_gb300, S, got[k])
+            b = sync_planes(srp_gb300, S, ref[k])
+            for name, x, y in zip(("color", "depth", "stencil"), a, b):
+                assert np.array_equal(x, y), f"framebuffer {k}: {name} differs"
+        for fb in list(ref.values()) + list(got.values()):
+            S.srpFreeFramebuffer(fb)
+    finally:
+        for sc in scenes:
+            sc.close()
+
+
+@pytest.mark.parametrize("i", [0, 3, 7, 12, 21, 30])
+def test_batch_scene_matches_oracle(built_library, oracle_exe, i):
+    """Scenes of a batch against the oracle's rendering of the same scene."""
+    import srp_gb300
+    L = srp_gb300.lib()
+    S = srp_gb300.scenes()
+    L.srpGpuSetFramebufferMode(1)
+    scenes = make_scenes(32, 0.25)
+    try:
+        fbs = [S.srpNewFramebuffer(sc.info.width, sc.info.height) for sc in scenes]
+        for sc, fb in zip(scenes, fbs):
+            S.scenePrepareFramebuffer(sc.ptr, fb)
+        srp_gb300.render_batch(scenes, fbs)
+        c, d, s = sync_planes(srp_gb300, S, fbs[i])
+        want = oracle_render(oracle_exe, "bscene", srp_gb300.batch_seed(BASE, i), 0.25)
+        assert want["hash"] == scenes[i].input_hash
+        got = {"color": c, "depth_bits": d, "stencil": s, "width": scenes[i].info.width,
+               "height": scenes[i].info.height}
+        compare_planes(got, want, f"batch scene {i}")
+        for fb in fbs:
+            S.srpFreeFramebuffer(fb)
+    finally:
+        for sc in scenes:
+            sc.close()
