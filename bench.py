@@ -150,6 +150,159 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+BATCH_BASE = 11
+BATCH_SCENES = 4096
+BATCH_WORKLOAD = ("batch: 4096 scenes, one textured Blinn-Phong mesh each (12-200k triangles, log-uniform), "
+                  "framebuffers 64-1024 per side (log-uniform), one srpGpuDrawBatch call")
+
+
+def cpu_batch_sample(scale, count, first=0):
+    """The oracle rendering scenes first..first+count-1 of the batch, one at a
+    time on one core: (seconds, fragments, scenes)."""
+    from srp_gb300 import batch_seed
+    exe = os.path.join(ROOT, "oracle", "_build", "port_scenes")
+    secs, frags = 0.0, 0
+    for i in range(first, first + count):
+        out = subprocess.check_output([exe, "time", "bscene", str(batch_seed(BATCH_BASE, i)), repr(float(scale)), "1"])
+        r = json.loads(out.decode().strip().splitlines()[-1])
+        secs += r["mean_s"]
+        frags += r["fragments"]
+    return secs, frags, count
+
+
+def run_reference_batch(args):
+    """The reference algorithm (CPU oracle) on all host cores over a sample of
+    the batch, one scene per task."""
+    import concurrent.futures as cf
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    from srp_gb300.build import build_oracle
+    build_oracle()
+    cores = os.cpu_count() or 1
+    sample = min(args.scenes, 16 * cores)
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=cores) as ex:
+        res = list(ex.map(lambda i: cpu_batch_sample(args.scale, 1, i), range(sample)))
+    wall = time.perf_counter() - t0
+    frags = sum(r[1] for r in res)
+    value = sample / wall
+    line = {"impl": "reference", "metric": "scenes/s", "value": round(value, 3), "unit": "scenes/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1000.0 * wall * args.scenes / sample, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": BATCH_WORKLOAD, "scenes": args.scenes, "mfrag_per_s": round(frags / wall / 1e6, 3)},
+            "cpu_baseline": {"value": round(value, 3), "unit": "scenes/s", "cores": cores, "kind": "port",
+                             "sample": f"scenes 0..{sample - 1} of the batch, {cores} threads, wall {wall:.1f}s"},
+            "e2e": {"value": round(value, 3), "unit": "scenes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_batch(args):
+    """The batched-scenes workload: all scenes drawn by one srpGpuDrawBatch
+    call per step (multi-draw passes)."""
+    import ctypes
+    import torch
+    import srp_gb300
+
+    srp_gb300.build()
+    L = srp_gb300.lib()
+    L.srpGpuSetFramebufferMode(srp_gb300.SRP_GPU_FB_DEVICE)
+    stream = torch.cuda.Stream()
+    L.srpGpuSetStream(ctypes.c_void_p(stream.cuda_stream))
+    t0 = time.perf_counter()
+    batch = [srp_gb300.Scene("bscene", srp_gb300.batch_seed(BATCH_BASE, i), args.scale) for i in range(args.scenes)]
+    gen_s = time.perf_counter() - t0
+    fbs = [sc.fb for sc in batch]
+    tris = sum(sc.info.inputTriangles for sc in batch)
+    pixels = sum(sc.info.width * sc.info.height for sc in batch)
+    h2d = sum(sc.info.vertexBytes + sc.info.indexBytes for sc in batch)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def prepare():
+        for sc in batch:
+            sc.prepare()
+
+    for _ in range(max(args.warmup, 1)):
+        with torch.cuda.stream(stream):
+            prepare()
+            srp_gb300.render_batch(batch, fbs)
+    torch.cuda.synchronize()
+    L.srpGpuResetStats()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    times = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+            prepare()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            srp_gb300.render_batch(batch, fbs)
+            e1.record(stream)
+        stream.synchronize()
+        times.append(e0.elapsed_time(e1))
+    st = srp_gb300.SRPGpuStats()
+    L.srpGpuGetStats(ctypes.byref(st))
+    frags = st.fragments / max(args.steps, 1)
+    e2e = []
+    for _ in range(max(1, args.steps // 2)):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for sc in batch:
+            sc.upload()
+        prepare()
+        srp_gb300.render_batch(batch, fbs)
+        for sc in batch:
+            sc.sync()
+        e2e.append(time.perf_counter() - t1)
+    clk = clocks.stop()
+    L.srpGpuSetProfiling(1)
+    L.srpGpuResetProfile()
+    with torch.cuda.stream(stream):
+        prepare()
+        srp_gb300.render_batch(batch, fbs)
+    prof = srp_gb300.SRPGpuProfile()
+    L.srpGpuGetProfile(ctypes.byref(prof))
+    L.srpGpuSetProfiling(0)
+    stage_ms = {n: prof.ms[i] for i, n in enumerate(srp_gb300.STAGES)}
+    total_ms = sum(times)
+    step_s = total_ms / args.steps / 1000.0
+    peak, peak_kind = peaks()
+    resolve_bytes = prof.resolveItems * 68 + pixels * 14
+    resolve_gbs = resolve_bytes / (stage_ms["resolve"] / 1000.0) / 1e9 if stage_ms["resolve"] > 0 else 0.0
+    e2e_s = sum(e2e) / len(e2e)
+    line = {
+        "metric": "scenes/s", "value": round(args.scenes / step_s, 2), "unit": "scenes/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": BATCH_WORKLOAD, "scenes": args.scenes, "scale": args.scale, "triangles": tris,
+                   "pixels": pixels, "fragments_per_step": frags, "mfrag_per_s": round(frags / step_s / 1e6, 1),
+                   "mtri_per_s": round(tris / step_s / 1e6, 1), "generation_s": round(gen_s, 1),
+                   "l2": "flushed between steps (256 MB write)"},
+        "clocks": clk,
+        "e2e": {"value": round(args.scenes / e2e_s, 2), "unit": "scenes/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(pixels * 9)},
+        "gpu_launches": int(st.kernelLaunches),
+        "roofline": {"bound": "hbm", "achieved": round(resolve_gbs, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(resolve_gbs / peak, 5), "traffic": None,
+                     "kernel": "resolve stage (k_tile_classify + k_resolve + k_resolve_heavy, multi-draw)",
+                     "algorithmic_bytes_per_step": int(resolve_bytes), "ms_per_step": round(stage_ms["resolve"], 3),
+                     "note": f"peak {peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "stages_ms_per_step": {k: round(v, 3) for k, v in stage_ms.items()},
+    }
+    if not args.no_cpu_baseline:
+        from srp_gb300.build import build_oracle
+        build_oracle()
+        secs, cfr, cnt = cpu_batch_sample(args.scale, 48)
+        line["cpu_baseline"] = {"value": round(cnt / secs, 3), "unit": "scenes/s", "cores": 1, "kind": "port",
+                                "sample": f"scenes 0..{cnt - 1} of the batch on 1 host core, "
+                                          f"{round(cfr / secs / 1e6, 2)} Mfrag/s"}
+    print(json.dumps(line))
+    for sc in batch:
+        sc.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -158,7 +311,12 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="frame", choices=["frame", "batch"],
+                    help="frame: the 2M-triangle 1080p frame (default); batch: the batched-scenes workload")
+    ap.add_argument("--scenes", type=int, default=BATCH_SCENES, help="scenes per batch (--workload batch)")
     args = ap.parse_args()
+    if args.workload == "batch":
+        return run_reference_batch(args) if args.impl == "reference" else run_batch(args)
     if args.impl == "reference":
         return run_reference(args)
 
