@@ -154,8 +154,8 @@ struct DeviceCounters {
 	unsigned long long clipTris;     /* triangles clipped by the pre-pass */
 	unsigned int errors;             /* bit mask, see kErr* */
 	unsigned int lookbackTicket;
-	unsigned int nonEmptyTiles;
-	unsigned int pad;
+	unsigned int nonEmptyTiles;      /* heavy tiles listed by k_tile_classify */
+	unsigned int abort;              /* set by k_check: a count exceeded its buffer, skip the rest */
 };
 
 enum : unsigned {

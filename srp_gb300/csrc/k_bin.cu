@@ -23,10 +23,21 @@ constexpr int kMaxPasses = 3;                       /* keys up to 24 bits */
 
 /* Digit counts of every pass in one read of the keys (the totals do not
  * depend on the order the passes leave the keys in). */
-__global__ void __launch_bounds__(kSortThreads) k_radix_global_hist(const uint32_t* keys, uint32_t n, uint32_t passes,
-                                                                   uint32_t* ghist)
+/* The number of pairs, as counted by setup (at most the scratch's size), or 0
+ * once the draw has been aborted. */
+__device__ __forceinline__ uint32_t pairCount(const DeviceCounters* ctr, uint32_t cap)
+{
+	if (ctr->abort) return 0;
+	const unsigned long long n = ctr->entries;
+	return n < cap ? (uint32_t) n : cap;
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_radix_global_hist(const uint32_t* keys, const DeviceCounters* ctr,
+                                                                   uint32_t cap, uint32_t passes, uint32_t* ghist)
 {
 	__shared__ uint32_t h[kMaxPasses][256];
+	const uint32_t n = pairCount(ctr, cap);
+	if (n == 0) return;
 	for (int i = threadIdx.x; i < kMaxPasses * 256; i += kSortThreads) (&h[0][0])[i] = 0;
 	__syncthreads();
 	for (uint32_t i = blockIdx.x * kSortThreads + threadIdx.x; i < n; i += gridDim.x * kSortThreads) {
@@ -70,11 +81,16 @@ __device__ __forceinline__ uint32_t lookBackStrided(const uint32_t* status, long
  * counts over rounds that follow input order; each block publishes its 256
  * digit counts and walks back over its predecessors' (decoupled look-back,
  * one thread per digit) to find where its run of each digit starts. */
-__global__ void __launch_bounds__(kSortThreads) k_radix_onesweep(const uint32_t* keysIn, const uint32_t* valsIn, uint32_t n,
+__global__ void __launch_bounds__(kSortThreads) k_radix_onesweep(const uint32_t* keysIn, const uint32_t* valsIn,
+                                                                const DeviceCounters* ctr, uint32_t cap,
                                                                 uint32_t shift, const uint32_t* ghistPass,
                                                                 uint32_t* status, uint32_t* ticket, uint32_t* errors,
                                                                 uint32_t* keysOut, uint32_t* valsOut)
 {
+	/* the grid is sized for the scratch; blocks past the real count leave at
+	 * once (their successors, which would look back at them, leave too) */
+	const uint32_t n = pairCount(ctr, cap);
+	if ((unsigned long long) blockIdx.x * kSortTileItems >= n) return;
 	__shared__ uint32_t cnt[kSortWarps][256];
 	__shared__ uint32_t digitBase[256];
 	__shared__ uint32_t digitStart[256];
@@ -139,14 +155,16 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_onesweep(const uint32_t*
 	}
 }
 
-__global__ void k_tile_ranges(const uint32_t* keys, uint32_t n, uint32_t numTiles, uint32_t* start, uint32_t* end)
+__global__ void k_tile_ranges(const uint32_t* keys, const DeviceCounters* ctr, uint32_t cap, uint32_t numTiles,
+                              uint32_t* start, uint32_t* end)
 {
-	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= n) return;
-	const uint32_t k = keys[i];
-	if (k >= numTiles) return;
-	if (i == 0 || keys[i - 1] != k) start[k] = i;
-	if (i == n - 1 || keys[i + 1] != k) end[k] = i + 1;
+	const uint32_t n = pairCount(ctr, cap);
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		const uint32_t k = keys[i];
+		if (k >= numTiles) continue;
+		if (i == 0 || keys[i - 1] != k) start[k] = i;
+		if (i == n - 1 || keys[i + 1] != k) end[k] = i + 1;
+	}
 }
 
 static uint32_t sortBlocks(uint32_t n) { return (n + kSortTileItems - 1) / kSortTileItems; }
@@ -156,24 +174,25 @@ size_t sortHistWords(uint32_t n) { return (size_t) kMaxPasses * 256 + (size_t) k
 
 size_t sortPartialWords(uint32_t) { return 8; }
 
-void sortEntries(const DrawParams& P, uint32_t n, uint32_t keyBits, uint32_t* keysAlt, uint32_t* valsAlt,
+void sortEntries(const DrawParams& P, uint32_t keyBits, uint32_t* keysAlt, uint32_t* valsAlt,
                  uint32_t* hist, uint32_t*, uint32_t** keysOut, uint32_t** valsOut, cudaStream_t s)
 {
 	uint32_t* kin = P.keys;
 	uint32_t* vin = P.vals;
 	uint32_t* kout = keysAlt;
 	uint32_t* vout = valsAlt;
-	const uint32_t nb = sortBlocks(n);
+	const uint32_t cap = P.entryCap;
+	const uint32_t nb = sortBlocks(cap);
 	const uint32_t passes = (keyBits + 7) / 8;
-	if (n > 1 && passes) {
+	if (cap > 0 && passes) {
 		uint32_t* ghist = hist;
 		uint32_t* tickets = hist + kMaxPasses * 256;
 		uint32_t* status = tickets + 8;
-		cudaMemsetAsync(hist, 0, sortHistWords(n) * 4, s);
+		cudaMemsetAsync(hist, 0, sortHistWords(cap) * 4, s);
 		const uint32_t hb = nb < 152u * 4u ? nb : 152u * 4u;
-		k_radix_global_hist<<<hb, kSortThreads, 0, s>>>(kin, n, passes, ghist);
+		k_radix_global_hist<<<hb, kSortThreads, 0, s>>>(kin, P.ctr, cap, passes, ghist);
 		for (uint32_t p = 0; p < passes; ++p) {
-			k_radix_onesweep<<<nb, kSortThreads, 0, s>>>(kin, vin, n, 8 * p, ghist + 256 * p,
+			k_radix_onesweep<<<nb, kSortThreads, 0, s>>>(kin, vin, P.ctr, cap, 8 * p, ghist + 256 * p,
 			                                            status + (size_t) p * 256 * nb, tickets + p, &P.ctr->errors,
 			                                            kout, vout);
 			uint32_t* t = kin; kin = kout; kout = t;
@@ -184,10 +203,12 @@ void sortEntries(const DrawParams& P, uint32_t n, uint32_t keyBits, uint32_t* ke
 	*valsOut = vin;
 }
 
-void launchTileRanges(const DrawParams& P, const uint32_t* keys, uint32_t n, uint32_t numTiles, cudaStream_t s)
+void launchTileRanges(const DrawParams& P, const uint32_t* keys, uint32_t numTiles, cudaStream_t s)
 {
-	if (!n) return;
-	k_tile_ranges<<<(n + 255) / 256, 256, 0, s>>>(keys, n, numTiles, P.tileStart, P.tileEnd);
+	const uint32_t cap = P.entryCap;
+	if (!cap) return;
+	const uint32_t blocks = (cap + 255) / 256 < 152u * 16u ? (cap + 255) / 256 : 152u * 16u;
+	k_tile_ranges<<<blocks, 256, 0, s>>>(keys, P.ctr, cap, numTiles, P.tileStart, P.tileEnd);
 }
 
 }  // namespace srpg

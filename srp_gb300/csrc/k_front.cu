@@ -45,6 +45,17 @@ __global__ void k_reset(const __grid_constant__ DrawParams P)
 	}
 }
 
+/* Abort flag of a draw (one thread, after setup): any count above the
+ * buffer it was meant for, or a bad index, stops the rest of the draw. */
+__global__ void k_check(const __grid_constant__ DrawParams P)
+{
+	if (threadIdx.x != 0) return;
+	const DeviceCounters& c = *P.ctr;
+	const bool over = c.clipVerts > P.clipCap || c.prims > P.primCap || c.entries > P.entryCap ||
+	                  c.bigJobs > P.bigCap || c.tableWords > P.tableCap || c.clipTris > P.clipPolyCap;
+	if (over || (c.errors & (kErrCapacity | kErrBadIndex | kErrSpin))) P.ctr->abort = 1u;
+}
+
 __device__ __forceinline__ unsigned long long fetchIndexRaw(const void* indices, int indexSize, unsigned long long i)
 {
 	switch (indexSize) {
@@ -874,8 +885,10 @@ __device__ void fillLambdaTable(const DrawParams& P, const TriRaster& R, int fir
 
 /* Entries of primitives covering more than kSmallEntries tiles: one block per
  * primitive writes its tiles row by row (and a triangle's lambda table). */
-__global__ void k_big_entries(const __grid_constant__ DrawParams P, uint32_t nJobs)
+__global__ void k_big_entries(const __grid_constant__ DrawParams P)
 {
+	if (P.ctr->abort) return;
+	const uint32_t nJobs = (uint32_t) min(P.ctr->bigJobs, (unsigned long long) P.bigCap);
 	for (uint32_t j = blockIdx.x; j < nJobs; j += gridDim.x) {
 		const uint4 job = P.bigJobs[j];
 		int x0, y0, x1;
@@ -899,8 +912,10 @@ __global__ void k_big_entries(const __grid_constant__ DrawParams P, uint32_t nJo
 
 /* Lambda tables of all big triangles: blockIdx.y walks the jobs, the
  * blockIdx.x blocks of a job share its (row, column-run) work items. */
-__global__ void k_lambda_tables(const __grid_constant__ DrawParams P, uint32_t nJobs)
+__global__ void k_lambda_tables(const __grid_constant__ DrawParams P)
 {
+	if (P.ctr->abort) return;
+	const uint32_t nJobs = (uint32_t) min(P.ctr->bigJobs, (unsigned long long) P.bigCap);
 	for (uint32_t j = blockIdx.y; j < nJobs; j += gridDim.y) {
 		const uint4 job = P.bigJobs[j];
 		if (job.z != kKindTri) continue;
@@ -956,8 +971,10 @@ constexpr uint32_t kShortLine = 48;   /* steps one thread walks on its own */
 
 /* One thread per line; lines longer than kShortLine steps are queued for
  * k_line_frags_long. */
-__global__ void k_line_frags(const __grid_constant__ DrawParams P, uint32_t nLines)
+__global__ void k_line_frags(const __grid_constant__ DrawParams P)
 {
+	if (P.ctr->abort) return;
+	const uint32_t nLines = (uint32_t) min(P.ctr->prims, (unsigned long long) P.primCap);
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	unsigned long long passed = 0;
 	if (i < nLines) {
@@ -977,6 +994,7 @@ __global__ void k_line_frags(const __grid_constant__ DrawParams P, uint32_t nLin
 /* Long lines: one warp per line, lane l walks a contiguous run of steps. */
 __global__ void k_line_frags_long(const __grid_constant__ DrawParams P)
 {
+	if (P.ctr->abort) return;
 	const uint32_t lane = threadIdx.x & 31;
 	const uint32_t nLong = (uint32_t) min(P.ctr->lineFrags, (unsigned long long) P.bigCap);
 	const uint32_t warps = gridDim.x * (blockDim.x / 32);
@@ -1253,8 +1271,10 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_multi(const __grid_cons
 }
 
 /* k_big_entries for a pass: the job's third word is its draw. */
-__global__ void k_big_entries_multi(const __grid_constant__ DrawParams P, uint32_t nJobs)
+__global__ void k_big_entries_multi(const __grid_constant__ DrawParams P)
 {
+	if (P.ctr->abort) return;
+	const uint32_t nJobs = (uint32_t) min(P.ctr->bigJobs, (unsigned long long) P.bigCap);
 	for (uint32_t j = blockIdx.x; j < nJobs; j += gridDim.x) {
 		const uint4 job = P.bigJobs[j];
 		const TriRaster& R = P.triR[job.x];
@@ -1273,8 +1293,10 @@ __global__ void k_big_entries_multi(const __grid_constant__ DrawParams P, uint32
 }
 
 /* Lambda tables of a pass's big triangles (every job is a triangle). */
-__global__ void k_lambda_tables_multi(const __grid_constant__ DrawParams P, uint32_t nJobs)
+__global__ void k_lambda_tables_multi(const __grid_constant__ DrawParams P)
 {
+	if (P.ctr->abort) return;
+	const uint32_t nJobs = (uint32_t) min(P.ctr->bigJobs, (unsigned long long) P.bigCap);
 	for (uint32_t j = blockIdx.y; j < nJobs; j += gridDim.y) {
 		const uint4 job = P.bigJobs[j];
 		fillLambdaTable(P, P.triR[job.x], blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
@@ -1328,17 +1350,23 @@ void launchClipPrepass(const DrawParams& P, cudaStream_t s)
 	if (blocks) k_clip_prepass<<<blocks, kSetupThreads, 0, s>>>(P);
 }
 
-void launchBigEntries(const DrawParams& P, uint32_t nJobs, cudaStream_t s)
+/* Grids for a job count the device holds: sized from the hint, any size is
+ * correct since the kernels stride over the jobs. */
+static unsigned bigBlocks(uint32_t hint) { return hint < 64u ? 64u : (hint < 152u * 16u ? hint : 152u * 16u); }
+static unsigned tableRows(uint32_t hint) { return hint < 64u ? 64u : (hint < 65535u ? hint : 65535u); }
+
+void launchCheck(const DrawParams& P, cudaStream_t s) { k_check<<<1, 32, 0, s>>>(P); }
+
+void launchBigEntries(const DrawParams& P, uint32_t jobsHint, cudaStream_t s)
 {
-	if (!nJobs) return;
-	k_big_entries<<<nJobs < 152u * 16u ? nJobs : 152u * 16u, 256, 0, s>>>(P, nJobs);
-	k_lambda_tables<<<dim3(8, nJobs < 65535u ? nJobs : 65535u), 256, 0, s>>>(P, nJobs);
+	k_big_entries<<<bigBlocks(jobsHint), 256, 0, s>>>(P);
+	k_lambda_tables<<<dim3(8, tableRows(jobsHint)), 256, 0, s>>>(P);
 }
 
-void launchLineFrags(const DrawParams& P, uint32_t nLines, cudaStream_t s)
+void launchLineFrags(const DrawParams& P, cudaStream_t s)
 {
-	if (!nLines) return;
-	k_line_frags<<<(nLines + 127) / 128, 128, 0, s>>>(P, nLines);
+	if (!P.primCap) return;
+	k_line_frags<<<(P.primCap + 127) / 128, 128, 0, s>>>(P);
 	k_line_frags_long<<<152 * 8, 128, 0, s>>>(P);
 }
 
@@ -1370,11 +1398,10 @@ void launchSetupMulti(const DrawParams& P, cudaStream_t s)
 	if (blocks) k_setup_multi<<<blocks, kSetupThreads, 0, s>>>(P);
 }
 
-void launchBigEntriesMulti(const DrawParams& P, uint32_t nJobs, cudaStream_t s)
+void launchBigEntriesMulti(const DrawParams& P, uint32_t jobsHint, cudaStream_t s)
 {
-	if (!nJobs) return;
-	k_big_entries_multi<<<nJobs < 152u * 16u ? nJobs : 152u * 16u, 256, 0, s>>>(P, nJobs);
-	k_lambda_tables_multi<<<dim3(8, nJobs < 65535u ? nJobs : 65535u), 256, 0, s>>>(P, nJobs);
+	k_big_entries_multi<<<bigBlocks(jobsHint), 256, 0, s>>>(P);
+	k_lambda_tables_multi<<<dim3(8, tableRows(jobsHint)), 256, 0, s>>>(P);
 }
 
 }  // namespace srpg

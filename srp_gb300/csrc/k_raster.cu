@@ -341,7 +341,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(const __grid_con
 	__shared__ uint32_t sSpan[kResolveWarps][32];
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const uint32_t tile = blockIdx.x * kResolveWarps + warp;
-	if (tile >= numTiles) return;
+	if (tile >= numTiles || P.ctr->abort) return;
 	const uint32_t s = P.tileStart[tile], e = P.tileEnd[tile];
 	if (s >= e) return;
 	if (LATE_FS == 0 && e - s > kHeavyItems) return;  /* k_resolve_heavy's */
@@ -504,7 +504,7 @@ __global__ void __launch_bounds__(kHeavyThreads) k_resolve_heavy(const __grid_co
 
 	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 	const DrawState& st = P.st;
-	const uint32_t nHeavy = P.ctr->nonEmptyTiles;
+	const uint32_t nHeavy = P.ctr->abort ? 0u : P.ctr->nonEmptyTiles;
 	for (uint32_t h = blockIdx.x; h < nHeavy; h += gridDim.x) {
 		const uint32_t tile = heavy[h];
 		const uint32_t s = P.tileStart[tile], e = P.tileEnd[tile];
@@ -577,7 +577,7 @@ __global__ void __launch_bounds__(kHeavyThreads) k_resolve_heavy(const __grid_co
 __global__ void k_tile_classify(const __grid_constant__ DrawParams P, uint32_t numTiles, uint32_t* heavy)
 {
 	const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-	if (t >= numTiles) return;
+	if (t >= numTiles || P.ctr->abort) return;
 	const uint32_t n = P.tileEnd[t] - P.tileStart[t];
 	if (P.tileEnd[t] > P.tileStart[t] && n > kHeavyItems) heavy[atomicAdd(&P.ctr->nonEmptyTiles, 1u)] = t;
 }
@@ -589,7 +589,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_shade(const __grid_const
 {
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const uint32_t tile = blockIdx.x * kResolveWarps + warp;
-	if (tile >= numTiles) return;
+	if (tile >= numTiles || P.ctr->abort) return;
 	if (P.tileStart[tile] >= P.tileEnd[tile]) return;
 	const TileCtx c = tileCtx<MULTI>(P, tile);
 	const int x0 = c.x0, y0 = c.y0;

@@ -84,18 +84,27 @@ void launchReset(const DrawParams& P, cudaStream_t s);
 void launchIndexRange(const DrawParams& P, cudaStream_t s);
 void launchVertex(const DrawParams& P, unsigned long long first, unsigned long long n, cudaStream_t s);
 void launchSetup(const DrawParams& P, cudaStream_t s);
+/* After setup: sets the abort flag when any count exceeds its buffer (or an
+ * index was bad). Every later kernel reads its sizes from the counters, not
+ * from the host, and does nothing once the flag is set, so a draw can be
+ * enqueued to the end before the host has seen its counts. */
+void launchCheck(const DrawParams& P, cudaStream_t s);
 void launchClipPrepass(const DrawParams& P, cudaStream_t s);
-void launchBigEntries(const DrawParams& P, uint32_t nJobs, cudaStream_t s);
-void launchLineFrags(const DrawParams& P, uint32_t nLines, cudaStream_t s);
+/* jobsHint (the big-primitive count of a similar earlier draw) only sizes
+ * the grids; the kernels loop over the count the device holds. */
+void launchBigEntries(const DrawParams& P, uint32_t jobsHint, cudaStream_t s);
+void launchLineFrags(const DrawParams& P, cudaStream_t s);
 /* k_front.cu, multi-draw pass */
 void launchVertexMulti(const DrawParams& P, uint32_t blocks, int maxStride, cudaStream_t s);
 void launchClipPrepassMulti(const DrawParams& P, cudaStream_t s);
 void launchSetupMulti(const DrawParams& P, cudaStream_t s);
-void launchBigEntriesMulti(const DrawParams& P, uint32_t nJobs, cudaStream_t s);
+void launchBigEntriesMulti(const DrawParams& P, uint32_t jobsHint, cudaStream_t s);
 /* k_bin.cu */
-void sortEntries(const DrawParams& P, uint32_t n, uint32_t keyBits, uint32_t* keysAlt, uint32_t* valsAlt,
+/* Sorts the draw's (tile, item) pairs by tile, stably; their number is read
+ * from the counters (at most P.entryCap, the size the scratch is for). */
+void sortEntries(const DrawParams& P, uint32_t keyBits, uint32_t* keysAlt, uint32_t* valsAlt,
                  uint32_t* hist, uint32_t* partials, uint32_t** keysOut, uint32_t** valsOut, cudaStream_t s);
-void launchTileRanges(const DrawParams& P, const uint32_t* keys, uint32_t n, uint32_t numTiles, cudaStream_t s);
+void launchTileRanges(const DrawParams& P, const uint32_t* keys, uint32_t numTiles, cudaStream_t s);
 size_t sortHistWords(uint32_t n);
 size_t sortPartialWords(uint32_t n);
 /* k_raster.cu */

@@ -92,6 +92,7 @@ struct Lib {
 	/* heavy-tile resolve runs here, beside the light tiles on `stream` */
 	cudaStream_t auxStream = nullptr;
 	cudaEvent_t forkEvent = nullptr, joinEvent = nullptr;
+	cudaEvent_t ctrEvent = nullptr;   /* recorded after a draw's counters are copied to hostCtr */
 	SRPGpuFramebufferMode fbMode = SRP_GPU_FB_COHERENT;
 	Registry reg;
 	/* scratch pools, grown on demand */
@@ -110,7 +111,11 @@ struct Lib {
 	cudaEvent_t openEvent = nullptr;
 	unsigned long long tableCap = 1ull << 22;  /* floats */
 	uint32_t clipPolyCap = 1 << 14;
-	double entryRatio = 4.0;
+	/* (tile, item) pairs per input primitive seen last, per kind of item
+	 * (triangle, line fragment, point): sizes the pair buffers of the next
+	 * draw of that kind, whose count the host does not wait for */
+	double entryRatio[3] = { 4.0, 64.0, 4.0 };
+	uint32_t bigJobsSeen[3] = { 1024, 0, 1024 };   /* big primitives of the last draw, per kind */
 };
 
 Lib g;
@@ -124,7 +129,9 @@ bool ensureInit(const char* fn)
 	cudaDeviceGetStreamPriorityRange(&loPri, &hiPri);
 	if (!cudaOk(cudaStreamCreateWithPriority(&g.auxStream, cudaStreamNonBlocking, hiPri), fn, "cudaStreamCreate") ||
 	    !cudaOk(cudaEventCreateWithFlags(&g.forkEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
-	    !cudaOk(cudaEventCreateWithFlags(&g.joinEvent, cudaEventDisableTiming), fn, "cudaEventCreate")) return false;
+	    !cudaOk(cudaEventCreateWithFlags(&g.joinEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
+	    !cudaOk(cudaEventCreateWithFlags(&g.ctrEvent, cudaEventDisableTiming), fn,
+	            "cudaEventCreate")) return false;
 	if (!cudaOk(cudaMallocHost((void**) &g.hostCtr, sizeof(DeviceCounters)), fn, "cudaMallocHost")) return false;
 	if (!g.ctr.reserve(sizeof(DeviceCounters), fn) || !g.minmax.reserve(16, fn)) return false;
 	cudaMemset(g.ctr.ptr, 0, sizeof(DeviceCounters));
@@ -846,8 +853,13 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 	if (g.fbMode == SRP_GPU_FB_COHERENT) fbUpload(fb, fx);
 
 	uint32_t primCap = (uint32_t) std::min<size_t>(nIn * outPer + 4096, 0x3FFFFFFFu);
-	uint32_t entryCap = (uint32_t) std::min<double>(primCap * g.entryRatio + 4096, 4.0e9);
-	for (int attempt = 0; attempt < 4; ++attempt) {
+	uint32_t entryCap = (uint32_t) std::min<double>((double) (nIn * outPer) * g.entryRatio[kind] + 4096, 4.0e9);
+	const uint32_t keyBits = bitsFor(numTiles);
+	const bool late = sp->fs->mayOverwriteDepth && shadeSupportsLateDepth(fsId);
+	bool drawn = false;
+	for (int attempt = 0; attempt < 4 && !drawn; ++attempt) {
+		/* long lines are queued in the big-job buffer: room for every line */
+		if (kind == kKindLineFrag && g.bigCap < primCap) g.bigCap = primCap;
 		const uint32_t rows = (uint32_t) vb->nVertices + g.clipRows;
 		const size_t nw = (size_t) std::max(P.L.nWords, 1);
 		const uint32_t blocks = (uint32_t) ((nIn + kSetupThreads - 1) / kSetupThreads);
@@ -855,9 +867,13 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		          g.vset0.reserve((size_t) vb->nVertices * 16 + 16, FN) && g.vset1.reserve((size_t) vb->nVertices * 16 + 16, FN) &&
 		          g.lookback.reserve((size_t) std::max(blocks, 1u) * 8, FN) &&
 		          g.keys.reserve((size_t) entryCap * 4, FN) && g.vals.reserve((size_t) entryCap * 4, FN) &&
+		          g.keys2.reserve((size_t) entryCap * 4, FN) && g.vals2.reserve((size_t) entryCap * 4, FN) &&
+		          g.hist.reserve(sortHistWords(entryCap) * 4, FN) && g.partials.reserve(sortPartialWords(entryCap) * 4 + 64, FN) &&
 		          g.big.reserve((size_t) g.bigCap * 16, FN) && g.table.reserve((size_t) g.tableCap * 4, FN) &&
 		          g.clipSlot.reserve((size_t) nIn * 4 + 4, FN) &&
-		          g.clipPolys.reserve((size_t) g.clipPolyCap * (1 + kMaxPoly) * 4, FN);
+		          g.clipPolys.reserve((size_t) g.clipPolyCap * (1 + kMaxPoly) * 4, FN) &&
+		          g.tileStart.reserve((size_t) (numTiles + 1) * 4, FN) && g.tileEnd.reserve((size_t) (numTiles + 1) * 4, FN) &&
+		          g.winner.reserve(fb->size * 4 + 4, FN) && g.heavy.reserve((size_t) (numTiles + 1) * 4, FN);
 		if (kind == kKindTri) ok = ok && g.triR.reserve((size_t) primCap * sizeof(TriRaster), FN) &&
 		                           g.triA.reserve((size_t) primCap * sizeof(TriAttr), FN);
 		else if (kind == kKindPoint) ok = ok && g.points.reserve((size_t) primCap * sizeof(PointRec), FN);
@@ -888,7 +904,11 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		P.clipPolyCap = g.clipPolyCap;
 		P.tableCap = g.tableCap;
 		P.lookback = g.lookback.as<unsigned long long>();
+		P.tileStart = g.tileStart.as<uint32_t>();
+		P.tileEnd = g.tileEnd.as<uint32_t>();
+		P.winner = g.winner.as<int32_t>();
 
+		/* the whole draw is enqueued before the host looks at any count */
 		stageBegin();
 		launchReset(P, g.stream);
 		if (ib) launchIndexRange(P, g.stream);
@@ -899,21 +919,50 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, g.stream);
 		if (isTri(prim)) launchClipPrepass(P, g.stream);
 		launchSetup(P, g.stream);
-		stageEnd(SRP_GPU_STAGE_SETUP, isTri(prim) ? 2 : 1);
-		g.launches += 3 + (ib ? 1 : 0) + (isTri(prim) ? 1 : 0);
-		if (!cudaOk(cudaGetLastError(), FN, "launch") || !readCounters()) return;
+		launchCheck(P, g.stream);
+		stageEnd(SRP_GPU_STAGE_SETUP, isTri(prim) ? 3 : 2);
+		cudaMemcpyAsync(g.hostCtr, g.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, g.stream);
+		cudaEventRecord(g.ctrEvent, g.stream);
+		g.launches += 4 + (ib ? 1 : 0) + (isTri(prim) ? 1 : 0);
+		stageBegin();
+		int binLaunches = 0;
+		if (kind == kKindLineFrag) { launchLineFrags(P, g.stream); binLaunches += 2; }
+		else { launchBigEntries(P, g.bigJobsSeen[kind], g.stream); binLaunches += 2; }
+		uint32_t* sk;
+		uint32_t* sv;
+		sortEntries(P, keyBits, g.keys2.as<uint32_t>(), g.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
+		            g.partials.as<uint32_t>(), &sk, &sv, g.stream);
+		cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, g.stream);
+		cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, g.stream);
+		launchTileRanges(P, sk, numTiles, g.stream);
+		binLaunches += 1 + (int) (keyBits / 8) + 1;
+		stageEnd(SRP_GPU_STAGE_BIN, binLaunches);
+		if (late) {
+			stageBegin();
+			launchResolveLate(P, kind, sv, numTiles, g.stream);
+			stageEnd(SRP_GPU_STAGE_RESOLVE, 1);
+		} else {
+			stageBegin();
+			launchResolve(P, kind, sv, numTiles, g.heavy.as<uint32_t>(), g.stream, g.auxStream, g.forkEvent,
+			              g.joinEvent);
+			stageEnd(SRP_GPU_STAGE_RESOLVE, 3);
+			stageBegin();
+			launchShade(P, kind, numTiles, g.stream);
+			stageEnd(SRP_GPU_STAGE_SHADE, 1);
+		}
+		g.launches += binLaunches + (late ? 1 : 4);
+		if (!cudaOk(cudaGetLastError(), FN, "launch")) return;
+		/* wait for the setup counters only; the rest of the draw runs on */
+		if (!cudaOk(cudaEventSynchronize(g.ctrEvent), FN, "kernel execution")) return;
 		const DeviceCounters c = *g.hostCtr;
 		if (c.errors & kErrBadIndex) {
 			SRP_ERROR(FN, "Vertex index out of range of the vertex buffer (%zu vertices)", vb->nVertices);
 			return;
 		}
 		if (c.errors & kErrSpin) { SRP_ERROR(FN, "Ordered-compaction wait timed out"); return; }
-		/* capacities are decided from the counters themselves: every
-		 * overflow, whichever kernel met it, shows up as a count above the
-		 * buffer it was meant for */
-		const bool over = c.clipVerts > g.clipRows || c.prims > primCap || c.entries > entryCap || c.bigJobs > g.bigCap ||
-		                  c.tableWords > g.tableCap || c.clipTris > g.clipPolyCap;
-		if ((c.errors & kErrCapacity) || over) {
+		if (c.abort) {
+			/* the enqueued rest of the draw skipped itself; grow and draw again */
+			cudaStreamSynchronize(g.stream);
 			bool grew = false;
 			if (c.clipVerts > g.clipRows) { g.clipRows = (uint32_t) std::min<unsigned long long>(c.clipVerts * 2, 0x7FFFFFFF); grew = true; }
 			if (c.prims > primCap) { primCap = (uint32_t) std::min<unsigned long long>(c.prims + 1024, 0x3FFFFFFF); grew = true; }
@@ -924,66 +973,16 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			if (!grew) { SRP_ERROR(FN, "Scratch capacity exceeded"); return; }
 			continue;
 		}
-		if (c.prims) g.entryRatio = std::max(1.0, std::min(64.0, (double) c.entries / (double) c.prims * 1.25));
+		g.entryRatio[kind] = std::max(0.25, std::min(4096.0, (double) c.entries / (double) (nIn * outPer) * 1.25));
+		g.bigJobsSeen[kind] = (uint32_t) std::min<unsigned long long>(c.bigJobs, 1u << 30);
 		g.stats.primitives += c.prims;
 		g.stats.binEntries += c.entries;
 		g.stats.clipOverflows += c.clipOverflow;
-		const uint32_t E = (uint32_t) c.entries;
-		stageBegin();
-		int binLaunches = 0;
-		if (kind == kKindLineFrag) {
-			/* the long-line queue reuses the big-job buffer: room for every line */
-			if (c.prims > g.bigCap) {
-				g.bigCap = (uint32_t) c.prims;
-				if (!g.big.reserve((size_t) g.bigCap * 16, FN)) return;
-				P.bigJobs = g.big.as<uint4>();
-				P.bigCap = g.bigCap;
-			}
-			launchLineFrags(P, (uint32_t) c.prims, g.stream);
-			binLaunches += 2;
-		}
-		else if (c.bigJobs) { launchBigEntries(P, (uint32_t) c.bigJobs, g.stream); binLaunches += 2; }
-		g.launches += binLaunches;
-		if (E == 0) { stageEnd(SRP_GPU_STAGE_BIN, binLaunches); break; }
-		/* sort (tile, item) pairs by tile, keeping item order */
-		const uint32_t keyBits = bitsFor(numTiles);
-		if (!g.keys2.reserve((size_t) E * 4, FN) || !g.vals2.reserve((size_t) E * 4, FN) ||
-		    !g.hist.reserve(sortHistWords(E) * 4, FN) || !g.partials.reserve(sortPartialWords(E) * 4 + 64, FN) ||
-		    !g.tileStart.reserve((size_t) (numTiles + 1) * 4, FN) || !g.tileEnd.reserve((size_t) (numTiles + 1) * 4, FN) ||
-		    !g.winner.reserve(fb->size * 4 + 4, FN) || !g.heavy.reserve((size_t) (numTiles + 1) * 4, FN)) return;
-		uint32_t* sk;
-		uint32_t* sv;
-		sortEntries(P, E, keyBits, g.keys2.as<uint32_t>(), g.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
-		            g.partials.as<uint32_t>(), &sk, &sv, g.stream);
-		g.launches += 1 + keyBits / 8;
-		P.tileStart = g.tileStart.as<uint32_t>();
-		P.tileEnd = g.tileEnd.as<uint32_t>();
-		P.winner = g.winner.as<int32_t>();
-		cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, g.stream);
-		cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, g.stream);
-		launchTileRanges(P, sk, E, numTiles, g.stream);
-		stageEnd(SRP_GPU_STAGE_BIN, binLaunches + 1 + (int) (keyBits / 8) + 1);
-		const bool late = sp->fs->mayOverwriteDepth && shadeSupportsLateDepth(fsId);
 		g.profile.resolveTiles += numTiles;
-		g.profile.resolveItems += E;
-		if (late) {
-			stageBegin();
-			launchResolveLate(P, kind, sv, numTiles, g.stream);
-			stageEnd(SRP_GPU_STAGE_RESOLVE, 1);
-			g.launches += 2;
-		} else {
-			stageBegin();
-			launchResolve(P, kind, sv, numTiles, g.heavy.as<uint32_t>(), g.stream, g.auxStream, g.forkEvent,
-			              g.joinEvent);
-			stageEnd(SRP_GPU_STAGE_RESOLVE, 3);
-			stageBegin();
-			launchShade(P, kind, numTiles, g.stream);
-			stageEnd(SRP_GPU_STAGE_SHADE, 1);
-			g.launches += 5;
-		}
-		cudaOk(cudaGetLastError(), FN, "launch");
-		break;
+		g.profile.resolveItems += c.entries;
+		drawn = true;
 	}
+	if (!drawn) { SRP_ERROR(FN, "Scratch capacity could not be sized for the draw"); return; }
 	++g.stats.draws;
 	if (g.fbMode == SRP_GPU_FB_COHERENT) fbDownload(fb, fx);
 }
@@ -1185,7 +1184,8 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		for (size_t k = 0; k < n; ++k) fbUpload(draws[idx[k]].framebuffer, fbFind(draws[idx[k]].framebuffer));
 
 	uint32_t primCap = (uint32_t) std::min<unsigned long long>((unsigned long long) nIn + 4096, 0x3FFFFFFFu);
-	uint32_t entryCap = (uint32_t) std::min<double>(primCap * g.entryRatio + 4096, 4.0e9);
+	uint32_t entryCap = (uint32_t) std::min<double>((double) nIn * g.entryRatio[kKindTri] + 4096, 4.0e9);
+	const uint32_t keyBits = bitsFor(numTiles);
 	bool drawn = false;
 	for (int attempt = 0; attempt < 4 && !drawn; ++attempt) {
 		const unsigned long long rows = (unsigned long long) vRows + g.clipRows;
@@ -1195,11 +1195,15 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		          g.vset0.reserve((size_t) vRows * 16 + 16, FN) && g.vset1.reserve((size_t) vRows * 16 + 16, FN) &&
 		          g.lookback.reserve((size_t) std::max(blocks, 1u) * 8, FN) &&
 		          g.keys.reserve((size_t) entryCap * 4, FN) && g.vals.reserve((size_t) entryCap * 4, FN) &&
+		          g.keys2.reserve((size_t) entryCap * 4, FN) && g.vals2.reserve((size_t) entryCap * 4, FN) &&
+		          g.hist.reserve(sortHistWords(entryCap) * 4, FN) && g.partials.reserve(sortPartialWords(entryCap) * 4 + 64, FN) &&
 		          g.big.reserve((size_t) g.bigCap * 16, FN) && g.table.reserve((size_t) g.tableCap * 4, FN) &&
 		          g.clipSlot.reserve((size_t) nIn * 4 + 4, FN) &&
 		          g.clipPolys.reserve((size_t) g.clipPolyCap * (1 + kMaxPoly) * 4, FN) &&
 		          g.triR.reserve((size_t) primCap * sizeof(TriRaster), FN) &&
-		          g.triA.reserve((size_t) primCap * sizeof(TriAttr), FN);
+		          g.triA.reserve((size_t) primCap * sizeof(TriAttr), FN) &&
+		          g.tileStart.reserve((size_t) (numTiles + 1) * 4, FN) && g.tileEnd.reserve((size_t) (numTiles + 1) * 4, FN) &&
+		          g.heavy.reserve((size_t) (numTiles + 1) * 4, FN);
 		if (!ok) return false;
 		P.clip = g.clip.as<float4>();
 		P.vset0 = g.vset0.as<float4>();
@@ -1221,6 +1225,8 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		P.clipPolys = g.clipPolys.as<uint32_t>();
 		P.clipPolyCap = g.clipPolyCap;
 		P.lookback = g.lookback.as<unsigned long long>();
+		P.tileStart = g.tileStart.as<uint32_t>();
+		P.tileEnd = g.tileEnd.as<uint32_t>();
 
 		stageBegin();
 		launchReset(P, g.stream);
@@ -1230,12 +1236,33 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, g.stream);
 		launchClipPrepassMulti(P, g.stream);
 		launchSetupMulti(P, g.stream);
-		stageEnd(SRP_GPU_STAGE_SETUP, 2);
-		g.launches += 4;
-		if (!cudaOk(cudaGetLastError(), FN, "launch") || !readCounters()) return false;
+		launchCheck(P, g.stream);
+		stageEnd(SRP_GPU_STAGE_SETUP, 3);
+		cudaMemcpyAsync(g.hostCtr, g.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, g.stream);
+		cudaEventRecord(g.ctrEvent, g.stream);
+		stageBegin();
+		launchBigEntriesMulti(P, g.bigJobsSeen[kKindTri], g.stream);
+		uint32_t* sk;
+		uint32_t* sv;
+		sortEntries(P, keyBits, g.keys2.as<uint32_t>(), g.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
+		            g.partials.as<uint32_t>(), &sk, &sv, g.stream);
+		cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, g.stream);
+		cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, g.stream);
+		launchTileRanges(P, sk, numTiles, g.stream);
+		stageEnd(SRP_GPU_STAGE_BIN, 2 + 1 + (int) (keyBits / 8) + 1);
+		stageBegin();
+		launchResolveMulti(P, sv, numTiles, g.heavy.as<uint32_t>(), g.stream, g.auxStream, g.forkEvent, g.joinEvent);
+		stageEnd(SRP_GPU_STAGE_RESOLVE, 3);
+		stageBegin();
+		launchShadeMulti(P, numTiles, g.stream);
+		stageEnd(SRP_GPU_STAGE_SHADE, 1);
+		g.launches += 5 + 2 + 1 + keyBits / 8 + 1 + 4;
+		if (!cudaOk(cudaGetLastError(), FN, "launch")) return false;
+		if (!cudaOk(cudaEventSynchronize(g.ctrEvent), FN, "kernel execution")) return false;
 		const DeviceCounters c = *g.hostCtr;
 		if (c.errors & kErrBadIndex) {
 			/* some draw indexes past its vertex buffer: let each report alone */
+			cudaStreamSynchronize(g.stream);
 			for (size_t k = 0; k < n; ++k) {
 				const SRPGpuDraw& d = draws[idx[k]];
 				drawBuffer(d.indexBuffer, d.vertexBuffer, d.framebuffer, d.program, d.primitive, d.startIndex, d.count);
@@ -1243,9 +1270,8 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 			return true;
 		}
 		if (c.errors & kErrSpin) { SRP_ERROR(FN, "Ordered-compaction wait timed out"); return false; }
-		const bool over = c.clipVerts > g.clipRows || c.prims > primCap || c.entries > entryCap || c.bigJobs > g.bigCap ||
-		                  c.tableWords > g.tableCap || c.clipTris > g.clipPolyCap;
-		if ((c.errors & kErrCapacity) || over) {
+		if (c.abort) {
+			cudaStreamSynchronize(g.stream);
 			bool grew = false;
 			if (c.clipVerts > g.clipRows) { g.clipRows = (uint32_t) std::min<unsigned long long>(c.clipVerts * 2, 0x7FFFFFFF); grew = true; }
 			if (c.prims > primCap) { primCap = (uint32_t) std::min<unsigned long long>(c.prims + 1024, 0x3FFFFFFF); grew = true; }
@@ -1256,43 +1282,14 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 			if (!grew) { SRP_ERROR(FN, "Scratch capacity exceeded"); return false; }
 			continue;
 		}
-		if (c.prims) g.entryRatio = std::max(1.0, std::min(64.0, (double) c.entries / (double) c.prims * 1.25));
+		g.entryRatio[kKindTri] = std::max(0.25, std::min(4096.0, (double) c.entries / (double) nIn * 1.25));
+		g.bigJobsSeen[kKindTri] = (uint32_t) std::min<unsigned long long>(c.bigJobs, 1u << 30);
 		g.stats.primitives += c.prims;
 		g.stats.binEntries += c.entries;
 		g.stats.clipOverflows += c.clipOverflow;
-		const uint32_t E = (uint32_t) c.entries;
-		stageBegin();
-		int binLaunches = 0;
-		if (c.bigJobs) { launchBigEntriesMulti(P, (uint32_t) c.bigJobs, g.stream); binLaunches += 2; }
-		g.launches += binLaunches;
-		drawn = true;
-		if (E == 0) { stageEnd(SRP_GPU_STAGE_BIN, binLaunches); break; }
-		const uint32_t keyBits = bitsFor(numTiles);
-		if (!g.keys2.reserve((size_t) E * 4, FN) || !g.vals2.reserve((size_t) E * 4, FN) ||
-		    !g.hist.reserve(sortHistWords(E) * 4, FN) || !g.partials.reserve(sortPartialWords(E) * 4 + 64, FN) ||
-		    !g.tileStart.reserve((size_t) (numTiles + 1) * 4, FN) || !g.tileEnd.reserve((size_t) (numTiles + 1) * 4, FN) ||
-		    !g.heavy.reserve((size_t) (numTiles + 1) * 4, FN)) return false;
-		uint32_t* sk;
-		uint32_t* sv;
-		sortEntries(P, E, keyBits, g.keys2.as<uint32_t>(), g.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
-		            g.partials.as<uint32_t>(), &sk, &sv, g.stream);
-		g.launches += 1 + keyBits / 8;
-		P.tileStart = g.tileStart.as<uint32_t>();
-		P.tileEnd = g.tileEnd.as<uint32_t>();
-		cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, g.stream);
-		cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, g.stream);
-		launchTileRanges(P, sk, E, numTiles, g.stream);
-		stageEnd(SRP_GPU_STAGE_BIN, binLaunches + 1 + (int) (keyBits / 8) + 1);
 		g.profile.resolveTiles += numTiles;
-		g.profile.resolveItems += E;
-		stageBegin();
-		launchResolveMulti(P, sv, numTiles, g.heavy.as<uint32_t>(), g.stream, g.auxStream, g.forkEvent, g.joinEvent);
-		stageEnd(SRP_GPU_STAGE_RESOLVE, 3);
-		stageBegin();
-		launchShadeMulti(P, numTiles, g.stream);
-		stageEnd(SRP_GPU_STAGE_SHADE, 1);
-		g.launches += 5;
-		cudaOk(cudaGetLastError(), FN, "launch");
+		g.profile.resolveItems += c.entries;
+		drawn = true;
 	}
 	if (!drawn) SRP_ERROR(FN, "Scratch capacity could not be sized for the pass");
 	g.stats.draws += n;

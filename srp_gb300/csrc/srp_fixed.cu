@@ -262,18 +262,19 @@ extern "C" int srpGpuDrawFixedScratch(const SRPIndexBuffer* ib, const SRPVertexB
 	if (c.errors & kErrCapacity) { fixedDrawError(kFn, "Fixed scratch capacity exceeded; nothing was drawn"); return -1; }
 
 	const uint32_t E = (uint32_t) c.entries;
-	if (lineFrags) { launchLineFrags(P, (uint32_t) c.prims, s); launches += 2; }
+	/* the rest of the draw takes its sizes from the counters on the device */
+	if (lineFrags) { launchLineFrags(P, s); launches += 2; }
 	else if (c.bigJobs) { launchBigEntries(P, (uint32_t) c.bigJobs, s); launches += 2; }
 	if (E) {
 		const uint32_t keyBits = keyBitsFor(info.numTiles);
 		uint32_t* sk;
 		uint32_t* sv;
-		sortEntries(P, E, keyBits, (uint32_t*) (base + oKeys2), (uint32_t*) (base + oVals2), (uint32_t*) (base + oHist),
+		sortEntries(P, keyBits, (uint32_t*) (base + oKeys2), (uint32_t*) (base + oVals2), (uint32_t*) (base + oHist),
 		            (uint32_t*) (base + oPartials), &sk, &sv, s);
 		launches += 1 + keyBits / 8;
 		cudaMemsetAsync(P.tileStart, 0, (size_t) info.numTiles * 4, s);
 		cudaMemsetAsync(P.tileEnd, 0, (size_t) info.numTiles * 4, s);
-		launchTileRanges(P, sk, E, info.numTiles, s);
+		launchTileRanges(P, sk, info.numTiles, s);
 		if (info.late) {
 			launchResolveLate(P, info.kind, sv, info.numTiles, s);
 			launches += 2;
