@@ -82,6 +82,74 @@ typedef struct SRPGpuDraw
  *  a message, is issued through the ordinary path at its place in the order. */
 void srpGpuDrawBatch(const SRPGpuDraw* draws, size_t n);
 
+/* --------------------------------------------------- learned shading */
+
+/* A small MLP that stands in for an expensive fragment shader. None of this
+ * has a counterpart in kitrofimov/srp. The network maps a 6-band sin/cos
+ * encoding of the fragment's world position, unit normal and unit view
+ * direction (108 inputs) through three hidden layers of 64 ReLU units to
+ * RGB. It learns from fragments the shader itself shaded, is trained on the
+ * GPU (fp32, Adam), and shades on the tensor cores (bf16 weights, fp32
+ * accumulation). Coverage, depth, stencil and the visible fragment never
+ * depend on it: only the colour of the visible fragment does. The one
+ * shader with a learned stand-in is srpFsMarble (world-space varyings of
+ * srpVsWorld). */
+typedef struct SRPGpuMlp SRPGpuMlp;
+
+/** A network with seeded random weights and room for sampleCapacity
+ *  captured fragments. */
+SRPGpuMlp* srpGpuMlpCreate(uint64_t seed, size_t sampleCapacity);
+void srpGpuMlpFree(SRPGpuMlp* mlp);
+
+/** While set, every draw shaded by `target` records 1 of every `every`
+ *  shaded pixels (position, normal, view direction, colour) into mlp, up to
+ *  its capacity. mlp NULL stops the capture. */
+void srpGpuMlpCapture(SRPGpuMlp* mlp, void (*target)(SRPFragmentShaderIn*, SRPFragmentShaderOut*), uint32_t every);
+size_t srpGpuMlpSampleCount(const SRPGpuMlp* mlp);
+/** Append samples given by the host: 12 floats each (position, normal, view
+ *  direction, RGB). Returns 0, or -1 beyond the capacity. */
+int srpGpuMlpAddSamples(SRPGpuMlp* mlp, const float* samples, size_t n);
+
+/** Train on the samples: `steps` Adam steps (cosine-decayed rate from
+ *  learningRate) over random batches of `batch`. Returns the mean squared
+ *  error of the last batch, or a negative value on failure. */
+float srpGpuMlpTrain(SRPGpuMlp* mlp, int steps, int batch, float learningRate);
+
+/** Draws whose fragment shader is `target` are shaded by mlp. 1 pixel in
+ *  judgeEvery is also shaded by `target`; a draw whose PSNR over those
+ *  pixels is below minPsnrDb is shaded again by `target` alone. mlp NULL
+ *  turns learned shading off. */
+void srpGpuSetLearnedShading(void (*target)(SRPFragmentShaderIn*, SRPFragmentShaderOut*), SRPGpuMlp* mlp,
+                             float minPsnrDb, uint32_t judgeEvery);
+
+typedef struct SRPGpuLearnedStats
+{
+	uint64_t draws;              /* learned-shaded draws */
+	uint64_t fallbacks;          /* of them, shaded again by the target shader */
+	uint64_t judgedDraws;        /* draws with at least one judged pixel */
+	uint64_t judgedChannels;     /* colour channels compared with the target */
+	double squaredError;         /* summed over the judged channels (range [0, 1]) */
+	double lastPsnrDb, minPsnrDb;
+	float maxChannelError;
+} SRPGpuLearnedStats;
+
+/** Statistics since the last reset (reading them does not wait for the GPU:
+ *  every learned-shaded draw is judged before it returns). */
+void srpGpuGetLearnedStats(SRPGpuLearnedStats* stats);
+void srpGpuResetLearnedStats(void);
+
+/** The network's parameters as one fp32 vector (W1 [108][64], b1, W2 [64][64],
+ *  b2, W3 [64][64], b3, W4 [64][3], b4), for inspection and tests. */
+size_t srpGpuMlpParamCount(void);
+void srpGpuMlpGetParams(const SRPGpuMlp* mlp, float* params);
+void srpGpuMlpSetParams(SRPGpuMlp* mlp, const float* params);
+/** RGB (unclamped) of n samples: fp32 on CUDA cores (tensorCores 0) or the
+ *  shading path's bf16 tensor-core evaluation (1). Returns 0 on success. */
+int srpGpuMlpEvaluate(SRPGpuMlp* mlp, const float* samples, size_t n, float* rgb, int tensorCores);
+/** Gradient of the mean squared error over n samples (in order) with
+ *  respect to the parameters, and the summed squared error. */
+int srpGpuMlpGradients(SRPGpuMlp* mlp, const float* samples, size_t n, float* grad, double* sse);
+
 /* ------------------------------------------------- fixed-scratch draw */
 
 /** Size of the device array that srpGpuDrawFixedScratch takes its scratch

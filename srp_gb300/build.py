@@ -20,7 +20,7 @@ LIB = os.path.join(PKG, "lib")
 OBJ = os.path.join(PKG, "_build")
 INC = os.path.join(ROOT, "include")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CU_SOURCES = ["k_front.cu", "k_bin.cu", "k_raster.cu", "srp_api.cu", "srp_fixed.cu"]
+CU_SOURCES = ["k_front.cu", "k_bin.cu", "k_raster.cu", "k_mlp.cu", "srp_api.cu", "srp_fixed.cu", "srp_learned.cu"]
 C_SOURCES = ["srp_math.c", "imageio.c"]
 
 

@@ -22,6 +22,7 @@
 
 #include "device_common.cuh"
 #include "kernels.h"
+#include "mlp_infer.cuh"
 #include "srp/buffer.h"
 
 namespace srpg {
@@ -61,15 +62,13 @@ __device__ __forceinline__ void runFS(SRPFragmentShaderIn* in, SRPFragmentShader
 	}
 }
 
-/* Shader inputs of `item` at pixel (gx, gy) and the shader call
- * (fragCoord and varyings as built by src/raster/triangle.c:89-99,
- * line.c:62-75, point.c:107-116). */
-template <int KIND, int FS>
-__device__ __forceinline__ void shadeItem(const DrawParams& P, const unsigned char* uniform, uint32_t primBase,
-                                          uint32_t item, int gx, int gy, SRPFragmentShaderOut& out)
+/* Shader inputs of `item` at pixel (gx, gy): fragCoord and varyings as
+ * built by src/raster/triangle.c:89-99, line.c:62-75, point.c:107-116.
+ * The varyings go to `words`, which in.varyings points at. */
+template <int KIND>
+__device__ __forceinline__ void fragmentIn(const DrawParams& P, const unsigned char* uniform, uint32_t primBase,
+                                           uint32_t item, int gx, int gy, SRPFragmentShaderIn& in, uint32_t* words)
 {
-	uint32_t words[kMaxVaryingWords];
-	SRPFragmentShaderIn in;
 	in.uniform = (SRPUniform*) uniform;
 	in.varyings = (SRPInterpolated*) words;
 	if (KIND == kKindTri) {
@@ -125,9 +124,25 @@ __device__ __forceinline__ void shadeItem(const DrawParams& P, const unsigned ch
 		in.frontFacing = true;
 		in.primitiveID = R.id;
 	}
+}
+
+template <int FS>
+__device__ __forceinline__ void runShader(SRPFragmentShaderIn& in, SRPFragmentShaderOut& out)
+{
 	out.color[0] = out.color[1] = out.color[2] = out.color[3] = 0.0f;
 	out.fragDepth = __int_as_float(0x7FC00000);
 	runFS<FS>(&in, &out);
+}
+
+/* The shader call for `item` at pixel (gx, gy). */
+template <int KIND, int FS>
+__device__ __forceinline__ void shadeItem(const DrawParams& P, const unsigned char* uniform, uint32_t primBase,
+                                          uint32_t item, int gx, int gy, SRPFragmentShaderOut& out)
+{
+	uint32_t words[kMaxVaryingWords];
+	SRPFragmentShaderIn in;
+	fragmentIn<KIND>(P, uniform, primBase, item, gx, gy, in, words);
+	runShader<FS>(in, out);
 }
 
 /* Record of an item, by kind (loaded ahead of use by k_resolve_heavy). */
@@ -276,11 +291,56 @@ __device__ __forceinline__ int findOwner(const uint32_t* off, uint32_t p)
 	return lo;
 }
 
+/* ------------------------------------------------------ learned shading */
+
+constexpr int kLearnedBias = 3 * kMlpHid + kMlpOut + 1;   /* floats, padded to 16 bytes */
+constexpr size_t kLearnedSmem = (size_t) kMlpBf16 * 2 + kLearnedBias * 4 + (size_t) kResolveWarps * 64 * 9 * 4 +
+                                (size_t) kResolveWarps * 64 * 4 * 4;
+
+__device__ __forceinline__ float clamp01f(float x) { return x < 0.0f ? 0.0f : (x > 1.0f ? 1.0f : x); }
+
+/* 1 pixel in `every`, by a hash of the pixel and a seed. */
+__device__ __forceinline__ bool pixelSampled(int gx, int gy, uint32_t seed, uint32_t every)
+{
+	if (every <= 1) return every == 1;
+	uint32_t h = (uint32_t) gx * 0x9E3779B1u ^ (uint32_t) gy * 0x85EBCA77u ^ seed * 0xC2B2AE3Du;
+	h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12; h *= 0x297A2D39u; h ^= h >> 15;
+	return h % every == 0;
+}
+
+/* The learned network's inputs at a fragment: world position and normal
+ * (varyings 0..5 of srpVsWorld), the normal normalised and the view direction
+ * towards the uniform's camera, as the lighting shaders compute them. */
+__device__ __forceinline__ void learnedInputs(const unsigned char* uniform, const uint32_t* words, float* x9)
+{
+	const SRPStdUniform* u = (const SRPStdUniform*) uniform;
+	float n[3], v[3];
+	for (int k = 0; k < 3; ++k) {
+		x9[k] = __uint_as_float(words[k]);
+		n[k] = __uint_as_float(words[3 + k]);
+		v[k] = u->cameraPos[k] - x9[k];
+	}
+	srpslNormalize3(n);
+	srpslNormalize3(v);
+	for (int k = 0; k < 3; ++k) { x9[3 + k] = n[k]; x9[6 + k] = v[k]; }
+}
+
+__device__ void captureSample(const DrawParams& P, const unsigned char* uniform, const uint32_t* words,
+                              const SRPFragmentShaderOut& out)
+{
+	const unsigned long long slot = atomicAdd(P.captureCount, 1ull);
+	if (slot >= P.captureCap) return;
+	float* s = P.capture + slot * kSampleFloats;
+	learnedInputs(uniform, words, s);
+	for (int k = 0; k < 3; ++k) s[9 + k] = clamp01f(out.color[k]);
+}
+
 /* Where a tile's pixels live: its origin in its framebuffer, the
  * framebuffer's size and planes, and the uniform and primitive-id base of
  * its draw. A single draw takes them from the parameters; a multi-draw pass
  * (MULTI) from the descriptor of the draw the global tile belongs to. */
 struct TileCtx {
+	uint32_t d;          /* draw of the tile (0 for a single draw) */
 	int x0, y0, W, H;
 	uint32_t* color;
 	float* depth;
@@ -308,6 +368,7 @@ __device__ __forceinline__ TileCtx tileCtx(const DrawParams& P, uint32_t tile)
 		const uint32_t d = tileDraw(P.tPrefix, P.nDraws, tile);
 		const DrawDesc& D = P.draws[d];
 		const uint32_t lt = tile - P.tPrefix[d];
+		c.d = d;
 		c.x0 = (int) (lt % (uint32_t) D.tilesX) * kTile;
 		c.y0 = (int) (lt / (uint32_t) D.tilesX) * kTile;
 		c.W = D.W; c.H = D.H;
@@ -315,6 +376,7 @@ __device__ __forceinline__ TileCtx tileCtx(const DrawParams& P, uint32_t tile)
 		c.uniform = D.uniform;
 		c.primBase = P.primPrefix[d];
 	} else {
+		c.d = 0;
 		c.x0 = (int) (tile % (uint32_t) P.st.tilesX) * kTile;
 		c.y0 = (int) (tile / (uint32_t) P.st.tilesX) * kTile;
 		c.W = P.st.W; c.H = P.st.H;
@@ -592,6 +654,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_shade(const __grid_const
 	if (tile >= numTiles || P.ctr->abort) return;
 	if (P.tileStart[tile] >= P.tileEnd[tile]) return;
 	const TileCtx c = tileCtx<MULTI>(P, tile);
+	if (MULTI && P.redo && !P.redo[c.d]) return;
 	const int x0 = c.x0, y0 = c.y0;
 #pragma unroll
 	for (int p = 0; p < 2; ++p) {
@@ -602,8 +665,100 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_shade(const __grid_const
 		const int32_t w = c.winner[idx];
 		if (w < 0) continue;
 		SRPFragmentShaderOut out;
-		shadeItem<KIND, FS>(P, c.uniform, c.primBase, (uint32_t) w, gx, gy, out);
+		if constexpr (KIND == kKindTri && FS == SRP_GPU_FS_MARBLE) {
+			/* the shader learned shading stands in for: captured for training */
+			uint32_t words[kMaxVaryingWords];
+			SRPFragmentShaderIn in;
+			fragmentIn<KIND>(P, c.uniform, c.primBase, (uint32_t) w, gx, gy, in, words);
+			runShader<FS>(in, out);
+			if (P.capture && pixelSampled(gx, gy, P.sampleSeed + c.d, P.captureEvery))
+				captureSample(P, c.uniform, words, out);
+		} else {
+			shadeItem<KIND, FS>(P, c.uniform, c.primBase, (uint32_t) w, gx, gy, out);
+		}
 		c.color[idx] = packColor(out.color);
+	}
+}
+
+/* Learned shading of the winners of a tile: their inputs go to shared
+ * memory, the MLP runs on the tensor cores 16 pixels at a time
+ * (mlp_infer.cuh), and 1 pixel in judgeEvery is also shaded by the plain
+ * shader (FS) so that the host can judge the draw's error. */
+template <int KIND, int FS, bool MULTI>
+__global__ void __launch_bounds__(kResolveWarps * 32) k_shade_learned(const __grid_constant__ DrawParams P,
+                                                                     uint32_t numTiles)
+{
+	extern __shared__ uint32_t lsm[];
+	uint32_t* sw = lsm;
+	float* sb = (float*) (lsm + kMlpBf16 / 2);
+	float (*sx)[64][9] = (float (*)[64][9]) (sb + kLearnedBias);
+	float (*so)[64][4] = (float (*)[64][4]) (sx + kResolveWarps);
+	for (int i = threadIdx.x; i < kMlpBf16 / 2; i += blockDim.x) sw[i] = ((const uint32_t*) P.mlpW)[i];
+	for (int i = threadIdx.x; i < 3 * kMlpHid + kMlpOut; i += blockDim.x) sb[i] = P.mlpB[i];
+	__syncthreads();
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const uint32_t tile = blockIdx.x * kResolveWarps + warp;
+	if (tile >= numTiles || P.ctr->abort) return;
+	if (P.tileStart[tile] >= P.tileEnd[tile]) return;
+	const TileCtx c = tileCtx<MULTI>(P, tile);
+	int32_t win[2];
+	int gx[2], gy[2];
+	size_t idx[2];
+#pragma unroll
+	for (int p = 0; p < 2; ++p) {
+		const int q = lane + 32 * p;
+		gx[p] = c.x0 + (q & 7);
+		gy[p] = c.y0 + (q >> 3);
+		const bool valid = gx[p] < c.W && gy[p] < c.H;
+		idx[p] = valid ? (size_t) gy[p] * c.W + gx[p] : 0;
+		win[p] = valid ? c.winner[idx[p]] : -1;
+		float* x9 = sx[warp][q];
+		if (win[p] >= 0) {
+			uint32_t words[kMaxVaryingWords];
+			SRPFragmentShaderIn in;
+			fragmentIn<KIND>(P, c.uniform, c.primBase, (uint32_t) win[p], gx[p], gy[p], in, words);
+			learnedInputs(c.uniform, words, x9);
+		} else {
+#pragma unroll
+			for (int k = 0; k < 9; ++k) x9[k] = 0.0f;
+		}
+	}
+	__syncwarp();
+	const unsigned b0 = __ballot_sync(0xFFFFFFFFu, win[0] >= 0), b1 = __ballot_sync(0xFFFFFFFFu, win[1] >= 0);
+	const unsigned sliceBits[4] = { b0 & 0xFFFFu, b0 >> 16, b1 & 0xFFFFu, b1 >> 16 };
+#pragma unroll
+	for (int sl = 0; sl < 4; ++sl)
+		if (sliceBits[sl]) mlpSlice16(sx[warp] + 16 * sl, sw, sb, so[warp] + 16 * sl);
+	__syncwarp();
+	double err = 0.0, chans = 0.0;
+	float worst = 0.0f;
+#pragma unroll
+	for (int p = 0; p < 2; ++p) {
+		if (win[p] < 0) continue;
+		const int q = lane + 32 * p;
+		float col[4] = { clamp01f(so[warp][q][0]), clamp01f(so[warp][q][1]), clamp01f(so[warp][q][2]), 1.0f };
+		c.color[idx[p]] = packColor(col);
+		if (pixelSampled(gx[p], gy[p], P.sampleSeed + c.d, P.judgeEvery)) {
+			SRPFragmentShaderOut ref;
+			shadeItem<KIND, FS>(P, c.uniform, c.primBase, (uint32_t) win[p], gx[p], gy[p], ref);
+#pragma unroll
+			for (int k = 0; k < 3; ++k) {
+				const float dlt = col[k] - ref.color[k];
+				err += (double) dlt * dlt;
+				worst = fmaxf(worst, fabsf(dlt));
+			}
+			chans += 3.0;
+		}
+	}
+	for (int o = 16; o; o >>= 1) {
+		err += __shfl_xor_sync(0xFFFFFFFFu, err, o);
+		chans += __shfl_xor_sync(0xFFFFFFFFu, chans, o);
+		worst = fmaxf(worst, __shfl_xor_sync(0xFFFFFFFFu, worst, o));
+	}
+	if (lane == 0 && chans > 0.0) {
+		atomicAdd(&P.judge[2 * c.d], err);
+		atomicAdd(&P.judge[2 * c.d + 1], chans);
+		atomicMax(&P.judgeMax[c.d], __float_as_uint(worst));
 	}
 }
 
@@ -673,6 +828,13 @@ static void shadeKind(const DrawParams& P, uint32_t numTiles, cudaStream_t s)
 	case SRP_GPU_FS_DEPTH_OVERWRITE: k_shade<KIND, SRP_GPU_FS_DEPTH_OVERWRITE, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
 	case SRP_GPU_FS_FRAGCOORD: k_shade<KIND, SRP_GPU_FS_FRAGCOORD, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
 	case SRP_GPU_FS_FLAT_INT: k_shade<KIND, SRP_GPU_FS_FLAT_INT, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
+	case kFsLearned:
+		if constexpr (KIND == kKindTri) {
+			cudaFuncSetAttribute(k_shade_learned<KIND, SRP_GPU_FS_MARBLE, MULTI>,
+			                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int) kLearnedSmem);
+			k_shade_learned<KIND, SRP_GPU_FS_MARBLE, MULTI><<<b, t, kLearnedSmem, s>>>(P, numTiles);
+		}
+		break;
 	default: break;
 	}
 }

@@ -72,8 +72,29 @@ struct DrawParams {
 	const uint32_t* tPrefix;
 	const uint32_t* blkPrefix;
 	uint32_t* primPrefix;
+	/* learned shading (fsId == kFsLearned): the MLP's bf16 weights and fp32
+	 * biases; the plain shader that judges it (judgeFs) on 1 pixel in
+	 * judgeEvery; per draw d (0 for a single draw) the judge's squared-error
+	 * sum and channel count (judge[2d], judge[2d + 1]) and largest channel
+	 * error (judgeMax[d], float bits). redo: a multi-draw shade pass that
+	 * shades only the draws flagged there (fallback to the plain shader). */
+	const void* mlpW;
+	const float* mlpB;
+	int judgeFs;
+	uint32_t judgeEvery, sampleSeed;
+	double* judge;
+	unsigned int* judgeMax;
+	const uint8_t* redo;
+	/* fragment capture for training: 1 pixel in captureEvery shaded by the
+	 * plain shader adds (position, normal, view direction, colour) */
+	float* capture;
+	unsigned long long* captureCount;
+	uint32_t captureCap, captureEvery;
 	alignas(16) unsigned char uniform[kMaxUniformBytes];
 };
+
+/* Fragment-shader id of learned shading (not a user shader). */
+constexpr int kFsLearned = 100;
 
 constexpr int kTile = 8;              /* tile edge in pixels */
 constexpr int kSetupThreads = 256;

@@ -1,0 +1,60 @@
+/* The learned-shading network: a small MLP that stands in for an expensive
+ * fragment shader.
+ *
+ * Input: 6-band sin/cos positional encoding of the world position, the unit
+ * normal and the unit view direction (9 components x 6 bands x 2 = 108
+ * features). Three hidden layers of 64 ReLU units, 3 linear outputs (RGB,
+ * clamped to [0, 1] like the shader's output).
+ *
+ * Parameters are kept in fp32 (training, Adam) as one flat vector:
+ *   W1 [108][64], b1 [64], W2 [64][64], b2 [64], W3 [64][64], b3 [64],
+ *   W4 [64][3], b4 [3]           (W[k][n]: input k, output n)
+ * Inference uses a bf16 copy with each weight matrix transposed to [n][k]
+ * and k padded (to 120 for the first layer, 72 for the others, 8 outputs
+ * for the last) so that tensor-core B fragments load from shared memory
+ * without bank conflicts. */
+#pragma once
+
+#include <stdint.h>
+
+namespace srpg {
+
+constexpr int kMlpBands = 6;
+constexpr int kMlpIn = 9 * kMlpBands * 2;      /* 108 */
+constexpr int kMlpInPad = 112;                /* multiple of 16 (tensor-core K step) */
+constexpr int kMlpHid = 64;
+constexpr int kMlpOut = 3;
+
+/* fp32 parameter vector */
+constexpr int kOffW1 = 0;
+constexpr int kOffB1 = kOffW1 + kMlpIn * kMlpHid;
+constexpr int kOffW2 = kOffB1 + kMlpHid;
+constexpr int kOffB2 = kOffW2 + kMlpHid * kMlpHid;
+constexpr int kOffW3 = kOffB2 + kMlpHid;
+constexpr int kOffB3 = kOffW3 + kMlpHid * kMlpHid;
+constexpr int kOffW4 = kOffB3 + kMlpHid;
+constexpr int kOffB4 = kOffW4 + kMlpHid * kMlpOut;
+constexpr int kMlpParams = kOffB4 + kMlpOut;  /* 15491 */
+
+/* bf16 inference copy: transposed, padded rows */
+constexpr int kLd1 = 120;                     /* row pitch of W1t (k = 0..111 used, 108..111 zero) */
+constexpr int kLdH = 72;                      /* row pitch of W2t, W3t, W4t */
+constexpr int kOffT1 = 0;                     /* W1t [64][kLd1] */
+constexpr int kOffT2 = kOffT1 + kMlpHid * kLd1;
+constexpr int kOffT3 = kOffT2 + kMlpHid * kLdH;
+constexpr int kOffT4 = kOffT3 + kMlpHid * kLdH;   /* W4t [8][kLdH], rows 3..7 zero */
+constexpr int kMlpBf16 = kOffT4 + 8 * kLdH;        /* 17472 */
+
+/* One captured fragment: world position, unit normal, unit view direction
+ * and the shader's clamped RGB. */
+constexpr int kSampleFloats = 12;
+
+/* Feature f of the encoding: component c = f / 12 (position x, y, z,
+ * normal x, y, z, view x, y, z), band b = (f % 12) / 2, sine for even f,
+ * cosine for odd f, of 2^b * pi * value. */
+#if defined(__CUDACC__)
+__host__ __device__
+#endif
+inline float mlpBandScale(int b) { return 3.14159265358979f * (float) (1 << b); }
+
+}  // namespace srpg

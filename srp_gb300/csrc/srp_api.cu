@@ -28,6 +28,7 @@
 #include "gpu_types.h"
 #include "imageio.h"
 #include "kernels.h"
+#include "learned_internal.h"
 
 /* The reference requires the user program to define `SRPContext srpContext`.
  * A weak default lets the library also be used from programs (and language
@@ -856,6 +857,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 	uint32_t entryCap = (uint32_t) std::min<double>((double) (nIn * outPer) * g.entryRatio[kind] + 4096, 4.0e9);
 	const uint32_t keyBits = bitsFor(numTiles);
 	const bool late = sp->fs->mayOverwriteDepth && shadeSupportsLateDepth(fsId);
+	const bool learned = learnedPrepare(P, kind, late, 1, g.stream);
 	bool drawn = false;
 	for (int attempt = 0; attempt < 4 && !drawn; ++attempt) {
 		/* long lines are queued in the big-job buffer: room for every line */
@@ -983,6 +985,17 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		drawn = true;
 	}
 	if (!drawn) { SRP_ERROR(FN, "Scratch capacity could not be sized for the draw"); return; }
+	if (learned) {
+		/* the judge found the network too far from the shader: shade again */
+		uint8_t redo = 0;
+		if (learnedJudge(1, &redo, nullptr, g.stream)) {
+			P.fsId = P.judgeFs;
+			stageBegin();
+			launchShade(P, kind, numTiles, g.stream);
+			stageEnd(SRP_GPU_STAGE_SHADE, 1);
+			++g.launches;
+		}
+	}
 	++g.stats.draws;
 	if (g.fbMode == SRP_GPU_FB_COHERENT) fbDownload(fb, fx);
 }
@@ -1183,6 +1196,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	if (g.fbMode == SRP_GPU_FB_COHERENT)
 		for (size_t k = 0; k < n; ++k) fbUpload(draws[idx[k]].framebuffer, fbFind(draws[idx[k]].framebuffer));
 
+	const bool learned = learnedPrepare(P, kKindTri, false, (uint32_t) n, g.stream);
 	uint32_t primCap = (uint32_t) std::min<unsigned long long>((unsigned long long) nIn + 4096, 0x3FFFFFFFu);
 	uint32_t entryCap = (uint32_t) std::min<double>((double) nIn * g.entryRatio[kKindTri] + 4096, 4.0e9);
 	const uint32_t keyBits = bitsFor(numTiles);
@@ -1292,6 +1306,19 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		drawn = true;
 	}
 	if (!drawn) SRP_ERROR(FN, "Scratch capacity could not be sized for the pass");
+	if (drawn && learned) {
+		std::vector<uint8_t> redo(n);
+		const uint8_t* redoDev = nullptr;
+		if (learnedJudge((uint32_t) n, redo.data(), &redoDev, g.stream)) {
+			P.fsId = P.judgeFs;
+			P.redo = redoDev;
+			stageBegin();
+			launchShadeMulti(P, numTiles, g.stream);
+			stageEnd(SRP_GPU_STAGE_SHADE, 1);
+			++g.launches;
+			P.redo = nullptr;
+		}
+	}
 	g.stats.draws += n;
 	if (g.fbMode == SRP_GPU_FB_COHERENT)
 		for (size_t k = 0; k < n; ++k) fbDownload(draws[idx[k]].framebuffer, fbFind(draws[idx[k]].framebuffer));
@@ -1579,6 +1606,20 @@ void fixedDrawDownload(const SRPFramebuffer* fb)
 {
 	if (FbExtra* x = fbFind(fb)) fbDownload(fb, x);
 }
+
+void learnedError(const char* fmt, ...)
+{
+	if (!srpContext.messageCallback.func) return;
+	char buf[1024];
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(buf, sizeof buf, fmt, ap);
+	va_end(ap);
+	srpContext.messageCallback.func(SRP_MESSAGE_ERROR, SRP_MESSAGE_SEVERITY_HIGH, "srpGpuLearnedShading", buf,
+	                                srpContext.messageCallback.userParameter);
+}
+
+int learnedShaderId(void* fragmentShader) { return lookupFS(fragmentShader); }
 
 void fixedDrawAccount(const DeviceCounters& c, unsigned launches)
 {

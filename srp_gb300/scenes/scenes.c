@@ -1130,6 +1130,74 @@ static void buildLit(Scene* s, Rng* rng)
 	s->draws = 2;
 }
 
+/* The learned-shading workload: the soup's geometry (random geodesic
+ * spheres, about 20% of them cut by the near plane), triangles only, shaded
+ * by the expensive procedural shader -- 8-octave value-noise marble lit by
+ * 16 point lights (Blinn-Phong, shininess 64). The lights and the marble
+ * belong to the material, which every seed shares; the seed only places the
+ * spheres. */
+static void renderMSoup(Scene* s, SRPFramebuffer* fb)
+{
+	srpRasterFrontFace(SRP_WINDING_CCW);
+	srpRasterCullFace(SRP_FACE_BACK);
+	srpDepthTest(true);
+	srpDepthCompareOp(SRP_COMPARE_LESS);
+	drawI(s, 0, 0, fb, 0, SRP_PRIM_TRIANGLES, 0, s->ibytes[0] / 4);
+}
+
+static void buildMSoup(Scene* s, Rng* rng)
+{
+	s->W = 1920; s->H = 1080;
+	if (s->scale < 1.0) {
+		const double lin = dexp(0.5 * dlog(s->scale));
+		s->W = (int) (1920 * lin) & ~7; s->H = (int) (1080 * lin) & ~7;
+		if (s->W < 64) s->W = 64;
+		if (s->H < 48) s->H = 48;
+	}
+	const size_t target = (size_t) (2000000 * s->scale);
+	float* verts = NULL; uint32_t* idx = NULL;
+	size_t nv = 0, ni = 0, capv = 0, capi = 0;
+	uint32_t meshId = 0;
+	while (ni / 3 < target) {
+		double tris = logUniform(rng, 5000, 50000);
+		int f = (int) floor(sqrt(tris / 20) + 0.5);
+		double r = logUniform(rng, 0.05, 2.0);
+		double c[3];
+		if (rngU(rng) < 0.2) {
+			double zc = 0.1 + r * rngRange(rng, -0.5, 0.5);
+			double rho = sqrt(fmax(0.0, 1.2 * r * r - zc * zc)) + r * rngRange(rng, 0.0, 0.4);
+			double ang = rngRange(rng, 0, 2 * PI_D);
+			c[0] = rho * dcos(ang); c[1] = rho * dsin(ang); c[2] = zc;
+		} else {
+			c[0] = rngRange(rng, -10, 10); c[1] = rngRange(rng, -10, 10); c[2] = rngRange(rng, 0.5, 20.5);
+		}
+		appendGeodesic(&verts, &nv, &capv, &idx, &ni, &capi, f, c, r, meshId++, rng);
+	}
+	addVB(s, verts, 48, nv * 48);
+	addIB(s, SRP_UINT32, idx, ni * 4);
+	s->nTris = ni / 3;
+	free(verts); free(idx);
+	SRPStdUniform* u = &s->uni[0];
+	baseUniform(u);
+	u->projection = perspective60((float) s->W / (float) s->H, 0.1f, 100.f);
+	u->normalOffset = 3; u->uvOffset = 6;
+	u->nLights = 16;
+	Rng mat = { 0x5EED0F11A7E51A1Dull };   /* the material: the same for every seed */
+	for (int l = 0; l < 16; ++l) {
+		u->lightPos[l][0] = (float) rngRange(&mat, -12, 12);
+		u->lightPos[l][1] = (float) rngRange(&mat, -12, 12);
+		u->lightPos[l][2] = (float) rngRange(&mat, -2, 18);
+		for (int k = 0; k < 3; ++k) u->lightColor[l][k] = (float) rngRange(&mat, 0.1, 0.5);
+	}
+	SRPVaryingInfo v0[3] = { vi(3, SRP_FLOAT, SRP_INTERPOLATION_MODE_PERSPECTIVE),
+	                         vi(3, SRP_FLOAT, SRP_INTERPOLATION_MODE_PERSPECTIVE),
+	                         vi(2, SRP_FLOAT, SRP_INTERPOLATION_MODE_PERSPECTIVE) };
+	program(s, 0, srpVsWorld, srpFsMarble, 0, 3, v0);
+	s->depthInit = 1.0f;
+	s->render = renderMSoup;
+	s->draws = 1;
+}
+
 /* One scene of the batched workload: a single mesh of random triangles
  * (log-uniform 12 to 200k of them) in its own framebuffer (each side
  * log-uniform 64 to 1024), random camera, textured Blinn-Phong with one
@@ -1248,6 +1316,7 @@ static const SceneDef DEFS[] = {
 	{ "late_z", buildLateZ },
 	{ "lit", buildLit },
 	{ "bscene", buildBScene },
+	{ "msoup", buildMSoup },
 };
 
 const char* const* sceneNames(void)

@@ -1,0 +1,238 @@
+"""The learned-shading network: the CPU oracle checked against finite
+differences, the GPU kernels (gradients, fp32 and tensor-core forward, one
+Adam step) against the oracle, and learned shading in a draw (coverage,
+depth and stencil untouched; fallback to the shader below the PSNR bar)."""
+import ctypes
+import os
+import sys
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+import mlp_oracle as mo  # noqa: E402
+
+
+def random_samples(rng, n):
+    pos = rng.uniform(-3, 3, size=(n, 3))
+    nrm = rng.normal(size=(n, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    view = rng.normal(size=(n, 3))
+    view /= np.linalg.norm(view, axis=1, keepdims=True)
+    rgb = 0.5 + 0.4 * np.stack([np.sin(pos[:, 0]), np.cos(pos[:, 1]), nrm[:, 2] * view[:, 2]], axis=1)
+    return np.concatenate([pos, nrm, view, rgb], axis=1).astype(np.float32)
+
+
+def test_oracle_gradient_matches_finite_differences():
+    rng = np.random.default_rng(3)
+    p = rng.normal(scale=0.2, size=mo.N_PARAMS)
+    s = random_samples(rng, 16)
+    _, g = mo.loss_and_grad(p, s)
+    B = len(s)
+    for idx in rng.choice(mo.N_PARAMS, size=40, replace=False):
+        e = np.zeros_like(p)
+        e[idx] = 1e-6
+        lp, _ = mo.loss_and_grad(p + e, s)
+        lm, _ = mo.loss_and_grad(p - e, s)
+        num = (lp - lm) / (2e-6) / (3 * B)
+        assert abs(num - g[idx]) <= 1e-6 + 1e-4 * abs(num), (idx, num, g[idx])
+
+
+def test_oracle_batch_indices_are_in_range():
+    idx = mo.batch_indices(7, 5000, 1234)
+    assert idx.min() >= 0 and idx.max() < 1234 and len(np.unique(idx)) > 1000
+
+
+class Net:
+    def __init__(self, seed=5, capacity=1 << 16):
+        import srp_gb300
+        self.srp = srp_gb300
+        L = srp_gb300.lib()
+        vp, f32p = ctypes.c_void_p, ctypes.POINTER(ctypes.c_float)
+        for name, res, args in [
+            ("srpGpuMlpCreate", vp, [ctypes.c_uint64, ctypes.c_size_t]),
+            ("srpGpuMlpFree", None, [vp]),
+            ("srpGpuMlpParamCount", ctypes.c_size_t, []),
+            ("srpGpuMlpGetParams", None, [vp, f32p]),
+            ("srpGpuMlpSetParams", None, [vp, f32p]),
+            ("srpGpuMlpEvaluate", ctypes.c_int, [vp, f32p, ctypes.c_size_t, f32p, ctypes.c_int]),
+            ("srpGpuMlpGradients", ctypes.c_int, [vp, f32p, ctypes.c_size_t, f32p, ctypes.POINTER(ctypes.c_double)]),
+            ("srpGpuMlpAddSamples", ctypes.c_int, [vp, f32p, ctypes.c_size_t]),
+            ("srpGpuMlpTrain", ctypes.c_float, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_float]),
+            ("srpGpuMlpSampleCount", ctypes.c_size_t, [vp]),
+        ]:
+            fn = getattr(L, name)
+            fn.restype, fn.argtypes = res, args
+        self.L = L
+        self.m = L.srpGpuMlpCreate(seed, capacity)
+        assert self.m
+        assert L.srpGpuMlpParamCount() == mo.N_PARAMS
+
+    @staticmethod
+    def ptr(a):
+        return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+    def params(self):
+        p = np.zeros(mo.N_PARAMS, dtype=np.float32)
+        self.L.srpGpuMlpGetParams(self.m, self.ptr(p))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self.L.srpGpuMlpSetParams(self.m, self.ptr(p))
+
+    def evaluate(self, s, tc):
+        s = np.ascontiguousarray(s, dtype=np.float32)
+        out = np.zeros((len(s), 3), dtype=np.float32)
+        assert self.L.srpGpuMlpEvaluate(self.m, self.ptr(s), len(s), self.ptr(out), int(tc)) == 0
+        return out
+
+    def gradients(self, s):
+        s = np.ascontiguousarray(s, dtype=np.float32)
+        g = np.zeros(mo.N_PARAMS, dtype=np.float32)
+        sse = ctypes.c_double()
+        assert self.L.srpGpuMlpGradients(self.m, self.ptr(s), len(s), self.ptr(g), ctypes.byref(sse)) == 0
+        return sse.value, g
+
+    def close(self):
+        self.L.srpGpuMlpFree(self.m)
+
+
+@pytest.fixture()
+def net(built_library):
+    n = Net()
+    yield n
+    n.close()
+
+
+@pytest.mark.gpu
+def test_gpu_forward_matches_oracle(net):
+    rng = np.random.default_rng(11)
+    s = random_samples(rng, 3000)
+    want, _ = mo.forward(net.params().astype(np.float64), s)
+    got = net.evaluate(s, tc=False)
+    assert np.abs(got - want).max() < 2e-4 * max(1.0, np.abs(want).max())
+    # the shading path: bf16 weights and activations on the tensor cores
+    tc = net.evaluate(s, tc=True)
+    err = np.abs(tc - want)
+    assert err.max() < 0.05 * max(1.0, np.abs(want).max()), err.max()
+    assert err.mean() < 0.01 * max(1.0, np.abs(want).mean())
+
+
+@pytest.mark.gpu
+def test_gpu_gradients_match_oracle(net):
+    rng = np.random.default_rng(12)
+    s = random_samples(rng, 4096)
+    sse, g = net.gradients(s)
+    want_sse, want = mo.loss_and_grad(net.params().astype(np.float64), s)
+    assert abs(sse - want_sse) <= 1e-4 * want_sse
+    scale = np.abs(want).max()
+    assert np.abs(g - want).max() <= 2e-4 * scale, np.abs(g - want).max() / scale
+
+
+@pytest.mark.gpu
+def test_gpu_adam_step_matches_oracle(net):
+    """One training step: the device's batch choice, gradients and Adam."""
+    rng = np.random.default_rng(13)
+    s = random_samples(rng, 2000)
+    assert net.L.srpGpuMlpAddSamples(net.m, Net.ptr(s), len(s)) == 0
+    p0 = net.params().astype(np.float64)
+    B, lr = 1024, 1e-3
+    loss = net.L.srpGpuMlpTrain(net.m, 1, B, lr)
+    assert loss >= 0
+    batch = s[mo.batch_indices(0, B, len(s))]
+    sse, g = mo.loss_and_grad(p0, batch)
+    assert abs(loss - sse / (3 * B)) <= 1e-4 * sse / (3 * B)
+    want, _, _ = mo.adam_step(p0, g, np.zeros_like(p0), np.zeros_like(p0), 1, 1, lr)
+    got = net.params().astype(np.float64)
+    # the first Adam step moves each parameter by about lr * sign(grad): the
+    # sign of gradients within rounding of zero may differ
+    close = np.abs(got - want) <= 1e-6 + 1e-3 * lr
+    assert close.mean() > 0.995, close.mean()
+
+
+@pytest.mark.gpu
+def test_gpu_training_reduces_error(net):
+    rng = np.random.default_rng(14)
+    s = random_samples(rng, 20000)
+    assert net.L.srpGpuMlpAddSamples(net.m, Net.ptr(s), len(s)) == 0
+    before = float(np.mean((net.evaluate(s, tc=False) - s[:, 9:12]) ** 2))
+    loss = net.L.srpGpuMlpTrain(net.m, 400, 4096, 3e-3)
+    after = float(np.mean((net.evaluate(s, tc=False) - s[:, 9:12]) ** 2))
+    assert loss >= 0 and after < 0.2 * before, (before, after)
+
+
+class LearnedStats(ctypes.Structure):
+    _fields_ = [("draws", ctypes.c_uint64), ("fallbacks", ctypes.c_uint64), ("judgedDraws", ctypes.c_uint64),
+                ("judgedChannels", ctypes.c_uint64), ("squaredError", ctypes.c_double),
+                ("lastPsnrDb", ctypes.c_double), ("minPsnrDb", ctypes.c_double), ("maxChannelError", ctypes.c_float)]
+
+
+def sync_planes(S, fb):
+    import srp_gb300
+    S.srpGpuFramebufferSync(fb)
+    c, d, s = srp_gb300.framebuffer_arrays(fb)
+    return c, d.view(np.uint32), s
+
+
+@pytest.mark.gpu
+def test_learned_shading_in_a_draw(built_library):
+    """Capture fragments of the marble shader, train, then shade a held-out
+    scene with the network: depth and stencil are the plain draw's, colours
+    come from the network; below the PSNR bar the draw falls back to the
+    shader and matches the plain draw exactly."""
+    import srp_gb300
+    L, S = srp_gb300.lib(), srp_gb300.scenes()
+    L.srpGpuSetFramebufferMode(1)
+    vp = ctypes.c_void_p
+    L.srpGpuMlpCapture.argtypes = [vp, vp, ctypes.c_uint32]
+    L.srpGpuSetLearnedShading.argtypes = [vp, vp, ctypes.c_float, ctypes.c_uint32]
+    L.srpGpuGetLearnedStats.argtypes = [ctypes.POINTER(LearnedStats)]
+    marble = ctypes.cast(L.srpFsMarble, vp)
+    net = Net(capacity=1 << 20)
+    try:
+        L.srpGpuMlpCapture(net.m, marble, 2)
+        for seed in range(4):
+            sc = srp_gb300.Scene("msoup", 100 + seed, 0.04)
+            sc.prepare()
+            sc.render()
+            sc.close()
+        L.srpGpuMlpCapture(None, None, 0)
+        n = net.L.srpGpuMlpSampleCount(net.m)
+        assert n > 2000, n
+        assert net.L.srpGpuMlpTrain(net.m, 300, 4096, 3e-3) >= 0
+        sc = srp_gb300.Scene("msoup", 7, 0.05)
+        try:
+            sc.prepare()
+            sc.render()
+            plain = sync_planes(S, sc.fb)
+            covered = plain[1] != np.float32(1.0).view(np.uint32)
+            assert covered.sum() > 1000
+            L.srpGpuResetLearnedStats()
+            L.srpGpuSetLearnedShading(marble, net.m, 0.0, 16)
+            sc.prepare()
+            sc.render()
+            learned = sync_planes(S, sc.fb)
+            st = LearnedStats()
+            L.srpGpuGetLearnedStats(ctypes.byref(st))
+            assert st.draws == 1 and st.fallbacks == 0 and st.judgedChannels > 0
+            assert np.array_equal(learned[1], plain[1]) and np.array_equal(learned[2], plain[2])
+            assert np.array_equal(learned[0] == 0, plain[0] == 0)
+            assert (learned[0] != plain[0]).any()
+            assert 5.0 < st.lastPsnrDb < 100.0
+            # an unreachable bar: every draw is shaded again by the shader
+            L.srpGpuResetLearnedStats()
+            L.srpGpuSetLearnedShading(marble, net.m, 1000.0, 16)
+            sc.prepare()
+            sc.render()
+            fallback = sync_planes(S, sc.fb)
+            L.srpGpuGetLearnedStats(ctypes.byref(st))
+            assert st.draws == 1 and st.fallbacks == 1
+            for a, b in zip(fallback, plain):
+                assert np.array_equal(a, b)
+        finally:
+            L.srpGpuSetLearnedShading(None, None, 0.0, 0)
+            sc.close()
+    finally:
+        net.close()
+    assert L.srpGpuSynchronize() == 0
