@@ -24,7 +24,9 @@ same frame, one process per core. N > 1 runs independent replicas (the path
 does not shard across GPUs within a frame).
 """
 import argparse
+import ctypes
 import json
+import math
 import os
 import subprocess
 import sys
@@ -303,6 +305,139 @@ def run_batch(args):
         sc.close()
 
 
+LEARNED_WORKLOAD = ("learned: 2.0M-triangle geodesic-sphere soup at 1920x1080 shaded by 8-octave value-noise "
+                    "marble with 16 point lights (srpFsMarble), against its learned MLP stand-in")
+
+
+class LearnedStats(ctypes.Structure):
+    """SRPGpuLearnedStats of srp/gpu.h."""
+    _fields_ = [("draws", ctypes.c_uint64), ("fallbacks", ctypes.c_uint64), ("judgedDraws", ctypes.c_uint64),
+                ("judgedChannels", ctypes.c_uint64), ("squaredError", ctypes.c_double),
+                ("lastPsnrDb", ctypes.c_double), ("minPsnrDb", ctypes.c_double), ("maxChannelError", ctypes.c_float)]
+
+
+def run_learned(args):
+    """Train the learned stand-in of the marble shader on fragments of 32
+    training scenes, then time a held-out full-size frame shaded by the
+    shader, by the network alone, and by the network with the judge's
+    40 dB fallback."""
+    import ctypes
+    import torch
+    import srp_gb300
+
+    srp_gb300.build()
+    L = srp_gb300.lib()
+    vp = ctypes.c_void_p
+    L.srpGpuMlpCreate.restype = vp
+    L.srpGpuMlpCreate.argtypes = [ctypes.c_uint64, ctypes.c_size_t]
+    L.srpGpuMlpFree.argtypes = [vp]
+    L.srpGpuMlpCapture.argtypes = [vp, vp, ctypes.c_uint32]
+    L.srpGpuMlpSampleCount.restype = ctypes.c_size_t
+    L.srpGpuMlpSampleCount.argtypes = [vp]
+    L.srpGpuMlpTrain.restype = ctypes.c_float
+    L.srpGpuMlpTrain.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_float]
+    L.srpGpuSetLearnedShading.argtypes = [vp, vp, ctypes.c_float, ctypes.c_uint32]
+    L.srpGpuGetLearnedStats.argtypes = [ctypes.POINTER(LearnedStats)]
+    L.srpGpuSetFramebufferMode(srp_gb300.SRP_GPU_FB_DEVICE)
+    stream = torch.cuda.Stream()
+    L.srpGpuSetStream(ctypes.c_void_p(stream.cuda_stream))
+    marble = ctypes.cast(L.srpFsMarble, vp)
+    net = L.srpGpuMlpCreate(7, 4 << 20)
+    # training data: every shaded pixel of 32 smaller scenes (other seeds)
+    t0 = time.perf_counter()
+    L.srpGpuMlpCapture(net, marble, 1)
+    for i in range(32):
+        sc = srp_gb300.Scene("msoup", 1000 + i, 0.12)
+        sc.prepare()
+        sc.render()
+        sc.close()
+    L.srpGpuMlpCapture(None, None, 0)
+    samples = L.srpGpuMlpSampleCount(net)
+    capture_s = time.perf_counter() - t0
+    steps, batch = 3000, 16384
+    t0 = time.perf_counter()
+    final_mse = L.srpGpuMlpTrain(net, steps, batch, 2e-3)
+    train_s = time.perf_counter() - t0
+    sc = srp_gb300.Scene("msoup", SEED, 1.0)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed(frames):
+        ms, shade = [], []
+        for _ in range(frames):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+                sc.prepare()
+                L.srpGpuSetProfiling(1)
+                L.srpGpuResetProfile()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                sc.render()
+                e1.record(stream)
+            stream.synchronize()
+            prof = srp_gb300.SRPGpuProfile()
+            L.srpGpuGetProfile(ctypes.byref(prof))
+            L.srpGpuSetProfiling(0)
+            ms.append(e0.elapsed_time(e1))
+            shade.append(prof.ms[4])
+        return sorted(ms)[len(ms) // 2], sorted(shade)[len(shade) // 2]
+
+    L.srpGpuResetStats()
+    for _ in range(max(args.warmup, 1)):
+        sc.prepare()
+        sc.render()
+    torch.cuda.synchronize()
+    L.srpGpuResetStats()
+    sc.prepare()
+    sc.render()
+    st = srp_gb300.SRPGpuStats()
+    L.srpGpuGetStats(ctypes.byref(st))
+    frags = st.fragments
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    plain_ms, plain_shade = timed(args.steps)
+    L.srpGpuSetLearnedShading(marble, net, 0.0, 64)
+    for _ in range(2):
+        sc.prepare()
+        sc.render()
+    L.srpGpuResetLearnedStats()
+    mlp_ms, mlp_shade = timed(args.steps)
+    ls = LearnedStats()
+    L.srpGpuGetLearnedStats(ctypes.byref(ls))
+    psnr = 10.0 * math.log10(ls.judgedChannels / ls.squaredError) if ls.squaredError > 0 else None
+    L.srpGpuSetLearnedShading(marble, net, 40.0, 64)
+    L.srpGpuResetLearnedStats()
+    judged_ms, judged_shade = timed(args.steps)
+    lj = LearnedStats()
+    L.srpGpuGetLearnedStats(ctypes.byref(lj))
+    L.srpGpuSetLearnedShading(None, None, 0.0, 0)
+    clk = clocks.stop()
+    mfr = lambda ms: round(frags / (ms / 1000.0) / 1e6, 1)
+    line = {
+        "metric": "Mfrag/s", "value": mfr(judged_ms), "unit": "Mfrag/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(judged_ms, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16 (network), f32 (rest)", "data": "synthetic",
+        "config": {"workload": LEARNED_WORKLOAD, "seed": SEED, "fragments_per_frame": frags,
+                   "training": {"scenes": 32, "samples": samples, "capture_s": round(capture_s, 2),
+                                "steps": steps, "batch": batch, "train_s": round(train_s, 2),
+                                "final_batch_mse": round(final_mse, 6)}},
+        "plain": {"ms_per_frame": round(plain_ms, 4), "Mfrag_per_s": mfr(plain_ms), "shade_ms": round(plain_shade, 4)},
+        "learned_no_fallback": {"ms_per_frame": round(mlp_ms, 4), "Mfrag_per_s": mfr(mlp_ms),
+                                "shade_ms": round(mlp_shade, 4),
+                                "psnr_db": round(psnr, 2) if psnr else None,
+                                "max_channel_error": round(float(ls.maxChannelError), 4)},
+        "learned_with_judge_40db": {"ms_per_frame": round(judged_ms, 4), "Mfrag_per_s": mfr(judged_ms),
+                                    "shade_ms": round(judged_shade, 4), "draws": lj.draws,
+                                    "fallbacks": lj.fallbacks},
+        "shade_speedup_no_fallback": round(plain_shade / mlp_shade, 3) if mlp_shade > 0 else None,
+        "clocks": clk,
+        "gpu_launches": int(st.kernelLaunches),
+    }
+    print(json.dumps(line))
+    sc.close()
+    L.srpGpuMlpFree(net)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -311,12 +446,15 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="frame", choices=["frame", "batch"],
-                    help="frame: the 2M-triangle 1080p frame (default); batch: the batched-scenes workload")
+    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "learned"],
+                    help="frame: the 2M-triangle 1080p frame (default); batch: the batched-scenes workload; "
+                         "learned: the marble-shaded frame with its learned stand-in")
     ap.add_argument("--scenes", type=int, default=BATCH_SCENES, help="scenes per batch (--workload batch)")
     args = ap.parse_args()
     if args.workload == "batch":
         return run_reference_batch(args) if args.impl == "reference" else run_batch(args)
+    if args.workload == "learned":
+        return run_learned(args)
     if args.impl == "reference":
         return run_reference(args)
 
