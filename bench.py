@@ -313,7 +313,8 @@ class LearnedStats(ctypes.Structure):
     """SRPGpuLearnedStats of srp/gpu.h."""
     _fields_ = [("draws", ctypes.c_uint64), ("fallbacks", ctypes.c_uint64), ("judgedDraws", ctypes.c_uint64),
                 ("judgedChannels", ctypes.c_uint64), ("squaredError", ctypes.c_double),
-                ("lastPsnrDb", ctypes.c_double), ("minPsnrDb", ctypes.c_double), ("maxChannelError", ctypes.c_float)]
+                ("lastPsnrDb", ctypes.c_double), ("minPsnrDb", ctypes.c_double), ("maxChannelError", ctypes.c_float),
+                ("psnrHistogram", ctypes.c_uint64 * 6)]
 
 
 def run_learned(args):
@@ -328,20 +329,10 @@ def run_learned(args):
     srp_gb300.build()
     L = srp_gb300.lib()
     vp = ctypes.c_void_p
-    L.srpGpuMlpCreate.restype = vp
-    L.srpGpuMlpCreate.argtypes = [ctypes.c_uint64, ctypes.c_size_t]
-    L.srpGpuMlpFree.argtypes = [vp]
-    L.srpGpuMlpCapture.argtypes = [vp, vp, ctypes.c_uint32]
-    L.srpGpuMlpSampleCount.restype = ctypes.c_size_t
-    L.srpGpuMlpSampleCount.argtypes = [vp]
-    L.srpGpuMlpTrain.restype = ctypes.c_float
-    L.srpGpuMlpTrain.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_float]
-    L.srpGpuSetLearnedShading.argtypes = [vp, vp, ctypes.c_float, ctypes.c_uint32]
-    L.srpGpuGetLearnedStats.argtypes = [ctypes.POINTER(LearnedStats)]
+    marble = learned_api(L)
     L.srpGpuSetFramebufferMode(srp_gb300.SRP_GPU_FB_DEVICE)
     stream = torch.cuda.Stream()
     L.srpGpuSetStream(ctypes.c_void_p(stream.cuda_stream))
-    marble = ctypes.cast(L.srpFsMarble, vp)
     net = L.srpGpuMlpCreate(7, 4 << 20)
     # training data: every shaded pixel of 32 smaller scenes (other seeds)
     t0 = time.perf_counter()
@@ -354,11 +345,11 @@ def run_learned(args):
     L.srpGpuMlpCapture(None, None, 0)
     samples = L.srpGpuMlpSampleCount(net)
     capture_s = time.perf_counter() - t0
-    steps, batch = 3000, 16384
+    steps, batch = args.train_steps, 16384
     t0 = time.perf_counter()
     final_mse = L.srpGpuMlpTrain(net, steps, batch, 2e-3)
     train_s = time.perf_counter() - t0
-    sc = srp_gb300.Scene("msoup", SEED, 1.0)
+    sc = srp_gb300.Scene("msoup", SEED, args.scale)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     def timed(frames):
@@ -438,6 +429,125 @@ def run_learned(args):
     L.srpGpuMlpFree(net)
 
 
+BATCH_LEARNED_WORKLOAD = ("batch-learned: the 4096-scene batch shaded by 8-octave value-noise marble with 16 point "
+                          "lights (srpFsMarble), against its learned MLP stand-in with per-draw judging")
+
+
+def learned_api(L):
+    vp = ctypes.c_void_p
+    L.srpGpuMlpCreate.restype = vp
+    L.srpGpuMlpCreate.argtypes = [ctypes.c_uint64, ctypes.c_size_t]
+    L.srpGpuMlpFree.argtypes = [vp]
+    L.srpGpuMlpCapture.argtypes = [vp, vp, ctypes.c_uint32]
+    L.srpGpuMlpSampleCount.restype = ctypes.c_size_t
+    L.srpGpuMlpSampleCount.argtypes = [vp]
+    L.srpGpuMlpTrain.restype = ctypes.c_float
+    L.srpGpuMlpTrain.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_float]
+    L.srpGpuSetLearnedShading.argtypes = [vp, vp, ctypes.c_float, ctypes.c_uint32]
+    L.srpGpuGetLearnedStats.argtypes = [ctypes.POINTER(LearnedStats)]
+    return ctypes.cast(L.srpFsMarble, vp)
+
+
+def run_batch_learned(args):
+    """The batch of run_batch with the marble shader: trained on fragments of
+    512 other scenes, then timed plain, learned, and learned with the 40 dB
+    per-draw fallback."""
+    import torch
+    import srp_gb300
+
+    srp_gb300.build()
+    L = srp_gb300.lib()
+    marble = learned_api(L)
+    L.srpGpuSetFramebufferMode(srp_gb300.SRP_GPU_FB_DEVICE)
+    stream = torch.cuda.Stream()
+    L.srpGpuSetStream(ctypes.c_void_p(stream.cuda_stream))
+    net = L.srpGpuMlpCreate(7, 4 << 20)
+    t0 = time.perf_counter()
+    train = [srp_gb300.Scene("bmscene", srp_gb300.batch_seed(31, i), args.scale) for i in range(512)]
+    L.srpGpuMlpCapture(net, marble, 4)
+    for sc in train:
+        sc.prepare()
+    srp_gb300.render_batch(train, [sc.fb for sc in train])
+    L.srpGpuMlpCapture(None, None, 0)
+    samples = L.srpGpuMlpSampleCount(net)
+    for sc in train:
+        sc.close()
+    capture_s = time.perf_counter() - t0
+    steps, batch = args.train_steps, 16384
+    t0 = time.perf_counter()
+    final_mse = L.srpGpuMlpTrain(net, steps, batch, 2e-3)
+    train_s = time.perf_counter() - t0
+    batchs = [srp_gb300.Scene("bmscene", srp_gb300.batch_seed(BATCH_BASE, i), args.scale) for i in range(args.scenes)]
+    fbs = [sc.fb for sc in batchs]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed():
+        ms = []
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+                for sc in batchs:
+                    sc.prepare()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                srp_gb300.render_batch(batchs, fbs)
+                e1.record(stream)
+            stream.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return sorted(ms)[len(ms) // 2]
+
+    for _ in range(max(args.warmup, 1)):
+        for sc in batchs:
+            sc.prepare()
+        srp_gb300.render_batch(batchs, fbs)
+    torch.cuda.synchronize()
+    L.srpGpuResetStats()
+    for sc in batchs:
+        sc.prepare()
+    srp_gb300.render_batch(batchs, fbs)
+    st = srp_gb300.SRPGpuStats()
+    L.srpGpuGetStats(ctypes.byref(st))
+    frags = st.fragments
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    plain_ms = timed()
+    L.srpGpuSetLearnedShading(marble, net, 0.0, 64)
+    L.srpGpuResetLearnedStats()
+    learned_ms = timed()
+    ls = LearnedStats()
+    L.srpGpuGetLearnedStats(ctypes.byref(ls))
+    L.srpGpuSetLearnedShading(marble, net, 40.0, 64)
+    L.srpGpuResetLearnedStats()
+    judged_ms = timed()
+    lj = LearnedStats()
+    L.srpGpuGetLearnedStats(ctypes.byref(lj))
+    L.srpGpuSetLearnedShading(None, None, 0.0, 0)
+    clk = clocks.stop()
+    n = args.scenes
+    psnr = 10.0 * math.log10(ls.judgedChannels / ls.squaredError) if ls.squaredError > 0 else None
+    rate = lambda ms: {"ms_per_batch": round(ms, 3), "scenes_per_s": round(n / (ms / 1000.0), 1),
+                       "Mfrag_per_s": round(frags / (ms / 1000.0) / 1e6, 1)}
+    line = {
+        "metric": "scenes/s", "value": round(n / (judged_ms / 1000.0), 1), "unit": "scenes/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(judged_ms, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16 (network), f32 (rest)", "data": "synthetic",
+        "config": {"workload": BATCH_LEARNED_WORKLOAD, "scenes": n, "fragments_per_step": frags,
+                   "training": {"scenes": 512, "samples": samples, "capture_s": round(capture_s, 2), "steps": steps,
+                                "batch": batch, "train_s": round(train_s, 2), "final_batch_mse": round(final_mse, 6)}},
+        "plain": rate(plain_ms),
+        "learned_no_fallback": dict(rate(learned_ms), psnr_db=round(psnr, 2) if psnr else None,
+                                    psnr_histogram_lt20_20_25_30_35_40_ge40=list(ls.psnrHistogram)),
+        "learned_with_judge_40db": dict(rate(judged_ms), draws=lj.draws, fallbacks=lj.fallbacks,
+                                        fallback_rate=round(lj.fallbacks / max(lj.draws, 1), 4)),
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    for sc in batchs:
+        sc.close()
+    L.srpGpuMlpFree(net)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -446,15 +556,18 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "learned"],
+    ap.add_argument("--workload", default="frame", choices=["frame", "batch", "learned", "batch-learned"],
                     help="frame: the 2M-triangle 1080p frame (default); batch: the batched-scenes workload; "
                          "learned: the marble-shaded frame with its learned stand-in")
     ap.add_argument("--scenes", type=int, default=BATCH_SCENES, help="scenes per batch (--workload batch)")
+    ap.add_argument("--train-steps", type=int, default=3000, help="training steps (--workload learned, batch-learned)")
     args = ap.parse_args()
     if args.workload == "batch":
         return run_reference_batch(args) if args.impl == "reference" else run_batch(args)
     if args.workload == "learned":
         return run_learned(args)
+    if args.workload == "batch-learned":
+        return run_batch_learned(args)
     if args.impl == "reference":
         return run_reference(args)
 

@@ -680,6 +680,14 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_shade(const __grid_const
 	}
 }
 
+/* The plain shader on a judged pixel: rare, so kept out of line. */
+template <int KIND, int FS>
+__device__ __noinline__ void judgeShade(const DrawParams& P, const unsigned char* uniform, uint32_t primBase,
+                                        uint32_t item, int gx, int gy, SRPFragmentShaderOut& out)
+{
+	shadeItem<KIND, FS>(P, uniform, primBase, item, gx, gy, out);
+}
+
 /* Learned shading of the winners of a tile: their inputs go to shared
  * memory, the MLP runs on the tensor cores 16 pixels at a time
  * (mlp_infer.cuh), and 1 pixel in judgeEvery is also shaded by the plain
@@ -696,69 +704,73 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_shade_learned(const __gr
 	for (int i = threadIdx.x; i < kMlpBf16 / 2; i += blockDim.x) sw[i] = ((const uint32_t*) P.mlpW)[i];
 	for (int i = threadIdx.x; i < 3 * kMlpHid + kMlpOut; i += blockDim.x) sb[i] = P.mlpB[i];
 	__syncthreads();
+	if (P.ctr->abort) return;
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	const uint32_t tile = blockIdx.x * kResolveWarps + warp;
-	if (tile >= numTiles || P.ctr->abort) return;
-	if (P.tileStart[tile] >= P.tileEnd[tile]) return;
-	const TileCtx c = tileCtx<MULTI>(P, tile);
-	int32_t win[2];
-	int gx[2], gy[2];
-	size_t idx[2];
+	/* one tile per warp (the loop only runs again for grids smaller than the tiles) */
+	for (uint32_t tile = blockIdx.x * kResolveWarps + warp; tile < numTiles; tile += gridDim.x * kResolveWarps) {
+		if (P.tileStart[tile] >= P.tileEnd[tile]) continue;
+		const TileCtx c = tileCtx<MULTI>(P, tile);
+		int32_t win[2];
+		int gx[2], gy[2];
+		size_t idx[2];
 #pragma unroll
-	for (int p = 0; p < 2; ++p) {
-		const int q = lane + 32 * p;
-		gx[p] = c.x0 + (q & 7);
-		gy[p] = c.y0 + (q >> 3);
-		const bool valid = gx[p] < c.W && gy[p] < c.H;
-		idx[p] = valid ? (size_t) gy[p] * c.W + gx[p] : 0;
-		win[p] = valid ? c.winner[idx[p]] : -1;
-		float* x9 = sx[warp][q];
-		if (win[p] >= 0) {
-			uint32_t words[kMaxVaryingWords];
-			SRPFragmentShaderIn in;
-			fragmentIn<KIND>(P, c.uniform, c.primBase, (uint32_t) win[p], gx[p], gy[p], in, words);
-			learnedInputs(c.uniform, words, x9);
-		} else {
+		for (int p = 0; p < 2; ++p) {
+			const int q = lane + 32 * p;
+			gx[p] = c.x0 + (q & 7);
+			gy[p] = c.y0 + (q >> 3);
+			const bool valid = gx[p] < c.W && gy[p] < c.H;
+			idx[p] = valid ? (size_t) gy[p] * c.W + gx[p] : 0;
+			win[p] = valid ? c.winner[idx[p]] : -1;
+			float* x9 = sx[warp][q];
+			if (win[p] >= 0) {
+				uint32_t words[kMaxVaryingWords];
+				SRPFragmentShaderIn in;
+				fragmentIn<KIND>(P, c.uniform, c.primBase, (uint32_t) win[p], gx[p], gy[p], in, words);
+				learnedInputs(c.uniform, words, x9);
+			} else {
 #pragma unroll
-			for (int k = 0; k < 9; ++k) x9[k] = 0.0f;
-		}
-	}
-	__syncwarp();
-	const unsigned b0 = __ballot_sync(0xFFFFFFFFu, win[0] >= 0), b1 = __ballot_sync(0xFFFFFFFFu, win[1] >= 0);
-	const unsigned sliceBits[4] = { b0 & 0xFFFFu, b0 >> 16, b1 & 0xFFFFu, b1 >> 16 };
-#pragma unroll
-	for (int sl = 0; sl < 4; ++sl)
-		if (sliceBits[sl]) mlpSlice16(sx[warp] + 16 * sl, sw, sb, so[warp] + 16 * sl);
-	__syncwarp();
-	double err = 0.0, chans = 0.0;
-	float worst = 0.0f;
-#pragma unroll
-	for (int p = 0; p < 2; ++p) {
-		if (win[p] < 0) continue;
-		const int q = lane + 32 * p;
-		float col[4] = { clamp01f(so[warp][q][0]), clamp01f(so[warp][q][1]), clamp01f(so[warp][q][2]), 1.0f };
-		c.color[idx[p]] = packColor(col);
-		if (pixelSampled(gx[p], gy[p], P.sampleSeed + c.d, P.judgeEvery)) {
-			SRPFragmentShaderOut ref;
-			shadeItem<KIND, FS>(P, c.uniform, c.primBase, (uint32_t) win[p], gx[p], gy[p], ref);
-#pragma unroll
-			for (int k = 0; k < 3; ++k) {
-				const float dlt = col[k] - ref.color[k];
-				err += (double) dlt * dlt;
-				worst = fmaxf(worst, fabsf(dlt));
+				for (int k = 0; k < 9; ++k) x9[k] = 0.0f;
 			}
-			chans += 3.0;
 		}
-	}
-	for (int o = 16; o; o >>= 1) {
-		err += __shfl_xor_sync(0xFFFFFFFFu, err, o);
-		chans += __shfl_xor_sync(0xFFFFFFFFu, chans, o);
-		worst = fmaxf(worst, __shfl_xor_sync(0xFFFFFFFFu, worst, o));
-	}
-	if (lane == 0 && chans > 0.0) {
-		atomicAdd(&P.judge[2 * c.d], err);
-		atomicAdd(&P.judge[2 * c.d + 1], chans);
-		atomicMax(&P.judgeMax[c.d], __float_as_uint(worst));
+		__syncwarp();
+		const unsigned b0 = __ballot_sync(0xFFFFFFFFu, win[0] >= 0), b1 = __ballot_sync(0xFFFFFFFFu, win[1] >= 0);
+		const unsigned sliceBits[4] = { b0 & 0xFFFFu, b0 >> 16, b1 & 0xFFFFu, b1 >> 16 };
+		/* one copy of the network's code: the instruction cache holds it */
+#pragma unroll 1
+		for (int sl = 0; sl < 4; ++sl)
+			if (sliceBits[sl]) mlpSlice16(sx[warp] + 16 * sl, sw, sb, so[warp] + 16 * sl);
+		__syncwarp();
+		double err = 0.0, chans = 0.0;
+		float worst = 0.0f;
+#pragma unroll
+		for (int p = 0; p < 2; ++p) {
+			if (win[p] < 0) continue;
+			const int q = lane + 32 * p;
+			float col[4] = { clamp01f(so[warp][q][0]), clamp01f(so[warp][q][1]), clamp01f(so[warp][q][2]), 1.0f };
+			c.color[idx[p]] = packColor(col);
+			if (pixelSampled(gx[p], gy[p], P.sampleSeed + c.d, P.judgeEvery)) {
+				SRPFragmentShaderOut ref;
+				judgeShade<KIND, FS>(P, c.uniform, c.primBase, (uint32_t) win[p], gx[p], gy[p], ref);
+#pragma unroll
+				for (int k = 0; k < 3; ++k) {
+					const float dlt = col[k] - ref.color[k];
+					err += (double) dlt * dlt;
+					worst = fmaxf(worst, fabsf(dlt));
+				}
+				chans += 3.0;
+			}
+		}
+		for (int o = 16; o; o >>= 1) {
+			err += __shfl_xor_sync(0xFFFFFFFFu, err, o);
+			chans += __shfl_xor_sync(0xFFFFFFFFu, chans, o);
+			worst = fmaxf(worst, __shfl_xor_sync(0xFFFFFFFFu, worst, o));
+		}
+		if (lane == 0 && chans > 0.0) {
+			atomicAdd(&P.judge[2 * c.d], err);
+			atomicAdd(&P.judge[2 * c.d + 1], chans);
+			atomicMax(&P.judgeMax[c.d], __float_as_uint(worst));
+		}
+		__syncwarp();
 	}
 }
 

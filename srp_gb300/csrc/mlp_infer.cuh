@@ -70,8 +70,9 @@ __device__ __forceinline__ void mlpSlice16(const float (*in)[9], const uint32_t*
 			mma16816(acc[nt], a0, a1, a2, a3, row[(16 * j + 2 * t) >> 1], row[(16 * j + 8 + 2 * t) >> 1]);
 		}
 	}
-	/* layers 2 and 3: K = 64, N = 64, A fragments from the previous accumulators */
-#pragma unroll
+	/* layers 2 and 3: K = 64, N = 64, A fragments from the previous accumulators
+	 * (one copy of the code for both layers) */
+#pragma unroll 1
 	for (int layer = 0; layer < 2; ++layer) {
 		uint32_t a[4][4];
 #pragma unroll

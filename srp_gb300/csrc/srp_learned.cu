@@ -187,6 +187,8 @@ uint32_t learnedJudge(uint32_t nDraws, uint8_t* redo, const uint8_t** redoDev, c
 			st.lastPsnrDb = psnr;
 			if (st.judgedDraws == 0 || psnr < st.minPsnrDb) st.minPsnrDb = psnr;
 			++st.judgedDraws;
+			const int bin = psnr < 20 ? 0 : psnr < 25 ? 1 : psnr < 30 ? 2 : psnr < 35 ? 3 : psnr < 40 ? 4 : 5;
+			++st.psnrHistogram[bin];
 		}
 		if (worst > st.maxChannelError) st.maxChannelError = worst;
 		++st.draws;

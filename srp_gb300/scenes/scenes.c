@@ -1296,6 +1296,28 @@ static void buildBScene(Scene* s, Rng* rng)
 	s->draws = 1;
 }
 
+/* The batched learned-shading workload: a batched-workload scene shaded by
+ * the expensive marble shader with 16 point lights. The lights belong to the
+ * material, which every seed shares. */
+static void buildBMScene(Scene* s, Rng* rng)
+{
+	buildBScene(s, rng);
+	SRPStdUniform* u = &s->uni[0];
+	u->texture = NULL;
+	u->nLights = 16;
+	Rng mat = { 0xB1A5ED0F1A7E51A1ull };
+	for (int l = 0; l < 16; ++l) {
+		u->lightPos[l][0] = (float) rngRange(&mat, -4, 4);
+		u->lightPos[l][1] = (float) rngRange(&mat, -4, 4);
+		u->lightPos[l][2] = (float) rngRange(&mat, -6, 1);
+		for (int k = 0; k < 3; ++k) u->lightColor[l][k] = (float) rngRange(&mat, 0.1, 0.5);
+	}
+	SRPVaryingInfo v0[3] = { vi(3, SRP_FLOAT, SRP_INTERPOLATION_MODE_PERSPECTIVE),
+	                         vi(3, SRP_FLOAT, SRP_INTERPOLATION_MODE_PERSPECTIVE),
+	                         vi(2, SRP_FLOAT, SRP_INTERPOLATION_MODE_PERSPECTIVE) };
+	program(s, 0, srpVsWorld, srpFsMarble, 0, 3, v0);
+}
+
 /* ------------------------------------------------------------- registry */
 
 typedef struct SceneDef { const char* name; void (*build)(Scene*, Rng*); } SceneDef;
@@ -1317,6 +1339,7 @@ static const SceneDef DEFS[] = {
 	{ "lit", buildLit },
 	{ "bscene", buildBScene },
 	{ "msoup", buildMSoup },
+	{ "bmscene", buildBMScene },
 };
 
 const char* const* sceneNames(void)

@@ -165,7 +165,8 @@ def test_gpu_training_reduces_error(net):
 class LearnedStats(ctypes.Structure):
     _fields_ = [("draws", ctypes.c_uint64), ("fallbacks", ctypes.c_uint64), ("judgedDraws", ctypes.c_uint64),
                 ("judgedChannels", ctypes.c_uint64), ("squaredError", ctypes.c_double),
-                ("lastPsnrDb", ctypes.c_double), ("minPsnrDb", ctypes.c_double), ("maxChannelError", ctypes.c_float)]
+                ("lastPsnrDb", ctypes.c_double), ("minPsnrDb", ctypes.c_double), ("maxChannelError", ctypes.c_float),
+                ("psnrHistogram", ctypes.c_uint64 * 6)]
 
 
 def sync_planes(S, fb):
@@ -234,5 +235,63 @@ def test_learned_shading_in_a_draw(built_library):
             L.srpGpuSetLearnedShading(None, None, 0.0, 0)
             sc.close()
     finally:
+        net.close()
+    assert L.srpGpuSynchronize() == 0
+
+
+@pytest.mark.gpu
+def test_learned_shading_in_a_batch(built_library):
+    """Learned shading in multi-draw passes: per-draw judging, and per-draw
+    fallback that restores exactly the plain batch's images."""
+    import srp_gb300
+    L, S = srp_gb300.lib(), srp_gb300.scenes()
+    L.srpGpuSetFramebufferMode(1)
+    vp = ctypes.c_void_p
+    L.srpGpuMlpCapture.argtypes = [vp, vp, ctypes.c_uint32]
+    L.srpGpuSetLearnedShading.argtypes = [vp, vp, ctypes.c_float, ctypes.c_uint32]
+    L.srpGpuGetLearnedStats.argtypes = [ctypes.POINTER(LearnedStats)]
+    marble = ctypes.cast(L.srpFsMarble, vp)
+    net = Net(capacity=1 << 20)
+    train = [srp_gb300.Scene("bmscene", srp_gb300.batch_seed(31, i), 0.25) for i in range(24)]
+    evalb = [srp_gb300.Scene("bmscene", srp_gb300.batch_seed(41, i), 0.25) for i in range(16)]
+    try:
+        L.srpGpuMlpCapture(net.m, marble, 1)
+        for sc in train:
+            sc.prepare()
+        srp_gb300.render_batch(train, [sc.fb for sc in train])
+        L.srpGpuMlpCapture(None, None, 0)
+        assert net.L.srpGpuMlpSampleCount(net.m) > 1000
+        assert net.L.srpGpuMlpTrain(net.m, 200, 4096, 3e-3) >= 0
+
+        def run():
+            for sc in evalb:
+                sc.prepare()
+            srp_gb300.render_batch(evalb, [sc.fb for sc in evalb])
+            return [sync_planes(S, sc.fb) for sc in evalb]
+
+        plain = run()
+        st = LearnedStats()
+        try:
+            L.srpGpuResetLearnedStats()
+            L.srpGpuSetLearnedShading(marble, net.m, 0.0, 1)
+            learned = run()
+            L.srpGpuGetLearnedStats(ctypes.byref(st))
+            assert st.draws == len(evalb) and st.fallbacks == 0
+            assert sum(st.psnrHistogram) == st.judgedDraws > 0
+            for a, b in zip(learned, plain):
+                assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+            L.srpGpuResetLearnedStats()
+            L.srpGpuSetLearnedShading(marble, net.m, 1000.0, 1)
+            back = run()
+            L.srpGpuGetLearnedStats(ctypes.byref(st))
+            assert st.fallbacks == st.judgedDraws > 0
+            for a, b in zip(back, plain):
+                for x, y in zip(a, b):
+                    assert np.array_equal(x, y)
+        finally:
+            L.srpGpuSetLearnedShading(None, None, 0.0, 0)
+    finally:
+        for sc in train + evalb:
+            sc.close()
         net.close()
     assert L.srpGpuSynchronize() == 0
