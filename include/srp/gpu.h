@@ -131,6 +131,8 @@ typedef struct SRPGpuLearnedStats
 	double squaredError;         /* summed over the judged channels (range [0, 1]) */
 	double lastPsnrDb, minPsnrDb;
 	float maxChannelError;
+	/* judged draws by PSNR: < 20, 20-25, 25-30, 30-35, 35-40, >= 40 dB */
+	uint64_t psnrHistogram[6];
 } SRPGpuLearnedStats;
 
 /** Statistics since the last reset (reading them does not wait for the GPU:
@@ -143,8 +145,9 @@ void srpGpuResetLearnedStats(void);
 size_t srpGpuMlpParamCount(void);
 void srpGpuMlpGetParams(const SRPGpuMlp* mlp, float* params);
 void srpGpuMlpSetParams(SRPGpuMlp* mlp, const float* params);
-/** RGB (unclamped) of n samples: fp32 on CUDA cores (tensorCores 0) or the
- *  shading path's bf16 tensor-core evaluation (1). Returns 0 on success. */
+/** RGB (unclamped) of n samples: fp32 on CUDA cores (tensorCores 0) or, as
+ *  in the shading path, bf16 tcgen05 MMA with the accumulators in tensor
+ *  memory (1). Returns 0 on success. */
 int srpGpuMlpEvaluate(SRPGpuMlp* mlp, const float* samples, size_t n, float* rgb, int tensorCores);
 /** Gradient of the mean squared error over n samples (in order) with
  *  respect to the parameters, and the summed squared error. */

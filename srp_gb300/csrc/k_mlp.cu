@@ -18,7 +18,7 @@
 #include <stdint.h>
 
 #include "mlp.h"
-#include "mlp_infer.cuh"
+#include "tc5.cuh"
 
 namespace srpg {
 
@@ -168,26 +168,9 @@ __global__ void k_mlp_step_advance(int* step)
 	if (threadIdx.x == 0 && blockIdx.x == 0) *step += 1;
 }
 
-/* fp32 parameters -> transposed, padded bf16 weights and fp32 biases. */
-__global__ void k_mlp_pack(const float* p, __nv_bfloat16* w, float* bias)
+/* fp32 biases of the four layers, in one array [64 + 64 + 64 + 3]. */
+__global__ void k_mlp_pack_bias(const float* p, float* bias)
 {
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kMlpBf16; i += gridDim.x * blockDim.x) {
-		float v = 0.0f;
-		if (i < kOffT2) {
-			const int n = i / kLd1, k = i % kLd1;
-			if (k < kMlpIn) v = p[kOffW1 + k * kMlpHid + n];
-		} else if (i < kOffT4) {
-			const int l = i < kOffT3 ? 0 : 1;
-			const int j = i - (l ? kOffT3 : kOffT2);
-			const int n = j / kLdH, k = j % kLdH;
-			if (k < kMlpHid) v = p[(l ? kOffW3 : kOffW2) + k * kMlpHid + n];
-		} else {
-			const int j = i - kOffT4;
-			const int n = j / kLdH, k = j % kLdH;
-			if (n < kMlpOut && k < kMlpHid) v = p[kOffW4 + k * kMlpOut + n];
-		}
-		w[i] = __float2bfloat16_rn(v);
-	}
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * kMlpHid + kMlpOut; i += gridDim.x * blockDim.x) {
 		const int src = i < kMlpHid ? kOffB1 + i
 		              : i < 2 * kMlpHid ? kOffB2 + (i - kMlpHid)
@@ -196,30 +179,120 @@ __global__ void k_mlp_pack(const float* p, __nv_bfloat16* w, float* bias)
 	}
 }
 
-/* Tensor-core evaluation of n samples (tests compare it with the fp32 path):
- * one warp per 16 samples, weights staged in shared memory. */
-__global__ void __launch_bounds__(128) k_mlp_eval_tc(const float* samples, int n, const __nv_bfloat16* w,
-                                                     const float* bias, float* out)
+/* ------------------------------------------------- tcgen05 evaluation */
+
+
+__global__ void k_mlp_pack5(const float* p, uint8_t* out)
 {
-	__shared__ uint32_t sw[kMlpBf16 / 2];
-	__shared__ float sb[3 * kMlpHid + kMlpOut + 1];
-	__shared__ float sin_[4][16][9];
-	__shared__ float sout[4][16][4];
-	for (int i = threadIdx.x; i < kMlpBf16 / 2; i += blockDim.x) sw[i] = ((const uint32_t*) w)[i];
-	for (int i = threadIdx.x; i < 3 * kMlpHid + kMlpOut; i += blockDim.x) sb[i] = bias[i];
-	__syncthreads();
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	const int base = (blockIdx.x * 4 + warp) * 16;
-	if (base >= n) return;
-	if (lane < 16) {
-		const int r = min(base + lane, n - 1);
-		for (int c = 0; c < 9; ++c) sin_[warp][lane][c] = samples[(size_t) r * kSampleFloats + c];
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (int) (kTcWBytes / 2); i += gridDim.x * blockDim.x) {
+		/* which layer, and (n, k) inside it, for bf16 slot i */
+		const uint32_t byte = 2u * (uint32_t) i;
+		uint32_t base, K;
+		int layer;
+		if (byte < kTcW2) { base = kTcW1; K = kMlpInPad; layer = 0; }
+		else if (byte < kTcW3) { base = kTcW2; K = 64; layer = 1; }
+		else if (byte < kTcW4) { base = kTcW3; K = 64; layer = 2; }
+		else { base = kTcW4; K = 64; layer = 3; }
+		const uint32_t off = byte - base;
+		const uint32_t sbo = K / 8 * 128;
+		const int rg = (int) (off / sbo), rem = (int) (off % sbo);
+		const int kc = rem / 128, rr = (rem % 128) / 16, kk = (rem % 16) / 2;
+		const int n = rg * 8 + rr, k = kc * 8 + kk;
+		float v = 0.0f;
+		if (layer == 0) { if (k < kMlpIn) v = p[kOffW1 + k * kMlpHid + n]; }
+		else if (layer == 1) v = p[kOffW2 + k * kMlpHid + n];
+		else if (layer == 2) v = p[kOffW3 + k * kMlpHid + n];
+		else if (n < kMlpOut) v = p[kOffW4 + k * kMlpOut + n];
+		((__nv_bfloat16*) out)[i] = __float2bfloat16_rn(v);
 	}
-	__syncwarp();
-	mlpSlice16(sin_[warp], sw, sb, sout[warp]);
-	__syncwarp();
-	if (lane < 16 && base + lane < n)
-		for (int c = 0; c < kMlpOut; ++c) out[(size_t) (base + lane) * kMlpOut + c] = sout[warp][lane][c];
+}
+
+/* Evaluation of n samples, 128 per step, on tcgen05: the encoded inputs of a
+ * step form one 128-row A tile, every layer is one chain of K/16 MMAs into a
+ * 128 x 64 fp32 accumulator in tensor memory, and each warp moves its 32
+ * rows back through registers (bias, ReLU, bf16) into the next A tile. */
+__global__ void __launch_bounds__(128) k_mlp_eval_tc5(const float* samples, int n, const uint8_t* w5, const float* bias,
+                                                      float* out, unsigned* err)
+{
+	extern __shared__ __align__(1024) uint8_t tsm[];
+	uint8_t* sW = tsm;
+	uint8_t* sA = tsm + kTcWBytes;
+	float* sB = (float*) (sA + kTcABytes);
+	uint64_t* mbar = (uint64_t*) (sB + 208);
+	uint32_t* tslot = (uint32_t*) (mbar + 1);
+	const int tid = threadIdx.x, warp = tid >> 5;
+	for (int i = tid; i < (int) (kTcWBytes / 16); i += 128) ((uint4*) sW)[i] = ((const uint4*) w5)[i];
+	for (int i = tid; i < 3 * kMlpHid + kMlpOut; i += 128) sB[i] = bias[i];
+	const uint32_t mb = smemAddr(mbar);
+	if (tid == 0) mbarInit(mb, 1);
+	if (warp == 0) tcAlloc(smemAddr(tslot), kTcCols);
+	fenceProxyAsync();
+	tcFenceBefore();
+	__syncthreads();
+	tcFenceAfter();
+	const uint32_t tmem = *tslot;
+	const uint32_t laneBase = tmem + ((uint32_t) (warp * 32) << 16);
+	const uint32_t aAddr = smemAddr(sA), wAddr = smemAddr(sW);
+	uint32_t phase = 0;
+	bool ok = true;
+	for (int tile = blockIdx.x; tile * 128 < n; tile += gridDim.x) {
+		const int r = tid, s = tile * 128 + r;
+		const float* x9 = samples + (size_t) min(s, n - 1) * kSampleFloats;
+		for (int f = 0; f < kMlpInPad; f += 2) {
+			uint32_t v = 0;
+			if (f < kMlpIn) {
+				float sn, cs;
+				__sincosf(mlpBandScale((f % 12) / 2) * x9[f / 12], &sn, &cs);
+				v = packBf16(sn, cs);
+			}
+			*(uint32_t*) (sA + tcOffset(r, f, kMlpInPad)) = v;
+		}
+		fenceProxyAsync();
+		tcFenceBefore();
+		__syncthreads();
+		for (int layer = 0; layer < 4; ++layer) {
+			if (tid == 0) {
+				tcFenceAfter();
+				const int K = layer == 0 ? kMlpInPad : 64;
+				const uint32_t w = wAddr + (layer == 0 ? kTcW1 : layer == 1 ? kTcW2 : layer == 2 ? kTcW3 : kTcW4);
+				tcLayer(tmem, aAddr, w, K, layer < 3 ? 64 : 16);
+				tcCommit(mb);
+			}
+			const bool got = mbarWait(mb, phase);
+			phase ^= 1u;
+			if (!__syncthreads_and(got)) { ok = false; break; }
+			tcFenceAfter();
+			if (layer < 3) {
+				/* this thread's row: bias, ReLU, bf16 into the next A tile */
+				const float* b = sB + 64 * layer;
+				for (int c = 0; c < 64; c += 16) {
+					float v[16];
+					tcLoad16(laneBase + (uint32_t) c, v);
+#pragma unroll
+					for (int i = 0; i < 16; i += 2) {
+						const float x0 = fmaxf(v[i] + b[c + i], 0.0f), x1 = fmaxf(v[i + 1] + b[c + i + 1], 0.0f);
+						*(uint32_t*) (sA + tcOffset(r, c + i, 64)) = packBf16(x0, x1);
+					}
+				}
+				fenceProxyAsync();
+				tcFenceBefore();
+				__syncthreads();
+			} else {
+				float v[16];
+				tcLoad16(laneBase, v);
+				if (s < n)
+					for (int k = 0; k < kMlpOut; ++k) out[(size_t) s * kMlpOut + k] = v[k] + sB[3 * kMlpHid + k];
+				tcFenceBefore();
+				__syncthreads();
+			}
+		}
+		if (!ok) break;
+	}
+	if (!ok && tid == 0) atomicOr(err, 1u);
+	tcFenceBefore();
+	__syncthreads();
+	tcFenceAfter();
+	if (warp == 0) tcDealloc(tmem, kTcCols);
 }
 
 }  // namespace srpg
@@ -299,15 +372,20 @@ void mlpAdam(float* p, const float* grad, float* m, float* v, int* step, int tot
 	k_mlp_step_advance<<<1, 32, 0, s>>>(step);
 }
 
-void mlpPack(const float* p, void* w, float* bias, cudaStream_t s)
+void mlpPack5(const float* params, void* w5, float* bias, cudaStream_t s)
 {
-	k_mlp_pack<<<64, 256, 0, s>>>(p, (__nv_bfloat16*) w, bias);
+	k_mlp_pack5<<<64, 256, 0, s>>>(params, (uint8_t*) w5);
+	k_mlp_pack_bias<<<1, 256, 0, s>>>(params, bias);
 }
 
-void mlpEvalTensorCores(const float* samples, int n, const void* w, const float* bias, float* out, cudaStream_t s)
+void mlpEvalTcgen05(const float* samples, int n, const void* w5, const float* bias, float* out, unsigned* err,
+                    cudaStream_t s)
 {
 	if (n <= 0) return;
-	k_mlp_eval_tc<<<(n + 63) / 64, 128, 0, s>>>(samples, n, (const __nv_bfloat16*) w, bias, out);
+	cudaFuncSetAttribute(k_mlp_eval_tc5, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) kTcSmem);
+	const int tiles = (n + 127) / 128;
+	k_mlp_eval_tc5<<<tiles < 152 * 3 ? tiles : 152 * 3, 128, kTcSmem, s>>>(samples, n, (const uint8_t*) w5, bias, out,
+	                                                                        err);
 }
 
 }  // namespace srpg

@@ -22,7 +22,8 @@
 
 #include "device_common.cuh"
 #include "kernels.h"
-#include "mlp_infer.cuh"
+#include "mlp.h"
+#include "tc5.cuh"
 #include "srp/buffer.h"
 
 namespace srpg {
@@ -292,10 +293,6 @@ __device__ __forceinline__ int findOwner(const uint32_t* off, uint32_t p)
 }
 
 /* ------------------------------------------------------ learned shading */
-
-constexpr int kLearnedBias = 3 * kMlpHid + kMlpOut + 1;   /* floats, padded to 16 bytes */
-constexpr size_t kLearnedSmem = (size_t) kMlpBf16 * 2 + kLearnedBias * 4 + (size_t) kResolveWarps * 64 * 9 * 4 +
-                                (size_t) kResolveWarps * 64 * 4 * 4;
 
 __device__ __forceinline__ float clamp01f(float x) { return x < 0.0f ? 0.0f : (x > 1.0f ? 1.0f : x); }
 
@@ -688,78 +685,128 @@ __device__ __noinline__ void judgeShade(const DrawParams& P, const unsigned char
 	shadeItem<KIND, FS>(P, uniform, primBase, item, gx, gy, out);
 }
 
-/* Learned shading of the winners of a tile: their inputs go to shared
- * memory, the MLP runs on the tensor cores 16 pixels at a time
- * (mlp_infer.cuh), and 1 pixel in judgeEvery is also shaded by the plain
- * shader (FS) so that the host can judge the draw's error. */
+/* Learned shading on tcgen05: a CTA shades a pair of tiles (128 pixels, one
+ * per thread) as one 128-row MMA tile. Each thread builds its pixel's
+ * encoded inputs as row `tid` of the A tile; one thread issues each layer's
+ * MMAs into a 128 x 64 fp32 accumulator in tensor memory; each warp reads its
+ * 32 lanes (rows) back, adds the bias, applies ReLU and writes the next A
+ * tile, and finally its pixels' colours. 1 pixel in judgeEvery is also
+ * shaded by the plain shader (FS) and its error accumulated per draw for the
+ * host's judge. Every wait is bounded; on a timeout the kernel records
+ * kErrSpin, releases its tensor memory and returns. */
 template <int KIND, int FS, bool MULTI>
-__global__ void __launch_bounds__(kResolveWarps * 32) k_shade_learned(const __grid_constant__ DrawParams P,
-                                                                     uint32_t numTiles)
+__global__ void __launch_bounds__(128) k_shade_learned5(const __grid_constant__ DrawParams P, uint32_t numTiles)
 {
-	extern __shared__ uint32_t lsm[];
-	uint32_t* sw = lsm;
-	float* sb = (float*) (lsm + kMlpBf16 / 2);
-	float (*sx)[64][9] = (float (*)[64][9]) (sb + kLearnedBias);
-	float (*so)[64][4] = (float (*)[64][4]) (sx + kResolveWarps);
-	for (int i = threadIdx.x; i < kMlpBf16 / 2; i += blockDim.x) sw[i] = ((const uint32_t*) P.mlpW)[i];
-	for (int i = threadIdx.x; i < 3 * kMlpHid + kMlpOut; i += blockDim.x) sb[i] = P.mlpB[i];
+	extern __shared__ __align__(1024) uint8_t tsm[];
+	uint8_t* sW = tsm;
+	uint8_t* sA = tsm + kTcWBytes;
+	float* sB = (float*) (sA + kTcABytes);
+	uint64_t* mbar = (uint64_t*) (sB + 208);
+	uint32_t* tslot = (uint32_t*) (mbar + 1);
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	for (int i = tid; i < (int) (kTcWBytes / 16); i += 128) ((uint4*) sW)[i] = ((const uint4*) P.mlpW5)[i];
+	for (int i = tid; i < 3 * kMlpHid + kMlpOut; i += 128) sB[i] = P.mlpB[i];
+	const uint32_t mb = smemAddr(mbar);
+	if (tid == 0) mbarInit(mb, 1);
+	if (warp == 0) tcAlloc(smemAddr(tslot), kTcCols);
+	fenceProxyAsync();
+	tcFenceBefore();
 	__syncthreads();
-	if (P.ctr->abort) return;
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	/* one tile per warp (the loop only runs again for grids smaller than the tiles) */
-	for (uint32_t tile = blockIdx.x * kResolveWarps + warp; tile < numTiles; tile += gridDim.x * kResolveWarps) {
-		if (P.tileStart[tile] >= P.tileEnd[tile]) continue;
-		const TileCtx c = tileCtx<MULTI>(P, tile);
-		int32_t win[2];
-		int gx[2], gy[2];
-		size_t idx[2];
-#pragma unroll
-		for (int p = 0; p < 2; ++p) {
-			const int q = lane + 32 * p;
-			gx[p] = c.x0 + (q & 7);
-			gy[p] = c.y0 + (q >> 3);
-			const bool valid = gx[p] < c.W && gy[p] < c.H;
-			idx[p] = valid ? (size_t) gy[p] * c.W + gx[p] : 0;
-			win[p] = valid ? c.winner[idx[p]] : -1;
-			float* x9 = sx[warp][q];
-			if (win[p] >= 0) {
+	tcFenceAfter();
+	const uint32_t tmem = *tslot;
+	const uint32_t laneBase = tmem + ((uint32_t) (warp * 32) << 16);
+	const uint32_t aAddr = smemAddr(sA), wAddr = smemAddr(sW);
+	const int half = tid >> 6, q = tid & 63;
+	uint32_t phase = 0;
+	bool ok = P.ctr->abort == 0;
+	const uint32_t pairs = (numTiles + 1) / 2;
+	for (uint32_t pr = blockIdx.x; ok && pr < pairs; pr += gridDim.x) {
+		const uint32_t tile = 2 * pr + (uint32_t) half;
+		const bool have = tile < numTiles && P.tileStart[tile] < P.tileEnd[tile];
+		TileCtx c = {};
+		int gx = 0, gy = 0;
+		size_t idx = 0;
+		int32_t win = -1;
+		float x9[9] = { 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f };
+		if (have) {
+			c = tileCtx<MULTI>(P, tile);
+			gx = c.x0 + (q & 7);
+			gy = c.y0 + (q >> 3);
+			if (gx < c.W && gy < c.H) {
+				idx = (size_t) gy * c.W + gx;
+				win = c.winner[idx];
+			}
+			if (win >= 0) {
 				uint32_t words[kMaxVaryingWords];
 				SRPFragmentShaderIn in;
-				fragmentIn<KIND>(P, c.uniform, c.primBase, (uint32_t) win[p], gx[p], gy[p], in, words);
+				fragmentIn<KIND>(P, c.uniform, c.primBase, (uint32_t) win, gx, gy, in, words);
 				learnedInputs(c.uniform, words, x9);
-			} else {
-#pragma unroll
-				for (int k = 0; k < 9; ++k) x9[k] = 0.0f;
 			}
 		}
-		__syncwarp();
-		const unsigned b0 = __ballot_sync(0xFFFFFFFFu, win[0] >= 0), b1 = __ballot_sync(0xFFFFFFFFu, win[1] >= 0);
-		const unsigned sliceBits[4] = { b0 & 0xFFFFu, b0 >> 16, b1 & 0xFFFFu, b1 >> 16 };
-		/* one copy of the network's code: the instruction cache holds it */
-#pragma unroll 1
-		for (int sl = 0; sl < 4; ++sl)
-			if (sliceBits[sl]) mlpSlice16(sx[warp] + 16 * sl, sw, sb, so[warp] + 16 * sl);
-		__syncwarp();
+		if (!__syncthreads_or(win >= 0)) continue;
+		for (int f = 0; f < kMlpInPad; f += 2) {
+			uint32_t v = 0;
+			if (f < kMlpIn) {
+				float sn, cs;
+				__sincosf(mlpBandScale((f % 12) / 2) * x9[f / 12], &sn, &cs);
+				v = packBf16(sn, cs);
+			}
+			*(uint32_t*) (sA + tcOffset(tid, f, kMlpInPad)) = v;
+		}
+		fenceProxyAsync();
+		tcFenceBefore();
+		__syncthreads();
+		float rgb[3] = { 0.f, 0.f, 0.f };
+		for (int layer = 0; layer < 4; ++layer) {
+			if (tid == 0) {
+				tcFenceAfter();
+				const int K = layer == 0 ? kMlpInPad : 64;
+				const uint32_t w = wAddr + (layer == 0 ? kTcW1 : layer == 1 ? kTcW2 : layer == 2 ? kTcW3 : kTcW4);
+				tcLayer(tmem, aAddr, w, K, layer < 3 ? 64 : 16);
+				tcCommit(mb);
+			}
+			const bool got = mbarWait(mb, phase);
+			phase ^= 1u;
+			if (!__syncthreads_and(got)) { ok = false; break; }
+			tcFenceAfter();
+			if (layer < 3) {
+				const float* b = sB + 64 * layer;
+				for (int col = 0; col < 64; col += 16) {
+					float v[16];
+					tcLoad16(laneBase + (uint32_t) col, v);
+#pragma unroll
+					for (int i = 0; i < 16; i += 2) {
+						const float x0 = fmaxf(v[i] + b[col + i], 0.0f), x1 = fmaxf(v[i + 1] + b[col + i + 1], 0.0f);
+						*(uint32_t*) (sA + tcOffset(tid, col + i, 64)) = packBf16(x0, x1);
+					}
+				}
+				fenceProxyAsync();
+			} else {
+				float v[16];
+				tcLoad16(laneBase, v);
+				for (int k = 0; k < 3; ++k) rgb[k] = clamp01f(v[k] + sB[3 * kMlpHid + k]);
+			}
+			tcFenceBefore();
+			__syncthreads();
+		}
+		if (!ok) break;
 		double err = 0.0, chans = 0.0;
 		float worst = 0.0f;
-#pragma unroll
-		for (int p = 0; p < 2; ++p) {
-			if (win[p] < 0) continue;
-			const int q = lane + 32 * p;
-			float col[4] = { clamp01f(so[warp][q][0]), clamp01f(so[warp][q][1]), clamp01f(so[warp][q][2]), 1.0f };
-			c.color[idx[p]] = packColor(col);
-			if (pixelSampled(gx[p], gy[p], P.sampleSeed + c.d, P.judgeEvery)) {
+		if (win >= 0) {
+			float col[4] = { rgb[0], rgb[1], rgb[2], 1.0f };
+			c.color[idx] = packColor(col);
+			if (pixelSampled(gx, gy, P.sampleSeed + c.d, P.judgeEvery)) {
 				SRPFragmentShaderOut ref;
-				judgeShade<KIND, FS>(P, c.uniform, c.primBase, (uint32_t) win[p], gx[p], gy[p], ref);
-#pragma unroll
+				judgeShade<KIND, FS>(P, c.uniform, c.primBase, (uint32_t) win, gx, gy, ref);
 				for (int k = 0; k < 3; ++k) {
 					const float dlt = col[k] - ref.color[k];
 					err += (double) dlt * dlt;
 					worst = fmaxf(worst, fabsf(dlt));
 				}
-				chans += 3.0;
+				chans = 3.0;
 			}
 		}
+		/* a warp's 32 pixels lie in one tile, so in one draw */
 		for (int o = 16; o; o >>= 1) {
 			err += __shfl_xor_sync(0xFFFFFFFFu, err, o);
 			chans += __shfl_xor_sync(0xFFFFFFFFu, chans, o);
@@ -770,8 +817,12 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_shade_learned(const __gr
 			atomicAdd(&P.judge[2 * c.d + 1], chans);
 			atomicMax(&P.judgeMax[c.d], __float_as_uint(worst));
 		}
-		__syncwarp();
 	}
+	if (!ok && P.ctr->abort == 0 && tid == 0) atomicOr(&P.ctr->errors, kErrSpin);
+	tcFenceBefore();
+	__syncthreads();
+	tcFenceAfter();
+	if (warp == 0) tcDealloc(tmem, kTcCols);
 }
 
 /* ------------------------------------------------------------ launchers */
@@ -842,9 +893,12 @@ static void shadeKind(const DrawParams& P, uint32_t numTiles, cudaStream_t s)
 	case SRP_GPU_FS_FLAT_INT: k_shade<KIND, SRP_GPU_FS_FLAT_INT, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
 	case kFsLearned:
 		if constexpr (KIND == kKindTri) {
-			cudaFuncSetAttribute(k_shade_learned<KIND, SRP_GPU_FS_MARBLE, MULTI>,
-			                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int) kLearnedSmem);
-			k_shade_learned<KIND, SRP_GPU_FS_MARBLE, MULTI><<<b, t, kLearnedSmem, s>>>(P, numTiles);
+			/* a CTA per pair of tiles, a few CTAs per SM looping over the pairs */
+			const unsigned pairs = (numTiles + 1) / 2;
+			const unsigned blocks = pairs < 152u * 3u ? (pairs ? pairs : 1u) : 152u * 3u;
+			cudaFuncSetAttribute(k_shade_learned5<KIND, SRP_GPU_FS_MARBLE, MULTI>,
+			                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int) kTcSmem);
+			k_shade_learned5<KIND, SRP_GPU_FS_MARBLE, MULTI><<<blocks, 128, kTcSmem, s>>>(P, numTiles);
 		}
 		break;
 	default: break;

@@ -78,7 +78,7 @@ struct DrawParams {
 	 * sum and channel count (judge[2d], judge[2d + 1]) and largest channel
 	 * error (judgeMax[d], float bits). redo: a multi-draw shade pass that
 	 * shades only the draws flagged there (fallback to the plain shader). */
-	const void* mlpW;
+	const void* mlpW5;            /* bf16 weights in the tcgen05 operand layout */
 	const float* mlpB;
 	int judgeFs;
 	uint32_t judgeEvery, sampleSeed;

@@ -9,12 +9,11 @@
  * Parameters are kept in fp32 (training, Adam) as one flat vector:
  *   W1 [108][64], b1 [64], W2 [64][64], b2 [64], W3 [64][64], b3 [64],
  *   W4 [64][3], b4 [3]           (W[k][n]: input k, output n)
- * Inference uses a bf16 copy with each weight matrix transposed to [n][k]
- * and k padded (to 120 for the first layer, 72 for the others, 8 outputs
- * for the last) so that tensor-core B fragments load from shared memory
- * without bank conflicts. */
+ * Inference uses a bf16 copy of the weights in the operand layout of the
+ * tcgen05 tensor cores (below) and the fp32 biases. */
 #pragma once
 
+#include <stddef.h>
 #include <stdint.h>
 
 namespace srpg {
@@ -36,14 +35,17 @@ constexpr int kOffW4 = kOffB3 + kMlpHid;
 constexpr int kOffB4 = kOffW4 + kMlpHid * kMlpOut;
 constexpr int kMlpParams = kOffB4 + kMlpOut;  /* 15491 */
 
-/* bf16 inference copy: transposed, padded rows */
-constexpr int kLd1 = 120;                     /* row pitch of W1t (k = 0..111 used, 108..111 zero) */
-constexpr int kLdH = 72;                      /* row pitch of W2t, W3t, W4t */
-constexpr int kOffT1 = 0;                     /* W1t [64][kLd1] */
-constexpr int kOffT2 = kOffT1 + kMlpHid * kLd1;
-constexpr int kOffT3 = kOffT2 + kMlpHid * kLdH;
-constexpr int kOffT4 = kOffT3 + kMlpHid * kLdH;   /* W4t [8][kLdH], rows 3..7 zero */
-constexpr int kMlpBf16 = kOffT4 + 8 * kLdH;        /* 17472 */
+/* tcgen05 operands (the canonical K-major layout of tc5.cuh), one block per
+ * layer: W1 [64 n][112 k], W2 and W3 [64][64], W4 [16][64] (rows 3..15 zero);
+ * one 128-row A tile; one 128 x 64 fp32 accumulator in tensor memory. */
+constexpr uint32_t kTcW1 = 0;
+constexpr uint32_t kTcW2 = kTcW1 + 64 * kMlpInPad * 2;
+constexpr uint32_t kTcW3 = kTcW2 + 64 * 64 * 2;
+constexpr uint32_t kTcW4 = kTcW3 + 64 * 64 * 2;
+constexpr uint32_t kTcWBytes = kTcW4 + 16 * 64 * 2;        /* 32768 */
+constexpr uint32_t kTcABytes = 128 * kMlpInPad * 2;       /* 28672 */
+constexpr uint32_t kTcCols = 64;
+constexpr size_t kTcSmem = kTcWBytes + kTcABytes + 208 * 4 + 16;
 
 /* One captured fragment: world position, unit normal, unit view direction
  * and the shader's clamped RGB. */

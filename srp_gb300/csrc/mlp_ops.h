@@ -30,7 +30,10 @@ void mlpForward(const float* params, const MlpBatch& S, int B, cudaStream_t s);
  * is added to *sse */
 void mlpBackward(const float* params, float* grad, const MlpBatch& S, int B, double* sse, cudaStream_t s);
 void mlpAdam(float* params, const float* grad, float* m, float* v, int* step, int totalSteps, float lr, cudaStream_t s);
-void mlpPack(const float* params, void* w, float* bias, cudaStream_t s);
-void mlpEvalTensorCores(const float* samples, int n, const void* w, const float* bias, float* out, cudaStream_t s);
+/* bf16 weights in the tcgen05 operand layout of tc5.cuh (32768 bytes) and
+ * fp32 biases [64 + 64 + 64 + 3] */
+void mlpPack5(const float* params, void* w5, float* bias, cudaStream_t s);
+void mlpEvalTcgen05(const float* samples, int n, const void* w5, const float* bias, float* out, unsigned* err,
+                    cudaStream_t s);
 
 }  // namespace srpg

@@ -7,7 +7,7 @@
  *   train     Adam over random batches of the samples (k_mlp.cu); one step is
  *             captured in a CUDA graph and replayed
  *   shade     draws whose fragment shader is the target are shaded by the
- *             network on the tensor cores (k_shade_learned); 1 pixel in
+ *             network on the tcgen05 tensor cores (k_shade_learned5); 1 pixel in
  *             judgeEvery is shaded by the target as well, and a draw whose
  *             PSNR over those pixels is below the threshold is shaded again
  *             by the target alone (fallback)
@@ -35,7 +35,8 @@ struct SRPGpuMlp {
 	float* adamM = nullptr;
 	float* adamV = nullptr;
 	float* grad = nullptr;
-	void* packed = nullptr;      /* bf16 inference weights [kMlpBf16] */
+	void* packed5 = nullptr;     /* bf16 weights in the tcgen05 operand layout (32768 bytes) */
+	unsigned* tcErr = nullptr;   /* set by a tcgen05 kernel whose wait gave up */
 	float* bias = nullptr;       /* fp32 biases [3 * 64 + 3 + 1] */
 	float* samples = nullptr;    /* [capacity][kSampleFloats] */
 	unsigned long long* count = nullptr;
@@ -123,7 +124,7 @@ bool ensureJudge(uint32_t n)
 bool packIfNeeded(SRPGpuMlp* m)
 {
 	if (m->packedValid) return true;
-	mlpPack(m->params, m->packed, m->bias, m->stream);
+	mlpPack5(m->params, m->packed5, m->bias, m->stream);
 	if (!ok(cudaStreamSynchronize(m->stream), "srpGpuMlp pack")) return false;
 	m->packedValid = true;
 	return true;
@@ -138,7 +139,7 @@ namespace srpg {
 bool learnedPrepare(DrawParams& P, int kind, bool late, uint32_t nDraws, cudaStream_t s)
 {
 	P.capture = nullptr;
-	P.mlpW = nullptr;
+	P.mlpW5 = nullptr;
 	P.redo = nullptr;
 	L.seed = L.seed * 1664525u + 1013904223u;
 	P.sampleSeed = L.seed;
@@ -154,7 +155,7 @@ bool learnedPrepare(DrawParams& P, int kind, bool late, uint32_t nDraws, cudaStr
 	cudaMemsetAsync(L.judgeMax, 0, sizeof(unsigned int) * nDraws, s);
 	P.judgeFs = P.fsId;
 	P.fsId = kFsLearned;
-	P.mlpW = L.net->packed;
+	P.mlpW5 = L.net->packed5;
 	P.mlpB = L.net->bias;
 	P.judge = L.judge;
 	P.judgeMax = L.judgeMax;
@@ -213,7 +214,7 @@ SRPGpuMlp* srpGpuMlpCreate(uint64_t seed, size_t sampleCapacity)
 	bool good = ok(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking), "srpGpuMlpCreate") &&
 	            devAlloc(&m->params, kMlpParams, "srpGpuMlpCreate") && devAlloc(&m->adamM, kMlpParams, "srpGpuMlpCreate") &&
 	            devAlloc(&m->adamV, kMlpParams, "srpGpuMlpCreate") && devAlloc(&m->grad, kMlpParams, "srpGpuMlpCreate") &&
-	            ok(cudaMalloc(&m->packed, (size_t) kMlpBf16 * 2 + 16), "srpGpuMlpCreate") &&
+	            ok(cudaMalloc(&m->packed5, 32768 + 16), "srpGpuMlpCreate") && devAlloc(&m->tcErr, 1, "srpGpuMlpCreate") &&
 	            devAlloc(&m->bias, 3 * kMlpHid + kMlpOut + 1, "srpGpuMlpCreate") &&
 	            devAlloc(&m->count, 1, "srpGpuMlpCreate") && devAlloc(&m->step, 1, "srpGpuMlpCreate") &&
 	            devAlloc(&m->sse, 1, "srpGpuMlpCreate") &&
@@ -249,7 +250,8 @@ void srpGpuMlpFree(SRPGpuMlp* m)
 	if (L.net == m) L.net = nullptr;
 	if (m->stream) cudaStreamSynchronize(m->stream);
 	if (m->graph) cudaGraphExecDestroy(m->graph);
-	void* bufs[] = { m->params, m->adamM, m->adamV, m->grad, m->packed, m->bias, m->samples, m->count, m->step, m->sse,
+	void* bufs[] = { m->params, m->adamM, m->adamV, m->grad, m->packed5, m->tcErr, m->bias, m->samples,
+	                 m->count, m->step, m->sse,
 	                 m->batch.X, m->batch.T, m->batch.H1, m->batch.H2, m->batch.H3, m->batch.Y, m->batch.dY,
 	                 m->batch.dH3, m->batch.dH2, m->batch.dH1 };
 	for (void* b : bufs)
@@ -352,8 +354,15 @@ int srpGpuMlpEvaluate(SRPGpuMlp* m, const float* samples, size_t n, float* rgb, 
 	cudaMemcpyAsync(dSamples, samples, n * kSampleFloats * sizeof(float), cudaMemcpyHostToDevice, s);
 	int rc = 0;
 	if (tensorCores) {
+		unsigned err = 0;
 		if (!packIfNeeded(m)) rc = -1;
-		else mlpEvalTensorCores(dSamples, (int) n, m->packed, m->bias, dOut, s);
+		else {
+			cudaMemsetAsync(m->tcErr, 0, sizeof(unsigned), s);
+			mlpEvalTcgen05(dSamples, (int) n, m->packed5, m->bias, dOut, m->tcErr, s);
+			cudaMemcpyAsync(&err, m->tcErr, sizeof err, cudaMemcpyDeviceToHost, s);
+			if (!ok(cudaStreamSynchronize(s), "srpGpuMlpEvaluate")) rc = -1;
+			else if (err) { learnedError("srpGpuMlpEvaluate: a tensor-core wait timed out"); rc = -1; }
+		}
 	} else {
 		if (!reserveBatch(m, (int) n)) rc = -1;
 		else {
