@@ -50,6 +50,22 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def replica_throughput(local_ms, local_units, world, device):
+    """Whole-job throughput of independent replicas, one per rank: the units
+    every rank processed over the slowest rank's time. Returns (units per
+    second, that time in ms). With world > 1 it takes a process group; the
+    reduction carries only the two numbers, never frame data."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(local_ms)], dtype=torch.float64, device=device)
+        u = torch.tensor([float(local_units)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(u, op=dist.ReduceOp.SUM)
+        local_ms, local_units = float(t.item()), float(u.item())
+    return local_units / (local_ms / 1000.0), local_ms
+
+
 TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "resolve_soup_1080p.md")
 
 
@@ -650,12 +666,8 @@ def main():
     L.srpGpuSetProfiling(0)
     stage_ms = {n: prof.ms[i] / nprof for i, n in enumerate(srp_gb300.STAGES)}
     stage_launches = {n: prof.launches[i] / nprof for i, n in enumerate(srp_gb300.STAGES)}
-    total_ms = sum(times)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = frags_per_frame * args.steps * world / (total_ms / 1000.0) / 1e6
+    rate, total_ms = replica_throughput(sum(times), frags_per_frame * args.steps, world, "cuda")
+    value = rate / 1e6
     e2e_s = sum(e2e_times) / len(e2e_times)
     h2d = info.vertexBytes + info.indexBytes
     d2h = info.width * info.height * 9
