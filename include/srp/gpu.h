@@ -251,6 +251,13 @@ typedef struct SRPGpuProfile
 	uint64_t resolveItems;                 /* (tile, item) pairs it consumed */
 } SRPGpuProfile;
 
+/** Replay repeated draws from CUDA graphs (on by default). A draw's work
+ *  after its host-side preparation is captured once per distinct set of
+ *  draw parameters and launch sizes, and relaunched as two graphs when the
+ *  same draw comes again (the host reads the draw's counters between them).
+ *  Stage profiling launches directly. */
+void srpGpuSetDrawGraphs(int enable);
+
 /** Record CUDA events around every stage of every draw (off by default). */
 void srpGpuSetProfiling(int enable);
 /** Sum of the recorded stage times since the last reset (waits for the GPU). */

@@ -94,6 +94,7 @@ struct Lib {
 	cudaStream_t auxStream = nullptr;
 	cudaEvent_t forkEvent = nullptr, joinEvent = nullptr;
 	cudaEvent_t ctrEvent = nullptr;   /* recorded after a draw's counters are copied to hostCtr */
+	bool graphs = true;               /* replay repeated draws from captured CUDA graphs */
 	SRPGpuFramebufferMode fbMode = SRP_GPU_FB_COHERENT;
 	Registry reg;
 	/* scratch pools, grown on demand */
@@ -164,6 +165,88 @@ void stageEnd(int stage, int launches)
 	g.pending.push_back({ stage, { g.openEvent, e } });
 	g.profile.launches[stage] += (uint64_t) launches;
 	g.openEvent = nullptr;
+}
+
+/* Repeated draws replay CUDA graphs. A draw's work after its host-side
+ * preparation is two fixed sequences of launches: the head (reset up to the
+ * check kernel) and the tail (binning, sort, resolve, shade). Both depend
+ * only on the draw parameters and a few launch sizes, which together form
+ * the key; between the two the host copies the counters out directly. The
+ * cache keeps the most recent kGraphCache keys. */
+constexpr size_t kGraphCache = 64;
+
+struct GraphEntry {
+	std::vector<unsigned char> key;
+	cudaGraphExec_t head = nullptr, tail = nullptr;
+};
+
+std::vector<GraphEntry> graphCache;
+size_t graphNext = 0;
+
+GraphEntry* graphFind(const std::vector<unsigned char>& key)
+{
+	for (auto& e : graphCache)
+		if (e.key.size() == key.size() && memcmp(e.key.data(), key.data(), key.size()) == 0) return &e;
+	return nullptr;
+}
+
+/* Captures `enqueue` on the library's stream; null if the capture failed
+ * (the caller then launches directly). */
+template <class F> cudaGraphExec_t captureGraph(F&& enqueue)
+{
+	cudaGraph_t graph = nullptr;
+	cudaGraphExec_t exec = nullptr;
+	if (cudaStreamBeginCapture(g.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+	enqueue();
+	const cudaError_t e = cudaStreamEndCapture(g.stream, &graph);
+	if (e != cudaSuccess || !graph || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) exec = nullptr;
+	if (graph) cudaGraphDestroy(graph);
+	cudaGetLastError();
+	return exec;
+}
+
+/* Runs head and tail of a draw, from the graph cache when graphs are on and
+ * stage profiling is off (profiling records fresh events per draw). */
+template <class H, class T> void runHeadTail(const std::vector<unsigned char>& key, H&& head, T&& tail)
+{
+	if (!g.graphs || g.profiling) {
+		head();
+		cudaMemcpyAsync(g.hostCtr, g.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, g.stream);
+		cudaEventRecord(g.ctrEvent, g.stream);
+		tail();
+		return;
+	}
+	GraphEntry* e = graphFind(key);
+	if (!e) {
+		GraphEntry fresh;
+		fresh.key = key;
+		fresh.head = captureGraph(head);
+		fresh.tail = fresh.head ? captureGraph(tail) : nullptr;
+		if (graphCache.size() < kGraphCache) graphCache.push_back(std::move(fresh));
+		else {
+			GraphEntry& old = graphCache[graphNext++ % kGraphCache];
+			if (old.head) cudaGraphExecDestroy(old.head);
+			if (old.tail) cudaGraphExecDestroy(old.tail);
+			old = std::move(fresh);
+		}
+		e = graphFind(key);
+	}
+	if (e->head) cudaGraphLaunch(e->head, g.stream);
+	else head();
+	cudaMemcpyAsync(g.hostCtr, g.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, g.stream);
+	cudaEventRecord(g.ctrEvent, g.stream);
+	if (e->head && e->tail) cudaGraphLaunch(e->tail, g.stream);
+	else tail();
+}
+
+/* The key of a draw: its parameters and the host-side launch sizes. */
+std::vector<unsigned char> graphKey(const DrawParams& P, std::initializer_list<unsigned long long> sizes)
+{
+	std::vector<unsigned char> k(sizeof(DrawParams) + sizes.size() * 8);
+	memcpy(k.data(), &P, sizeof(DrawParams));
+	size_t o = sizeof(DrawParams);
+	for (unsigned long long v : sizes) { memcpy(k.data() + o, &v, 8); o += 8; }
+	return k;
 }
 
 }  // namespace
@@ -911,48 +994,50 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		P.winner = g.winner.as<int32_t>();
 
 		/* the whole draw is enqueued before the host looks at any count */
-		stageBegin();
-		launchReset(P, g.stream);
-		if (ib) launchIndexRange(P, g.stream);
-		if (ib) launchVertex(P, 0, vb->nVertices, g.stream);
-		else launchVertex(P, start, count, g.stream);
-		stageEnd(SRP_GPU_STAGE_VERTEX, ib ? 3 : 2);
-		stageBegin();
-		cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, g.stream);
-		if (isTri(prim)) launchClipPrepass(P, g.stream);
-		launchSetup(P, g.stream);
-		launchCheck(P, g.stream);
-		stageEnd(SRP_GPU_STAGE_SETUP, isTri(prim) ? 3 : 2);
-		cudaMemcpyAsync(g.hostCtr, g.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, g.stream);
-		cudaEventRecord(g.ctrEvent, g.stream);
-		g.launches += 4 + (ib ? 1 : 0) + (isTri(prim) ? 1 : 0);
-		stageBegin();
-		int binLaunches = 0;
-		if (kind == kKindLineFrag) { launchLineFrags(P, g.stream); binLaunches += 2; }
-		else { launchBigEntries(P, g.bigJobsSeen[kind], g.stream); binLaunches += 2; }
-		uint32_t* sk;
-		uint32_t* sv;
-		sortEntries(P, keyBits, g.keys2.as<uint32_t>(), g.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
-		            g.partials.as<uint32_t>(), &sk, &sv, g.stream);
-		cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, g.stream);
-		cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, g.stream);
-		launchTileRanges(P, sk, numTiles, g.stream);
-		binLaunches += 1 + (int) (keyBits / 8) + 1;
-		stageEnd(SRP_GPU_STAGE_BIN, binLaunches);
-		if (late) {
+		uint32_t* sk = nullptr;
+		uint32_t* sv = nullptr;
+		auto head = [&]() {
 			stageBegin();
-			launchResolveLate(P, kind, sv, numTiles, g.stream);
-			stageEnd(SRP_GPU_STAGE_RESOLVE, 1);
-		} else {
+			launchReset(P, g.stream);
+			if (ib) launchIndexRange(P, g.stream);
+			if (ib) launchVertex(P, 0, vb->nVertices, g.stream);
+			else launchVertex(P, start, count, g.stream);
+			stageEnd(SRP_GPU_STAGE_VERTEX, ib ? 3 : 2);
 			stageBegin();
-			launchResolve(P, kind, sv, numTiles, g.heavy.as<uint32_t>(), g.stream, g.auxStream, g.forkEvent,
-			              g.joinEvent);
-			stageEnd(SRP_GPU_STAGE_RESOLVE, 3);
+			cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, g.stream);
+			if (isTri(prim)) launchClipPrepass(P, g.stream);
+			launchSetup(P, g.stream);
+			launchCheck(P, g.stream);
+			stageEnd(SRP_GPU_STAGE_SETUP, isTri(prim) ? 3 : 2);
+		};
+		auto tail = [&]() {
 			stageBegin();
-			launchShade(P, kind, numTiles, g.stream);
-			stageEnd(SRP_GPU_STAGE_SHADE, 1);
-		}
-		g.launches += binLaunches + (late ? 1 : 4);
+			if (kind == kKindLineFrag) launchLineFrags(P, g.stream);
+			else launchBigEntries(P, g.bigJobsSeen[kind], g.stream);
+			sortEntries(P, keyBits, g.keys2.as<uint32_t>(), g.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
+			            g.partials.as<uint32_t>(), &sk, &sv, g.stream);
+			cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, g.stream);
+			cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, g.stream);
+			launchTileRanges(P, sk, numTiles, g.stream);
+			stageEnd(SRP_GPU_STAGE_BIN, 2 + 1 + (int) (keyBits / 8) + 1);
+			if (late) {
+				stageBegin();
+				launchResolveLate(P, kind, sv, numTiles, g.stream);
+				stageEnd(SRP_GPU_STAGE_RESOLVE, 1);
+			} else {
+				stageBegin();
+				launchResolve(P, kind, sv, numTiles, g.heavy.as<uint32_t>(), g.stream, g.auxStream, g.forkEvent,
+				              g.joinEvent);
+				stageEnd(SRP_GPU_STAGE_RESOLVE, 3);
+				stageBegin();
+				launchShade(P, kind, numTiles, g.stream);
+				stageEnd(SRP_GPU_STAGE_SHADE, 1);
+			}
+		};
+		runHeadTail(graphKey(P, { (unsigned long long) kind, late, ib != nullptr, start, count, vb->nVertices, blocks,
+		                          keyBits, numTiles, g.bigJobsSeen[kind], (unsigned long long) (uintptr_t) g.stream }),
+		            head, tail);
+		g.launches += 4 + (ib ? 1 : 0) + (isTri(prim) ? 1 : 0) + 2 + 1 + keyBits / 8 + 1 + (late ? 1 : 4);
 		if (!cudaOk(cudaGetLastError(), FN, "launch")) return;
 		/* wait for the setup counters only; the rest of the draw runs on */
 		if (!cudaOk(cudaEventSynchronize(g.ctrEvent), FN, "kernel execution")) return;
@@ -1242,34 +1327,39 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		P.tileStart = g.tileStart.as<uint32_t>();
 		P.tileEnd = g.tileEnd.as<uint32_t>();
 
-		stageBegin();
-		launchReset(P, g.stream);
-		launchVertexMulti(P, vBlocks, maxStride, g.stream);
-		stageEnd(SRP_GPU_STAGE_VERTEX, 2);
-		stageBegin();
-		cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, g.stream);
-		launchClipPrepassMulti(P, g.stream);
-		launchSetupMulti(P, g.stream);
-		launchCheck(P, g.stream);
-		stageEnd(SRP_GPU_STAGE_SETUP, 3);
-		cudaMemcpyAsync(g.hostCtr, g.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, g.stream);
-		cudaEventRecord(g.ctrEvent, g.stream);
-		stageBegin();
-		launchBigEntriesMulti(P, g.bigJobsSeen[kKindTri], g.stream);
-		uint32_t* sk;
-		uint32_t* sv;
-		sortEntries(P, keyBits, g.keys2.as<uint32_t>(), g.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
-		            g.partials.as<uint32_t>(), &sk, &sv, g.stream);
-		cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, g.stream);
-		cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, g.stream);
-		launchTileRanges(P, sk, numTiles, g.stream);
-		stageEnd(SRP_GPU_STAGE_BIN, 2 + 1 + (int) (keyBits / 8) + 1);
-		stageBegin();
-		launchResolveMulti(P, sv, numTiles, g.heavy.as<uint32_t>(), g.stream, g.auxStream, g.forkEvent, g.joinEvent);
-		stageEnd(SRP_GPU_STAGE_RESOLVE, 3);
-		stageBegin();
-		launchShadeMulti(P, numTiles, g.stream);
-		stageEnd(SRP_GPU_STAGE_SHADE, 1);
+		auto head = [&]() {
+			stageBegin();
+			launchReset(P, g.stream);
+			launchVertexMulti(P, vBlocks, maxStride, g.stream);
+			stageEnd(SRP_GPU_STAGE_VERTEX, 2);
+			stageBegin();
+			cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, g.stream);
+			launchClipPrepassMulti(P, g.stream);
+			launchSetupMulti(P, g.stream);
+			launchCheck(P, g.stream);
+			stageEnd(SRP_GPU_STAGE_SETUP, 3);
+		};
+		auto tail = [&]() {
+			stageBegin();
+			launchBigEntriesMulti(P, g.bigJobsSeen[kKindTri], g.stream);
+			uint32_t* sk;
+			uint32_t* sv;
+			sortEntries(P, keyBits, g.keys2.as<uint32_t>(), g.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
+			            g.partials.as<uint32_t>(), &sk, &sv, g.stream);
+			cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, g.stream);
+			cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, g.stream);
+			launchTileRanges(P, sk, numTiles, g.stream);
+			stageEnd(SRP_GPU_STAGE_BIN, 2 + 1 + (int) (keyBits / 8) + 1);
+			stageBegin();
+			launchResolveMulti(P, sv, numTiles, g.heavy.as<uint32_t>(), g.stream, g.auxStream, g.forkEvent, g.joinEvent);
+			stageEnd(SRP_GPU_STAGE_RESOLVE, 3);
+			stageBegin();
+			launchShadeMulti(P, numTiles, g.stream);
+			stageEnd(SRP_GPU_STAGE_SHADE, 1);
+		};
+		runHeadTail(graphKey(P, { vBlocks, (unsigned long long) maxStride, blocks, keyBits, numTiles,
+		                          g.bigJobsSeen[kKindTri], (unsigned long long) (uintptr_t) g.stream }),
+		            head, tail);
 		g.launches += 5 + 2 + 1 + keyBits / 8 + 1 + 4;
 		if (!cudaOk(cudaGetLastError(), FN, "launch")) return false;
 		if (!cudaOk(cudaEventSynchronize(g.ctrEvent), FN, "kernel execution")) return false;
@@ -1418,6 +1508,8 @@ void srpGpuResetStats(void)
 }
 
 void srpGpuSetProfiling(int enable) { g.profiling = enable != 0; }
+
+void srpGpuSetDrawGraphs(int enable) { g.graphs = enable != 0; }
 
 void srpGpuGetProfile(SRPGpuProfile* out)
 {

@@ -71,7 +71,6 @@ struct Learned {
 	uint8_t* redoDev = nullptr;
 	std::vector<double> hostJudge;
 	std::vector<unsigned int> hostMax;
-	uint32_t seed = 1;
 	SRPGpuLearnedStats stats = {};
 };
 
@@ -141,8 +140,9 @@ bool learnedPrepare(DrawParams& P, int kind, bool late, uint32_t nDraws, cudaStr
 	P.capture = nullptr;
 	P.mlpW5 = nullptr;
 	P.redo = nullptr;
-	L.seed = L.seed * 1664525u + 1013904223u;
-	P.sampleSeed = L.seed;
+	/* the pixels sampled for capture and judging follow a fixed hash of the
+	 * pixel and the draw, so a repeated draw has the same parameters */
+	P.sampleSeed = 0x51ED270Bu;
 	if (L.capture && P.fsId == L.captureFs && kind == kKindTri) {
 		P.capture = L.capture->samples;
 		P.captureCount = L.capture->count;

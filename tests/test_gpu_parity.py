@@ -2,6 +2,7 @@
 reference library) and against the CPU oracle at other seeds and full size.
 Coverage, depth and stencil must be bit-exact; colour within 1/255 per
 channel. Every call goes through the srp C API of libsrp_gb300.so."""
+import numpy as np
 import pytest
 
 from oracle_util import manifest, load_golden, oracle_render, compare_planes
@@ -47,3 +48,28 @@ def test_full_size_configs_match_oracle(built_library, oracle_exe, scene, seed):
     got = gpu_render(scene, seed, 1.0)
     compare_planes(got, want, f"{scene} full size")
     assert got["fragments"] == want["fragments"]
+
+
+@pytest.mark.parametrize("scene,scale", [("soup", 0.02), ("lit", 1.0), ("stencil", 1.0)])
+def test_graph_replay_matches_direct_launches(built_library, scene, scale):
+    """A repeated draw replays its captured CUDA graphs; the images equal those
+    of the same draws launched directly."""
+    import srp_gb300
+    L = srp_gb300.lib()
+    S = srp_gb300.scenes()
+    L.srpGpuSetFramebufferMode(srp_gb300.SRP_GPU_FB_DEVICE)
+    sc = srp_gb300.Scene(scene, 9, scale)
+    try:
+        frames = []
+        for graphs in (1, 1, 0):
+            L.srpGpuSetDrawGraphs(graphs)
+            sc.prepare()
+            sc.render()
+            frames.append(sc.planes())
+        assert L.srpGpuSynchronize() == 0
+        for f in frames[1:]:
+            for a, b in zip(f, frames[0]):
+                assert np.array_equal(a, b)
+    finally:
+        L.srpGpuSetDrawGraphs(1)
+        sc.close()
