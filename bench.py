@@ -240,6 +240,15 @@ def run_batch(args):
         for sc in batch:
             sc.prepare()
 
+    tuning = None
+    if not args.no_autotune:
+        with torch.cuda.stream(stream):
+            prepare()
+            t0 = time.perf_counter()
+            best = srp_gb300.autotune_batch(batch, fbs, 1)
+            tuning = {"heavy_items": best.heavyItems, "heavy_ctas_per_sm": best.heavyCtasPerSM,
+                      "autotune_s": round(time.perf_counter() - t0, 2)}
+
     for _ in range(max(args.warmup, 1)):
         with torch.cuda.stream(stream):
             prepare()
@@ -297,7 +306,7 @@ def run_batch(args):
         "config": {"workload": BATCH_WORKLOAD, "scenes": args.scenes, "scale": args.scale, "triangles": tris,
                    "pixels": pixels, "fragments_per_step": frags, "mfrag_per_s": round(frags / step_s / 1e6, 1),
                    "mtri_per_s": round(tris / step_s / 1e6, 1), "generation_s": round(gen_s, 1),
-                   "l2": "flushed between steps (256 MB write)"},
+                   "l2": "flushed between steps (256 MB write)", "tuning": tuning},
         "clocks": clk,
         "e2e": {"value": round(args.scenes / e2e_s, 2), "unit": "scenes/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(pixels * 9)},
@@ -577,6 +586,7 @@ def main():
                          "learned: the marble-shaded frame with its learned stand-in")
     ap.add_argument("--scenes", type=int, default=BATCH_SCENES, help="scenes per batch (--workload batch)")
     ap.add_argument("--train-steps", type=int, default=3000, help="training steps (--workload learned, batch-learned)")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default resolve tuning (--workload batch)")
     args = ap.parse_args()
     if args.workload == "batch":
         return run_reference_batch(args) if args.impl == "reference" else run_batch(args)

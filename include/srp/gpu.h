@@ -82,6 +82,27 @@ typedef struct SRPGpuDraw
  *  a message, is issued through the ordinary path at its place in the order. */
 void srpGpuDrawBatch(const SRPGpuDraw* draws, size_t n);
 
+/** Tuning of the resolve stage. Tiles with more than heavyItems (tile, item)
+ *  pairs are resolved by a 256-thread CTA each (8 warps per tile), the others
+ *  by one warp; the CTA kernel runs heavyCtasPerSM (1..3) CTAs per SM. The
+ *  tile itself is fixed at 8 x 8 pixels: the exact resolve's 64-bit coverage
+ *  masks depend on it. */
+typedef struct SRPGpuTuning
+{
+	uint32_t heavyItems;
+	uint32_t heavyCtasPerSM;
+} SRPGpuTuning;
+
+void srpGpuGetTuning(SRPGpuTuning* tuning);
+void srpGpuSetTuning(const SRPGpuTuning* tuning);
+
+/** Autotuner: draws the batch (srpGpuDrawBatch) `repeats` times under each
+ *  candidate tuning (heavyItems 32, 64, 96, 192, 384 x heavyCtasPerSM 1..3),
+ *  times it with CUDA events, and keeps the fastest as the library's tuning
+ *  (also returned in best). The framebuffers are drawn into repeatedly:
+ *  prepare them again afterwards. Returns 0 on success. */
+int srpGpuAutotune(const SRPGpuDraw* draws, size_t n, int repeats, SRPGpuTuning* best);
+
 /* --------------------------------------------------- learned shading */
 
 /* A small MLP that stands in for an expensive fragment shader. None of this

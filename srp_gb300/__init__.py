@@ -32,6 +32,10 @@ class SRPGpuDraw(ctypes.Structure):
                 ("startIndex", ctypes.c_size_t), ("count", ctypes.c_size_t)]
 
 
+class SRPGpuTuning(ctypes.Structure):
+    _fields_ = [("heavyItems", ctypes.c_uint32), ("heavyCtasPerSM", ctypes.c_uint32)]
+
+
 class SceneInfo(ctypes.Structure):
     _fields_ = [("width", ctypes.c_int), ("height", ctypes.c_int),
                 ("inputTriangles", ctypes.c_size_t), ("inputLines", ctypes.c_size_t),
@@ -106,6 +110,9 @@ def scenes():
         S.sceneDrawDesc.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(SRPGpuDraw)]
         S.sceneBatchRender.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t,
                                        ctypes.POINTER(SRPGpuDraw)]
+        S.sceneBatchAutotune.restype = ctypes.c_int
+        S.sceneBatchAutotune.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t,
+                                         ctypes.POINTER(SRPGpuDraw), ctypes.c_int, ctypes.POINTER(SRPGpuTuning)]
         _scenes = S
     return _scenes
 
@@ -202,6 +209,20 @@ def render_batch(batch, fbs):
     fp = (ctypes.c_void_p * n)(*fbs)
     scratch = (SRPGpuDraw * n)()
     S.sceneBatchRender(sp, fp, n, scratch)
+
+
+def autotune_batch(batch, fbs, repeats=1):
+    """srpGpuAutotune on the batch render_batch would draw; returns the chosen
+    SRPGpuTuning (the framebuffers must be prepared again)."""
+    S = scenes()
+    n = len(batch)
+    sp = (ctypes.c_void_p * n)(*[sc.ptr for sc in batch])
+    fp = (ctypes.c_void_p * n)(*fbs)
+    scratch = (SRPGpuDraw * n)()
+    best = SRPGpuTuning()
+    if S.sceneBatchAutotune(sp, fp, n, scratch, repeats, ctypes.byref(best)) != 0:
+        raise RuntimeError("srpGpuAutotune failed")
+    return best
 
 
 def render_scene(name, seed=1, scale=1.0):

@@ -41,8 +41,6 @@ constexpr int kResolveWarps = 4;
 /* row pitch of the per-item depth rows in shared memory: 65 keeps lanes that
  * write the same pixel of different items in different banks */
 constexpr int kDepRow = 65;
-/* tiles with more items than this are resolved by a whole CTA */
-constexpr uint32_t kHeavyItems = 96;
 constexpr int kHeavyThreads = 256;
 
 template <int FS>
@@ -403,7 +401,7 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(const __grid_con
 	if (tile >= numTiles || P.ctr->abort) return;
 	const uint32_t s = P.tileStart[tile], e = P.tileEnd[tile];
 	if (s >= e) return;
-	if (LATE_FS == 0 && e - s > kHeavyItems) return;  /* k_resolve_heavy's */
+	if (LATE_FS == 0 && e - s > P.heavyItems) return;  /* k_resolve_heavy's */
 	const DrawState& st = P.st;
 	const TileCtx c = tileCtx<MULTI>(P, tile);
 	const int x0 = c.x0, y0 = c.y0;
@@ -632,13 +630,13 @@ __global__ void __launch_bounds__(kHeavyThreads) k_resolve_heavy(const __grid_co
 	}
 }
 
-/* Lists the tiles with more than kHeavyItems items for k_resolve_heavy. */
+/* Lists the tiles with more than P.heavyItems items for k_resolve_heavy. */
 __global__ void k_tile_classify(const __grid_constant__ DrawParams P, uint32_t numTiles, uint32_t* heavy)
 {
 	const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
 	if (t >= numTiles || P.ctr->abort) return;
 	const uint32_t n = P.tileEnd[t] - P.tileStart[t];
-	if (P.tileEnd[t] > P.tileStart[t] && n > kHeavyItems) heavy[atomicAdd(&P.ctr->nonEmptyTiles, 1u)] = t;
+	if (P.tileEnd[t] > P.tileStart[t] && n > P.heavyItems) heavy[atomicAdd(&P.ctr->nonEmptyTiles, 1u)] = t;
 }
 
 /* Deferred shading: one shader invocation per pixel whose colour was written
@@ -834,7 +832,8 @@ static void launchHeavy(const DrawParams& P, const uint32_t* vals, uint32_t* hea
 {
 	const int smem = kHeavyThreads * kDepRow * 4;
 	cudaFuncSetAttribute(k_resolve_heavy<KIND, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-	k_resolve_heavy<KIND, MULTI><<<152 * 3, kHeavyThreads, smem, s>>>(P, vals, heavy);
+	const unsigned perSM = P.heavyCtasPerSM >= 1 && P.heavyCtasPerSM <= 3 ? P.heavyCtasPerSM : 3u;
+	k_resolve_heavy<KIND, MULTI><<<152 * perSM, kHeavyThreads, smem, s>>>(P, vals, heavy);
 }
 
 void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, uint32_t* heavy, cudaStream_t s,

@@ -67,6 +67,10 @@ struct DrawParams {
 	 * Primitive, entry and tile numbers are then global over the pass. */
 	const DrawDesc* draws;
 	uint32_t nDraws;
+	/* resolve tuning: tiles with more than heavyItems items are resolved by
+	 * a CTA (k_resolve_heavy, heavyCtasPerSM CTAs per SM), the others by a
+	 * warp (k_resolve) */
+	uint32_t heavyItems, heavyCtasPerSM;
 	const uint32_t* inPrefix;
 	const uint32_t* vPrefix;
 	const uint32_t* tPrefix;

@@ -95,6 +95,7 @@ struct Lib {
 	cudaEvent_t forkEvent = nullptr, joinEvent = nullptr;
 	cudaEvent_t ctrEvent = nullptr;   /* recorded after a draw's counters are copied to hostCtr */
 	bool graphs = true;               /* replay repeated draws from captured CUDA graphs */
+	SRPGpuTuning tune = { 96, 3 };    /* heavy-tile threshold, heavy-tile CTAs per SM */
 	SRPGpuFramebufferMode fbMode = SRP_GPU_FB_COHERENT;
 	Registry reg;
 	/* scratch pools, grown on demand */
@@ -909,6 +910,8 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 	static_assert(sizeof(SRPStdUniform) <= kMaxUniformBytes, "uniform too large");
 	P.vsId = vsId;
 	P.fsId = fsId;
+	P.heavyItems = g.tune.heavyItems;
+	P.heavyCtasPerSM = g.tune.heavyCtasPerSM;
 	P.prim = prim;
 	P.start = start;
 	P.count = count;
@@ -1210,6 +1213,8 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	st.tile = kTile;
 	P.vsId = lookupVS((void*) sp0->vs->shader);
 	P.fsId = lookupFS((void*) sp0->fs->shader);
+	P.heavyItems = g.tune.heavyItems;
+	P.heavyCtasPerSM = g.tune.heavyCtasPerSM;
 	P.prim = SRP_PRIM_TRIANGLES;
 
 	/* descriptors and prefix sums */
@@ -1511,6 +1516,46 @@ void srpGpuSetProfiling(int enable) { g.profiling = enable != 0; }
 
 void srpGpuSetDrawGraphs(int enable) { g.graphs = enable != 0; }
 
+void srpGpuGetTuning(SRPGpuTuning* t) { *t = g.tune; }
+
+void srpGpuSetTuning(const SRPGpuTuning* t)
+{
+	g.tune.heavyItems = t->heavyItems;
+	g.tune.heavyCtasPerSM = t->heavyCtasPerSM >= 1 && t->heavyCtasPerSM <= 3 ? t->heavyCtasPerSM : 3;
+}
+
+int srpGpuAutotune(const SRPGpuDraw* draws, size_t n, int repeats, SRPGpuTuning* best)
+{
+	if (!draws || !n || !ensureInit("srpGpuAutotune")) return -1;
+	static const uint32_t thresholds[] = { 32, 64, 96, 192, 384 };
+	cudaEvent_t e0 = takeEvent(), e1 = takeEvent();
+	const SRPGpuTuning start = g.tune;
+	SRPGpuTuning top = start;
+	float topMs = -1.0f;
+	srpGpuDrawBatch(draws, n);   /* warm-up: sizes the scratch */
+	for (uint32_t th : thresholds)
+		for (uint32_t per = 1; per <= 3; ++per) {
+			g.tune.heavyItems = th;
+			g.tune.heavyCtasPerSM = per;
+			srpGpuDrawBatch(draws, n);   /* first run captures the graphs for this tuning */
+			float ms = 0.0f;
+			cudaEventRecord(e0, g.stream);
+			for (int r = 0; r < (repeats > 0 ? repeats : 1); ++r) srpGpuDrawBatch(draws, n);
+			cudaEventRecord(e1, g.stream);
+			if (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+				g.tune = start;
+				SRP_ERROR("srpGpuAutotune", "timing failed");
+				return -1;
+			}
+			if (topMs < 0.0f || ms < topMs) { topMs = ms; top = g.tune; }
+		}
+	g.eventPool.push_back(e0);
+	g.eventPool.push_back(e1);
+	g.tune = top;
+	if (best) *best = top;
+	return 0;
+}
+
 void srpGpuGetProfile(SRPGpuProfile* out)
 {
 	if (g.init) {
@@ -1646,6 +1691,8 @@ int fixedDrawPrepare(DrawParams& P, const SRPIndexBuffer* ib, const SRPVertexBuf
 	}
 	P.vsId = vsId;
 	P.fsId = fsId;
+	P.heavyItems = g.tune.heavyItems;
+	P.heavyCtasPerSM = g.tune.heavyCtasPerSM;
 	P.prim = prim;
 	P.start = start;
 	P.count = count;

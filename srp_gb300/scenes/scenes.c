@@ -1452,6 +1452,15 @@ void sceneBatchRender(Scene** scenes, SRPFramebuffer** fbs, size_t n, SRPGpuDraw
 	for (size_t i = 0; i < n; ++i) sceneDrawDesc(scenes[i], fbs[i], &scratch[i]);
 	srpGpuDrawBatch(scratch, n);
 }
+
+int sceneBatchAutotune(Scene** scenes, SRPFramebuffer** fbs, size_t n, SRPGpuDraw* scratch, int repeats,
+                       SRPGpuTuning* best)
+{
+	resetContext();
+	bsceneState();
+	for (size_t i = 0; i < n; ++i) sceneDrawDesc(scenes[i], fbs[i], &scratch[i]);
+	return srpGpuAutotune(scratch, n, repeats, best);
+}
 #endif
 
 int sceneRunOnce(const char* name, uint64_t seed, double scale,

@@ -58,6 +58,9 @@ int sceneDumpInputs(const Scene* s, const char* path);
  * render of n scenes into their framebuffers with the scenes' state. */
 int sceneDrawDesc(Scene* s, SRPFramebuffer* fb, SRPGpuDraw* out);
 void sceneBatchRender(Scene** scenes, SRPFramebuffer** fbs, size_t n, SRPGpuDraw* scratch);
+/* srpGpuAutotune on that batch (the framebuffers must be prepared again). */
+int sceneBatchAutotune(Scene** scenes, SRPFramebuffer** fbs, size_t n, SRPGpuDraw* scratch, int repeats,
+                       SRPGpuTuning* best);
 #endif
 
 /* Convenience: create a framebuffer of the scene's size, prepare, render, copy

@@ -125,3 +125,41 @@ def test_batch_scene_matches_oracle(built_library, oracle_exe, i):
     finally:
         for sc in scenes:
             sc.close()
+
+
+def test_autotune_keeps_results_exact(built_library):
+    """The autotuner picks a resolve tuning; any tuning renders the same images."""
+    import srp_gb300
+    L = srp_gb300.lib()
+    S = srp_gb300.scenes()
+    L.srpGpuSetFramebufferMode(1)
+    L.srpGpuGetTuning.argtypes = [ctypes.POINTER(srp_gb300.SRPGpuTuning)]
+    L.srpGpuSetTuning.argtypes = [ctypes.POINTER(srp_gb300.SRPGpuTuning)]
+    scenes = make_scenes(12, 0.3)
+    default = srp_gb300.SRPGpuTuning()
+    L.srpGpuGetTuning(ctypes.byref(default))
+    try:
+        fbs = [sc.fb for sc in scenes]
+
+        def render():
+            for sc in scenes:
+                sc.prepare()
+            srp_gb300.render_batch(scenes, fbs)
+            return [sync_planes(srp_gb300, S, fb) for fb in fbs]
+
+        want = render()
+        for sc in scenes:
+            sc.prepare()
+        best = srp_gb300.autotune_batch(scenes, fbs, 1)
+        assert best.heavyItems in (32, 64, 96, 192, 384) and 1 <= best.heavyCtasPerSM <= 3
+        for tune in [(best.heavyItems, best.heavyCtasPerSM), (1, 1), (100000, 2)]:
+            L.srpGpuSetTuning(ctypes.byref(srp_gb300.SRPGpuTuning(*tune)))
+            got = render()
+            for a, b in zip(got, want):
+                for x, y in zip(a, b):
+                    assert np.array_equal(x, y), tune
+    finally:
+        L.srpGpuSetTuning(ctypes.byref(default))
+        for sc in scenes:
+            sc.close()
+    assert L.srpGpuSynchronize() == 0
