@@ -586,7 +586,7 @@ def main():
                          "learned: the marble-shaded frame with its learned stand-in")
     ap.add_argument("--scenes", type=int, default=BATCH_SCENES, help="scenes per batch (--workload batch)")
     ap.add_argument("--train-steps", type=int, default=3000, help="training steps (--workload learned, batch-learned)")
-    ap.add_argument("--no-autotune", action="store_true", help="keep the default resolve tuning (--workload batch)")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default resolve tuning (--workload frame, batch)")
     args = ap.parse_args()
     if args.workload == "batch":
         return run_reference_batch(args) if args.impl == "reference" else run_batch(args)
@@ -620,11 +620,25 @@ def main():
     def frame():
         sc.render()
 
-    # warm-up
+    # warm-up, then the library's online autotuner over whole frames
     for _ in range(max(args.warmup, 1)):
         with torch.cuda.stream(stream):
             sc.prepare()
             frame()
+    tuning = None
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            busy = 1
+            while busy:
+                sc.prepare()
+                frame()
+                busy = L.srpGpuAutotuneFrame()
+        best = srp_gb300.SRPGpuTuning()
+        L.srpGpuGetTuning.argtypes = [ctypes.POINTER(srp_gb300.SRPGpuTuning)]
+        L.srpGpuGetTuning(ctypes.byref(best))
+        tuning = {"heavy_items": best.heavyItems, "heavy_ctas_per_sm": best.heavyCtasPerSM,
+                  "autotune_s": round(time.perf_counter() - t0, 2)}
     torch.cuda.synchronize()
     L.srpGpuResetStats()
     st0 = srp_gb300.SRPGpuStats()
@@ -700,6 +714,7 @@ def main():
         "config": {"workload": WORKLOAD, "seed": SEED, "width": info.width, "height": info.height,
                    "triangles": info.inputTriangles, "lines": info.inputLines, "points": info.inputPoints,
                    "fragments_per_frame": frags_per_frame, "l2": "flushed between frames (256 MB write)",
+                   "tuning": tuning,
                    "frames_per_s": round(args.steps / (total_ms / 1000.0), 2),
                    "mtri_per_s": round(info.inputTriangles * args.steps / (total_ms / 1000.0) / 1e6, 2)},
         "clocks": clk,

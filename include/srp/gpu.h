@@ -103,6 +103,14 @@ void srpGpuSetTuning(const SRPGpuTuning* tuning);
  *  prepare them again afterwards. Returns 0 on success. */
 int srpGpuAutotune(const SRPGpuDraw* draws, size_t n, int repeats, SRPGpuTuning* best);
 
+/** Online autotuner for a frame loop: call once after each frame's draws.
+ *  Over the next 30 frames it tries the same candidates as srpGpuAutotune,
+ *  two frames each (the second one timed with CUDA events), then keeps the
+ *  fastest. Returns 1 while tuning, 0 once a tuning has been chosen (and on
+ *  every later call, until srpGpuAutotuneReset). */
+int srpGpuAutotuneFrame(void);
+void srpGpuAutotuneReset(void);
+
 /* --------------------------------------------------- learned shading */
 
 /* A small MLP that stands in for an expensive fragment shader. None of this

@@ -72,16 +72,52 @@ __device__ __forceinline__ unsigned long long fetchIndex(const DrawParams& P, un
 	return fetchIndexRaw(P.indices, P.indexSize, i);
 }
 
+/* Min/max over the elements of one aligned 16-byte word of the index
+ * buffer: all of them when the word lies inside the draw's byte range
+ * [b0, b1), else only those inside it. */
+template <typename I>
+__device__ __forceinline__ void wordRange(const uint4& q, unsigned long long at, unsigned long long b0,
+                                          unsigned long long b1, unsigned long long& lo, unsigned long long& hi)
+{
+	constexpr int n = 16 / (int) sizeof(I);
+	I e[n];
+	memcpy(e, &q, 16);
+	const bool whole = at >= b0 && at + 16 <= b1;
+#pragma unroll
+	for (int k = 0; k < n; ++k) {
+		const unsigned long long off = at + (unsigned long long) k * sizeof(I);
+		if (whole || (off >= b0 && off < b1)) {
+			const unsigned long long v = (unsigned long long) e[k];
+			lo = v < lo ? v : lo;
+			hi = v > hi ? v : hi;
+		}
+	}
+}
+
 /* min/max vertex index over the draw's index range
- * (src/pipeline/vertex_processing.c:90-112). */
+ * (src/pipeline/vertex_processing.c:90-112). The range's bytes are read as
+ * aligned 16-byte words, two independent loads per thread per iteration, so
+ * that enough bytes are in flight to stream the index buffer at HBM speed.
+ * Boundary words can reach up to 15 bytes past the last index: index
+ * buffers are allocated with 16 bytes of slack. */
 __global__ void k_index_range(const __grid_constant__ DrawParams P)
 {
+	const unsigned long long isz = (unsigned long long) P.indexSize;
+	const unsigned long long b0 = P.start * isz, b1 = (P.start + P.count) * isz;
+	const unsigned long long w0 = b0 >> 4, w1 = (b1 + 15) >> 4;
+	const uint4* words = (const uint4*) P.indices;
+	const unsigned long long stride = (unsigned long long) gridDim.x * blockDim.x;
 	unsigned long long lo = ~0ull, hi = 0;
-	for (unsigned long long i = blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; i < P.count;
-	     i += (unsigned long long) gridDim.x * blockDim.x) {
-		const unsigned long long v = fetchIndex(P, P.start + i);
-		lo = v < lo ? v : lo;
-		hi = v > hi ? v : hi;
+	for (unsigned long long w = w0 + blockIdx.x * (unsigned long long) blockDim.x + threadIdx.x; w < w1; w += 2 * stride) {
+		const bool two = w + stride < w1;
+		const uint4 a = __ldg(words + w);
+		const uint4 b = two ? __ldg(words + w + stride) : a;
+		switch (isz) {
+		case 1: wordRange<uint8_t>(a, w << 4, b0, b1, lo, hi); wordRange<uint8_t>(b, (two ? w + stride : w) << 4, b0, b1, lo, hi); break;
+		case 2: wordRange<uint16_t>(a, w << 4, b0, b1, lo, hi); wordRange<uint16_t>(b, (two ? w + stride : w) << 4, b0, b1, lo, hi); break;
+		case 4: wordRange<uint32_t>(a, w << 4, b0, b1, lo, hi); wordRange<uint32_t>(b, (two ? w + stride : w) << 4, b0, b1, lo, hi); break;
+		default: wordRange<unsigned long long>(a, w << 4, b0, b1, lo, hi); wordRange<unsigned long long>(b, (two ? w + stride : w) << 4, b0, b1, lo, hi); break;
+		}
 	}
 	for (int o = 16; o; o >>= 1) {
 		const unsigned long long l2 = __shfl_xor_sync(0xFFFFFFFFu, lo, o);
@@ -693,12 +729,16 @@ __device__ __forceinline__ unsigned long long orderedOffset(const DrawParams& P,
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__ DrawParams P)
+__global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup(const __grid_constant__ DrawParams P)
 {
 	__shared__ uint32_t sBlock;
 	__shared__ unsigned long long sWarp[kSetupThreads / 32];
 	__shared__ unsigned long long sPrefix;
-	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	/* an unclipped filled triangle's setup waits here across the scan, so
+	 * that it holds no registers meanwhile */
+	__shared__ TriRaster sR[MODE == kTriFill ? kSetupThreads : 1];
+	__shared__ TriAttr sA[MODE == kTriFill ? kSetupThreads : 1];
+	const int tid = threadIdx.x;
 	if (tid == 0) sBlock = atomicAdd(&P.ctr->lookbackTicket, 1u);
 	__syncthreads();
 	const uint32_t bid = sBlock;
@@ -762,9 +802,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
 		}
 	}
 	uint32_t nPrim = 0, nEnt = 0;
-	/* unclipped filled triangle: set up once, kept in registers across the scan */
-	TriRaster fR;
-	TriAttr fA;
+	/* unclipped filled triangle: set up once, kept in shared memory across the scan */
 	bool fOk = false;
 	if (live) {
 		if (MODE == kPoints) {
@@ -779,8 +817,15 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
 			nEnt = (uint32_t) L.steps + 1u;
 		} else if (!as.clipped) {
 			if (MODE == kTriFill) {
+				TriRaster fR;
+				TriAttr fA;
 				fOk = setupTriangle(P.st, P.st.W, P.st.H, as.sv[0], as.sv[1], as.sv[2], fR, fA);
-				if (fOk) { nPrim = 1; nEnt = tileCount(fR.minX, fR.minY, fR.maxX, fR.maxY); }
+				if (fOk) {
+					nPrim = 1;
+					nEnt = tileCount(fR.minX, fR.minY, fR.maxX, fR.maxY);
+					sR[tid] = fR;
+					sA[tid] = fA;
+				}
 			} else {
 				handleTriangle<MODE>(P, as.sv[0], as.sv[1], as.sv[2], false, nPrim, nEnt);
 			}
@@ -814,7 +859,11 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
 		} else atomicOr(&P.ctr->errors, kErrCapacity);
 	} else if (!as.clipped) {
 		if (MODE == kTriFill) {
-			if (fOk) writeTri(P, fR, fA, nEnt, primBase, entBase);
+			if (fOk) {
+				TriRaster fR = sR[tid];
+				TriAttr fA = sA[tid];
+				writeTri(P, fR, fA, nEnt, primBase, entBase);
+			}
 		} else {
 			handleTriangle<MODE>(P, as.sv[0], as.sv[1], as.sv[2], true, primBase, entBase);
 		}
@@ -830,7 +879,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(const __grid_constant__
  * Sutherland-Hodgman path runs here instead of inside the scan-coupled setup
  * blocks. The polygon (vertex count and vertex rows, new vertices included)
  * goes to a slot that k_setup reads back. */
-__global__ void __launch_bounds__(kSetupThreads) k_clip_prepass(const __grid_constant__ DrawParams P)
+__global__ void __launch_bounds__(kSetupThreads, 16) k_clip_prepass(const __grid_constant__ DrawParams P)
 {
 	const long long k = (long long) blockIdx.x * blockDim.x + threadIdx.x;
 	if (k >= P.nIn) return;
@@ -1125,7 +1174,7 @@ __device__ __forceinline__ bool triangleOfPass(const DrawParams& P, uint32_t k, 
 }
 
 /* Clip pre-pass of a pass (see k_clip_prepass). */
-__global__ void __launch_bounds__(kSetupThreads) k_clip_prepass_multi(const __grid_constant__ DrawParams P)
+__global__ void __launch_bounds__(kSetupThreads, 16) k_clip_prepass_multi(const __grid_constant__ DrawParams P)
 {
 	const long long k = (long long) blockIdx.x * blockDim.x + threadIdx.x;
 	if (k >= P.nIn) return;
@@ -1186,11 +1235,13 @@ __device__ __forceinline__ void writeTriMulti(const DrawParams& P, uint32_t d, i
  * draw's framebuffer size and tile grid. The first input triangle of every
  * draw records the number of surviving primitives before the draw, from
  * which primitive ids local to the draw are recovered. */
-__global__ void __launch_bounds__(kSetupThreads) k_setup_multi(const __grid_constant__ DrawParams P)
+__global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup_multi(const __grid_constant__ DrawParams P)
 {
 	__shared__ uint32_t sBlock;
 	__shared__ unsigned long long sWarp[kSetupThreads / 32];
 	__shared__ unsigned long long sPrefix;
+	__shared__ TriRaster sR[kSetupThreads];
+	__shared__ TriAttr sA[kSetupThreads];
 	const int tid = threadIdx.x;
 	if (tid == 0) sBlock = atomicAdd(&P.ctr->lookbackTicket, 1u);
 	__syncthreads();
@@ -1232,13 +1283,18 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_multi(const __grid_cons
 		}
 	}
 	uint32_t nPrim = 0, nEnt = 0;
-	TriRaster fR;
-	TriAttr fA;
 	bool fOk = false;
 	if (live) {
 		if (!clipped) {
+			TriRaster fR;
+			TriAttr fA;
 			fOk = setupTriangle(P.st, W, H, sv[0], sv[1], sv[2], fR, fA);
-			if (fOk) { nPrim = 1; nEnt = tileCount(fR.minX, fR.minY, fR.maxX, fR.maxY); }
+			if (fOk) {
+				nPrim = 1;
+				nEnt = tileCount(fR.minX, fR.minY, fR.maxX, fR.maxY);
+				sR[tid] = fR;
+				sA[tid] = fA;
+			}
 		} else {
 			const SV p0 = fromClip(W, H, poly[0]);
 			for (int f = 1; f + 1 < nPoly; ++f) {
@@ -1255,7 +1311,11 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_multi(const __grid_cons
 	if (first) P.primPrefix[d] = primBase;
 	if (!live) return;
 	if (!clipped) {
-		if (fOk) writeTriMulti(P, d, tilesX, tileBase, fR, fA, nEnt, primBase, entBase);
+		if (fOk) {
+			TriRaster fR = sR[tid];
+			TriAttr fA = sA[tid];
+			writeTriMulti(P, d, tilesX, tileBase, fR, fA, nEnt, primBase, entBase);
+		}
 	} else {
 		const SV p0 = fromClip(W, H, poly[0]);
 		for (int f = 1; f + 1 < nPoly; ++f) {
@@ -1309,7 +1369,9 @@ void launchReset(const DrawParams& P, cudaStream_t s) { k_reset<<<1, 32, 0, s>>>
 
 void launchIndexRange(const DrawParams& P, cudaStream_t s)
 {
-	unsigned long long blocks = (P.count + 255) / 256;
+	/* 16-byte words of the range, two per thread */
+	const unsigned long long words = (P.count * (unsigned long long) P.indexSize + 31) / 16;
+	unsigned long long blocks = (words + 511) / 512;
 	if (blocks > 152 * 8) blocks = 152 * 8;
 	if (blocks < 1) blocks = 1;
 	k_index_range<<<(unsigned) blocks, 256, 0, s>>>(P);

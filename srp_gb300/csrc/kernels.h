@@ -101,7 +101,11 @@ struct DrawParams {
 constexpr int kFsLearned = 100;
 
 constexpr int kTile = 8;              /* tile edge in pixels */
-constexpr int kSetupThreads = 256;
+/* Ordered setup: blocks of 128 threads, at least 10 resident per SM (48
+ * registers a thread). The block waits at its scan barriers for the
+ * look-back, so more, smaller resident blocks keep the SM busy meanwhile. */
+constexpr int kSetupThreads = 128;
+constexpr int kSetupBlocksPerSM = 10;
 constexpr int kSmallEntries = 16;     /* tiles a primitive may write inline */
 
 /* k_front.cu */

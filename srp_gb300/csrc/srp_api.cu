@@ -1524,6 +1524,51 @@ void srpGpuSetTuning(const SRPGpuTuning* t)
 	g.tune.heavyCtasPerSM = t->heavyCtasPerSM >= 1 && t->heavyCtasPerSM <= 3 ? t->heavyCtasPerSM : 3;
 }
 
+/* Online autotuning of a frame loop: two frames per candidate (the first
+ * captures the graphs of the new tuning, the second is timed). */
+namespace {
+struct FrameTuner {
+	int state = -1;          /* -1 idle, 0..2n-1 running, -2 done */
+	cudaEvent_t start = nullptr, stop = nullptr;
+	float best = -1.0f;
+	SRPGpuTuning bestTune = { 96, 3 };
+} tuner;
+const uint32_t kTuneThresholds[] = { 32, 64, 96, 192, 384 };
+constexpr int kTuneCandidates = 5 * 3;
+SRPGpuTuning tuneCandidate(int i) { return SRPGpuTuning{ kTuneThresholds[i / 3], (uint32_t) (i % 3 + 1) }; }
+}  // namespace
+
+int srpGpuAutotuneFrame(void)
+{
+	if (tuner.state == -2 || !ensureInit("srpGpuAutotuneFrame")) return 0;
+	if (!tuner.start) { tuner.start = takeEvent(); tuner.stop = takeEvent(); }
+	if (tuner.state >= 0 && (tuner.state & 1)) {
+		/* a timed frame just ended */
+		cudaEventRecord(tuner.stop, g.stream);
+		float ms = 0.0f;
+		if (cudaEventSynchronize(tuner.stop) == cudaSuccess && cudaEventElapsedTime(&ms, tuner.start, tuner.stop) == cudaSuccess &&
+		    (tuner.best < 0.0f || ms < tuner.best)) {
+			tuner.best = ms;
+			tuner.bestTune = g.tune;
+		}
+	}
+	++tuner.state;
+	if (tuner.state >= 2 * kTuneCandidates) {
+		g.tune = tuner.bestTune;
+		tuner.state = -2;
+		return 0;
+	}
+	g.tune = tuneCandidate(tuner.state / 2);
+	if (tuner.state & 1) cudaEventRecord(tuner.start, g.stream);
+	return 1;
+}
+
+void srpGpuAutotuneReset(void)
+{
+	tuner.state = -1;
+	tuner.best = -1.0f;
+}
+
 int srpGpuAutotune(const SRPGpuDraw* draws, size_t n, int repeats, SRPGpuTuning* best)
 {
 	if (!draws || !n || !ensureInit("srpGpuAutotune")) return -1;

@@ -163,3 +163,49 @@ def test_autotune_keeps_results_exact(built_library):
         for sc in scenes:
             sc.close()
     assert L.srpGpuSynchronize() == 0
+
+
+def test_frame_autotuner_ends_and_keeps_results_exact(built_library):
+    """The online frame autotuner ends 30 frames after its first call with a candidate tuning;
+    the frames it renders meanwhile are the same as the default tuning's."""
+    import srp_gb300
+    L = srp_gb300.lib()
+    S = srp_gb300.scenes()
+    L.srpGpuSetFramebufferMode(1)
+    L.srpGpuGetTuning.argtypes = [ctypes.POINTER(srp_gb300.SRPGpuTuning)]
+    L.srpGpuSetTuning.argtypes = [ctypes.POINTER(srp_gb300.SRPGpuTuning)]
+    scenes = make_scenes(4, 0.3)
+    default = srp_gb300.SRPGpuTuning()
+    L.srpGpuGetTuning(ctypes.byref(default))
+    try:
+        fbs = [sc.fb for sc in scenes]
+
+        def render():
+            for sc in scenes:
+                sc.prepare()
+            srp_gb300.render_batch(scenes, fbs)
+            return [sync_planes(srp_gb300, S, fb) for fb in fbs]
+
+        want = render()
+        L.srpGpuAutotuneReset()
+        frames = 0
+        while True:
+            got = render()
+            for a, b in zip(got, want):
+                for x, y in zip(a, b):
+                    assert np.array_equal(x, y), frames
+            frames += 1
+            if not L.srpGpuAutotuneFrame():
+                break
+            assert frames <= 31
+        assert frames == 31
+        best = srp_gb300.SRPGpuTuning()
+        L.srpGpuGetTuning(ctypes.byref(best))
+        assert best.heavyItems in (32, 64, 96, 192, 384) and 1 <= best.heavyCtasPerSM <= 3
+        assert L.srpGpuAutotuneFrame() == 0
+    finally:
+        L.srpGpuAutotuneReset()
+        L.srpGpuSetTuning(ctypes.byref(default))
+        for sc in scenes:
+            sc.close()
+    assert L.srpGpuSynchronize() == 0
