@@ -665,9 +665,11 @@ def main():
     L.srpGpuGetStats(ctypes.byref(st0))
     frags_per_frame = st0.fragments / max(args.steps, 1)
     launches = st0.kernelLaunches
-    # end-to-end through the API from host memory
+    clk = clocks.stop()
+    # end-to-end through the API from host memory (after the clock sampler has
+    # stopped: its nvidia-smi queries stall the host's CUDA calls now and then)
     e2e_times = []
-    for _ in range(max(2, args.steps // 2)):
+    for _ in range(max(5, args.steps)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         sc.upload()
@@ -675,7 +677,6 @@ def main():
         frame()
         sc.sync()
         e2e_times.append(time.perf_counter() - t0)
-    clk = clocks.stop()
     # per-stage device time (CUDA events inside the library) on separate frames
     L.srpGpuSetProfiling(1)
     L.srpGpuResetProfile()

@@ -12,6 +12,7 @@
 
 #include "device_common.cuh"
 #include "kernels.h"
+#include "launch.cuh"
 
 namespace srpg {
 
@@ -35,6 +36,7 @@ __device__ __forceinline__ uint32_t pairCount(const DeviceCounters* ctr, uint32_
 __global__ void __launch_bounds__(kSortThreads) k_radix_global_hist(const uint32_t* keys, const DeviceCounters* ctr,
                                                                    uint32_t cap, uint32_t passes, uint32_t* ghist)
 {
+	gridDepSync();
 	__shared__ uint32_t h[kMaxPasses][256];
 	const uint32_t n = pairCount(ctr, cap);
 	if (n == 0) return;
@@ -87,6 +89,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_onesweep(const uint32_t*
                                                                 uint32_t* status, uint32_t* ticket, uint32_t* errors,
                                                                 uint32_t* keysOut, uint32_t* valsOut)
 {
+	gridDepSync();
 	/* the grid is sized for the scratch; blocks past the real count leave at
 	 * once (their successors, which would look back at them, leave too) */
 	const uint32_t n = pairCount(ctr, cap);
@@ -158,6 +161,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_onesweep(const uint32_t*
 __global__ void k_tile_ranges(const uint32_t* keys, const DeviceCounters* ctr, uint32_t cap, uint32_t numTiles,
                               uint32_t* start, uint32_t* end)
 {
+	gridDepSync();
 	const uint32_t n = pairCount(ctr, cap);
 	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		const uint32_t k = keys[i];
@@ -190,9 +194,9 @@ void sortEntries(const DrawParams& P, uint32_t keyBits, uint32_t* keysAlt, uint3
 		uint32_t* status = tickets + 8;
 		cudaMemsetAsync(hist, 0, sortHistWords(cap) * 4, s);
 		const uint32_t hb = nb < 152u * 4u ? nb : 152u * 4u;
-		k_radix_global_hist<<<hb, kSortThreads, 0, s>>>(kin, P.ctr, cap, passes, ghist);
+		pdlLaunch(k_radix_global_hist, hb, kSortThreads, 0, s, kin, P.ctr, cap, passes, ghist);
 		for (uint32_t p = 0; p < passes; ++p) {
-			k_radix_onesweep<<<nb, kSortThreads, 0, s>>>(kin, vin, P.ctr, cap, 8 * p, ghist + 256 * p,
+			pdlLaunch(k_radix_onesweep, nb, kSortThreads, 0, s, kin, vin, P.ctr, cap, 8 * p, ghist + 256 * p,
 			                                            status + (size_t) p * 256 * nb, tickets + p, &P.ctr->errors,
 			                                            kout, vout);
 			uint32_t* t = kin; kin = kout; kout = t;
@@ -208,7 +212,7 @@ void launchTileRanges(const DrawParams& P, const uint32_t* keys, uint32_t numTil
 	const uint32_t cap = P.entryCap;
 	if (!cap) return;
 	const uint32_t blocks = (cap + 255) / 256 < 152u * 16u ? (cap + 255) / 256 : 152u * 16u;
-	k_tile_ranges<<<blocks, 256, 0, s>>>(keys, P.ctr, cap, numTiles, P.tileStart, P.tileEnd);
+	pdlLaunch(k_tile_ranges, blocks, 256, 0, s, keys, P.ctr, cap, numTiles, P.tileStart, P.tileEnd);
 }
 
 }  // namespace srpg

@@ -18,6 +18,7 @@
 
 #include "device_common.cuh"
 #include "kernels.h"
+#include "launch.cuh"
 #include "srp/buffer.h"
 
 namespace srpg {
@@ -35,6 +36,7 @@ namespace srpg {
 
 __global__ void k_reset(const __grid_constant__ DrawParams P)
 {
+	gridDepSync();
 	if (threadIdx.x == 0) {
 		/* per-draw counters start at zero; the fragment total accumulates */
 		DeviceCounters c = {};
@@ -49,6 +51,7 @@ __global__ void k_reset(const __grid_constant__ DrawParams P)
  * buffer it was meant for, or a bad index, stops the rest of the draw. */
 __global__ void k_check(const __grid_constant__ DrawParams P)
 {
+	gridDepSync();
 	if (threadIdx.x != 0) return;
 	const DeviceCounters& c = *P.ctr;
 	const bool over = c.clipVerts > P.clipCap || c.prims > P.primCap || c.entries > P.entryCap ||
@@ -102,6 +105,7 @@ __device__ __forceinline__ void wordRange(const uint4& q, unsigned long long at,
  * buffers are allocated with 16 bytes of slack. */
 __global__ void k_index_range(const __grid_constant__ DrawParams P)
 {
+	gridDepSync();
 	const unsigned long long isz = (unsigned long long) P.indexSize;
 	const unsigned long long b0 = P.start * isz, b1 = (P.start + P.count) * isz;
 	const unsigned long long w0 = b0 >> 4, w1 = (b1 + 15) >> 4;
@@ -220,6 +224,7 @@ template <int VS>
 __global__ void __launch_bounds__(kVertexThreads) k_vertex(const __grid_constant__ DrawParams P,
                                                              unsigned long long first, unsigned long long n)
 {
+	gridDepSync();
 	extern __shared__ uint32_t stage[];
 	unsigned long long lo, hi;
 	if (P.indexSize) { lo = P.minmax[0]; hi = P.minmax[1]; }
@@ -731,6 +736,7 @@ __device__ __forceinline__ unsigned long long orderedOffset(const DrawParams& P,
 template <int MODE>
 __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup(const __grid_constant__ DrawParams P)
 {
+	gridDepSync();
 	__shared__ uint32_t sBlock;
 	__shared__ unsigned long long sWarp[kSetupThreads / 32];
 	__shared__ unsigned long long sPrefix;
@@ -881,6 +887,7 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup(cons
  * goes to a slot that k_setup reads back. */
 __global__ void __launch_bounds__(kSetupThreads, 16) k_clip_prepass(const __grid_constant__ DrawParams P)
 {
+	gridDepSync();
 	const long long k = (long long) blockIdx.x * blockDim.x + threadIdx.x;
 	if (k >= P.nIn) return;
 	unsigned long long s[3];
@@ -936,6 +943,7 @@ __device__ void fillLambdaTable(const DrawParams& P, const TriRaster& R, int fir
  * primitive writes its tiles row by row (and a triangle's lambda table). */
 __global__ void k_big_entries(const __grid_constant__ DrawParams P)
 {
+	gridDepSync();
 	if (P.ctr->abort) return;
 	const uint32_t nJobs = (uint32_t) min(P.ctr->bigJobs, (unsigned long long) P.bigCap);
 	for (uint32_t j = blockIdx.x; j < nJobs; j += gridDim.x) {
@@ -963,6 +971,7 @@ __global__ void k_big_entries(const __grid_constant__ DrawParams P)
  * blockIdx.x blocks of a job share its (row, column-run) work items. */
 __global__ void k_lambda_tables(const __grid_constant__ DrawParams P)
 {
+	gridDepSync();
 	if (P.ctr->abort) return;
 	const uint32_t nJobs = (uint32_t) min(P.ctr->bigJobs, (unsigned long long) P.bigCap);
 	for (uint32_t j = blockIdx.y; j < nJobs; j += gridDim.y) {
@@ -1022,6 +1031,7 @@ constexpr uint32_t kShortLine = 48;   /* steps one thread walks on its own */
  * k_line_frags_long. */
 __global__ void k_line_frags(const __grid_constant__ DrawParams P)
 {
+	gridDepSync();
 	if (P.ctr->abort) return;
 	const uint32_t nLines = (uint32_t) min(P.ctr->prims, (unsigned long long) P.primCap);
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1043,6 +1053,7 @@ __global__ void k_line_frags(const __grid_constant__ DrawParams P)
 /* Long lines: one warp per line, lane l walks a contiguous run of steps. */
 __global__ void k_line_frags_long(const __grid_constant__ DrawParams P)
 {
+	gridDepSync();
 	if (P.ctr->abort) return;
 	const uint32_t lane = threadIdx.x & 31;
 	const uint32_t nLong = (uint32_t) min(P.ctr->lineFrags, (unsigned long long) P.bigCap);
@@ -1087,6 +1098,7 @@ __device__ __forceinline__ uint32_t drawOf(const uint32_t* prefix, uint32_t n, u
 template <int VS>
 __global__ void __launch_bounds__(kVertexThreads) k_vertex_multi(const __grid_constant__ DrawParams P)
 {
+	gridDepSync();
 	extern __shared__ uint32_t stage[];
 	const uint32_t d = drawOf(P.blkPrefix, P.nDraws, blockIdx.x);
 	const DrawDesc& D = P.draws[d];
@@ -1176,6 +1188,7 @@ __device__ __forceinline__ bool triangleOfPass(const DrawParams& P, uint32_t k, 
 /* Clip pre-pass of a pass (see k_clip_prepass). */
 __global__ void __launch_bounds__(kSetupThreads, 16) k_clip_prepass_multi(const __grid_constant__ DrawParams P)
 {
+	gridDepSync();
 	const long long k = (long long) blockIdx.x * blockDim.x + threadIdx.x;
 	if (k >= P.nIn) return;
 	uint32_t d, vi[3];
@@ -1237,6 +1250,7 @@ __device__ __forceinline__ void writeTriMulti(const DrawParams& P, uint32_t d, i
  * which primitive ids local to the draw are recovered. */
 __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup_multi(const __grid_constant__ DrawParams P)
 {
+	gridDepSync();
 	__shared__ uint32_t sBlock;
 	__shared__ unsigned long long sWarp[kSetupThreads / 32];
 	__shared__ unsigned long long sPrefix;
@@ -1333,6 +1347,7 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup_mult
 /* k_big_entries for a pass: the job's third word is its draw. */
 __global__ void k_big_entries_multi(const __grid_constant__ DrawParams P)
 {
+	gridDepSync();
 	if (P.ctr->abort) return;
 	const uint32_t nJobs = (uint32_t) min(P.ctr->bigJobs, (unsigned long long) P.bigCap);
 	for (uint32_t j = blockIdx.x; j < nJobs; j += gridDim.x) {
@@ -1355,6 +1370,7 @@ __global__ void k_big_entries_multi(const __grid_constant__ DrawParams P)
 /* Lambda tables of a pass's big triangles (every job is a triangle). */
 __global__ void k_lambda_tables_multi(const __grid_constant__ DrawParams P)
 {
+	gridDepSync();
 	if (P.ctr->abort) return;
 	const uint32_t nJobs = (uint32_t) min(P.ctr->bigJobs, (unsigned long long) P.bigCap);
 	for (uint32_t j = blockIdx.y; j < nJobs; j += gridDim.y) {
@@ -1365,7 +1381,7 @@ __global__ void k_lambda_tables_multi(const __grid_constant__ DrawParams P)
 
 /* ------------------------------------------------------------ launchers */
 
-void launchReset(const DrawParams& P, cudaStream_t s) { k_reset<<<1, 32, 0, s>>>(P); }
+void launchReset(const DrawParams& P, cudaStream_t s) { pdlLaunch(k_reset, 1, 32, 0, s, P); }
 
 void launchIndexRange(const DrawParams& P, cudaStream_t s)
 {
@@ -1374,7 +1390,7 @@ void launchIndexRange(const DrawParams& P, cudaStream_t s)
 	unsigned long long blocks = (words + 511) / 512;
 	if (blocks > 152 * 8) blocks = 152 * 8;
 	if (blocks < 1) blocks = 1;
-	k_index_range<<<(unsigned) blocks, 256, 0, s>>>(P);
+	pdlLaunch(k_index_range, (unsigned) blocks, 256, 0, s, P);
 }
 
 void launchVertex(const DrawParams& P, unsigned long long first, unsigned long long n, cudaStream_t s)
@@ -1385,11 +1401,11 @@ void launchVertex(const DrawParams& P, unsigned long long first, unsigned long l
 	switch (P.vsId) {
 	case SRP_GPU_VS_WORLD:
 		cudaFuncSetAttribute(k_vertex<SRP_GPU_VS_WORLD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-		k_vertex<SRP_GPU_VS_WORLD><<<blocks, kVertexThreads, smem, s>>>(P, first, n);
+		pdlLaunch(k_vertex<SRP_GPU_VS_WORLD>, blocks, kVertexThreads, smem, s, P, first, n);
 		break;
 	default:
 		cudaFuncSetAttribute(k_vertex<SRP_GPU_VS_TRANSFORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-		k_vertex<SRP_GPU_VS_TRANSFORM><<<blocks, kVertexThreads, smem, s>>>(P, first, n);
+		pdlLaunch(k_vertex<SRP_GPU_VS_TRANSFORM>, blocks, kVertexThreads, smem, s, P, first, n);
 		break;
 	}
 }
@@ -1399,17 +1415,17 @@ void launchSetup(const DrawParams& P, cudaStream_t s)
 	const unsigned blocks = (unsigned) ((P.nIn + kSetupThreads - 1) / kSetupThreads);
 	if (!blocks) return;
 	const bool tri = P.prim == SRP_PRIM_TRIANGLES || P.prim == SRP_PRIM_TRIANGLE_STRIP || P.prim == SRP_PRIM_TRIANGLE_FAN;
-	if (tri && P.st.polygonMode == SRP_POLYGON_MODE_LINE) k_setup<kTriLine><<<blocks, kSetupThreads, 0, s>>>(P);
-	else if (tri && P.st.polygonMode == SRP_POLYGON_MODE_POINT) k_setup<kTriPoint><<<blocks, kSetupThreads, 0, s>>>(P);
-	else if (tri) k_setup<kTriFill><<<blocks, kSetupThreads, 0, s>>>(P);
-	else if (P.prim == SRP_PRIM_POINTS) k_setup<kPoints><<<blocks, kSetupThreads, 0, s>>>(P);
-	else k_setup<kLines><<<blocks, kSetupThreads, 0, s>>>(P);
+	if (tri && P.st.polygonMode == SRP_POLYGON_MODE_LINE) pdlLaunch(k_setup<kTriLine>, blocks, kSetupThreads, 0, s, P);
+	else if (tri && P.st.polygonMode == SRP_POLYGON_MODE_POINT) pdlLaunch(k_setup<kTriPoint>, blocks, kSetupThreads, 0, s, P);
+	else if (tri) pdlLaunch(k_setup<kTriFill>, blocks, kSetupThreads, 0, s, P);
+	else if (P.prim == SRP_PRIM_POINTS) pdlLaunch(k_setup<kPoints>, blocks, kSetupThreads, 0, s, P);
+	else pdlLaunch(k_setup<kLines>, blocks, kSetupThreads, 0, s, P);
 }
 
 void launchClipPrepass(const DrawParams& P, cudaStream_t s)
 {
 	const unsigned blocks = (unsigned) ((P.nIn + kSetupThreads - 1) / kSetupThreads);
-	if (blocks) k_clip_prepass<<<blocks, kSetupThreads, 0, s>>>(P);
+	if (blocks) pdlLaunch(k_clip_prepass, blocks, kSetupThreads, 0, s, P);
 }
 
 /* Grids for a job count the device holds: sized from the hint, any size is
@@ -1417,19 +1433,19 @@ void launchClipPrepass(const DrawParams& P, cudaStream_t s)
 static unsigned bigBlocks(uint32_t hint) { return hint < 64u ? 64u : (hint < 152u * 16u ? hint : 152u * 16u); }
 static unsigned tableRows(uint32_t hint) { return hint < 64u ? 64u : (hint < 65535u ? hint : 65535u); }
 
-void launchCheck(const DrawParams& P, cudaStream_t s) { k_check<<<1, 32, 0, s>>>(P); }
+void launchCheck(const DrawParams& P, cudaStream_t s) { pdlLaunch(k_check, 1, 32, 0, s, P); }
 
 void launchBigEntries(const DrawParams& P, uint32_t jobsHint, cudaStream_t s)
 {
-	k_big_entries<<<bigBlocks(jobsHint), 256, 0, s>>>(P);
-	k_lambda_tables<<<dim3(8, tableRows(jobsHint)), 256, 0, s>>>(P);
+	pdlLaunch(k_big_entries, bigBlocks(jobsHint), 256, 0, s, P);
+	pdlLaunch(k_lambda_tables, dim3(8, tableRows(jobsHint)), 256, 0, s, P);
 }
 
 void launchLineFrags(const DrawParams& P, cudaStream_t s)
 {
 	if (!P.primCap) return;
-	k_line_frags<<<(P.primCap + 127) / 128, 128, 0, s>>>(P);
-	k_line_frags_long<<<152 * 8, 128, 0, s>>>(P);
+	pdlLaunch(k_line_frags, (P.primCap + 127) / 128, 128, 0, s, P);
+	pdlLaunch(k_line_frags_long, 152 * 8, 128, 0, s, P);
 }
 
 void launchVertexMulti(const DrawParams& P, uint32_t blocks, int maxStride, cudaStream_t s)
@@ -1439,11 +1455,11 @@ void launchVertexMulti(const DrawParams& P, uint32_t blocks, int maxStride, cuda
 	switch (P.vsId) {
 	case SRP_GPU_VS_WORLD:
 		cudaFuncSetAttribute(k_vertex_multi<SRP_GPU_VS_WORLD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-		k_vertex_multi<SRP_GPU_VS_WORLD><<<blocks, kVertexThreads, smem, s>>>(P);
+		pdlLaunch(k_vertex_multi<SRP_GPU_VS_WORLD>, blocks, kVertexThreads, smem, s, P);
 		break;
 	default:
 		cudaFuncSetAttribute(k_vertex_multi<SRP_GPU_VS_TRANSFORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-		k_vertex_multi<SRP_GPU_VS_TRANSFORM><<<blocks, kVertexThreads, smem, s>>>(P);
+		pdlLaunch(k_vertex_multi<SRP_GPU_VS_TRANSFORM>, blocks, kVertexThreads, smem, s, P);
 		break;
 	}
 }
@@ -1451,19 +1467,19 @@ void launchVertexMulti(const DrawParams& P, uint32_t blocks, int maxStride, cuda
 void launchClipPrepassMulti(const DrawParams& P, cudaStream_t s)
 {
 	const unsigned blocks = (unsigned) ((P.nIn + kSetupThreads - 1) / kSetupThreads);
-	if (blocks) k_clip_prepass_multi<<<blocks, kSetupThreads, 0, s>>>(P);
+	if (blocks) pdlLaunch(k_clip_prepass_multi, blocks, kSetupThreads, 0, s, P);
 }
 
 void launchSetupMulti(const DrawParams& P, cudaStream_t s)
 {
 	const unsigned blocks = (unsigned) ((P.nIn + kSetupThreads - 1) / kSetupThreads);
-	if (blocks) k_setup_multi<<<blocks, kSetupThreads, 0, s>>>(P);
+	if (blocks) pdlLaunch(k_setup_multi, blocks, kSetupThreads, 0, s, P);
 }
 
 void launchBigEntriesMulti(const DrawParams& P, uint32_t jobsHint, cudaStream_t s)
 {
-	k_big_entries_multi<<<bigBlocks(jobsHint), 256, 0, s>>>(P);
-	k_lambda_tables_multi<<<dim3(8, tableRows(jobsHint)), 256, 0, s>>>(P);
+	pdlLaunch(k_big_entries_multi, bigBlocks(jobsHint), 256, 0, s, P);
+	pdlLaunch(k_lambda_tables_multi, dim3(8, tableRows(jobsHint)), 256, 0, s, P);
 }
 
 }  // namespace srpg

@@ -22,6 +22,7 @@
 
 #include "device_common.cuh"
 #include "kernels.h"
+#include "launch.cuh"
 #include "mlp.h"
 #include "tc5.cuh"
 #include "srp/buffer.h"
@@ -389,6 +390,7 @@ template <int KIND, int LATE_FS, bool MULTI = false>
 __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve(const __grid_constant__ DrawParams P,
                                                                const uint32_t* vals, uint32_t numTiles)
 {
+	gridDepSync();
 	__shared__ unsigned long long sMask[kResolveWarps][32];
 	__shared__ uint32_t sItem[kResolveWarps][32];
 	__shared__ uint32_t sFlag[kResolveWarps][32];
@@ -555,6 +557,7 @@ template <int KIND, bool MULTI = false>
 __global__ void __launch_bounds__(kHeavyThreads) k_resolve_heavy(const __grid_constant__ DrawParams P,
                                                                 const uint32_t* vals, const uint32_t* heavy)
 {
+	gridDepSync();
 	extern __shared__ float hDep[];                 /* [kHeavyThreads][kDepRow] */
 	__shared__ uint32_t ballots[kHeavyThreads / 32][64];
 	__shared__ uint32_t hFlag[kHeavyThreads], hItem[kHeavyThreads];
@@ -633,6 +636,7 @@ __global__ void __launch_bounds__(kHeavyThreads) k_resolve_heavy(const __grid_co
 /* Lists the tiles with more than P.heavyItems items for k_resolve_heavy. */
 __global__ void k_tile_classify(const __grid_constant__ DrawParams P, uint32_t numTiles, uint32_t* heavy)
 {
+	gridDepSync();
 	const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
 	if (t >= numTiles || P.ctr->abort) return;
 	const uint32_t n = P.tileEnd[t] - P.tileStart[t];
@@ -644,6 +648,7 @@ __global__ void k_tile_classify(const __grid_constant__ DrawParams P, uint32_t n
 template <int KIND, int FS, bool MULTI = false>
 __global__ void __launch_bounds__(kResolveWarps * 32) k_shade(const __grid_constant__ DrawParams P, uint32_t numTiles)
 {
+	gridDepSync();
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	const uint32_t tile = blockIdx.x * kResolveWarps + warp;
 	if (tile >= numTiles || P.ctr->abort) return;
@@ -695,6 +700,7 @@ __device__ __noinline__ void judgeShade(const DrawParams& P, const unsigned char
 template <int KIND, int FS, bool MULTI>
 __global__ void __launch_bounds__(128) k_shade_learned5(const __grid_constant__ DrawParams P, uint32_t numTiles)
 {
+	gridDepSync();
 	extern __shared__ __align__(1024) uint8_t tsm[];
 	uint8_t* sW = tsm;
 	uint8_t* sA = tsm + kTcWBytes;
@@ -833,14 +839,14 @@ static void launchHeavy(const DrawParams& P, const uint32_t* vals, uint32_t* hea
 	const int smem = kHeavyThreads * kDepRow * 4;
 	cudaFuncSetAttribute(k_resolve_heavy<KIND, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 	const unsigned perSM = P.heavyCtasPerSM >= 1 && P.heavyCtasPerSM <= 3 ? P.heavyCtasPerSM : 3u;
-	k_resolve_heavy<KIND, MULTI><<<152 * perSM, kHeavyThreads, smem, s>>>(P, vals, heavy);
+	pdlLaunch(k_resolve_heavy<KIND, MULTI>, 152 * perSM, kHeavyThreads, smem, s, P, vals, heavy);
 }
 
 void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, uint32_t* heavy, cudaStream_t s,
                    cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join)
 {
 	const unsigned b = tileBlocks(numTiles);
-	k_tile_classify<<<(numTiles + 255) / 256, 256, 0, s>>>(P, numTiles, heavy);
+	pdlLaunch(k_tile_classify, (numTiles + 255) / 256, 256, 0, s, P, numTiles, heavy);
 	const bool split = aux && fork && join;
 	cudaStream_t hs = s;
 	if (split) {
@@ -850,13 +856,13 @@ void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t
 	}
 	if (kind == kKindTri) {
 		launchHeavy<kKindTri>(P, vals, heavy, hs);
-		k_resolve<kKindTri, 0><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+		pdlLaunch(k_resolve<kKindTri, 0>, b, kResolveWarps * 32, 0, s, P, vals, numTiles);
 	} else if (kind == kKindPoint) {
 		launchHeavy<kKindPoint>(P, vals, heavy, hs);
-		k_resolve<kKindPoint, 0><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+		pdlLaunch(k_resolve<kKindPoint, 0>, b, kResolveWarps * 32, 0, s, P, vals, numTiles);
 	} else {
 		launchHeavy<kKindLineFrag>(P, vals, heavy, hs);
-		k_resolve<kKindLineFrag, 0><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+		pdlLaunch(k_resolve<kKindLineFrag, 0>, b, kResolveWarps * 32, 0, s, P, vals, numTiles);
 	}
 	if (split) {
 		cudaEventRecord(join, aux);
@@ -869,9 +875,9 @@ bool shadeSupportsLateDepth(int fsId) { return fsId == SRP_GPU_FS_DEPTH_OVERWRIT
 void launchResolveLate(const DrawParams& P, int kind, const uint32_t* vals, uint32_t numTiles, cudaStream_t s)
 {
 	const unsigned b = tileBlocks(numTiles);
-	if (kind == kKindTri) k_resolve<kKindTri, SRP_GPU_FS_DEPTH_OVERWRITE><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
-	else if (kind == kKindPoint) k_resolve<kKindPoint, SRP_GPU_FS_DEPTH_OVERWRITE><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
-	else k_resolve<kKindLineFrag, SRP_GPU_FS_DEPTH_OVERWRITE><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+	if (kind == kKindTri) pdlLaunch(k_resolve<kKindTri, SRP_GPU_FS_DEPTH_OVERWRITE>, b, kResolveWarps * 32, 0, s, P, vals, numTiles);
+	else if (kind == kKindPoint) pdlLaunch(k_resolve<kKindPoint, SRP_GPU_FS_DEPTH_OVERWRITE>, b, kResolveWarps * 32, 0, s, P, vals, numTiles);
+	else pdlLaunch(k_resolve<kKindLineFrag, SRP_GPU_FS_DEPTH_OVERWRITE>, b, kResolveWarps * 32, 0, s, P, vals, numTiles);
 }
 
 template <int KIND, bool MULTI = false>
@@ -880,16 +886,16 @@ static void shadeKind(const DrawParams& P, uint32_t numTiles, cudaStream_t s)
 	const unsigned b = tileBlocks(numTiles);
 	const unsigned t = kResolveWarps * 32;
 	switch (P.fsId) {
-	case SRP_GPU_FS_VARYING_COLOR: k_shade<KIND, SRP_GPU_FS_VARYING_COLOR, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_SOLID: k_shade<KIND, SRP_GPU_FS_SOLID, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_PRIMITIVE_ID: k_shade<KIND, SRP_GPU_FS_PRIMITIVE_ID, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_TEXTURE: k_shade<KIND, SRP_GPU_FS_TEXTURE, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_TEXTURE_MODULATE: k_shade<KIND, SRP_GPU_FS_TEXTURE_MODULATE, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_BLINN_PHONG: k_shade<KIND, SRP_GPU_FS_BLINN_PHONG, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_MARBLE: k_shade<KIND, SRP_GPU_FS_MARBLE, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_DEPTH_OVERWRITE: k_shade<KIND, SRP_GPU_FS_DEPTH_OVERWRITE, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_FRAGCOORD: k_shade<KIND, SRP_GPU_FS_FRAGCOORD, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
-	case SRP_GPU_FS_FLAT_INT: k_shade<KIND, SRP_GPU_FS_FLAT_INT, MULTI><<<b, t, 0, s>>>(P, numTiles); break;
+	case SRP_GPU_FS_VARYING_COLOR: pdlLaunch(k_shade<KIND, SRP_GPU_FS_VARYING_COLOR, MULTI>, b, t, 0, s, P, numTiles); break;
+	case SRP_GPU_FS_SOLID: pdlLaunch(k_shade<KIND, SRP_GPU_FS_SOLID, MULTI>, b, t, 0, s, P, numTiles); break;
+	case SRP_GPU_FS_PRIMITIVE_ID: pdlLaunch(k_shade<KIND, SRP_GPU_FS_PRIMITIVE_ID, MULTI>, b, t, 0, s, P, numTiles); break;
+	case SRP_GPU_FS_TEXTURE: pdlLaunch(k_shade<KIND, SRP_GPU_FS_TEXTURE, MULTI>, b, t, 0, s, P, numTiles); break;
+	case SRP_GPU_FS_TEXTURE_MODULATE: pdlLaunch(k_shade<KIND, SRP_GPU_FS_TEXTURE_MODULATE, MULTI>, b, t, 0, s, P, numTiles); break;
+	case SRP_GPU_FS_BLINN_PHONG: pdlLaunch(k_shade<KIND, SRP_GPU_FS_BLINN_PHONG, MULTI>, b, t, 0, s, P, numTiles); break;
+	case SRP_GPU_FS_MARBLE: pdlLaunch(k_shade<KIND, SRP_GPU_FS_MARBLE, MULTI>, b, t, 0, s, P, numTiles); break;
+	case SRP_GPU_FS_DEPTH_OVERWRITE: pdlLaunch(k_shade<KIND, SRP_GPU_FS_DEPTH_OVERWRITE, MULTI>, b, t, 0, s, P, numTiles); break;
+	case SRP_GPU_FS_FRAGCOORD: pdlLaunch(k_shade<KIND, SRP_GPU_FS_FRAGCOORD, MULTI>, b, t, 0, s, P, numTiles); break;
+	case SRP_GPU_FS_FLAT_INT: pdlLaunch(k_shade<KIND, SRP_GPU_FS_FLAT_INT, MULTI>, b, t, 0, s, P, numTiles); break;
 	case kFsLearned:
 		if constexpr (KIND == kKindTri) {
 			/* a CTA per pair of tiles, a few CTAs per SM looping over the pairs */
@@ -897,7 +903,7 @@ static void shadeKind(const DrawParams& P, uint32_t numTiles, cudaStream_t s)
 			const unsigned blocks = pairs < 152u * 3u ? (pairs ? pairs : 1u) : 152u * 3u;
 			cudaFuncSetAttribute(k_shade_learned5<KIND, SRP_GPU_FS_MARBLE, MULTI>,
 			                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int) kTcSmem);
-			k_shade_learned5<KIND, SRP_GPU_FS_MARBLE, MULTI><<<blocks, 128, kTcSmem, s>>>(P, numTiles);
+			pdlLaunch(k_shade_learned5<KIND, SRP_GPU_FS_MARBLE, MULTI>, blocks, 128, kTcSmem, s, P, numTiles);
 		}
 		break;
 	default: break;
@@ -915,7 +921,7 @@ void launchResolveMulti(const DrawParams& P, const uint32_t* vals, uint32_t numT
                         cudaStream_t aux, cudaEvent_t fork, cudaEvent_t join)
 {
 	const unsigned b = tileBlocks(numTiles);
-	k_tile_classify<<<(numTiles + 255) / 256, 256, 0, s>>>(P, numTiles, heavy);
+	pdlLaunch(k_tile_classify, (numTiles + 255) / 256, 256, 0, s, P, numTiles, heavy);
 	const bool split = aux && fork && join;
 	cudaStream_t hs = s;
 	if (split) {
@@ -924,7 +930,7 @@ void launchResolveMulti(const DrawParams& P, const uint32_t* vals, uint32_t numT
 		hs = aux;
 	}
 	launchHeavy<kKindTri, true>(P, vals, heavy, hs);
-	k_resolve<kKindTri, 0, true><<<b, kResolveWarps * 32, 0, s>>>(P, vals, numTiles);
+	pdlLaunch(k_resolve<kKindTri, 0, true>, b, kResolveWarps * 32, 0, s, P, vals, numTiles);
 	if (split) {
 		cudaEventRecord(join, aux);
 		cudaStreamWaitEvent(s, join, 0);
