@@ -54,6 +54,26 @@ void srpGpuFramebufferUpload(const SRPFramebuffer* fb);
 /** Fill the selected device planes with constants (stream-ordered). */
 void srpGpuFramebufferFill(const SRPFramebuffer* fb, uint32_t color, float depth, uint8_t stencil,
                            unsigned planes);
+/** srpGpuFramebufferFill of n framebuffers in one launch. */
+void srpGpuFramebufferFillBatch(const SRPFramebuffer* const* fbs, size_t n, uint32_t color, float depth,
+                                uint8_t stencil, unsigned planes);
+
+/* ------------------------------------------- asynchronous transfers */
+
+/* Stream-ordered versions of the transfers for programs that move many
+ * buffers per frame: they only enqueue the copy and return. The host memory
+ * they read or write belongs to the library until the next srpGpuSynchronize
+ * (the caller must not change a source, nor read a destination, before it);
+ * from page-locked memory the copies then run at the host link's speed
+ * without a round trip per call. None has a counterpart in the reference. */
+
+/** srpVertexBufferCopyData without waiting for the copy. */
+void srpGpuVertexBufferCopyDataAsync(SRPVertexBuffer* buffer, size_t stride, size_t nBytes, const void* data);
+/** srpIndexBufferCopyData without waiting for the copy. */
+void srpGpuIndexBufferCopyDataAsync(SRPIndexBuffer* buffer, SRPType type, size_t nBytes, const void* data);
+/** srpGpuFramebufferSync without waiting: the host arrays are current after
+ *  the next srpGpuSynchronize. */
+void srpGpuFramebufferSyncAsync(const SRPFramebuffer* fb);
 
 /* ----------------------------------------------------- batched draws */
 
@@ -104,10 +124,11 @@ void srpGpuSetTuning(const SRPGpuTuning* tuning);
 int srpGpuAutotune(const SRPGpuDraw* draws, size_t n, int repeats, SRPGpuTuning* best);
 
 /** Online autotuner for a frame loop: call once after each frame's draws.
- *  Over the next 30 frames it tries the same candidates as srpGpuAutotune,
- *  two frames each (the second one timed with CUDA events), then keeps the
- *  fastest. Returns 1 while tuning, 0 once a tuning has been chosen (and on
- *  every later call, until srpGpuAutotuneReset). */
+ *  Over the next 60 frames it tries the same candidates as srpGpuAutotune,
+ *  four frames each (the last three timed one by one with CUDA events), then
+ *  keeps the candidate with the fastest frame. Returns 1 while tuning, 0 once
+ *  a tuning has been chosen (and on every later call, until
+ *  srpGpuAutotuneReset). */
 int srpGpuAutotuneFrame(void);
 void srpGpuAutotuneReset(void);
 

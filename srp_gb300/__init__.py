@@ -165,6 +165,10 @@ class Scene:
     def upload(self):
         self.S.sceneUpload(self.ptr)
 
+    def upload_async(self):
+        """upload() with srpGpu*CopyDataAsync: complete after srpGpuSynchronize."""
+        self.S.sceneUploadAsync(self.ptr)
+
     def prepare(self):
         self.S.scenePrepareFramebuffer(self.ptr, self.fb)
 
@@ -173,6 +177,10 @@ class Scene:
 
     def sync(self):
         self.S.srpGpuFramebufferSync(self.fb)
+
+    def sync_async(self):
+        """sync() with srpGpuFramebufferSyncAsync: complete after srpGpuSynchronize."""
+        self.S.srpGpuFramebufferSyncAsync(self.fb)
 
     def planes(self):
         self.sync()
@@ -209,6 +217,15 @@ def render_batch(batch, fbs):
     fp = (ctypes.c_void_p * n)(*fbs)
     scratch = (SRPGpuDraw * n)()
     S.sceneBatchRender(sp, fp, n, scratch)
+
+
+def prepare_batch(batch, fbs):
+    """Prepare the framebuffers of a batch in one srpGpuFramebufferFillBatch."""
+    S = scenes()
+    n = len(batch)
+    sp = (ctypes.c_void_p * n)(*[sc.ptr for sc in batch])
+    fp = (ctypes.c_void_p * n)(*fbs)
+    S.scenePrepareBatch(sp, fp, n)
 
 
 def autotune_batch(batch, fbs, repeats=1):

@@ -13,12 +13,15 @@
  * k_raster.cu; nothing is rendered on the host. */
 #include <cuda_runtime.h>
 #include <stdarg.h>
+#include <stddef.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
+#include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "srp/srp.h"
@@ -101,6 +104,7 @@ struct Lib {
 	/* scratch pools, grown on demand */
 	DeviceBuffer clip, vset0, vset1, vary, triR, triA, lines, points, frags, keys, vals, keys2, vals2, big, lookback;
 	DeviceBuffer hist, partials, tileStart, tileEnd, winner, minmax, ctr, table, heavy, clipSlot, clipPolys;
+	DeviceBuffer fillTargets;   /* srpGpuFramebufferFillBatch */
 	DeviceCounters* hostCtr = nullptr;
 	SRPGpuStats stats = {};
 	unsigned long long launches = 0;
@@ -394,6 +398,15 @@ static bool copyToDevice(DeviceBuffer& dev, const void* data, size_t nBytes, con
 	return true;
 }
 
+/* CopyData without the wait: the copy is only enqueued, and the caller keeps
+ * `data` unchanged until the stream has passed it. */
+static bool copyToDeviceAsync(DeviceBuffer& dev, const void* data, size_t nBytes, const char* fn)
+{
+	if (!ensureInit(fn) || !dev.reserve(nBytes + 16, fn)) return false;
+	if (!nBytes) return true;
+	return cudaOk(cudaMemcpyAsync(dev.ptr, data, nBytes, cudaMemcpyHostToDevice, g.stream), fn, "cudaMemcpyAsync");
+}
+
 static void* pinnedRealloc(void* old, size_t n)
 {
 	if (old) cudaFreeHost(old);
@@ -432,6 +445,16 @@ void srpVertexBufferCopyData(SRPVertexBuffer* b, size_t stride, size_t nBytes, c
 	b->dirty = true;
 }
 
+void srpGpuVertexBufferCopyDataAsync(SRPVertexBuffer* b, size_t stride, size_t nBytes, const void* data)
+{
+	if (!gpuPresent()) { srpVertexBufferCopyData(b, stride, nBytes, data); return; }
+	b->stride = stride;
+	b->nVertices = stride ? nBytes / stride : 0;
+	b->nBytes = nBytes;
+	b->dirty = !copyToDeviceAsync(b->dev, data, nBytes, "srpGpuVertexBufferCopyDataAsync");
+	if (b->dirty) srpVertexBufferCopyData(b, stride, nBytes, data);
+}
+
 SRPIndexBuffer* srpNewIndexBuffer(void) { return new SRPIndexBuffer(); }
 
 void srpFreeIndexBuffer(SRPIndexBuffer* b)
@@ -458,6 +481,17 @@ void srpIndexBufferCopyData(SRPIndexBuffer* b, SRPType type, size_t nBytes, cons
 	b->dirty = true;
 }
 
+void srpGpuIndexBufferCopyDataAsync(SRPIndexBuffer* b, SRPType type, size_t nBytes, const void* data)
+{
+	if (!gpuPresent()) { srpIndexBufferCopyData(b, type, nBytes, data); return; }
+	b->type = type;
+	b->elemSize = indexTypeSize(type);
+	b->nIndices = b->elemSize ? nBytes / b->elemSize : 0;
+	b->nBytes = nBytes;
+	b->dirty = !copyToDeviceAsync(b->dev, data, nBytes, "srpGpuIndexBufferCopyDataAsync");
+	if (b->dirty) srpIndexBufferCopyData(b, type, nBytes, data);
+}
+
 }  // extern "C"
 
 /* ------------------------------------------------------------ framebuffer */
@@ -470,18 +504,40 @@ struct FbExtra {
 };
 /* The public struct has no room for device pointers; they live in a side
  * table keyed by the framebuffer address. */
-std::vector<std::pair<const SRPFramebuffer*, FbExtra>> fbTable;
+std::unordered_map<const SRPFramebuffer*, FbExtra> fbTable;
 
 FbExtra* fbFind(const SRPFramebuffer* fb)
 {
-	for (auto& e : fbTable) if (e.first == fb) return &e.second;
-	return nullptr;
+	auto it = fbTable.find(fb);
+	return it == fbTable.end() ? nullptr : &it->second;
 }
 }  // namespace
 
 __global__ void k_fill32(uint32_t* p, uint32_t v, size_t n)
 {
 	for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n; i += (size_t) gridDim.x * blockDim.x) p[i] = v;
+}
+
+/* One framebuffer of srpGpuFramebufferFillBatch. */
+struct FillTarget {
+	uint32_t* color;
+	uint32_t* depth;
+	uint8_t* stencil;
+	size_t size;
+};
+
+/* blockIdx.y strides over the framebuffers, blockIdx.x over their pixels */
+__global__ void k_fill_batch(const FillTarget* t, size_t n, uint32_t color, uint32_t depth, uint8_t stencil,
+                             unsigned planes)
+{
+	for (size_t f = blockIdx.y; f < n; f += gridDim.y) {
+		const FillTarget T = t[f];
+		for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < T.size; i += (size_t) gridDim.x * blockDim.x) {
+			if (planes & SRP_GPU_FILL_COLOR) T.color[i] = color;
+			if (planes & SRP_GPU_FILL_DEPTH) T.depth[i] = depth;
+			if (planes & SRP_GPU_FILL_STENCIL) T.stencil[i] = stencil;
+		}
+	}
 }
 
 static void fill32(uint32_t* p, uint32_t v, size_t n)
@@ -492,18 +548,41 @@ static void fill32(uint32_t* p, uint32_t v, size_t n)
 	++g.launches;
 }
 
+/* The planes of a framebuffer made by srpNewFramebuffer are one block on
+ * each side (colour, depth, stencil); a program may have pointed the public
+ * arrays elsewhere, in which case they are copied one by one. */
+static bool fbContiguous(const SRPFramebuffer* fb)
+{
+	const size_t n = fb->size ? fb->size : 1;
+	return (unsigned char*) fb->depth == (unsigned char*) fb->color + 4 * n &&
+	       fb->stencil == (unsigned char*) fb->color + 8 * n;
+}
+
 static void fbUpload(const SRPFramebuffer* fb, FbExtra* x)
 {
+	if (fbContiguous(fb)) {
+		cudaMemcpyAsync(x->color, fb->color, 9 * fb->size, cudaMemcpyHostToDevice, g.stream);
+		return;
+	}
 	cudaMemcpyAsync(x->color, fb->color, 4 * fb->size, cudaMemcpyHostToDevice, g.stream);
 	cudaMemcpyAsync(x->depth, fb->depth, 4 * fb->size, cudaMemcpyHostToDevice, g.stream);
 	cudaMemcpyAsync(x->stencil, fb->stencil, fb->size, cudaMemcpyHostToDevice, g.stream);
 }
 
-static void fbDownload(const SRPFramebuffer* fb, FbExtra* x)
+static void fbDownloadAsync(const SRPFramebuffer* fb, FbExtra* x)
 {
+	if (fbContiguous(fb)) {
+		cudaMemcpyAsync(fb->color, x->color, 9 * fb->size, cudaMemcpyDeviceToHost, g.stream);
+		return;
+	}
 	cudaMemcpyAsync(fb->color, x->color, 4 * fb->size, cudaMemcpyDeviceToHost, g.stream);
 	cudaMemcpyAsync(fb->depth, x->depth, 4 * fb->size, cudaMemcpyDeviceToHost, g.stream);
 	cudaMemcpyAsync(fb->stencil, x->stencil, fb->size, cudaMemcpyDeviceToHost, g.stream);
+}
+
+static void fbDownload(const SRPFramebuffer* fb, FbExtra* x)
+{
+	fbDownloadAsync(fb, x);
 	cudaStreamSynchronize(g.stream);
 }
 
@@ -518,21 +597,22 @@ SRPFramebuffer* srpNewFramebuffer(size_t w, size_t h)
 	}
 	SRPFramebuffer* fb = (SRPFramebuffer*) calloc(1, sizeof(SRPFramebuffer));
 	fb->width = w; fb->height = h; fb->size = w * h;
-	fb->color = (uint32_t*) pinnedRealloc(nullptr, 4 * fb->size);
-	fb->depth = (float*) pinnedRealloc(nullptr, 4 * fb->size);
-	fb->stencil = (uint8_t*) pinnedRealloc(nullptr, fb->size);
-	memset(fb->color, 0, 4 * fb->size);
-	memset(fb->depth, 0, 4 * fb->size);
-	memset(fb->stencil, 0, fb->size);
-	FbExtra x;
+	/* the three planes, host and device alike, are one block each:
+	 * colour (4 B/px), depth (4 B/px), stencil (1 B/px), so that a sync is one copy */
 	const size_t n = fb->size ? fb->size : 1;
-	if (!cudaOk(cudaMalloc(&x.color, 4 * n), "srpNewFramebuffer", "cudaMalloc") ||
-	    !cudaOk(cudaMalloc(&x.depth, 4 * n), "srpNewFramebuffer", "cudaMalloc") ||
-	    !cudaOk(cudaMalloc(&x.stencil, n), "srpNewFramebuffer", "cudaMalloc")) return fb;
-	cudaMemsetAsync(x.color, 0, 4 * n, g.stream);
-	cudaMemsetAsync(x.depth, 0, 4 * n, g.stream);
-	cudaMemsetAsync(x.stencil, 0, n, g.stream);
-	fbTable.push_back({ fb, x });
+	unsigned char* host = (unsigned char*) pinnedRealloc(nullptr, 9 * n);
+	memset(host, 0, 9 * n);
+	fb->color = (uint32_t*) host;
+	fb->depth = (float*) (host + 4 * n);
+	fb->stencil = host + 8 * n;
+	FbExtra x;
+	unsigned char* dev = nullptr;
+	if (!cudaOk(cudaMalloc(&dev, 9 * n), "srpNewFramebuffer", "cudaMalloc")) return fb;
+	x.color = (uint32_t*) dev;
+	x.depth = (float*) (dev + 4 * n);
+	x.stencil = dev + 8 * n;
+	cudaMemsetAsync(dev, 0, 9 * n, g.stream);
+	fbTable[fb] = x;
 	return fb;
 }
 
@@ -540,17 +620,12 @@ void srpFreeFramebuffer(SRPFramebuffer* fb)
 {
 	if (!fb) return;
 	cudaStreamSynchronize(g.stream);
-	for (size_t i = 0; i < fbTable.size(); ++i)
-		if (fbTable[i].first == fb) {
-			cudaFree(fbTable[i].second.color);
-			cudaFree(fbTable[i].second.depth);
-			cudaFree(fbTable[i].second.stencil);
-			fbTable.erase(fbTable.begin() + (long) i);
-			break;
-		}
-	cudaFreeHost(fb->color);
-	cudaFreeHost(fb->depth);
-	cudaFreeHost(fb->stencil);
+	auto it = fbTable.find(fb);
+	if (it != fbTable.end()) {
+		cudaFree(it->second.color);  /* base of the planes' block */
+		fbTable.erase(it);
+	}
+	cudaFreeHost(fb->color);  /* base of the planes' block */
 	free(fb);
 }
 
@@ -573,6 +648,42 @@ void srpGpuFramebufferSync(const SRPFramebuffer* fb)
 {
 	FbExtra* x = fbFind(fb);
 	if (x) fbDownload(fb, x);
+}
+
+void srpGpuFramebufferSyncAsync(const SRPFramebuffer* fb)
+{
+	FbExtra* x = fbFind(fb);
+	if (x) fbDownloadAsync(fb, x);
+}
+
+void srpGpuFramebufferFillBatch(const SRPFramebuffer* const* fbs, size_t n, uint32_t color, float depth,
+                                uint8_t stencil, unsigned planes)
+{
+	const char* FN = "srpGpuFramebufferFillBatch";
+	if (!n || !fbs || !ensureInit(FN)) return;
+	std::vector<FillTarget> t;
+	t.reserve(n);
+	for (size_t i = 0; i < n; ++i) {
+		FbExtra* x = fbFind(fbs[i]);
+		if (!x) { SRP_ERROR(FN, "Framebuffer %zu was not created by srpNewFramebuffer", i); return; }
+		t.push_back(FillTarget{ x->color, (uint32_t*) x->depth, x->stencil, fbs[i]->size });
+	}
+	if (!g.fillTargets.reserve(n * sizeof(FillTarget), FN)) return;
+	/* from pageable memory: returns once the host vector has been read */
+	if (!cudaOk(cudaMemcpyAsync(g.fillTargets.ptr, t.data(), n * sizeof(FillTarget), cudaMemcpyHostToDevice, g.stream),
+	            FN, "cudaMemcpyAsync")) return;
+	uint32_t dbits;
+	memcpy(&dbits, &depth, 4);
+	const unsigned ys = (unsigned) std::min<size_t>(n, 65535);
+	k_fill_batch<<<dim3(16, ys), 256, 0, g.stream>>>(g.fillTargets.as<FillTarget>(), n, color, dbits, stencil, planes);
+	++g.launches;
+	if (g.fbMode == SRP_GPU_FB_COHERENT)
+		for (size_t i = 0; i < n; ++i)
+			for (size_t p = 0; p < fbs[i]->size; ++p) {
+				if (planes & SRP_GPU_FILL_COLOR) fbs[i]->color[p] = color;
+				if (planes & SRP_GPU_FILL_DEPTH) fbs[i]->depth[p] = depth;
+				if (planes & SRP_GPU_FILL_STENCIL) fbs[i]->stencil[p] = stencil;
+			}
 }
 
 void srpGpuFramebufferUpload(const SRPFramebuffer* fb)
@@ -1171,7 +1282,28 @@ size_t passInputs(const SRPGpuDraw& d)
 	return n <= 0x7FFFFFFFull ? n : 0;
 }
 
-std::vector<DrawDesc> passDesc;
+/* Page-locked host staging that only grows. */
+struct PinnedBuffer {
+	void* ptr = nullptr;
+	size_t bytes = 0;
+	bool reserve(size_t need)
+	{
+		if (need <= bytes) return true;
+		if (ptr) cudaFreeHost(ptr);
+		ptr = nullptr;
+		bytes = 0;
+		const size_t nb = std::max(need, bytes + bytes / 2);
+		if (cudaMallocHost(&ptr, nb) != cudaSuccess) { cudaGetLastError(); return false; }
+		bytes = nb;
+		return true;
+	}
+	template <class T> T* as() const { return (T*) ptr; }
+};
+
+/* The descriptors and prefix sums of a pass are staged in page-locked memory
+ * so that their upload is asynchronous; a pass waits for its setup counters,
+ * which follow the upload on the stream, before the staging is reused. */
+PinnedBuffer passDesc;
 std::vector<uint32_t> passPrefix;   /* in, v, t, blk: 4 x (n + 1) */
 DeviceBuffer passDescDev, passPrefixDev, passPrimPrefix, passWinner;
 
@@ -1218,7 +1350,11 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	P.prim = SRP_PRIM_TRIANGLES;
 
 	/* descriptors and prefix sums */
-	passDesc.assign(n, DrawDesc());
+	if (!passDesc.reserve(n * sizeof(DrawDesc))) {
+		SRP_ERROR(FN, "cudaMallocHost failed for %zu draw descriptors", n);
+		return false;
+	}
+	DrawDesc* desc = passDesc.as<DrawDesc>();
 	passPrefix.assign(4 * (n + 1), 0u);
 	uint32_t* pIn = passPrefix.data();
 	uint32_t* pV = pIn + (n + 1);
@@ -1233,7 +1369,8 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		SRPIndexBuffer* ib = (SRPIndexBuffer*) d.indexBuffer;
 		if (!uploadVB(vb) || (ib && !uploadIB(ib))) return false;
 		FbExtra* fx = fbFind(d.framebuffer);
-		DrawDesc& D = passDesc[k];
+		DrawDesc& D = desc[k];
+		memset(&D, 0, offsetof(DrawDesc, uniform));
 		D.vertices = vb->dev.as<unsigned char>();
 		D.indices = ib ? ib->dev.ptr : nullptr;
 		D.indexSize = ib ? (int) ib->elemSize : 0;
@@ -1256,6 +1393,8 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 				u.texture = (SRPTexture*) t->desc;
 			}
 			memcpy(D.uniform, &u, sizeof u);
+		} else {
+			memset(D.uniform, 0, sizeof D.uniform);
 		}
 		maxStride = std::max(maxStride, D.stride);
 		pIn[k + 1] = pIn[k] + (uint32_t) nInOf[k];
@@ -1269,8 +1408,8 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	if (!passDescDev.reserve(n * sizeof(DrawDesc), FN) || !passPrefixDev.reserve(passPrefix.size() * 4, FN) ||
 	    !passPrimPrefix.reserve((n + 1) * 4, FN) || !passWinner.reserve(pix * 4 + 4, FN))
 		return false;
-	for (size_t k = 0; k < n; ++k) passDesc[k].winner = passWinner.as<int32_t>() + pixBase[k];
-	cudaMemcpyAsync(passDescDev.ptr, passDesc.data(), n * sizeof(DrawDesc), cudaMemcpyHostToDevice, g.stream);
+	for (size_t k = 0; k < n; ++k) desc[k].winner = passWinner.as<int32_t>() + pixBase[k];
+	cudaMemcpyAsync(passDescDev.ptr, desc, n * sizeof(DrawDesc), cudaMemcpyHostToDevice, g.stream);
 	cudaMemcpyAsync(passPrefixDev.ptr, passPrefix.data(), passPrefix.size() * 4, cudaMemcpyHostToDevice, g.stream);
 	P.draws = passDescDev.as<DrawDesc>();
 	P.nDraws = (uint32_t) n;
@@ -1442,28 +1581,34 @@ void srpGpuDrawBatch(const SRPGpuDraw* draws, size_t n)
 	const unsigned long long kMaxIn = 0x7FFFFFFFull, kMaxRows = 0x7FFFFFFFull - (1ull << 24), kMaxTiles = 1ull << 24;
 	size_t i = 0;
 	std::vector<size_t> idx, nInOf;
-	std::vector<const SRPFramebuffer*> fbs;
+	std::unordered_set<const SRPFramebuffer*> fbs;
 	while (i < n) {
 		idx.clear(); nInOf.clear(); fbs.clear();
 		unsigned long long in = 0, rows = 0, tiles = 0;
 		VaryingLayout L0;
 		int vs0 = 0, fs0 = 0;
+		const SRPVertexShader* vsSeen = nullptr;   /* a vertex shader whose layout equals L0 */
 		size_t j = i;
 		for (; j < n; ++j) {
 			const SRPGpuDraw& d = draws[j];
 			const size_t k = passInputs(d);
 			if (!k) break;
 			const int vs = lookupVS((void*) d.program->vs->shader), fs = lookupFS((void*) d.program->fs->shader);
-			VaryingLayout L;
-			if (!buildLayout(d.program->vs, L)) break;
-			if (idx.empty()) { L0 = L; vs0 = vs; fs0 = fs; }
-			else if (vs != vs0 || fs != fs0 || memcmp(&L, &L0, sizeof L) != 0) break;
-			if (std::find(fbs.begin(), fbs.end(), d.framebuffer) != fbs.end()) break;
+			if (d.program->vs != vsSeen || idx.empty()) {
+				VaryingLayout L;
+				if (!buildLayout(d.program->vs, L)) break;
+				if (idx.empty()) L0 = L;
+				else if (memcmp(&L, &L0, sizeof L) != 0) break;
+				vsSeen = d.program->vs;
+			}
+			if (idx.empty()) { vs0 = vs; fs0 = fs; }
+			else if (vs != vs0 || fs != fs0) break;
+			if (!fbs.insert(d.framebuffer).second) break;
 			const unsigned long long t = (unsigned long long) ((d.framebuffer->width + kTile - 1) / kTile) *
 			                             ((d.framebuffer->height + kTile - 1) / kTile);
 			if (in + k > kMaxIn || rows + d.vertexBuffer->nVertices > kMaxRows || tiles + t >= kMaxTiles) break;
 			in += k; rows += d.vertexBuffer->nVertices; tiles += t;
-			idx.push_back(j); nInOf.push_back(k); fbs.push_back(d.framebuffer);
+			idx.push_back(j); nInOf.push_back(k);
 		}
 		if (idx.size() >= 2) {
 			for (size_t k : idx) warnExcess(draws[k].primitive, draws[k].count);
@@ -1524,11 +1669,13 @@ void srpGpuSetTuning(const SRPGpuTuning* t)
 	g.tune.heavyCtasPerSM = t->heavyCtasPerSM >= 1 && t->heavyCtasPerSM <= 3 ? t->heavyCtasPerSM : 3;
 }
 
-/* Online autotuning of a frame loop: two frames per candidate (the first
- * captures the graphs of the new tuning, the second is timed). */
+/* Online autotuning of a frame loop: kTuneFrames frames per candidate, the
+ * first of which captures the graphs of the new tuning; the others are timed
+ * one by one and the candidate scores its fastest frame. */
 namespace {
+constexpr int kTuneFrames = 4;
 struct FrameTuner {
-	int state = -1;          /* -1 idle, 0..2n-1 running, -2 done */
+	int state = -1;          /* -1 idle, 0 .. kTuneFrames * candidates - 1 running, -2 done */
 	cudaEvent_t start = nullptr, stop = nullptr;
 	float best = -1.0f;
 	SRPGpuTuning bestTune = { 96, 3 };
@@ -1542,7 +1689,7 @@ int srpGpuAutotuneFrame(void)
 {
 	if (tuner.state == -2 || !ensureInit("srpGpuAutotuneFrame")) return 0;
 	if (!tuner.start) { tuner.start = takeEvent(); tuner.stop = takeEvent(); }
-	if (tuner.state >= 0 && (tuner.state & 1)) {
+	if (tuner.state >= 0 && tuner.state % kTuneFrames != 0) {
 		/* a timed frame just ended */
 		cudaEventRecord(tuner.stop, g.stream);
 		float ms = 0.0f;
@@ -1553,13 +1700,13 @@ int srpGpuAutotuneFrame(void)
 		}
 	}
 	++tuner.state;
-	if (tuner.state >= 2 * kTuneCandidates) {
+	if (tuner.state >= kTuneFrames * kTuneCandidates) {
 		g.tune = tuner.bestTune;
 		tuner.state = -2;
 		return 0;
 	}
-	g.tune = tuneCandidate(tuner.state / 2);
-	if (tuner.state & 1) cudaEventRecord(tuner.start, g.stream);
+	g.tune = tuneCandidate(tuner.state / kTuneFrames);
+	if (tuner.state % kTuneFrames != 0) cudaEventRecord(tuner.start, g.stream);
 	return 1;
 }
 

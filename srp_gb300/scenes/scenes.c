@@ -1453,6 +1453,27 @@ void sceneBatchRender(Scene** scenes, SRPFramebuffer** fbs, size_t n, SRPGpuDraw
 	srpGpuDrawBatch(scratch, n);
 }
 
+void sceneUploadAsync(Scene* s)
+{
+	for (int k = 0; k < s->nvb; ++k) srpGpuVertexBufferCopyDataAsync(s->vb[k], s->vstride[k], s->vbytes[k], s->vdata[k]);
+	for (int k = 0; k < s->nib; ++k) srpGpuIndexBufferCopyDataAsync(s->ib[k], s->itype[k], s->ibytes[k], s->idata[k]);
+}
+
+void scenePrepareBatch(Scene** scenes, SRPFramebuffer** fbs, size_t n)
+{
+	if (!n) return;
+	int same = 1;
+	for (size_t i = 1; i < n; ++i)
+		if (scenes[i]->depthInit != scenes[0]->depthInit || scenes[i]->stencilInit != scenes[0]->stencilInit) same = 0;
+	if (!same) {
+		for (size_t i = 0; i < n; ++i) scenePrepareFramebuffer(scenes[i], fbs[i]);
+		return;
+	}
+	/* srpFramebufferClear (colour 0) followed by the scene's depth and stencil */
+	srpGpuFramebufferFillBatch((const SRPFramebuffer* const*) fbs, n, 0u, scenes[0]->depthInit, scenes[0]->stencilInit,
+	                           SRP_GPU_FILL_COLOR | SRP_GPU_FILL_DEPTH | SRP_GPU_FILL_STENCIL);
+}
+
 int sceneBatchAutotune(Scene** scenes, SRPFramebuffer** fbs, size_t n, SRPGpuDraw* scratch, int repeats,
                        SRPGpuTuning* best)
 {

@@ -61,6 +61,12 @@ void sceneBatchRender(Scene** scenes, SRPFramebuffer** fbs, size_t n, SRPGpuDraw
 /* srpGpuAutotune on that batch (the framebuffers must be prepared again). */
 int sceneBatchAutotune(Scene** scenes, SRPFramebuffer** fbs, size_t n, SRPGpuDraw* scratch, int repeats,
                        SRPGpuTuning* best);
+/* sceneUpload with the asynchronous copies (srpGpu*CopyDataAsync): the
+ * scene's host data must stay unchanged until srpGpuSynchronize. */
+void sceneUploadAsync(Scene* s);
+/* scenePrepareFramebuffer of n scenes in one srpGpuFramebufferFillBatch when
+ * they share their initial depth and stencil (else one by one). */
+void scenePrepareBatch(Scene** scenes, SRPFramebuffer** fbs, size_t n);
 #endif
 
 /* Convenience: create a framebuffer of the scene's size, prepare, render, copy
