@@ -592,6 +592,8 @@ def main():
     ap.add_argument("--scenes", type=int, default=BATCH_SCENES, help="scenes per batch (--workload batch)")
     ap.add_argument("--train-steps", type=int, default=3000, help="training steps (--workload learned, batch-learned)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default resolve tuning (--workload frame, batch)")
+    ap.add_argument("--no-graphs", action="store_true",
+                    help="launch every kernel directly instead of replaying captured CUDA graphs (srpGpuSetDrawGraphs(0))")
     args = ap.parse_args()
     if args.workload == "batch":
         return run_reference_batch(args) if args.impl == "reference" else run_batch(args)
@@ -616,6 +618,8 @@ def main():
     srp_gb300.build()
     L = srp_gb300.lib()
     L.srpGpuSetFramebufferMode(srp_gb300.SRP_GPU_FB_DEVICE)
+    if args.no_graphs:
+        L.srpGpuSetDrawGraphs(0)
     stream = torch.cuda.Stream()
     L.srpGpuSetStream(ctypes.c_void_p(stream.cuda_stream))
     sc = srp_gb300.Scene(SCENE, SEED + rank, args.scale)
@@ -719,6 +723,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "seed": SEED, "width": info.width, "height": info.height,
+                   "graphs": not args.no_graphs,
                    "triangles": info.inputTriangles, "lines": info.inputLines, "points": info.inputPoints,
                    "fragments_per_frame": frags_per_frame, "l2": "flushed between frames (256 MB write)",
                    "tuning": tuning,

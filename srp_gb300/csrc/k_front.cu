@@ -123,15 +123,24 @@ __global__ void k_index_range(const __grid_constant__ DrawParams P)
 		default: wordRange<unsigned long long>(a, w << 4, b0, b1, lo, hi); wordRange<unsigned long long>(b, (two ? w + stride : w) << 4, b0, b1, lo, hi); break;
 		}
 	}
+	/* warp, then block reduction: two atomics per block on the shared pair */
+	__shared__ unsigned long long sLo[8], sHi[8];
 	for (int o = 16; o; o >>= 1) {
 		const unsigned long long l2 = __shfl_xor_sync(0xFFFFFFFFu, lo, o);
 		const unsigned long long h2 = __shfl_xor_sync(0xFFFFFFFFu, hi, o);
 		lo = l2 < lo ? l2 : lo;
 		hi = h2 > hi ? h2 : hi;
 	}
-	if ((threadIdx.x & 31) == 0) {
-		atomicMin(&P.minmax[0], lo);
-		atomicMax(&P.minmax[1], hi);
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	if (lane == 0) { sLo[warp] = lo; sHi[warp] = hi; }
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		for (int w = 1; w < (int) (blockDim.x >> 5); ++w) {
+			lo = sLo[w] < lo ? sLo[w] : lo;
+			hi = sHi[w] > hi ? sHi[w] : hi;
+		}
+		if (lo != ~0ull) atomicMin(&P.minmax[0], lo);
+		if (hi != 0ull) atomicMax(&P.minmax[1], hi);
 	}
 }
 
