@@ -662,6 +662,10 @@ def main():
         with torch.cuda.stream(stream):
             flush.fill_(1.0)
             sc.prepare()
+            # the library's front stream (vertex, setup, binning) is not ordered
+            # after this stream's earlier work: let the flush and the clear
+            # finish first, so that every draw of the frame runs after e0
+            stream.synchronize()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)

@@ -307,6 +307,11 @@ typedef struct SRPGpuProfile
  *  same draw comes again (the host reads the draw's counters between them).
  *  Stage profiling launches directly. */
 void srpGpuSetDrawGraphs(int enable);
+/** Overlap of consecutive draws (default on): a draw's vertex, setup and
+ *  binning stages run on a second stream of the library, beside the previous
+ *  draw's resolve and shading, which stay in submission order on the
+ *  library's stream. Results are identical either way. */
+void srpGpuSetDrawOverlap(int enable);
 
 /** Record CUDA events around every stage of every draw (off by default). */
 void srpGpuSetProfiling(int enable);

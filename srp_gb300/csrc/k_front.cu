@@ -1447,6 +1447,10 @@ void launchCheck(const DrawParams& P, cudaStream_t s) { pdlLaunch(k_check, 1, 32
 void launchBigEntries(const DrawParams& P, uint32_t jobsHint, cudaStream_t s)
 {
 	pdlLaunch(k_big_entries, bigBlocks(jobsHint), 256, 0, s, P);
+}
+
+void launchLambdaTables(const DrawParams& P, uint32_t jobsHint, cudaStream_t s)
+{
 	pdlLaunch(k_lambda_tables, dim3(8, tableRows(jobsHint)), 256, 0, s, P);
 }
 
@@ -1488,6 +1492,10 @@ void launchSetupMulti(const DrawParams& P, cudaStream_t s)
 void launchBigEntriesMulti(const DrawParams& P, uint32_t jobsHint, cudaStream_t s)
 {
 	pdlLaunch(k_big_entries_multi, bigBlocks(jobsHint), 256, 0, s, P);
+}
+
+void launchLambdaTablesMulti(const DrawParams& P, uint32_t jobsHint, cudaStream_t s)
+{
 	pdlLaunch(k_lambda_tables_multi, dim3(8, tableRows(jobsHint)), 256, 0, s, P);
 }
 

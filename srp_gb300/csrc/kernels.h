@@ -122,12 +122,15 @@ void launchClipPrepass(const DrawParams& P, cudaStream_t s);
 /* jobsHint (the big-primitive count of a similar earlier draw) only sizes
  * the grids; the kernels loop over the count the device holds. */
 void launchBigEntries(const DrawParams& P, uint32_t jobsHint, cudaStream_t s);
+/* lambda tables of the big triangles (triangle draws) */
+void launchLambdaTables(const DrawParams& P, uint32_t jobsHint, cudaStream_t s);
 void launchLineFrags(const DrawParams& P, cudaStream_t s);
 /* k_front.cu, multi-draw pass */
 void launchVertexMulti(const DrawParams& P, uint32_t blocks, int maxStride, cudaStream_t s);
 void launchClipPrepassMulti(const DrawParams& P, cudaStream_t s);
 void launchSetupMulti(const DrawParams& P, cudaStream_t s);
 void launchBigEntriesMulti(const DrawParams& P, uint32_t jobsHint, cudaStream_t s);
+void launchLambdaTablesMulti(const DrawParams& P, uint32_t jobsHint, cudaStream_t s);
 /* k_bin.cu */
 /* Sorts the draw's (tile, item) pairs by tile, stably; their number is read
  * from the counters (at most P.entryCap, the size the scratch is for). */

@@ -89,6 +89,19 @@ struct Registry {
 	std::vector<std::pair<void*, int>> vs, fs;
 };
 
+/* What one draw's resolve and shading read, written by its front stages:
+ * two sets alternate between consecutive single draws, so that the front of
+ * draw N+1 can run while draw N resolves and shades. A set's next front
+ * waits for rasterDone, recorded after the back of the draw that used it. */
+struct DrawSet {
+	DeviceBuffer ctr, tileStart, tileEnd, heavy, vary, triR, triA, points, lines, frags, table;
+	DeviceBuffer keys, vals, keys2, vals2;
+	DeviceCounters* hostCtr = nullptr;
+	cudaEvent_t ctrEvent = nullptr;    /* recorded after the counters are copied to hostCtr */
+	cudaEvent_t binDone = nullptr;     /* front stages done (front stream) */
+	cudaEvent_t rasterDone = nullptr;  /* resolve and shade done (`stream`) */
+};
+
 struct Lib {
 	bool init = false;
 	cudaStream_t stream = nullptr;
@@ -96,16 +109,21 @@ struct Lib {
 	/* heavy-tile resolve runs here, beside the light tiles on `stream` */
 	cudaStream_t auxStream = nullptr;
 	cudaEvent_t forkEvent = nullptr, joinEvent = nullptr;
-	cudaEvent_t ctrEvent = nullptr;   /* recorded after a draw's counters are copied to hostCtr */
+	/* a draw's vertex, setup and binning run on frontStream, its resolve and
+	 * shading on `stream`, so that the next draw's front overlaps them */
+	cudaStream_t frontStream = nullptr;
+	bool overlap = true;
 	bool graphs = true;               /* replay repeated draws from captured CUDA graphs */
 	SRPGpuTuning tune = { 96, 3 };    /* heavy-tile threshold, heavy-tile CTAs per SM */
 	SRPGpuFramebufferMode fbMode = SRP_GPU_FB_COHERENT;
 	Registry reg;
 	/* scratch pools, grown on demand */
-	DeviceBuffer clip, vset0, vset1, vary, triR, triA, lines, points, frags, keys, vals, keys2, vals2, big, lookback;
-	DeviceBuffer hist, partials, tileStart, tileEnd, winner, minmax, ctr, table, heavy, clipSlot, clipPolys;
+	/* used by the front stages only (and by multi-draw passes) */
+	DeviceBuffer clip, vset0, vset1, big, lookback, hist, partials, minmax, clipSlot, clipPolys;
+	DeviceBuffer winner;        /* resolve and shade, always on `stream` */
 	DeviceBuffer fillTargets;   /* srpGpuFramebufferFillBatch */
-	DeviceCounters* hostCtr = nullptr;
+	DrawSet sets[2];            /* alternating between consecutive single draws */
+	int setNext = 0;
 	SRPGpuStats stats = {};
 	unsigned long long launches = 0;
 	uint32_t clipRows = 4096;
@@ -137,11 +155,17 @@ bool ensureInit(const char* fn)
 	if (!cudaOk(cudaStreamCreateWithPriority(&g.auxStream, cudaStreamNonBlocking, hiPri), fn, "cudaStreamCreate") ||
 	    !cudaOk(cudaEventCreateWithFlags(&g.forkEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 	    !cudaOk(cudaEventCreateWithFlags(&g.joinEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
-	    !cudaOk(cudaEventCreateWithFlags(&g.ctrEvent, cudaEventDisableTiming), fn,
-	            "cudaEventCreate")) return false;
-	if (!cudaOk(cudaMallocHost((void**) &g.hostCtr, sizeof(DeviceCounters)), fn, "cudaMallocHost")) return false;
-	if (!g.ctr.reserve(sizeof(DeviceCounters), fn) || !g.minmax.reserve(16, fn)) return false;
-	cudaMemset(g.ctr.ptr, 0, sizeof(DeviceCounters));
+	    !cudaOk(cudaStreamCreateWithFlags(&g.frontStream, cudaStreamNonBlocking), fn, "cudaStreamCreate")) return false;
+	for (DrawSet& S : g.sets) {
+		if (!cudaOk(cudaEventCreateWithFlags(&S.ctrEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
+		    !cudaOk(cudaEventCreateWithFlags(&S.binDone, cudaEventDisableTiming), fn, "cudaEventCreate") ||
+		    !cudaOk(cudaEventCreateWithFlags(&S.rasterDone, cudaEventDisableTiming), fn, "cudaEventCreate") ||
+		    !cudaOk(cudaMallocHost((void**) &S.hostCtr, sizeof(DeviceCounters)), fn, "cudaMallocHost") ||
+		    !S.ctr.reserve(sizeof(DeviceCounters), fn)) return false;
+		memset(S.hostCtr, 0, sizeof(DeviceCounters));
+		cudaMemset(S.ctr.ptr, 0, sizeof(DeviceCounters));
+	}
+	if (!g.minmax.reserve(16, fn)) return false;
 	g.init = true;
 	return true;
 }
@@ -182,7 +206,7 @@ constexpr size_t kGraphCache = 64;
 
 struct GraphEntry {
 	std::vector<unsigned char> key;
-	cudaGraphExec_t head = nullptr, tail = nullptr;
+	cudaGraphExec_t head = nullptr, bin = nullptr, back = nullptr;
 };
 
 std::vector<GraphEntry> graphCache;
@@ -195,53 +219,67 @@ GraphEntry* graphFind(const std::vector<unsigned char>& key)
 	return nullptr;
 }
 
-/* Captures `enqueue` on the library's stream; null if the capture failed
- * (the caller then launches directly). */
-template <class F> cudaGraphExec_t captureGraph(F&& enqueue)
+/* Captures `enqueue` on stream s; null if the capture failed (the caller
+ * then launches directly). */
+template <class F> cudaGraphExec_t captureGraph(cudaStream_t s, F&& enqueue)
 {
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
-	if (cudaStreamBeginCapture(g.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+	if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { cudaGetLastError(); return nullptr; }
 	enqueue();
-	const cudaError_t e = cudaStreamEndCapture(g.stream, &graph);
+	const cudaError_t e = cudaStreamEndCapture(s, &graph);
 	if (e != cudaSuccess || !graph || cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) exec = nullptr;
 	if (graph) cudaGraphDestroy(graph);
 	cudaGetLastError();
 	return exec;
 }
 
-/* Runs head and tail of a draw, from the graph cache when graphs are on and
- * stage profiling is off (profiling records fresh events per draw). */
-template <class H, class T> void runHeadTail(const std::vector<unsigned char>& key, H&& head, T&& tail)
+/* Runs a draw as three sequences:
+ * - head: reset up to the check kernel, on the front stream `fs`;
+ * - bin: lambda tables, binning and sort, on `fs`;
+ * - back: resolve and shade, on the library's stream.
+ * With fs != stream the back waits for the bin through the set's binDone
+ * event and records rasterDone. Between head and bin the counters are copied
+ * to the set's host mirror. Each sequence replays its captured CUDA graph when
+ * graphs are on and stage profiling is off (profiling records fresh events
+ * per draw). */
+template <class H, class B, class K>
+void runDrawSeq(const std::vector<unsigned char>& key, DrawSet& S, cudaStream_t fs, H&& head, B&& bin, K&& back)
 {
-	if (!g.graphs || g.profiling) {
-		head();
-		cudaMemcpyAsync(g.hostCtr, g.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, g.stream);
-		cudaEventRecord(g.ctrEvent, g.stream);
-		tail();
-		return;
-	}
-	GraphEntry* e = graphFind(key);
-	if (!e) {
-		GraphEntry fresh;
-		fresh.key = key;
-		fresh.head = captureGraph(head);
-		fresh.tail = fresh.head ? captureGraph(tail) : nullptr;
-		if (graphCache.size() < kGraphCache) graphCache.push_back(std::move(fresh));
-		else {
-			GraphEntry& old = graphCache[graphNext++ % kGraphCache];
-			if (old.head) cudaGraphExecDestroy(old.head);
-			if (old.tail) cudaGraphExecDestroy(old.tail);
-			old = std::move(fresh);
-		}
+	GraphEntry* e = nullptr;
+	if (g.graphs && !g.profiling) {
 		e = graphFind(key);
+		if (!e) {
+			GraphEntry fresh;
+			fresh.key = key;
+			fresh.head = captureGraph(fs, head);
+			fresh.bin = fresh.head ? captureGraph(fs, bin) : nullptr;
+			fresh.back = fresh.bin ? captureGraph(g.stream, back) : nullptr;
+			if (graphCache.size() < kGraphCache) graphCache.push_back(std::move(fresh));
+			else {
+				GraphEntry& old = graphCache[graphNext++ % kGraphCache];
+				if (old.head) cudaGraphExecDestroy(old.head);
+				if (old.bin) cudaGraphExecDestroy(old.bin);
+				if (old.back) cudaGraphExecDestroy(old.back);
+				old = std::move(fresh);
+			}
+			e = graphFind(key);
+		}
+		if (e && !(e->head && e->bin && e->back)) e = nullptr;
 	}
-	if (e->head) cudaGraphLaunch(e->head, g.stream);
+	if (e) cudaGraphLaunch(e->head, fs);
 	else head();
-	cudaMemcpyAsync(g.hostCtr, g.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, g.stream);
-	cudaEventRecord(g.ctrEvent, g.stream);
-	if (e->head && e->tail) cudaGraphLaunch(e->tail, g.stream);
-	else tail();
+	cudaMemcpyAsync(S.hostCtr, S.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, fs);
+	cudaEventRecord(S.ctrEvent, fs);
+	if (e) cudaGraphLaunch(e->bin, fs);
+	else bin();
+	if (fs != g.stream) {
+		cudaEventRecord(S.binDone, fs);
+		cudaStreamWaitEvent(g.stream, S.binDone, 0);
+	}
+	if (e) cudaGraphLaunch(e->back, g.stream);
+	else back();
+	if (fs != g.stream) cudaEventRecord(S.rasterDone, g.stream);
 }
 
 /* The key of a draw: its parameters and the host-side launch sizes. */
@@ -346,6 +384,7 @@ struct SRPVertexBuffer {
 	unsigned char* host = nullptr;    /* staging copy made by CopyData */
 	DeviceBuffer dev;
 	bool dirty = false;
+	cudaEvent_t ready = nullptr;      /* recorded after the last upload (library stream) */
 };
 
 struct SRPIndexBuffer {
@@ -354,7 +393,20 @@ struct SRPIndexBuffer {
 	unsigned char* host = nullptr;
 	DeviceBuffer dev;
 	bool dirty = false;
+	cudaEvent_t ready = nullptr;
 };
+
+/* Marks the end of an upload into a buffer: the front stream of a later
+ * draw waits for it. */
+static void markUpload(cudaEvent_t& ready)
+{
+	if (!ready && cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) != cudaSuccess) {
+		cudaGetLastError();
+		ready = nullptr;
+		return;
+	}
+	cudaEventRecord(ready, g.stream);
+}
 
 static size_t indexTypeSize(SRPType t)
 {
@@ -425,6 +477,7 @@ SRPVertexBuffer* srpNewVertexBuffer(void) { return new SRPVertexBuffer(); }
 void srpFreeVertexBuffer(SRPVertexBuffer* b)
 {
 	if (!b) return;
+	if (b->ready) cudaEventDestroy(b->ready);
 	if (b->host) cudaFreeHost(b->host);
 	if (b->dev.ptr) cudaFree(b->dev.ptr);
 	delete b;
@@ -437,7 +490,7 @@ void srpVertexBufferCopyData(SRPVertexBuffer* b, size_t stride, size_t nBytes, c
 	b->nBytes = nBytes;
 	if (gpuPresent()) {
 		b->dirty = !copyToDevice(b->dev, data, nBytes, "srpVertexBufferCopyData");
-		if (!b->dirty) return;
+		if (!b->dirty) { markUpload(b->ready); return; }
 	}
 	/* no device: keep a host copy, uploaded by the first draw */
 	if (nBytes > b->cap) { b->host = (unsigned char*) pinnedRealloc(b->host, nBytes); b->cap = nBytes; }
@@ -453,6 +506,7 @@ void srpGpuVertexBufferCopyDataAsync(SRPVertexBuffer* b, size_t stride, size_t n
 	b->nBytes = nBytes;
 	b->dirty = !copyToDeviceAsync(b->dev, data, nBytes, "srpGpuVertexBufferCopyDataAsync");
 	if (b->dirty) srpVertexBufferCopyData(b, stride, nBytes, data);
+	else markUpload(b->ready);
 }
 
 SRPIndexBuffer* srpNewIndexBuffer(void) { return new SRPIndexBuffer(); }
@@ -460,6 +514,7 @@ SRPIndexBuffer* srpNewIndexBuffer(void) { return new SRPIndexBuffer(); }
 void srpFreeIndexBuffer(SRPIndexBuffer* b)
 {
 	if (!b) return;
+	if (b->ready) cudaEventDestroy(b->ready);
 	if (b->host) cudaFreeHost(b->host);
 	if (b->dev.ptr) cudaFree(b->dev.ptr);
 	delete b;
@@ -474,7 +529,7 @@ void srpIndexBufferCopyData(SRPIndexBuffer* b, SRPType type, size_t nBytes, cons
 	b->nBytes = nBytes;
 	if (gpuPresent()) {
 		b->dirty = !copyToDevice(b->dev, data, nBytes, "srpIndexBufferCopyData");
-		if (!b->dirty) return;
+		if (!b->dirty) { markUpload(b->ready); return; }
 	}
 	if (nBytes > b->cap) { b->host = (unsigned char*) pinnedRealloc(b->host, nBytes); b->cap = nBytes; }
 	if (nBytes) memcpy(b->host, data, nBytes);
@@ -490,6 +545,7 @@ void srpGpuIndexBufferCopyDataAsync(SRPIndexBuffer* b, SRPType type, size_t nByt
 	b->nBytes = nBytes;
 	b->dirty = !copyToDeviceAsync(b->dev, data, nBytes, "srpGpuIndexBufferCopyDataAsync");
 	if (b->dirty) srpIndexBufferCopyData(b, type, nBytes, data);
+	else markUpload(b->ready);
 }
 
 }  // extern "C"
@@ -932,6 +988,7 @@ static bool uploadVB(SRPVertexBuffer* vb)
 	if (!vb->dev.reserve(vb->nBytes + 16, "srpDraw")) return false;
 	if (vb->nBytes) cudaMemcpyAsync(vb->dev.ptr, vb->host, vb->nBytes, cudaMemcpyHostToDevice, g.stream);
 	vb->dirty = false;
+	markUpload(vb->ready);
 	return true;
 }
 
@@ -941,6 +998,7 @@ static bool uploadIB(SRPIndexBuffer* ib)
 	if (!ib->dev.reserve(ib->nBytes + 16, "srpDraw")) return false;
 	if (ib->nBytes) cudaMemcpyAsync(ib->dev.ptr, ib->host, ib->nBytes, cudaMemcpyHostToDevice, g.stream);
 	ib->dirty = false;
+	markUpload(ib->ready);
 	return true;
 }
 
@@ -951,10 +1009,15 @@ static uint32_t bitsFor(uint32_t n)
 	return (b + 7) / 8 * 8;
 }
 
-static bool readCounters()
+/* Copies both sets' counters to their host mirrors (waits for the GPU) and
+ * returns the fragments counted by all draws. */
+static unsigned long long readCounters()
 {
-	cudaMemcpyAsync(g.hostCtr, g.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, g.stream);
-	return cudaOk(cudaStreamSynchronize(g.stream), "srpDraw", "kernel execution");
+	cudaStreamSynchronize(g.frontStream);
+	for (DrawSet& S : g.sets)
+		cudaMemcpyAsync(S.hostCtr, S.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, g.stream);
+	if (!cudaOk(cudaStreamSynchronize(g.stream), "srpDraw", "kernel execution")) return 0;
+	return g.sets[0].hostCtr->fragments + g.sets[1].hostCtr->fragments;
 }
 
 /* The GPU pipeline for one draw call. */
@@ -979,6 +1042,10 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 	static DrawParams P;
 	memset(&P, 0, sizeof P);
 	if (!buildLayout(sp->vs, P.L)) return;
+	/* this draw's scratch set and front stream */
+	DrawSet& S = g.sets[g.setNext];
+	g.setNext ^= 1;
+	const cudaStream_t fs = (g.overlap && !g.profiling) ? g.frontStream : g.stream;
 	/* state snapshot */
 	DrawState& st = P.st;
 	st.W = (int) fb->width; st.H = (int) fb->height;
@@ -1041,7 +1108,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		}
 	}
 	P.minmax = g.minmax.as<unsigned long long>();
-	P.ctr = g.ctr.as<DeviceCounters>();
+	P.ctr = S.ctr.as<DeviceCounters>();
 	P.color = fx->color;
 	P.depth = fx->depth;
 	P.stencil = fx->stencil;
@@ -1062,49 +1129,49 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		const uint32_t rows = (uint32_t) vb->nVertices + g.clipRows;
 		const size_t nw = (size_t) std::max(P.L.nWords, 1);
 		const uint32_t blocks = (uint32_t) ((nIn + kSetupThreads - 1) / kSetupThreads);
-		bool ok = g.clip.reserve((size_t) rows * 16, FN) && g.vary.reserve((size_t) rows * nw * 4, FN) &&
+		bool ok = g.clip.reserve((size_t) rows * 16, FN) && S.vary.reserve((size_t) rows * nw * 4, FN) &&
 		          g.vset0.reserve((size_t) vb->nVertices * 16 + 16, FN) && g.vset1.reserve((size_t) vb->nVertices * 16 + 16, FN) &&
 		          g.lookback.reserve((size_t) std::max(blocks, 1u) * 8, FN) &&
-		          g.keys.reserve((size_t) entryCap * 4, FN) && g.vals.reserve((size_t) entryCap * 4, FN) &&
-		          g.keys2.reserve((size_t) entryCap * 4, FN) && g.vals2.reserve((size_t) entryCap * 4, FN) &&
+		          S.keys.reserve((size_t) entryCap * 4, FN) && S.vals.reserve((size_t) entryCap * 4, FN) &&
+		          S.keys2.reserve((size_t) entryCap * 4, FN) && S.vals2.reserve((size_t) entryCap * 4, FN) &&
 		          g.hist.reserve(sortHistWords(entryCap) * 4, FN) && g.partials.reserve(sortPartialWords(entryCap) * 4 + 64, FN) &&
-		          g.big.reserve((size_t) g.bigCap * 16, FN) && g.table.reserve((size_t) g.tableCap * 4, FN) &&
+		          g.big.reserve((size_t) g.bigCap * 16, FN) && S.table.reserve((size_t) g.tableCap * 4, FN) &&
 		          g.clipSlot.reserve((size_t) nIn * 4 + 4, FN) &&
 		          g.clipPolys.reserve((size_t) g.clipPolyCap * (1 + kMaxPoly) * 4, FN) &&
-		          g.tileStart.reserve((size_t) (numTiles + 1) * 4, FN) && g.tileEnd.reserve((size_t) (numTiles + 1) * 4, FN) &&
-		          g.winner.reserve(fb->size * 4 + 4, FN) && g.heavy.reserve((size_t) (numTiles + 1) * 4, FN);
-		if (kind == kKindTri) ok = ok && g.triR.reserve((size_t) primCap * sizeof(TriRaster), FN) &&
-		                           g.triA.reserve((size_t) primCap * sizeof(TriAttr), FN);
-		else if (kind == kKindPoint) ok = ok && g.points.reserve((size_t) primCap * sizeof(PointRec), FN);
-		else ok = ok && g.lines.reserve((size_t) primCap * sizeof(LineRec), FN) &&
-		          g.frags.reserve((size_t) entryCap * sizeof(LineFrag), FN);
+		          S.tileStart.reserve((size_t) (numTiles + 1) * 4, FN) && S.tileEnd.reserve((size_t) (numTiles + 1) * 4, FN) &&
+		          g.winner.reserve(fb->size * 4 + 4, FN) && S.heavy.reserve((size_t) (numTiles + 1) * 4, FN);
+		if (kind == kKindTri) ok = ok && S.triR.reserve((size_t) primCap * sizeof(TriRaster), FN) &&
+		                           S.triA.reserve((size_t) primCap * sizeof(TriAttr), FN);
+		else if (kind == kKindPoint) ok = ok && S.points.reserve((size_t) primCap * sizeof(PointRec), FN);
+		else ok = ok && S.lines.reserve((size_t) primCap * sizeof(LineRec), FN) &&
+		          S.frags.reserve((size_t) entryCap * sizeof(LineFrag), FN);
 		if (!ok) return;
 		P.clip = g.clip.as<float4>();
 		P.vset0 = g.vset0.as<float4>();
 		P.vset1 = g.vset1.as<float4>();
-		P.vary = g.vary.as<uint32_t>();
+		P.vary = S.vary.as<uint32_t>();
 		P.clipBase = (uint32_t) vb->nVertices;
 		P.clipCap = g.clipRows;
-		P.triR = g.triR.as<TriRaster>();
-		P.triA = g.triA.as<TriAttr>();
-		P.lines = g.lines.as<LineRec>();
-		P.points = g.points.as<PointRec>();
-		P.frags = g.frags.as<LineFrag>();
+		P.triR = S.triR.as<TriRaster>();
+		P.triA = S.triA.as<TriAttr>();
+		P.lines = S.lines.as<LineRec>();
+		P.points = S.points.as<PointRec>();
+		P.frags = S.frags.as<LineFrag>();
 		P.primCap = primCap;
 		P.fragCap = kind == kKindLineFrag ? entryCap : 0;
-		P.keys = g.keys.as<uint32_t>();
-		P.vals = g.vals.as<uint32_t>();
+		P.keys = S.keys.as<uint32_t>();
+		P.vals = S.vals.as<uint32_t>();
 		P.entryCap = entryCap;
 		P.bigJobs = g.big.as<uint4>();
 		P.bigCap = g.bigCap;
-		P.table = g.table.as<float>();
+		P.table = S.table.as<float>();
 		P.clipSlot = g.clipSlot.as<uint32_t>();
 		P.clipPolys = g.clipPolys.as<uint32_t>();
 		P.clipPolyCap = g.clipPolyCap;
 		P.tableCap = g.tableCap;
 		P.lookback = g.lookback.as<unsigned long long>();
-		P.tileStart = g.tileStart.as<uint32_t>();
-		P.tileEnd = g.tileEnd.as<uint32_t>();
+		P.tileStart = S.tileStart.as<uint32_t>();
+		P.tileEnd = S.tileEnd.as<uint32_t>();
 		P.winner = g.winner.as<int32_t>();
 
 		/* the whole draw is enqueued before the host looks at any count */
@@ -1112,35 +1179,39 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		uint32_t* sv = nullptr;
 		auto head = [&]() {
 			stageBegin();
-			launchReset(P, g.stream);
-			if (ib) launchIndexRange(P, g.stream);
-			if (ib) launchVertex(P, 0, vb->nVertices, g.stream);
-			else launchVertex(P, start, count, g.stream);
+			launchReset(P, fs);
+			if (ib) launchIndexRange(P, fs);
+			if (ib) launchVertex(P, 0, vb->nVertices, fs);
+			else launchVertex(P, start, count, fs);
 			stageEnd(SRP_GPU_STAGE_VERTEX, ib ? 3 : 2);
 			stageBegin();
-			cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, g.stream);
-			if (isTri(prim)) launchClipPrepass(P, g.stream);
-			launchSetup(P, g.stream);
-			launchCheck(P, g.stream);
+			cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, fs);
+			if (isTri(prim)) launchClipPrepass(P, fs);
+			launchSetup(P, fs);
+			launchCheck(P, fs);
 			stageEnd(SRP_GPU_STAGE_SETUP, isTri(prim) ? 3 : 2);
 		};
-		auto tail = [&]() {
+		auto bin = [&]() {
 			stageBegin();
-			if (kind == kKindLineFrag) launchLineFrags(P, g.stream);
-			else launchBigEntries(P, g.bigJobsSeen[kind], g.stream);
-			sortEntries(P, keyBits, g.keys2.as<uint32_t>(), g.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
-			            g.partials.as<uint32_t>(), &sk, &sv, g.stream);
-			cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, g.stream);
-			cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, g.stream);
-			launchTileRanges(P, sk, numTiles, g.stream);
+			/* lambda tables only for triangles (a point draw has none) */
+			if (kind == kKindTri) launchLambdaTables(P, g.bigJobsSeen[kind], fs);
+			if (kind == kKindLineFrag) launchLineFrags(P, fs);
+			else launchBigEntries(P, g.bigJobsSeen[kind], fs);
+			sortEntries(P, keyBits, S.keys2.as<uint32_t>(), S.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
+			            g.partials.as<uint32_t>(), &sk, &sv, fs);
+			cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, fs);
+			cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, fs);
+			launchTileRanges(P, sk, numTiles, fs);
 			stageEnd(SRP_GPU_STAGE_BIN, 2 + 1 + (int) (keyBits / 8) + 1);
+		};
+		auto back = [&]() {
 			if (late) {
 				stageBegin();
 				launchResolveLate(P, kind, sv, numTiles, g.stream);
 				stageEnd(SRP_GPU_STAGE_RESOLVE, 1);
 			} else {
 				stageBegin();
-				launchResolve(P, kind, sv, numTiles, g.heavy.as<uint32_t>(), g.stream, g.auxStream, g.forkEvent,
+				launchResolve(P, kind, sv, numTiles, S.heavy.as<uint32_t>(), g.stream, g.auxStream, g.forkEvent,
 				              g.joinEvent);
 				stageEnd(SRP_GPU_STAGE_RESOLVE, 3);
 				stageBegin();
@@ -1148,14 +1219,23 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 				stageEnd(SRP_GPU_STAGE_SHADE, 1);
 			}
 		};
-		runHeadTail(graphKey(P, { (unsigned long long) kind, late, ib != nullptr, start, count, vb->nVertices, blocks,
-		                          keyBits, numTiles, g.bigJobsSeen[kind], (unsigned long long) (uintptr_t) g.stream }),
-		            head, tail);
-		g.launches += 4 + (ib ? 1 : 0) + (isTri(prim) ? 1 : 0) + 2 + 1 + keyBits / 8 + 1 + (late ? 1 : 4);
+		/* the front waits for the last back that used this set, and for the
+		 * uploads of the buffers it reads (both on the library's stream) */
+		if (fs != g.stream) {
+			cudaStreamWaitEvent(fs, S.rasterDone, 0);
+			if (vb->ready) cudaStreamWaitEvent(fs, vb->ready, 0);
+			if (ib && ib->ready) cudaStreamWaitEvent(fs, ib->ready, 0);
+		}
+		runDrawSeq(graphKey(P, { (unsigned long long) kind, late, ib != nullptr, start, count, vb->nVertices, blocks,
+		                         keyBits, numTiles, g.bigJobsSeen[kind], (unsigned long long) (uintptr_t) g.stream,
+		                         (unsigned long long) (uintptr_t) fs }),
+		           S, fs, head, bin, back);
+		g.launches += 4 + (ib ? 1 : 0) + (isTri(prim) ? 1 : 0) + (kind == kKindPoint ? 1 : 2) + 1 + keyBits / 8 + 1 +
+		              (late ? 1 : 4);
 		if (!cudaOk(cudaGetLastError(), FN, "launch")) return;
 		/* wait for the setup counters only; the rest of the draw runs on */
-		if (!cudaOk(cudaEventSynchronize(g.ctrEvent), FN, "kernel execution")) return;
-		const DeviceCounters c = *g.hostCtr;
+		if (!cudaOk(cudaEventSynchronize(S.ctrEvent), FN, "kernel execution")) return;
+		const DeviceCounters c = *S.hostCtr;
 		if (c.errors & kErrBadIndex) {
 			SRP_ERROR(FN, "Vertex index out of range of the vertex buffer (%zu vertices)", vb->nVertices);
 			return;
@@ -1163,6 +1243,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		if (c.errors & kErrSpin) { SRP_ERROR(FN, "Ordered-compaction wait timed out"); return; }
 		if (c.abort) {
 			/* the enqueued rest of the draw skipped itself; grow and draw again */
+			cudaStreamSynchronize(fs);
 			cudaStreamSynchronize(g.stream);
 			bool grew = false;
 			if (c.clipVerts > g.clipRows) { g.clipRows = (uint32_t) std::min<unsigned long long>(c.clipVerts * 2, 0x7FFFFFFF); grew = true; }
@@ -1193,6 +1274,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			launchShade(P, kind, numTiles, g.stream);
 			stageEnd(SRP_GPU_STAGE_SHADE, 1);
 			++g.launches;
+			if (fs != g.stream) cudaEventRecord(S.rasterDone, g.stream);
 		}
 	}
 	++g.stats.draws;
@@ -1313,6 +1395,13 @@ DeviceBuffer passDescDev, passPrefixDev, passPrimPrefix, passWinner;
  * varying layout, distinct framebuffers). Returns false (after a message)
  * only on a CUDA failure; draws that hit a bad vertex index are re-run one
  * by one so that each reports as the ordinary draw does. */
+/* After a pass (on the library's stream, with the first scratch set and the
+ * shared front buffers): the next single draws' fronts wait for it. */
+static void markPassDone()
+{
+	for (DrawSet& S : g.sets) cudaEventRecord(S.rasterDone, g.stream);
+}
+
 static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, const std::vector<size_t>& nInOf)
 {
 	const char* FN = "srpGpuDrawBatch";
@@ -1320,6 +1409,9 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	const SRPShaderProgram* sp0 = draws[idx[0]].program;
 	static DrawParams P;
 	memset(&P, 0, sizeof P);
+	/* a pass runs on the library's stream with the first scratch set; later
+	 * single draws' fronts wait for it through both sets' rasterDone */
+	DrawSet& S = g.sets[0];
 	if (!buildLayout(sp0->vs, P.L)) return true;
 	DrawState& st = P.st;
 	st.frontFaceCW = srpContext.raster.frontFace == SRP_WINDING_CW;
@@ -1421,7 +1513,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	P.nIn = (int) nIn;
 	P.nVertices = vRows;
 	P.minmax = g.minmax.as<unsigned long long>();
-	P.ctr = g.ctr.as<DeviceCounters>();
+	P.ctr = S.ctr.as<DeviceCounters>();
 	if (g.fbMode == SRP_GPU_FB_COHERENT)
 		for (size_t k = 0; k < n; ++k) fbUpload(draws[idx[k]].framebuffer, fbFind(draws[idx[k]].framebuffer));
 
@@ -1434,42 +1526,42 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		const unsigned long long rows = (unsigned long long) vRows + g.clipRows;
 		const size_t nw = (size_t) std::max(P.L.nWords, 1);
 		const uint32_t blocks = (nIn + kSetupThreads - 1) / kSetupThreads;
-		bool ok = g.clip.reserve(rows * 16, FN) && g.vary.reserve(rows * nw * 4, FN) &&
+		bool ok = g.clip.reserve(rows * 16, FN) && S.vary.reserve(rows * nw * 4, FN) &&
 		          g.vset0.reserve((size_t) vRows * 16 + 16, FN) && g.vset1.reserve((size_t) vRows * 16 + 16, FN) &&
 		          g.lookback.reserve((size_t) std::max(blocks, 1u) * 8, FN) &&
-		          g.keys.reserve((size_t) entryCap * 4, FN) && g.vals.reserve((size_t) entryCap * 4, FN) &&
-		          g.keys2.reserve((size_t) entryCap * 4, FN) && g.vals2.reserve((size_t) entryCap * 4, FN) &&
+		          S.keys.reserve((size_t) entryCap * 4, FN) && S.vals.reserve((size_t) entryCap * 4, FN) &&
+		          S.keys2.reserve((size_t) entryCap * 4, FN) && S.vals2.reserve((size_t) entryCap * 4, FN) &&
 		          g.hist.reserve(sortHistWords(entryCap) * 4, FN) && g.partials.reserve(sortPartialWords(entryCap) * 4 + 64, FN) &&
-		          g.big.reserve((size_t) g.bigCap * 16, FN) && g.table.reserve((size_t) g.tableCap * 4, FN) &&
+		          g.big.reserve((size_t) g.bigCap * 16, FN) && S.table.reserve((size_t) g.tableCap * 4, FN) &&
 		          g.clipSlot.reserve((size_t) nIn * 4 + 4, FN) &&
 		          g.clipPolys.reserve((size_t) g.clipPolyCap * (1 + kMaxPoly) * 4, FN) &&
-		          g.triR.reserve((size_t) primCap * sizeof(TriRaster), FN) &&
-		          g.triA.reserve((size_t) primCap * sizeof(TriAttr), FN) &&
-		          g.tileStart.reserve((size_t) (numTiles + 1) * 4, FN) && g.tileEnd.reserve((size_t) (numTiles + 1) * 4, FN) &&
-		          g.heavy.reserve((size_t) (numTiles + 1) * 4, FN);
+		          S.triR.reserve((size_t) primCap * sizeof(TriRaster), FN) &&
+		          S.triA.reserve((size_t) primCap * sizeof(TriAttr), FN) &&
+		          S.tileStart.reserve((size_t) (numTiles + 1) * 4, FN) && S.tileEnd.reserve((size_t) (numTiles + 1) * 4, FN) &&
+		          S.heavy.reserve((size_t) (numTiles + 1) * 4, FN);
 		if (!ok) return false;
 		P.clip = g.clip.as<float4>();
 		P.vset0 = g.vset0.as<float4>();
 		P.vset1 = g.vset1.as<float4>();
-		P.vary = g.vary.as<uint32_t>();
+		P.vary = S.vary.as<uint32_t>();
 		P.clipBase = vRows;
 		P.clipCap = g.clipRows;
-		P.triR = g.triR.as<TriRaster>();
-		P.triA = g.triA.as<TriAttr>();
+		P.triR = S.triR.as<TriRaster>();
+		P.triA = S.triA.as<TriAttr>();
 		P.primCap = primCap;
-		P.keys = g.keys.as<uint32_t>();
-		P.vals = g.vals.as<uint32_t>();
+		P.keys = S.keys.as<uint32_t>();
+		P.vals = S.vals.as<uint32_t>();
 		P.entryCap = entryCap;
 		P.bigJobs = g.big.as<uint4>();
 		P.bigCap = g.bigCap;
-		P.table = g.table.as<float>();
+		P.table = S.table.as<float>();
 		P.tableCap = g.tableCap;
 		P.clipSlot = g.clipSlot.as<uint32_t>();
 		P.clipPolys = g.clipPolys.as<uint32_t>();
 		P.clipPolyCap = g.clipPolyCap;
 		P.lookback = g.lookback.as<unsigned long long>();
-		P.tileStart = g.tileStart.as<uint32_t>();
-		P.tileEnd = g.tileEnd.as<uint32_t>();
+		P.tileStart = S.tileStart.as<uint32_t>();
+		P.tileEnd = S.tileEnd.as<uint32_t>();
 
 		auto head = [&]() {
 			stageBegin();
@@ -1483,31 +1575,35 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 			launchCheck(P, g.stream);
 			stageEnd(SRP_GPU_STAGE_SETUP, 3);
 		};
-		auto tail = [&]() {
+		uint32_t* sk = nullptr;
+		uint32_t* sv = nullptr;
+		auto bin = [&]() {
 			stageBegin();
+			launchLambdaTablesMulti(P, g.bigJobsSeen[kKindTri], g.stream);
 			launchBigEntriesMulti(P, g.bigJobsSeen[kKindTri], g.stream);
-			uint32_t* sk;
-			uint32_t* sv;
-			sortEntries(P, keyBits, g.keys2.as<uint32_t>(), g.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
+			sortEntries(P, keyBits, S.keys2.as<uint32_t>(), S.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
 			            g.partials.as<uint32_t>(), &sk, &sv, g.stream);
 			cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, g.stream);
 			cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, g.stream);
 			launchTileRanges(P, sk, numTiles, g.stream);
 			stageEnd(SRP_GPU_STAGE_BIN, 2 + 1 + (int) (keyBits / 8) + 1);
+		};
+		auto back = [&]() {
 			stageBegin();
-			launchResolveMulti(P, sv, numTiles, g.heavy.as<uint32_t>(), g.stream, g.auxStream, g.forkEvent, g.joinEvent);
+			launchResolveMulti(P, sv, numTiles, S.heavy.as<uint32_t>(), g.stream, g.auxStream, g.forkEvent, g.joinEvent);
 			stageEnd(SRP_GPU_STAGE_RESOLVE, 3);
 			stageBegin();
 			launchShadeMulti(P, numTiles, g.stream);
 			stageEnd(SRP_GPU_STAGE_SHADE, 1);
 		};
-		runHeadTail(graphKey(P, { vBlocks, (unsigned long long) maxStride, blocks, keyBits, numTiles,
-		                          g.bigJobsSeen[kKindTri], (unsigned long long) (uintptr_t) g.stream }),
-		            head, tail);
+		runDrawSeq(graphKey(P, { vBlocks, (unsigned long long) maxStride, blocks, keyBits, numTiles,
+		                         g.bigJobsSeen[kKindTri], (unsigned long long) (uintptr_t) g.stream }),
+		           S, g.stream, head, bin, back);
+		markPassDone();
 		g.launches += 5 + 2 + 1 + keyBits / 8 + 1 + 4;
 		if (!cudaOk(cudaGetLastError(), FN, "launch")) return false;
-		if (!cudaOk(cudaEventSynchronize(g.ctrEvent), FN, "kernel execution")) return false;
-		const DeviceCounters c = *g.hostCtr;
+		if (!cudaOk(cudaEventSynchronize(S.ctrEvent), FN, "kernel execution")) return false;
+		const DeviceCounters c = *S.hostCtr;
 		if (c.errors & kErrBadIndex) {
 			/* some draw indexes past its vertex buffer: let each report alone */
 			cudaStreamSynchronize(g.stream);
@@ -1556,6 +1652,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	g.stats.draws += n;
 	if (g.fbMode == SRP_GPU_FB_COHERENT)
 		for (size_t k = 0; k < n; ++k) fbDownload(draws[idx[k]].framebuffer, fbFind(draws[idx[k]].framebuffer));
+	markPassDone();
 	return true;
 }
 
@@ -1642,17 +1739,18 @@ int srpGpuSynchronize(void)
 void srpGpuGetStats(SRPGpuStats* s)
 {
 	if (!g.init) { memset(s, 0, sizeof *s); return; }
-	readCounters();
+	const unsigned long long frags = readCounters();
 	*s = g.stats;
-	s->fragments = g.hostCtr->fragments;
+	s->fragments = frags;
 	s->kernelLaunches = g.launches;
 }
 
 void srpGpuResetStats(void)
 {
 	if (!g.init) return;
+	cudaStreamSynchronize(g.frontStream);
 	cudaStreamSynchronize(g.stream);
-	cudaMemset(g.ctr.ptr, 0, sizeof(DeviceCounters));
+	for (DrawSet& S : g.sets) cudaMemset(S.ctr.ptr, 0, sizeof(DeviceCounters));
 	g.stats = SRPGpuStats();
 	g.launches = 0;
 }
@@ -1660,6 +1758,13 @@ void srpGpuResetStats(void)
 void srpGpuSetProfiling(int enable) { g.profiling = enable != 0; }
 
 void srpGpuSetDrawGraphs(int enable) { g.graphs = enable != 0; }
+
+void srpGpuSetDrawOverlap(int enable)
+{
+	if (!ensureInit("srpGpuSetDrawOverlap")) return;
+	cudaStreamSynchronize(g.frontStream);
+	g.overlap = enable != 0;
+}
 
 void srpGpuGetTuning(SRPGpuTuning* t) { *t = g.tune; }
 

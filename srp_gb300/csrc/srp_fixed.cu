@@ -264,7 +264,11 @@ extern "C" int srpGpuDrawFixedScratch(const SRPIndexBuffer* ib, const SRPVertexB
 	const uint32_t E = (uint32_t) c.entries;
 	/* the rest of the draw takes its sizes from the counters on the device */
 	if (lineFrags) { launchLineFrags(P, s); launches += 2; }
-	else if (c.bigJobs) { launchBigEntries(P, (uint32_t) c.bigJobs, s); launches += 2; }
+	else if (c.bigJobs) {
+		launchBigEntries(P, (uint32_t) c.bigJobs, s);
+		launchLambdaTables(P, (uint32_t) c.bigJobs, s);
+		launches += 2;
+	}
 	if (E) {
 		const uint32_t keyBits = keyBitsFor(info.numTiles);
 		uint32_t* sk;

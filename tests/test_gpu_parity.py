@@ -73,3 +73,31 @@ def test_graph_replay_matches_direct_launches(built_library, scene, scale):
     finally:
         L.srpGpuSetDrawGraphs(1)
         sc.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scene,scale", [("soup", 0.5), ("clip_tris", 1.0), ("topologies", 1.0), ("late_z", 1.0)])
+def test_overlapped_draws_match_serial_draws(built_library, scene, scale):
+    """Consecutive draws overlap (front stages of draw N+1 beside the resolve
+    and shading of draw N, two scratch sets); frames rendered that way, with
+    and without graph replay, equal the frames of strictly serial draws."""
+    import srp_gb300
+    L = srp_gb300.lib()
+    L.srpGpuSetFramebufferMode(srp_gb300.SRP_GPU_FB_DEVICE)
+    sc = srp_gb300.Scene(scene, 11, scale)
+    try:
+        frames = []
+        for overlap, graphs in ((0, 0), (1, 0), (1, 1), (1, 1), (1, 1)):
+            L.srpGpuSetDrawOverlap(overlap)
+            L.srpGpuSetDrawGraphs(graphs)
+            sc.prepare()
+            sc.render()
+            frames.append(sc.planes())
+        assert L.srpGpuSynchronize() == 0
+        for f in frames[1:]:
+            for a, b in zip(f, frames[0]):
+                assert np.array_equal(a, b)
+    finally:
+        L.srpGpuSetDrawOverlap(1)
+        L.srpGpuSetDrawGraphs(1)
+        sc.close()
