@@ -98,6 +98,7 @@ struct DrawSet {
 	DeviceBuffer keys, vals, keys2, vals2;
 	DeviceCounters* hostCtr = nullptr;
 	cudaEvent_t ctrEvent = nullptr;    /* recorded after the counters are copied to hostCtr */
+	cudaEvent_t headDone = nullptr;    /* vertex and setup done (front stream) */
 	cudaEvent_t binDone = nullptr;     /* front stages done (front stream) */
 	cudaEvent_t rasterDone = nullptr;  /* resolve and shade done (`stream`) */
 };
@@ -158,6 +159,7 @@ bool ensureInit(const char* fn)
 	    !cudaOk(cudaStreamCreateWithFlags(&g.frontStream, cudaStreamNonBlocking), fn, "cudaStreamCreate")) return false;
 	for (DrawSet& S : g.sets) {
 		if (!cudaOk(cudaEventCreateWithFlags(&S.ctrEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
+		    !cudaOk(cudaEventCreateWithFlags(&S.headDone, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 		    !cudaOk(cudaEventCreateWithFlags(&S.binDone, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 		    !cudaOk(cudaEventCreateWithFlags(&S.rasterDone, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 		    !cudaOk(cudaMallocHost((void**) &S.hostCtr, sizeof(DeviceCounters)), fn, "cudaMallocHost") ||
@@ -206,7 +208,7 @@ constexpr size_t kGraphCache = 64;
 
 struct GraphEntry {
 	std::vector<unsigned char> key;
-	cudaGraphExec_t head = nullptr, bin = nullptr, back = nullptr;
+	cudaGraphExec_t head = nullptr, mid = nullptr, bin = nullptr, back = nullptr;
 };
 
 std::vector<GraphEntry> graphCache;
@@ -234,17 +236,20 @@ template <class F> cudaGraphExec_t captureGraph(cudaStream_t s, F&& enqueue)
 	return exec;
 }
 
-/* Runs a draw as three sequences:
+/* Runs a draw as four sequences:
  * - head: reset up to the check kernel, on the front stream `fs`;
- * - bin: lambda tables, binning and sort, on `fs`;
+ * - mid: work that needs the head but not the binning (the lambda tables),
+ *   on the library's stream, beside the bin;
+ * - bin: binning and sort, on `fs`;
  * - back: resolve and shade, on the library's stream.
- * With fs != stream the back waits for the bin through the set's binDone
- * event and records rasterDone. Between head and bin the counters are copied
- * to the set's host mirror. Each sequence replays its captured CUDA graph when
- * graphs are on and stage profiling is off (profiling records fresh events
- * per draw). */
-template <class H, class B, class K>
-void runDrawSeq(const std::vector<unsigned char>& key, DrawSet& S, cudaStream_t fs, H&& head, B&& bin, K&& back)
+ * With fs != stream, mid waits for the head through the set's headDone event
+ * and back for the bin through binDone; back records rasterDone. Between
+ * head and bin the counters are copied to the set's host mirror. Each
+ * sequence replays its captured CUDA graph when graphs are on and stage
+ * profiling is off (profiling records fresh events per draw). */
+template <class H, class M, class B, class K>
+void runDrawSeq(const std::vector<unsigned char>& key, DrawSet& S, cudaStream_t fs, H&& head, bool hasMid, M&& mid,
+                B&& bin, K&& back)
 {
 	GraphEntry* e = nullptr;
 	if (g.graphs && !g.profiling) {
@@ -253,24 +258,32 @@ void runDrawSeq(const std::vector<unsigned char>& key, DrawSet& S, cudaStream_t 
 			GraphEntry fresh;
 			fresh.key = key;
 			fresh.head = captureGraph(fs, head);
-			fresh.bin = fresh.head ? captureGraph(fs, bin) : nullptr;
+			fresh.mid = fresh.head && hasMid ? captureGraph(g.stream, mid) : nullptr;
+			fresh.bin = fresh.head && (fresh.mid || !hasMid) ? captureGraph(fs, bin) : nullptr;
 			fresh.back = fresh.bin ? captureGraph(g.stream, back) : nullptr;
 			if (graphCache.size() < kGraphCache) graphCache.push_back(std::move(fresh));
 			else {
 				GraphEntry& old = graphCache[graphNext++ % kGraphCache];
-				if (old.head) cudaGraphExecDestroy(old.head);
-				if (old.bin) cudaGraphExecDestroy(old.bin);
-				if (old.back) cudaGraphExecDestroy(old.back);
+				for (cudaGraphExec_t x : { old.head, old.mid, old.bin, old.back })
+					if (x) cudaGraphExecDestroy(x);
 				old = std::move(fresh);
 			}
 			e = graphFind(key);
 		}
-		if (e && !(e->head && e->bin && e->back)) e = nullptr;
+		if (e && !(e->head && (e->mid || !hasMid) && e->bin && e->back)) e = nullptr;
 	}
 	if (e) cudaGraphLaunch(e->head, fs);
 	else head();
 	cudaMemcpyAsync(S.hostCtr, S.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, fs);
 	cudaEventRecord(S.ctrEvent, fs);
+	if (hasMid) {
+		if (fs != g.stream) {
+			cudaEventRecord(S.headDone, fs);
+			cudaStreamWaitEvent(g.stream, S.headDone, 0);
+		}
+		if (e) cudaGraphLaunch(e->mid, g.stream);
+		else mid();
+	}
 	if (e) cudaGraphLaunch(e->bin, fs);
 	else bin();
 	if (fs != g.stream) {
@@ -1191,10 +1204,15 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			launchCheck(P, fs);
 			stageEnd(SRP_GPU_STAGE_SETUP, isTri(prim) ? 3 : 2);
 		};
+		/* lambda tables (triangles only): needed by the resolve, not by the
+		 * binning, so they run on the library's stream beside the bin */
+		auto mid = [&]() {
+			stageBegin();
+			launchLambdaTables(P, g.bigJobsSeen[kind], g.stream);
+			stageEnd(SRP_GPU_STAGE_BIN, 1);
+		};
 		auto bin = [&]() {
 			stageBegin();
-			/* lambda tables only for triangles (a point draw has none) */
-			if (kind == kKindTri) launchLambdaTables(P, g.bigJobsSeen[kind], fs);
 			if (kind == kKindLineFrag) launchLineFrags(P, fs);
 			else launchBigEntries(P, g.bigJobsSeen[kind], fs);
 			sortEntries(P, keyBits, S.keys2.as<uint32_t>(), S.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
@@ -1229,7 +1247,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		runDrawSeq(graphKey(P, { (unsigned long long) kind, late, ib != nullptr, start, count, vb->nVertices, blocks,
 		                         keyBits, numTiles, g.bigJobsSeen[kind], (unsigned long long) (uintptr_t) g.stream,
 		                         (unsigned long long) (uintptr_t) fs }),
-		           S, fs, head, bin, back);
+		           S, fs, head, kind == kKindTri, mid, bin, back);
 		g.launches += 4 + (ib ? 1 : 0) + (isTri(prim) ? 1 : 0) + (kind == kKindPoint ? 1 : 2) + 1 + keyBits / 8 + 1 +
 		              (late ? 1 : 4);
 		if (!cudaOk(cudaGetLastError(), FN, "launch")) return;
@@ -1598,7 +1616,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		};
 		runDrawSeq(graphKey(P, { vBlocks, (unsigned long long) maxStride, blocks, keyBits, numTiles,
 		                         g.bigJobsSeen[kKindTri], (unsigned long long) (uintptr_t) g.stream }),
-		           S, g.stream, head, bin, back);
+		           S, g.stream, head, false, [] {}, bin, back);
 		markPassDone();
 		g.launches += 5 + 2 + 1 + keyBits / 8 + 1 + 4;
 		if (!cudaOk(cudaGetLastError(), FN, "launch")) return false;
@@ -1724,6 +1742,7 @@ void srpGpuDrawBatch(const SRPGpuDraw* draws, size_t n)
 void srpGpuSetStream(void* stream)
 {
 	if (!ensureInit("srpGpuSetStream")) return;
+	cudaStreamSynchronize(g.frontStream);
 	cudaStreamSynchronize(g.stream);
 	g.stream = stream ? (cudaStream_t) stream : g.ownStream;
 }
