@@ -640,7 +640,10 @@ def main():
         with torch.cuda.stream(stream):
             busy = 1
             while busy:
+                # tuned under the conditions of the timed frames below
+                flush.fill_(1.0)
                 sc.prepare()
+                stream.synchronize()
                 frame()
                 busy = L.srpGpuAutotuneFrame()
         best = srp_gb300.SRPGpuTuning()

@@ -125,10 +125,10 @@ int srpGpuAutotune(const SRPGpuDraw* draws, size_t n, int repeats, SRPGpuTuning*
 
 /** Online autotuner for a frame loop: call once after each frame's draws.
  *  Over the next 60 frames it tries the same candidates as srpGpuAutotune,
- *  four frames each (the last three timed one by one with CUDA events), then
- *  keeps the candidate with the fastest frame. Returns 1 while tuning, 0 once
- *  a tuning has been chosen (and on every later call, until
- *  srpGpuAutotuneReset). */
+ *  four frames each (the last three timed one by one with CUDA events, from
+ *  the frame's first draw to this call), then keeps the candidate with the
+ *  fastest frame. Returns 1 while tuning, 0 once a tuning has been chosen
+ *  (and on every later call, until srpGpuAutotuneReset). */
 int srpGpuAutotuneFrame(void);
 void srpGpuAutotuneReset(void);
 

@@ -288,12 +288,11 @@ __global__ void __launch_bounds__(kVertexThreads) k_vertex(const __grid_constant
 	 * clip coordinates, so the divide and the double-precision viewport step
 	 * are skipped for outside vertices */
 	const uint32_t code = outcode(clip);
+	P.codes[v] = (uint8_t) code;
 	if (code == 0) {
 		const VSet vs = vertexSetup(P.st, clip);
 		P.vset0[v] = make_float4(vs.nx, vs.ny, vs.sx, vs.sy);
 		P.vset1[v] = make_float4(vs.c, vs.iw, vs.nz, __uint_as_float(0u));
-	} else {
-		P.vset1[v] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(code));
 	}
 	const int nw = P.L.nWords;
 	uint32_t* dst = P.vary + v * (unsigned long long) nw;
@@ -656,7 +655,7 @@ __device__ __forceinline__ bool vertexIndex(const DrawParams& P, unsigned long l
 
 __device__ __forceinline__ uint32_t vertexCode(const DrawParams& P, uint32_t vi)
 {
-	return __float_as_uint(P.vset1[vi].w);
+	return P.codes[vi];
 }
 
 __device__ __forceinline__ SV loadSV(const DrawParams& P, uint32_t vi)
@@ -1155,12 +1154,11 @@ __global__ void __launch_bounds__(kVertexThreads) k_vertex_multi(const __grid_co
 	const unsigned long long row = P.vPrefix[d] + v;
 	P.clip[row] = clip;
 	const uint32_t code = outcode(clip);
+	P.codes[row] = (uint8_t) code;
 	if (code == 0) {
 		const VSet vs = vertexSetup(D.W, D.H, clip);
 		P.vset0[row] = make_float4(vs.nx, vs.ny, vs.sx, vs.sy);
 		P.vset1[row] = make_float4(vs.c, vs.iw, vs.nz, __uint_as_float(0u));
-	} else {
-		P.vset1[row] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(code));
 	}
 	const int nw = P.L.nWords;
 	uint32_t* dst = P.vary + row * (unsigned long long) nw;

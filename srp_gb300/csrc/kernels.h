@@ -25,7 +25,9 @@ struct DrawParams {
 	 * [clipBase, clipBase + clipCap) created by clipping */
 	float4* clip;
 	float4* vset0;                 /* per vertex: ndc x, ndc y, screen x, screen y */
-	float4* vset1;                 /* per vertex: z_ndc/w, 1/w, z_ndc, outcode bits */
+	float4* vset1;                 /* per vertex inside the frustum: z_ndc/w, 1/w, z_ndc, 0 */
+	uint8_t* codes;                /* per vertex: outcode bits (one byte, so that the
+	                                  clip and cull tests of setup read 32 vertices a sector) */
 	uint32_t* vary;
 	uint32_t clipBase, clipCap;
 	unsigned long long* minmax;    /* [0] min, [1] max vertex index referenced */

@@ -120,11 +120,14 @@ struct Lib {
 	Registry reg;
 	/* scratch pools, grown on demand */
 	/* used by the front stages only (and by multi-draw passes) */
-	DeviceBuffer clip, vset0, vset1, big, lookback, hist, partials, minmax, clipSlot, clipPolys;
+	DeviceBuffer clip, vset0, vset1, codes, big, lookback, hist, partials, minmax, clipSlot, clipPolys;
 	DeviceBuffer winner;        /* resolve and shade, always on `stream` */
 	DeviceBuffer fillTargets;   /* srpGpuFramebufferFillBatch */
 	DrawSet sets[2];            /* alternating between consecutive single draws */
 	int setNext = 0;
+	/* the frame autotuner's start event, recorded by the next draw */
+	cudaEvent_t tuneStart = nullptr;
+	bool tuneArmed = false;
 	SRPGpuStats stats = {};
 	unsigned long long launches = 0;
 	uint32_t clipRows = 4096;
@@ -1055,6 +1058,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 	static DrawParams P;
 	memset(&P, 0, sizeof P);
 	if (!buildLayout(sp->vs, P.L)) return;
+	if (g.tuneArmed) { cudaEventRecord(g.tuneStart, g.stream); g.tuneArmed = false; }
 	/* this draw's scratch set and front stream */
 	DrawSet& S = g.sets[g.setNext];
 	g.setNext ^= 1;
@@ -1144,6 +1148,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		const uint32_t blocks = (uint32_t) ((nIn + kSetupThreads - 1) / kSetupThreads);
 		bool ok = g.clip.reserve((size_t) rows * 16, FN) && S.vary.reserve((size_t) rows * nw * 4, FN) &&
 		          g.vset0.reserve((size_t) vb->nVertices * 16 + 16, FN) && g.vset1.reserve((size_t) vb->nVertices * 16 + 16, FN) &&
+		          g.codes.reserve((size_t) vb->nVertices + 16, FN) &&
 		          g.lookback.reserve((size_t) std::max(blocks, 1u) * 8, FN) &&
 		          S.keys.reserve((size_t) entryCap * 4, FN) && S.vals.reserve((size_t) entryCap * 4, FN) &&
 		          S.keys2.reserve((size_t) entryCap * 4, FN) && S.vals2.reserve((size_t) entryCap * 4, FN) &&
@@ -1162,6 +1167,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		P.clip = g.clip.as<float4>();
 		P.vset0 = g.vset0.as<float4>();
 		P.vset1 = g.vset1.as<float4>();
+		P.codes = g.codes.as<uint8_t>();
 		P.vary = S.vary.as<uint32_t>();
 		P.clipBase = (uint32_t) vb->nVertices;
 		P.clipCap = g.clipRows;
@@ -1427,6 +1433,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	const SRPShaderProgram* sp0 = draws[idx[0]].program;
 	static DrawParams P;
 	memset(&P, 0, sizeof P);
+	if (g.tuneArmed) { cudaEventRecord(g.tuneStart, g.stream); g.tuneArmed = false; }
 	/* a pass runs on the library's stream with the first scratch set; later
 	 * single draws' fronts wait for it through both sets' rasterDone */
 	DrawSet& S = g.sets[0];
@@ -1546,6 +1553,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		const uint32_t blocks = (nIn + kSetupThreads - 1) / kSetupThreads;
 		bool ok = g.clip.reserve(rows * 16, FN) && S.vary.reserve(rows * nw * 4, FN) &&
 		          g.vset0.reserve((size_t) vRows * 16 + 16, FN) && g.vset1.reserve((size_t) vRows * 16 + 16, FN) &&
+		          g.codes.reserve((size_t) vRows + 16, FN) &&
 		          g.lookback.reserve((size_t) std::max(blocks, 1u) * 8, FN) &&
 		          S.keys.reserve((size_t) entryCap * 4, FN) && S.vals.reserve((size_t) entryCap * 4, FN) &&
 		          S.keys2.reserve((size_t) entryCap * 4, FN) && S.vals2.reserve((size_t) entryCap * 4, FN) &&
@@ -1561,6 +1569,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		P.clip = g.clip.as<float4>();
 		P.vset0 = g.vset0.as<float4>();
 		P.vset1 = g.vset1.as<float4>();
+		P.codes = g.codes.as<uint8_t>();
 		P.vary = S.vary.as<uint32_t>();
 		P.clipBase = vRows;
 		P.clipCap = g.clipRows;
@@ -1800,7 +1809,7 @@ namespace {
 constexpr int kTuneFrames = 4;
 struct FrameTuner {
 	int state = -1;          /* -1 idle, 0 .. kTuneFrames * candidates - 1 running, -2 done */
-	cudaEvent_t start = nullptr, stop = nullptr;
+	cudaEvent_t stop = nullptr;   /* the start event is g.tuneStart */
 	float best = -1.0f;
 	SRPGpuTuning bestTune = { 96, 3 };
 } tuner;
@@ -1812,12 +1821,12 @@ SRPGpuTuning tuneCandidate(int i) { return SRPGpuTuning{ kTuneThresholds[i / 3],
 int srpGpuAutotuneFrame(void)
 {
 	if (tuner.state == -2 || !ensureInit("srpGpuAutotuneFrame")) return 0;
-	if (!tuner.start) { tuner.start = takeEvent(); tuner.stop = takeEvent(); }
+	if (!tuner.stop) { g.tuneStart = takeEvent(); tuner.stop = takeEvent(); }
 	if (tuner.state >= 0 && tuner.state % kTuneFrames != 0) {
 		/* a timed frame just ended */
 		cudaEventRecord(tuner.stop, g.stream);
 		float ms = 0.0f;
-		if (cudaEventSynchronize(tuner.stop) == cudaSuccess && cudaEventElapsedTime(&ms, tuner.start, tuner.stop) == cudaSuccess &&
+		if (cudaEventSynchronize(tuner.stop) == cudaSuccess && cudaEventElapsedTime(&ms, g.tuneStart, tuner.stop) == cudaSuccess &&
 		    (tuner.best < 0.0f || ms < tuner.best)) {
 			tuner.best = ms;
 			tuner.bestTune = g.tune;
@@ -1830,7 +1839,9 @@ int srpGpuAutotuneFrame(void)
 		return 0;
 	}
 	g.tune = tuneCandidate(tuner.state / kTuneFrames);
-	if (tuner.state % kTuneFrames != 0) cudaEventRecord(tuner.start, g.stream);
+	/* the timed frame starts with its first draw (not now: the caller may
+	 * clear or upload first) */
+	g.tuneArmed = tuner.state % kTuneFrames != 0;
 	return 1;
 }
 
@@ -1838,6 +1849,7 @@ void srpGpuAutotuneReset(void)
 {
 	tuner.state = -1;
 	tuner.best = -1.0f;
+	g.tuneArmed = false;
 }
 
 int srpGpuAutotune(const SRPGpuDraw* draws, size_t n, int repeats, SRPGpuTuning* best)

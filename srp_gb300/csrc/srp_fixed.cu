@@ -139,6 +139,7 @@ extern "C" int srpGpuDrawFixedScratch(const SRPIndexBuffer* ib, const SRPVertexB
 	const size_t oClip = cv.take(rows * 16);
 	const size_t oSet0 = cv.take(nV * 16 + 16);
 	const size_t oSet1 = cv.take(nV * 16 + 16);
+	const size_t oCodes = cv.take(nV + 16);
 	const size_t oVary = cv.take(rows * nw * 4);
 	const size_t oSlot = cv.take(info.nIn * 4 + 4);
 	const size_t oPolys = cv.take(kClipPolys * (1 + kMaxPoly) * 4);
@@ -189,6 +190,7 @@ extern "C" int srpGpuDrawFixedScratch(const SRPIndexBuffer* ib, const SRPVertexB
 	P.clip = (float4*) (base + oClip);
 	P.vset0 = (float4*) (base + oSet0);
 	P.vset1 = (float4*) (base + oSet1);
+	P.codes = (uint8_t*) (base + oCodes);
 	P.vary = (uint32_t*) (base + oVary);
 	P.clipBase = (uint32_t) nV;
 	P.clipCap = (uint32_t) kClipRows;
