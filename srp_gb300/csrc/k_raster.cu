@@ -545,6 +545,86 @@ __device__ __forceinline__ bool applyFragment(const DrawState& st, bool front, f
 	return true;
 }
 
+/* Light tiles of line fragments (early depth test). Every item is one
+ * fragment on one pixel, so no coverage masks are needed: a warp takes 32
+ * fragments at a time, the lanes whose fragments land on the same pixel find
+ * each other with match.any, and the first of them applies the group's
+ * fragments in item order to that pixel's depth/stencil state, which the
+ * warp keeps in shared memory for the whole tile. */
+__global__ void __launch_bounds__(kResolveWarps * 32) k_resolve_frags(const __grid_constant__ DrawParams P,
+                                                                     const uint32_t* vals, uint32_t numTiles)
+{
+	gridDepSync();
+	__shared__ float sDepth[kResolveWarps][64];
+	__shared__ uint32_t sSten[kResolveWarps][64];
+	__shared__ int32_t sWin[kResolveWarps][64];
+	__shared__ float sFd[kResolveWarps][32];
+	__shared__ uint32_t sFi[kResolveWarps][32];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const uint32_t tile = blockIdx.x * kResolveWarps + warp;
+	if (tile >= numTiles || P.ctr->abort) return;
+	const uint32_t s = P.tileStart[tile], e = P.tileEnd[tile];
+	if (s >= e || e - s > P.heavyItems) return;  /* empty, or k_resolve_heavy's */
+	const DrawState& st = P.st;
+	const TileCtx c = tileCtx<false>(P, tile);
+	const int x0 = c.x0, y0 = c.y0;
+	size_t idx[2];
+	bool valid[2];
+#pragma unroll
+	for (int p = 0; p < 2; ++p) {
+		const int q = lane + 32 * p;
+		const int gx = x0 + (q & 7), gy = y0 + (q >> 3);
+		valid[p] = gx < c.W && gy < c.H;
+		idx[p] = valid[p] ? (size_t) gy * c.W + gx : 0;
+		sDepth[warp][q] = valid[p] ? c.depth[idx[p]] : 0.0f;
+		sSten[warp][q] = valid[p] ? c.stencil[idx[p]] : 0u;
+		sWin[warp][q] = -1;
+	}
+	__syncwarp();
+	for (uint32_t b = s; b < e; b += 32) {
+		const uint32_t n = min(32u, e - b);
+		int q = -1;
+		float d = 0.0f;
+		uint32_t item = 0;
+		if ((uint32_t) lane < n) {
+			item = vals[b + lane];
+			const LineFrag F = P.frags[item];
+			/* the logical pixel, as the reference indexes it (px may equal the width) */
+			const unsigned long long at = (unsigned long long) (long long) F.py * (unsigned long long) st.W
+			                            + (unsigned long long) (long long) F.px;
+			const int gx = (int) (at % (unsigned long long) st.W), gy = (int) (at / (unsigned long long) st.W);
+			const int qq = (gy - y0) * kTile + (gx - x0);
+			if (qq >= 0 && qq < 64) q = qq;
+			d = F.depth;
+		}
+		sFd[warp][lane] = d;
+		sFi[warp][lane] = item;
+		const unsigned peers = __match_any_sync(0xFFFFFFFFu, q);
+		__syncwarp();
+		if (q >= 0 && lane == __ffs(peers) - 1) {
+			float depth = sDepth[warp][q];
+			uint32_t sten = sSten[warp][q];
+			int32_t win = sWin[warp][q];
+			for (unsigned m = peers; m; m &= m - 1) {
+				const int j = __ffs(m) - 1;
+				if (applyFragment(st, true, sFd[warp][j], depth, sten)) win = (int32_t) sFi[warp][j];
+			}
+			sDepth[warp][q] = depth;
+			sSten[warp][q] = sten;
+			sWin[warp][q] = win;
+		}
+		__syncwarp();
+	}
+#pragma unroll
+	for (int p = 0; p < 2; ++p) {
+		if (!valid[p]) continue;
+		const int q = lane + 32 * p;
+		c.depth[idx[p]] = sDepth[warp][q];
+		c.stencil[idx[p]] = (uint8_t) sSten[warp][q];
+		c.winner[idx[p]] = sWin[warp][q];
+	}
+}
+
 /* Tiles with many items (typically far-away meshes whose thousands of tiny
  * triangles land in a handful of tiles): a CTA takes 256 consecutive items
  * at a time, every thread evaluates one item's coverage and depths, warp
@@ -862,7 +942,7 @@ void launchResolve(const DrawParams& P, int kind, const uint32_t* vals, uint32_t
 		pdlLaunch(k_resolve<kKindPoint, 0>, b, kResolveWarps * 32, 0, s, P, vals, numTiles);
 	} else {
 		launchHeavy<kKindLineFrag>(P, vals, heavy, hs);
-		pdlLaunch(k_resolve<kKindLineFrag, 0>, b, kResolveWarps * 32, 0, s, P, vals, numTiles);
+		pdlLaunch(k_resolve_frags, b, kResolveWarps * 32, 0, s, P, vals, numTiles);
 	}
 	if (split) {
 		cudaEventRecord(join, aux);

@@ -241,3 +241,39 @@ def test_fixed_scratch_rejects_oversized_draws(api):
     assert rc == 0 and not api.errors(), api.errors()
     assert_same(api.planes(fb), api.planes(ordinary), "draw after rejections")
     assert L.srpGpuSynchronize() == 0
+
+
+def test_fixed_scratch_between_overlapped_draws(api):
+    """Ordinary draws overlap (the next draw's front stages beside the current
+    draw's resolve); fixed-scratch draws interleaved with them, all into one
+    framebuffer without waiting in between, give the image of the same
+    sequence drawn strictly serially."""
+    L = api.L
+    L.srpGpuSetFramebufferMode(1)
+    L.srpGpuSetDrawOverlap.argtypes = [ctypes.c_int]
+    rng = np.random.default_rng(99)
+    W, H = 512, 384
+    tris = [api.vertex_buffer(triangle_soup(rng, 3000)) for _ in range(3)]
+    walk = api.vertex_buffer(random_walk(rng, 2000))
+
+    def sequence(fb):
+        L.srpDrawVertexBuffer(tris[0], fb, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, 9000)
+        assert L.srpGpuDrawFixedScratch(None, walk, fb, ctypes.byref(api.prog), SRP_PRIM_LINE_STRIP, 0, 2000) == 0
+        L.srpDrawVertexBuffer(tris[1], fb, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, 9000)
+        L.srpDrawVertexBuffer(walk, fb, ctypes.byref(api.prog), SRP_PRIM_LINE_STRIP, 0, 2000)
+        assert L.srpGpuDrawFixedScratch(None, tris[2], fb, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, 9000) == 0
+        L.srpDrawVertexBuffer(tris[2], fb, ctypes.byref(api.prog), SRP_PRIM_LINE_STRIP, 0, 9000)
+        return api.planes(fb)
+
+    try:
+        L.srpGpuSetDrawOverlap(0)
+        want = sequence(api.framebuffer(W, H))
+        L.srpGpuSetDrawOverlap(1)
+        got = sequence(api.framebuffer(W, H))
+        got2 = sequence(api.framebuffer(W, H))
+    finally:
+        L.srpGpuSetDrawOverlap(1)
+    assert not api.errors(), api.errors()
+    assert_same(got, want, "overlapped sequence")
+    assert_same(got2, want, "overlapped sequence, graphs replayed")
+    assert L.srpGpuSynchronize() == 0
