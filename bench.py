@@ -132,6 +132,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def host_cpu():
+    """The host CPU's model name (lscpu) and the number of cores the process sees."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return {"model": model or platform.machine(), "nproc": os.cpu_count()}
+
+
 def cpu_frame(scale, frames, seed=SEED):
     exe = os.path.join(ROOT, "oracle", "_build", "port_scenes")
     out = subprocess.check_output([exe, "time", SCENE, str(seed), repr(float(scale)), str(frames)]).decode()
@@ -163,6 +178,7 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": {"workload": WORKLOAD, "seed": SEED},
             "cpu_baseline": {"value": round(value, 3), "unit": "Mfrag/s", "cores": cores, "kind": "port",
+                             "host": host_cpu(),
                              "sample": f"{frames} full frames per core, {cores} processes, wall {wall:.1f}s"},
             "e2e": {"value": round(value, 3), "unit": "Mfrag/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -756,10 +772,10 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         from srp_gb300.build import build_oracle
         build_oracle()
-        r = cpu_frame(1.0, 3)
+        r = cpu_frame(1.0, 5)
         line["cpu_baseline"] = {"value": round(r["fragments"] / r["mean_s"] / 1e6, 3), "unit": "Mfrag/s",
-                                "cores": 1, "kind": "port",
-                                "sample": "3 full frames of the same workload on 1 host core"}
+                                "cores": 1, "kind": "port", "host": host_cpu(),
+                                "sample": "5 full frames of the same workload on 1 host core (mean frame time)"}
     if rank == 0:
         print(json.dumps(line))
     sc.close()
