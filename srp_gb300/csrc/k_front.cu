@@ -236,7 +236,8 @@ __global__ void __launch_bounds__(kVertexThreads) k_vertex(const __grid_constant
 	gridDepSync();
 	extern __shared__ uint32_t stage[];
 	unsigned long long lo, hi;
-	if (P.indexSize) { lo = P.minmax[0]; hi = P.minmax[1]; }
+	if (P.indexSize && P.shadeAll) { lo = 0; hi = P.nVertices ? P.nVertices - 1 : 0; }
+	else if (P.indexSize) { lo = P.minmax[0]; hi = P.minmax[1]; }
 	else { lo = P.start; hi = P.start + P.count - 1; }
 	if (hi >= P.nVertices) {
 		if (threadIdx.x == 0 && blockIdx.x == 0 && P.indexSize) atomicOr(&P.ctr->errors, kErrBadIndex);

@@ -15,6 +15,8 @@ struct DrawParams {
 	int vsId, fsId;
 	int prim;                      /* SRPPrimitive of the draw */
 	int indexSize;                 /* 0: non-indexed, else 1/2/4/8 bytes */
+	int shadeAll;                  /* indexed: shade every vertex of the buffer instead of
+	                                  the index range found by k_index_range */
 	const void* indices;           /* device copy of the index buffer */
 	unsigned long long start, count;
 	const unsigned char* vertices; /* device copy of the vertex buffer (user AoS) */

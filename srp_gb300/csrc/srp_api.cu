@@ -1119,6 +1119,10 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		if (!uploadIB(ib)) return;
 		P.indices = ib->dev.ptr;
 		P.indexSize = (int) ib->elemSize;
+		/* as many indices as vertices: the range very likely covers the
+		 * buffer, so every vertex is shaded (the shader is a pure function;
+		 * unreferenced results are never read) and the range pass is skipped */
+		P.shadeAll = count >= vb->nVertices ? 1 : 0;
 		if (ib->type != SRP_UINT8 && ib->type != SRP_UINT16 && ib->type != SRP_UINT32 && ib->type != SRP_UINT64) {
 			SRP_ERROR("indexIndexBuffer", "Unexpected type (%i)", (int) ib->type);
 			return;
@@ -1199,10 +1203,10 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		auto head = [&]() {
 			stageBegin();
 			launchReset(P, fs);
-			if (ib) launchIndexRange(P, fs);
+			if (ib && !P.shadeAll) launchIndexRange(P, fs);
 			if (ib) launchVertex(P, 0, vb->nVertices, fs);
 			else launchVertex(P, start, count, fs);
-			stageEnd(SRP_GPU_STAGE_VERTEX, ib ? 3 : 2);
+			stageEnd(SRP_GPU_STAGE_VERTEX, ib && !P.shadeAll ? 3 : 2);
 			stageBegin();
 			cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, fs);
 			if (isTri(prim)) launchClipPrepass(P, fs);
@@ -1254,7 +1258,8 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		                         keyBits, numTiles, g.bigJobsSeen[kind], (unsigned long long) (uintptr_t) g.stream,
 		                         (unsigned long long) (uintptr_t) fs }),
 		           S, fs, head, kind == kKindTri, mid, bin, back);
-		g.launches += 4 + (ib ? 1 : 0) + (isTri(prim) ? 1 : 0) + (kind == kKindPoint ? 1 : 2) + 1 + keyBits / 8 + 1 +
+		g.launches += 4 + (ib && !P.shadeAll ? 1 : 0) + (isTri(prim) ? 1 : 0) + (kind == kKindPoint ? 1 : 2) + 1 +
+		              keyBits / 8 + 1 +
 		              (late ? 1 : 4);
 		if (!cudaOk(cudaGetLastError(), FN, "launch")) return;
 		/* wait for the setup counters only; the rest of the draw runs on */
