@@ -211,7 +211,7 @@ constexpr size_t kGraphCache = 64;
 
 struct GraphEntry {
 	std::vector<unsigned char> key;
-	cudaGraphExec_t head = nullptr, mid = nullptr, bin = nullptr, back = nullptr;
+	cudaGraphExec_t head = nullptr, head2 = nullptr, mid = nullptr, bin = nullptr, back = nullptr;
 };
 
 std::vector<GraphEntry> graphCache;
@@ -239,8 +239,10 @@ template <class F> cudaGraphExec_t captureGraph(cudaStream_t s, F&& enqueue)
 	return exec;
 }
 
-/* Runs a draw as four sequences:
- * - head: reset up to the check kernel, on the front stream `fs`;
+/* Runs a draw as five sequences:
+ * - head and head2: reset up to the check kernel, on the front stream `fs`,
+ *   split so that `between` (an upload the second part needs) can be waited
+ *   for in the middle;
  * - mid: work that needs the head but not the binning (the lambda tables),
  *   on the library's stream, beside the bin;
  * - bin: binning and sort, on `fs`;
@@ -250,9 +252,9 @@ template <class F> cudaGraphExec_t captureGraph(cudaStream_t s, F&& enqueue)
  * head and bin the counters are copied to the set's host mirror. Each
  * sequence replays its captured CUDA graph when graphs are on and stage
  * profiling is off (profiling records fresh events per draw). */
-template <class H, class M, class B, class K>
-void runDrawSeq(const std::vector<unsigned char>& key, DrawSet& S, cudaStream_t fs, H&& head, bool hasMid, M&& mid,
-                B&& bin, K&& back)
+template <class H, class H2, class M, class B, class K>
+void runDrawSeq(const std::vector<unsigned char>& key, DrawSet& S, cudaStream_t fs, H&& head, cudaEvent_t between,
+                H2&& head2, bool hasMid, M&& mid, B&& bin, K&& back)
 {
 	GraphEntry* e = nullptr;
 	if (g.graphs && !g.profiling) {
@@ -261,22 +263,27 @@ void runDrawSeq(const std::vector<unsigned char>& key, DrawSet& S, cudaStream_t 
 			GraphEntry fresh;
 			fresh.key = key;
 			fresh.head = captureGraph(fs, head);
-			fresh.mid = fresh.head && hasMid ? captureGraph(g.stream, mid) : nullptr;
-			fresh.bin = fresh.head && (fresh.mid || !hasMid) ? captureGraph(fs, bin) : nullptr;
+			fresh.head2 = fresh.head ? captureGraph(fs, head2) : nullptr;
+			fresh.mid = fresh.head2 && hasMid ? captureGraph(g.stream, mid) : nullptr;
+			fresh.bin = fresh.head2 && (fresh.mid || !hasMid) ? captureGraph(fs, bin) : nullptr;
 			fresh.back = fresh.bin ? captureGraph(g.stream, back) : nullptr;
 			if (graphCache.size() < kGraphCache) graphCache.push_back(std::move(fresh));
 			else {
 				GraphEntry& old = graphCache[graphNext++ % kGraphCache];
-				for (cudaGraphExec_t x : { old.head, old.mid, old.bin, old.back })
+				for (cudaGraphExec_t x : { old.head, old.head2, old.mid, old.bin, old.back })
 					if (x) cudaGraphExecDestroy(x);
 				old = std::move(fresh);
 			}
 			e = graphFind(key);
 		}
-		if (e && !(e->head && (e->mid || !hasMid) && e->bin && e->back)) e = nullptr;
+		if (e && !(e->head && e->head2 && (e->mid || !hasMid) && e->bin && e->back)) e = nullptr;
 	}
 	if (e) cudaGraphLaunch(e->head, fs);
 	else head();
+	/* an input the second part of the head needs, uploaded meanwhile */
+	if (between && fs != g.stream) cudaStreamWaitEvent(fs, between, 0);
+	if (e) cudaGraphLaunch(e->head2, fs);
+	else head2();
 	cudaMemcpyAsync(S.hostCtr, S.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, fs);
 	cudaEventRecord(S.ctrEvent, fs);
 	if (hasMid) {
@@ -1207,6 +1214,8 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			if (ib) launchVertex(P, 0, vb->nVertices, fs);
 			else launchVertex(P, start, count, fs);
 			stageEnd(SRP_GPU_STAGE_VERTEX, ib && !P.shadeAll ? 3 : 2);
+		};
+		auto head2 = [&]() {
 			stageBegin();
 			cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, fs);
 			if (isTri(prim)) launchClipPrepass(P, fs);
@@ -1248,16 +1257,19 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			}
 		};
 		/* the front waits for the last back that used this set, and for the
-		 * uploads of the buffers it reads (both on the library's stream) */
+		 * uploads of the buffers it reads (both on the library's stream); when
+		 * the whole vertex buffer is shaded, the vertex stage needs no indices
+		 * and the index upload is waited for before setup only */
+		const bool lateIb = ib && P.shadeAll && ib->ready;
 		if (fs != g.stream) {
 			cudaStreamWaitEvent(fs, S.rasterDone, 0);
 			if (vb->ready) cudaStreamWaitEvent(fs, vb->ready, 0);
-			if (ib && ib->ready) cudaStreamWaitEvent(fs, ib->ready, 0);
+			if (ib && ib->ready && !lateIb) cudaStreamWaitEvent(fs, ib->ready, 0);
 		}
 		runDrawSeq(graphKey(P, { (unsigned long long) kind, late, ib != nullptr, start, count, vb->nVertices, blocks,
 		                         keyBits, numTiles, g.bigJobsSeen[kind], (unsigned long long) (uintptr_t) g.stream,
 		                         (unsigned long long) (uintptr_t) fs }),
-		           S, fs, head, kind == kKindTri, mid, bin, back);
+		           S, fs, head, lateIb ? ib->ready : nullptr, head2, kind == kKindTri, mid, bin, back);
 		g.launches += 4 + (ib && !P.shadeAll ? 1 : 0) + (isTri(prim) ? 1 : 0) + (kind == kKindPoint ? 1 : 2) + 1 +
 		              keyBits / 8 + 1 +
 		              (late ? 1 : 4);
@@ -1600,6 +1612,8 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 			launchReset(P, g.stream);
 			launchVertexMulti(P, vBlocks, maxStride, g.stream);
 			stageEnd(SRP_GPU_STAGE_VERTEX, 2);
+		};
+		auto head2 = [&]() {
 			stageBegin();
 			cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, g.stream);
 			launchClipPrepassMulti(P, g.stream);
@@ -1630,7 +1644,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		};
 		runDrawSeq(graphKey(P, { vBlocks, (unsigned long long) maxStride, blocks, keyBits, numTiles,
 		                         g.bigJobsSeen[kKindTri], (unsigned long long) (uintptr_t) g.stream }),
-		           S, g.stream, head, false, [] {}, bin, back);
+		           S, g.stream, head, nullptr, head2, false, [] {}, bin, back);
 		markPassDone();
 		g.launches += 5 + 2 + 1 + keyBits / 8 + 1 + 4;
 		if (!cudaOk(cudaGetLastError(), FN, "launch")) return false;

@@ -1455,8 +1455,14 @@ void sceneBatchRender(Scene** scenes, SRPFramebuffer** fbs, size_t n, SRPGpuDraw
 
 void sceneUploadAsync(Scene* s)
 {
-	for (int k = 0; k < s->nvb; ++k) srpGpuVertexBufferCopyDataAsync(s->vb[k], s->vstride[k], s->vbytes[k], s->vdata[k]);
-	for (int k = 0; k < s->nib; ++k) srpGpuIndexBufferCopyDataAsync(s->ib[k], s->itype[k], s->ibytes[k], s->idata[k]);
+	/* the first draw's buffers first (vertex, then index buffer), so that its
+	 * vertex stage can start while the rest is still on the way */
+	for (int k = 0; k < s->nvb; ++k) {
+		srpGpuVertexBufferCopyDataAsync(s->vb[k], s->vstride[k], s->vbytes[k], s->vdata[k]);
+		if (k == 0 && s->nib > 0) srpGpuIndexBufferCopyDataAsync(s->ib[0], s->itype[0], s->ibytes[0], s->idata[0]);
+	}
+	for (int k = 1; k < s->nib; ++k) srpGpuIndexBufferCopyDataAsync(s->ib[k], s->itype[k], s->ibytes[k], s->idata[k]);
+	if (s->nvb == 0 && s->nib > 0) srpGpuIndexBufferCopyDataAsync(s->ib[0], s->itype[0], s->ibytes[0], s->idata[0]);
 }
 
 void scenePrepareBatch(Scene** scenes, SRPFramebuffer** fbs, size_t n)
