@@ -96,6 +96,8 @@ struct Registry {
 struct DrawSet {
 	DeviceBuffer ctr, tileStart, tileEnd, heavy, vary, triR, triA, points, lines, frags, table;
 	DeviceBuffer keys, vals, keys2, vals2;
+	/* multi-draw passes: descriptors, prefix sums, primitive bases, winners */
+	DeviceBuffer passDesc, passPrefix, passPrimPrefix, passWinner;
 	DeviceCounters* hostCtr = nullptr;
 	cudaEvent_t ctrEvent = nullptr;    /* recorded after the counters are copied to hostCtr */
 	cudaEvent_t headDone = nullptr;    /* vertex and setup done (front stream) */
@@ -408,6 +410,7 @@ struct SRPVertexBuffer {
 	DeviceBuffer dev;
 	bool dirty = false;
 	cudaEvent_t ready = nullptr;      /* recorded after the last upload (library stream) */
+	bool pending = false;             /* uploaded since a pass's front last waited for it */
 };
 
 struct SRPIndexBuffer {
@@ -417,11 +420,12 @@ struct SRPIndexBuffer {
 	DeviceBuffer dev;
 	bool dirty = false;
 	cudaEvent_t ready = nullptr;
+	bool pending = false;
 };
 
 /* Marks the end of an upload into a buffer: the front stream of a later
  * draw waits for it. */
-static void markUpload(cudaEvent_t& ready)
+static void markUpload(cudaEvent_t& ready, bool& pending)
 {
 	if (!ready && cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) != cudaSuccess) {
 		cudaGetLastError();
@@ -429,6 +433,7 @@ static void markUpload(cudaEvent_t& ready)
 		return;
 	}
 	cudaEventRecord(ready, g.stream);
+	pending = true;
 }
 
 static size_t indexTypeSize(SRPType t)
@@ -513,7 +518,7 @@ void srpVertexBufferCopyData(SRPVertexBuffer* b, size_t stride, size_t nBytes, c
 	b->nBytes = nBytes;
 	if (gpuPresent()) {
 		b->dirty = !copyToDevice(b->dev, data, nBytes, "srpVertexBufferCopyData");
-		if (!b->dirty) { markUpload(b->ready); return; }
+		if (!b->dirty) { markUpload(b->ready, b->pending); return; }
 	}
 	/* no device: keep a host copy, uploaded by the first draw */
 	if (nBytes > b->cap) { b->host = (unsigned char*) pinnedRealloc(b->host, nBytes); b->cap = nBytes; }
@@ -529,7 +534,7 @@ void srpGpuVertexBufferCopyDataAsync(SRPVertexBuffer* b, size_t stride, size_t n
 	b->nBytes = nBytes;
 	b->dirty = !copyToDeviceAsync(b->dev, data, nBytes, "srpGpuVertexBufferCopyDataAsync");
 	if (b->dirty) srpVertexBufferCopyData(b, stride, nBytes, data);
-	else markUpload(b->ready);
+	else markUpload(b->ready, b->pending);
 }
 
 SRPIndexBuffer* srpNewIndexBuffer(void) { return new SRPIndexBuffer(); }
@@ -552,7 +557,7 @@ void srpIndexBufferCopyData(SRPIndexBuffer* b, SRPType type, size_t nBytes, cons
 	b->nBytes = nBytes;
 	if (gpuPresent()) {
 		b->dirty = !copyToDevice(b->dev, data, nBytes, "srpIndexBufferCopyData");
-		if (!b->dirty) { markUpload(b->ready); return; }
+		if (!b->dirty) { markUpload(b->ready, b->pending); return; }
 	}
 	if (nBytes > b->cap) { b->host = (unsigned char*) pinnedRealloc(b->host, nBytes); b->cap = nBytes; }
 	if (nBytes) memcpy(b->host, data, nBytes);
@@ -568,7 +573,7 @@ void srpGpuIndexBufferCopyDataAsync(SRPIndexBuffer* b, SRPType type, size_t nByt
 	b->nBytes = nBytes;
 	b->dirty = !copyToDeviceAsync(b->dev, data, nBytes, "srpGpuIndexBufferCopyDataAsync");
 	if (b->dirty) srpIndexBufferCopyData(b, type, nBytes, data);
-	else markUpload(b->ready);
+	else markUpload(b->ready, b->pending);
 }
 
 }  // extern "C"
@@ -1011,7 +1016,7 @@ static bool uploadVB(SRPVertexBuffer* vb)
 	if (!vb->dev.reserve(vb->nBytes + 16, "srpDraw")) return false;
 	if (vb->nBytes) cudaMemcpyAsync(vb->dev.ptr, vb->host, vb->nBytes, cudaMemcpyHostToDevice, g.stream);
 	vb->dirty = false;
-	markUpload(vb->ready);
+	markUpload(vb->ready, vb->pending);
 	return true;
 }
 
@@ -1021,7 +1026,7 @@ static bool uploadIB(SRPIndexBuffer* ib)
 	if (!ib->dev.reserve(ib->nBytes + 16, "srpDraw")) return false;
 	if (ib->nBytes) cudaMemcpyAsync(ib->dev.ptr, ib->host, ib->nBytes, cudaMemcpyHostToDevice, g.stream);
 	ib->dirty = false;
-	markUpload(ib->ready);
+	markUpload(ib->ready, ib->pending);
 	return true;
 }
 
@@ -1428,7 +1433,7 @@ struct PinnedBuffer {
  * which follow the upload on the stream, before the staging is reused. */
 PinnedBuffer passDesc;
 std::vector<uint32_t> passPrefix;   /* in, v, t, blk: 4 x (n + 1) */
-DeviceBuffer passDescDev, passPrefixDev, passPrimPrefix, passWinner;
+
 
 }  // namespace
 
@@ -1451,9 +1456,12 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	static DrawParams P;
 	memset(&P, 0, sizeof P);
 	if (g.tuneArmed) { cudaEventRecord(g.tuneStart, g.stream); g.tuneArmed = false; }
-	/* a pass runs on the library's stream with the first scratch set; later
-	 * single draws' fronts wait for it through both sets' rasterDone */
-	DrawSet& S = g.sets[0];
+	/* a pass takes the next scratch set like a single draw; its front stages
+	 * run on the front stream beside the previous pass's resolve and shading
+	 * (except with learned shading, whose judge reshades on the library's
+	 * stream: such a pass runs there whole) */
+	DrawSet& S = g.sets[g.setNext];
+	g.setNext ^= 1;
 	if (!buildLayout(sp0->vs, P.L)) return true;
 	DrawState& st = P.st;
 	st.frontFaceCW = srpContext.raster.frontFace == SRP_WINDING_CW;
@@ -1539,19 +1547,17 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		pix += d.framebuffer->size;
 	}
 	const uint32_t nIn = pIn[n], vRows = pV[n], numTiles = pT[n], vBlocks = pB[n];
-	if (!passDescDev.reserve(n * sizeof(DrawDesc), FN) || !passPrefixDev.reserve(passPrefix.size() * 4, FN) ||
-	    !passPrimPrefix.reserve((n + 1) * 4, FN) || !passWinner.reserve(pix * 4 + 4, FN))
+	if (!S.passDesc.reserve(n * sizeof(DrawDesc), FN) || !S.passPrefix.reserve(passPrefix.size() * 4, FN) ||
+	    !S.passPrimPrefix.reserve((n + 1) * 4, FN) || !S.passWinner.reserve(pix * 4 + 4, FN))
 		return false;
-	for (size_t k = 0; k < n; ++k) desc[k].winner = passWinner.as<int32_t>() + pixBase[k];
-	cudaMemcpyAsync(passDescDev.ptr, desc, n * sizeof(DrawDesc), cudaMemcpyHostToDevice, g.stream);
-	cudaMemcpyAsync(passPrefixDev.ptr, passPrefix.data(), passPrefix.size() * 4, cudaMemcpyHostToDevice, g.stream);
-	P.draws = passDescDev.as<DrawDesc>();
+	for (size_t k = 0; k < n; ++k) desc[k].winner = S.passWinner.as<int32_t>() + pixBase[k];
+	P.draws = S.passDesc.as<DrawDesc>();
 	P.nDraws = (uint32_t) n;
-	P.inPrefix = passPrefixDev.as<uint32_t>();
+	P.inPrefix = S.passPrefix.as<uint32_t>();
 	P.vPrefix = P.inPrefix + (n + 1);
 	P.tPrefix = P.vPrefix + (n + 1);
 	P.blkPrefix = P.tPrefix + (n + 1);
-	P.primPrefix = passPrimPrefix.as<uint32_t>();
+	P.primPrefix = S.passPrimPrefix.as<uint32_t>();
 	P.nIn = (int) nIn;
 	P.nVertices = vRows;
 	P.minmax = g.minmax.as<unsigned long long>();
@@ -1560,6 +1566,35 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		for (size_t k = 0; k < n; ++k) fbUpload(draws[idx[k]].framebuffer, fbFind(draws[idx[k]].framebuffer));
 
 	const bool learned = learnedPrepare(P, kKindTri, false, (uint32_t) n, g.stream);
+	const cudaStream_t fs = (g.overlap && !g.profiling && !learned) ? g.frontStream : g.stream;
+	if (fs != g.stream) {
+		/* the front waits for the last back that used this set and for the
+		 * uploads of the draws' buffers since a front last waited for them (one
+		 * event of the library's stream stands for many) */
+		cudaStreamWaitEvent(fs, S.rasterDone, 0);
+		size_t pending = 0;
+		for (size_t k = 0; k < n; ++k) {
+			const SRPGpuDraw& d = draws[idx[k]];
+			pending += ((SRPVertexBuffer*) d.vertexBuffer)->pending;
+			if (d.indexBuffer) pending += ((SRPIndexBuffer*) d.indexBuffer)->pending;
+		}
+		if (pending > 64) {
+			cudaEventRecord(S.headDone, g.stream);
+			cudaStreamWaitEvent(fs, S.headDone, 0);
+		}
+		for (size_t k = 0; k < n; ++k) {
+			const SRPGpuDraw& d = draws[idx[k]];
+			SRPVertexBuffer* vb = (SRPVertexBuffer*) d.vertexBuffer;
+			SRPIndexBuffer* ib = (SRPIndexBuffer*) d.indexBuffer;
+			if (vb->pending && pending <= 64) cudaStreamWaitEvent(fs, vb->ready, 0);
+			if (ib && ib->pending && pending <= 64) cudaStreamWaitEvent(fs, ib->ready, 0);
+			vb->pending = false;
+			if (ib) ib->pending = false;
+		}
+	}
+	/* descriptors and prefix sums go up on the front stream, ahead of the head */
+	cudaMemcpyAsync(S.passDesc.ptr, desc, n * sizeof(DrawDesc), cudaMemcpyHostToDevice, fs);
+	cudaMemcpyAsync(S.passPrefix.ptr, passPrefix.data(), passPrefix.size() * 4, cudaMemcpyHostToDevice, fs);
 	uint32_t primCap = (uint32_t) std::min<unsigned long long>((unsigned long long) nIn + 4096, 0x3FFFFFFFu);
 	uint32_t entryCap = (uint32_t) std::min<double>((double) nIn * g.entryRatio[kKindTri] + 4096, 4.0e9);
 	const uint32_t keyBits = bitsFor(numTiles);
@@ -1609,29 +1644,29 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 
 		auto head = [&]() {
 			stageBegin();
-			launchReset(P, g.stream);
-			launchVertexMulti(P, vBlocks, maxStride, g.stream);
+			launchReset(P, fs);
+			launchVertexMulti(P, vBlocks, maxStride, fs);
 			stageEnd(SRP_GPU_STAGE_VERTEX, 2);
 		};
 		auto head2 = [&]() {
 			stageBegin();
-			cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, g.stream);
-			launchClipPrepassMulti(P, g.stream);
-			launchSetupMulti(P, g.stream);
-			launchCheck(P, g.stream);
+			cudaMemsetAsync(P.lookback, 0, (size_t) blocks * 8, fs);
+			launchClipPrepassMulti(P, fs);
+			launchSetupMulti(P, fs);
+			launchCheck(P, fs);
 			stageEnd(SRP_GPU_STAGE_SETUP, 3);
 		};
 		uint32_t* sk = nullptr;
 		uint32_t* sv = nullptr;
 		auto bin = [&]() {
 			stageBegin();
-			launchLambdaTablesMulti(P, g.bigJobsSeen[kKindTri], g.stream);
-			launchBigEntriesMulti(P, g.bigJobsSeen[kKindTri], g.stream);
+			launchLambdaTablesMulti(P, g.bigJobsSeen[kKindTri], fs);
+			launchBigEntriesMulti(P, g.bigJobsSeen[kKindTri], fs);
 			sortEntries(P, keyBits, S.keys2.as<uint32_t>(), S.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
-			            g.partials.as<uint32_t>(), &sk, &sv, g.stream);
-			cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, g.stream);
-			cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, g.stream);
-			launchTileRanges(P, sk, numTiles, g.stream);
+			            g.partials.as<uint32_t>(), &sk, &sv, fs);
+			cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, fs);
+			cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, fs);
+			launchTileRanges(P, sk, numTiles, fs);
 			stageEnd(SRP_GPU_STAGE_BIN, 2 + 1 + (int) (keyBits / 8) + 1);
 		};
 		auto back = [&]() {
@@ -1643,15 +1678,17 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 			stageEnd(SRP_GPU_STAGE_SHADE, 1);
 		};
 		runDrawSeq(graphKey(P, { vBlocks, (unsigned long long) maxStride, blocks, keyBits, numTiles,
-		                         g.bigJobsSeen[kKindTri], (unsigned long long) (uintptr_t) g.stream }),
-		           S, g.stream, head, nullptr, head2, false, [] {}, bin, back);
-		markPassDone();
+		                         g.bigJobsSeen[kKindTri], (unsigned long long) (uintptr_t) g.stream,
+		                         (unsigned long long) (uintptr_t) fs }),
+		           S, fs, head, nullptr, head2, false, [] {}, bin, back);
+		if (fs == g.stream) markPassDone();
 		g.launches += 5 + 2 + 1 + keyBits / 8 + 1 + 4;
 		if (!cudaOk(cudaGetLastError(), FN, "launch")) return false;
 		if (!cudaOk(cudaEventSynchronize(S.ctrEvent), FN, "kernel execution")) return false;
 		const DeviceCounters c = *S.hostCtr;
 		if (c.errors & kErrBadIndex) {
 			/* some draw indexes past its vertex buffer: let each report alone */
+			cudaStreamSynchronize(fs);
 			cudaStreamSynchronize(g.stream);
 			for (size_t k = 0; k < n; ++k) {
 				const SRPGpuDraw& d = draws[idx[k]];
@@ -1661,6 +1698,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		}
 		if (c.errors & kErrSpin) { SRP_ERROR(FN, "Ordered-compaction wait timed out"); return false; }
 		if (c.abort) {
+			cudaStreamSynchronize(fs);
 			cudaStreamSynchronize(g.stream);
 			bool grew = false;
 			if (c.clipVerts > g.clipRows) { g.clipRows = (uint32_t) std::min<unsigned long long>(c.clipVerts * 2, 0x7FFFFFFF); grew = true; }
@@ -1698,7 +1736,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	g.stats.draws += n;
 	if (g.fbMode == SRP_GPU_FB_COHERENT)
 		for (size_t k = 0; k < n; ++k) fbDownload(draws[idx[k]].framebuffer, fbFind(draws[idx[k]].framebuffer));
-	markPassDone();
+	if (fs == g.stream) markPassDone();
 	return true;
 }
 
@@ -1715,6 +1753,8 @@ void srpDrawIndexBuffer(const SRPIndexBuffer* ib, const SRPVertexBuffer* vb, con
 {
 	drawBuffer(ib, vb, fb, sp, prim, start, count);
 }
+
+constexpr size_t kPassDraws = 1024;
 
 void srpGpuDrawBatch(const SRPGpuDraw* draws, size_t n)
 {
@@ -1750,6 +1790,9 @@ void srpGpuDrawBatch(const SRPGpuDraw* draws, size_t n)
 			const unsigned long long t = (unsigned long long) ((d.framebuffer->width + kTile - 1) / kTile) *
 			                             ((d.framebuffer->height + kTile - 1) / kTile);
 			if (in + k > kMaxIn || rows + d.vertexBuffer->nVertices > kMaxRows || tiles + t >= kMaxTiles) break;
+			/* passes of at most kPassDraws draws, so that the front stages of
+			 * one pass overlap the resolve and shading of the previous one */
+			if (idx.size() >= kPassDraws) break;
 			in += k; rows += d.vertexBuffer->nVertices; tiles += t;
 			idx.push_back(j); nInOf.push_back(k);
 		}

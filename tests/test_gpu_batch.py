@@ -249,3 +249,36 @@ def test_async_transfers_and_fill_batch_match_the_synchronous_path(built_library
         for sc in scenes:
             sc.close()
     assert L.srpGpuSynchronize() == 0
+
+
+def test_overlapped_passes_match_serial_passes(built_library):
+    """A batch of more than 1024 draws runs as several passes whose front
+    stages overlap the previous pass's resolve and shading (two scratch sets);
+    its images equal those of the same batch drawn with every stage on one
+    stream, also when the graphs are replayed."""
+    import srp_gb300
+    L = srp_gb300.lib()
+    S = srp_gb300.scenes()
+    L.srpGpuSetFramebufferMode(1)
+    scenes = make_scenes(1100, 0.1)
+    try:
+        fbs = [sc.fb for sc in scenes]
+
+        def render():
+            srp_gb300.prepare_batch(scenes, fbs)
+            srp_gb300.render_batch(scenes, fbs)
+            return [sync_planes(srp_gb300, S, fb) for fb in fbs]
+
+        L.srpGpuSetDrawOverlap(0)
+        want = render()
+        L.srpGpuSetDrawOverlap(1)
+        for _ in range(2):
+            got = render()
+            for i, (a, b) in enumerate(zip(got, want)):
+                for x, y in zip(a, b):
+                    assert np.array_equal(x, y), i
+    finally:
+        L.srpGpuSetDrawOverlap(1)
+        for sc in scenes:
+            sc.close()
+    assert L.srpGpuSynchronize() == 0
