@@ -39,6 +39,7 @@ __device__ __forceinline__ void rasterTexSample(const void* tex, float u, float 
 namespace srpg {
 
 constexpr int kResolveWarps = 4;
+constexpr int kShadeTiles = 2;     /* tiles per block of k_shade (64 threads each) */
 /* Light tiles of a multi-draw pass: items per chunk of a warp. Fewer than
  * the 32 lanes, so that the per-item depth rows take half the shared memory
  * and 8 blocks (64 registers a thread) fit an SM: the many light tiles of a
@@ -733,24 +734,23 @@ __global__ void k_tile_classify(const __grid_constant__ DrawParams P, uint32_t n
 /* Deferred shading: one shader invocation per pixel whose colour was written
  * by the resolve pass. */
 template <int KIND, int FS, bool MULTI = false>
-__global__ void __launch_bounds__(kResolveWarps * 32) k_shade(const __grid_constant__ DrawParams P, uint32_t numTiles)
+__global__ void __launch_bounds__(kShadeTiles * 64) k_shade(const __grid_constant__ DrawParams P, uint32_t numTiles)
 {
 	gridDepSync();
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	const uint32_t tile = blockIdx.x * kResolveWarps + warp;
+	/* one pixel a thread, two warps a tile */
+	const uint32_t tile = blockIdx.x * kShadeTiles + (threadIdx.x >> 6);
+	const int q = threadIdx.x & 63;
 	if (tile >= numTiles || P.ctr->abort) return;
 	if (P.tileStart[tile] >= P.tileEnd[tile]) return;
 	const TileCtx c = tileCtx<MULTI>(P, tile);
 	if (MULTI && P.redo && !P.redo[c.d]) return;
 	const int x0 = c.x0, y0 = c.y0;
-#pragma unroll
-	for (int p = 0; p < 2; ++p) {
-		const int q = lane + 32 * p;
+	{
 		const int gx = x0 + (q & 7), gy = y0 + (q >> 3);
-		if (gx >= c.W || gy >= c.H) continue;
+		if (gx >= c.W || gy >= c.H) return;
 		const size_t idx = (size_t) gy * c.W + gx;
 		const int32_t w = c.winner[idx];
-		if (w < 0) continue;
+		if (w < 0) return;
 		SRPFragmentShaderOut out;
 		if constexpr (KIND == kKindTri && FS == SRP_GPU_FS_MARBLE) {
 			/* the shader learned shading stands in for: captured for training */
@@ -970,8 +970,8 @@ void launchResolveLate(const DrawParams& P, int kind, const uint32_t* vals, uint
 template <int KIND, bool MULTI = false>
 static void shadeKind(const DrawParams& P, uint32_t numTiles, cudaStream_t s)
 {
-	const unsigned b = tileBlocks(numTiles);
-	const unsigned t = kResolveWarps * 32;
+	const unsigned b = (numTiles + kShadeTiles - 1) / kShadeTiles;
+	const unsigned t = kShadeTiles * 64;
 	switch (P.fsId) {
 	case SRP_GPU_FS_VARYING_COLOR: pdlLaunch(k_shade<KIND, SRP_GPU_FS_VARYING_COLOR, MULTI>, b, t, 0, s, P, numTiles); break;
 	case SRP_GPU_FS_SOLID: pdlLaunch(k_shade<KIND, SRP_GPU_FS_SOLID, MULTI>, b, t, 0, s, P, numTiles); break;
