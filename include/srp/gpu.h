@@ -47,6 +47,11 @@ SRPGpuFramebufferMode srpGpuGetFramebufferMode(void);
 void srpGpuFramebufferSync(const SRPFramebuffer* fb);
 /** Copy the host arrays to the device planes. */
 void srpGpuFramebufferUpload(const SRPFramebuffer* fb);
+/** Sync the framebuffer and write its colour plane as a PNG (RGBA8, alpha
+ *  255, top row first): what the reference's test harness does with
+ *  stb_image_write (tests/utils/save.c:3-34), without the dependency.
+ *  Returns 0 on success. */
+int srpGpuSaveFramebufferPNG(const SRPFramebuffer* fb, const char* path);
 
 #define SRP_GPU_FILL_COLOR   1u
 #define SRP_GPU_FILL_DEPTH   2u

@@ -176,3 +176,78 @@ int srpImageWritePPM(const char* path, const uint8_t* rgb, int width, int height
 	fclose(f);
 	return ok;
 }
+
+/* ------------------------------------------------------------ PNG writer */
+
+/* CRC-32 (ISO 3309, as PNG chunks use it), bitwise. */
+static uint32_t png_crc(uint32_t crc, const unsigned char* p, size_t n)
+{
+	crc = ~crc;
+	for (size_t i = 0; i < n; ++i) {
+		crc ^= p[i];
+		for (int k = 0; k < 8; ++k) crc = (crc >> 1) ^ (0xEDB88320u & (0u - (crc & 1u)));
+	}
+	return ~crc;
+}
+
+static void put32(unsigned char* p, uint32_t v)
+{
+	p[0] = (unsigned char) (v >> 24); p[1] = (unsigned char) (v >> 16);
+	p[2] = (unsigned char) (v >> 8); p[3] = (unsigned char) v;
+}
+
+static int png_chunk(FILE* f, const char* type, const unsigned char* data, size_t n)
+{
+	unsigned char hdr[8];
+	put32(hdr, (uint32_t) n);
+	memcpy(hdr + 4, type, 4);
+	uint32_t crc = png_crc(0, hdr + 4, 4);
+	crc = png_crc(crc, data, n);
+	unsigned char tail[4];
+	put32(tail, crc);
+	return fwrite(hdr, 1, 8, f) == 8 && (n == 0 || fwrite(data, 1, n, f) == n) && fwrite(tail, 1, 4, f) == 4;
+}
+
+int srpImageWritePNG(const char* path, const uint8_t* rgba, int width, int height)
+{
+	if (width <= 0 || height <= 0) return 0;
+	/* filter byte 0 (none) before every row of RGBA8 */
+	const size_t row = (size_t) width * 4 + 1, raw = row * (size_t) height;
+	/* zlib stream of stored deflate blocks (at most 65535 bytes each) */
+	const size_t blocks = (raw + 65534) / 65535;
+	const size_t zn = 2 + raw + blocks * 5 + 4;
+	unsigned char* z = (unsigned char*) malloc(zn);
+	if (!z) return 0;
+	size_t o = 0;
+	z[o++] = 0x78; z[o++] = 0x01;
+	uint32_t a = 1, b = 0;   /* Adler-32 of the uncompressed bytes */
+	size_t done = 0;
+	for (int y = 0; y < height; ++y) {
+		for (size_t i = 0; i < row; ++i) {
+			if (done % 65535 == 0) {
+				const size_t len = raw - done < 65535 ? raw - done : 65535;
+				z[o++] = (unsigned char) (done + len == raw ? 1 : 0);
+				z[o++] = (unsigned char) len; z[o++] = (unsigned char) (len >> 8);
+				z[o++] = (unsigned char) ~len; z[o++] = (unsigned char) (~len >> 8);
+			}
+			const unsigned char v = i == 0 ? 0 : rgba[(size_t) y * width * 4 + (i - 1)];
+			z[o++] = v;
+			a = (a + v) % 65521u;
+			b = (b + a) % 65521u;
+			++done;
+		}
+	}
+	put32(z + o, (b << 16) | a);
+	o += 4;
+	FILE* f = fopen(path, "wb");
+	if (!f) { free(z); return 0; }
+	unsigned char ihdr[13];
+	put32(ihdr, (uint32_t) width);
+	put32(ihdr + 4, (uint32_t) height);
+	ihdr[8] = 8; ihdr[9] = 6; ihdr[10] = 0; ihdr[11] = 0; ihdr[12] = 0;   /* RGBA8, no interlace */
+	int ok = fwrite("\x89PNG\r\n\x1a\n", 1, 8, f) == 8 && png_chunk(f, "IHDR", ihdr, 13) &&
+	         png_chunk(f, "IDAT", z, o) && png_chunk(f, "IEND", NULL, 0);
+	ok = fclose(f) == 0 && ok;
+	free(z);
+	return ok;
+}

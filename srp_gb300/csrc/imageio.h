@@ -9,6 +9,9 @@ typedef struct SRPImage { uint8_t* rgb; int width; int height; } SRPImage;
 int srpImageLoad(const char* path, SRPImage* img, const char** err);
 /* Write RGB8 as binary PPM. Returns 1 on success. */
 int srpImageWritePPM(const char* path, const uint8_t* rgb, int width, int height);
+/* Write RGBA8 rows (top first) as a PNG of stored (uncompressed) deflate
+ * blocks; needs no zlib. Returns 1 on success. */
+int srpImageWritePNG(const char* path, const uint8_t* rgba, int width, int height);
 #ifdef __cplusplus
 }
 #endif

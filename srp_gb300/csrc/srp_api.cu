@@ -734,6 +734,32 @@ void srpGpuFramebufferSync(const SRPFramebuffer* fb)
 	if (x) fbDownload(fb, x);
 }
 
+int srpGpuSaveFramebufferPNG(const SRPFramebuffer* fb, const char* path)
+{
+	const char* FN = "srpGpuSaveFramebufferPNG";
+	if (!fb || !path) return 1;
+	FbExtra* x = fbFind(fb);
+	if (!x) { SRP_ERROR(FN, "Framebuffer was not created by srpNewFramebuffer"); return 1; }
+	/* the host planes are current in the coherent mode (and may hold the
+	 * program's own edits); in the device mode they are refreshed first */
+	if (g.fbMode == SRP_GPU_FB_DEVICE) fbDownload(fb, x);
+	/* as the reference's test harness saves images: R, G, B from the packed
+	 * colour, alpha 255 (tests/utils/save.c:3-34) */
+	std::vector<uint8_t> rgba(fb->size * 4);
+	for (size_t i = 0; i < fb->size; ++i) {
+		const uint32_t c = fb->color[i];
+		rgba[4 * i + 0] = (uint8_t) (c >> 24);
+		rgba[4 * i + 1] = (uint8_t) (c >> 16);
+		rgba[4 * i + 2] = (uint8_t) (c >> 8);
+		rgba[4 * i + 3] = 0xFF;
+	}
+	if (!srpImageWritePNG(path, rgba.data(), (int) fb->width, (int) fb->height)) {
+		SRP_ERROR(FN, "Cannot write %s", path);
+		return 1;
+	}
+	return 0;
+}
+
 void srpGpuFramebufferSyncAsync(const SRPFramebuffer* fb)
 {
 	FbExtra* x = fbFind(fb);
