@@ -156,6 +156,7 @@ struct DeviceCounters {
 	unsigned int lookbackTicket;
 	unsigned int nonEmptyTiles;      /* heavy tiles listed by k_tile_classify */
 	unsigned int abort;              /* set by k_check: a count exceeded its buffer, skip the rest */
+	unsigned int learnedPairs;       /* next tile pair for learned shading's groups to take */
 };
 
 enum : unsigned {

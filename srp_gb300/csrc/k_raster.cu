@@ -767,62 +767,72 @@ __global__ void __launch_bounds__(kShadeTiles * 64) k_shade(const __grid_constan
 	}
 }
 
-/* The plain shader on a judged pixel: rare, so kept out of line. */
-template <int KIND, int FS>
-__device__ __noinline__ void judgeShade(const DrawParams& P, const unsigned char* uniform, uint32_t primBase,
-                                        uint32_t item, int gx, int gy, SRPFragmentShaderOut& out)
-{
-	shadeItem<KIND, FS>(P, uniform, primBase, item, gx, gy, out);
-}
+/* Learned shading on tcgen05. A CTA holds kLearnGroups independent groups of
+ * 4 warps that share one copy of the weights in shared memory; each group
+ * shades a pair of tiles (128 pixels, one per thread) at a time as one
+ * 128-row MMA tile, with its own A tile, 64 TMEM columns, mbarrier and named
+ * barrier, so that one group's fragment loads and encoding overlap another
+ * group's MMA chain. Groups take the tile pairs in order from a counter of
+ * the draw, one at a time, so that the CTAs end together. In a group each thread builds its pixel's encoded inputs
+ * as row `gt` of the A tile; one thread issues each layer's MMAs into a
+ * 128 x 64 fp32 accumulator in tensor memory; each warp reads its 32 lanes
+ * (rows) back, adds the bias, applies ReLU and writes the next A tile, and
+ * finally its pixels' colours. The judge runs afterwards as its own pass
+ * (k_judge_learned). Every wait is bounded; on a timeout the group records
+ * kErrSpin and stops, and the CTA releases its tensor memory and returns. */
+constexpr int kLearnGroups = 6;
+constexpr int kLearnThreads = 128 * kLearnGroups;
+constexpr uint32_t kLearnCols = 512;   /* kLearnGroups x 64 columns, rounded up to a power of two */
+constexpr size_t kLearnSmem = kTcWBytes + (size_t) kLearnGroups * kTcABytes + 208 * 4 + kLearnGroups * 8 + 16 +
+                              kLearnGroups * 4;
+static_assert(kLearnGroups * 64 <= (int) kLearnCols && kLearnCols <= 512, "TMEM columns");
+static_assert(kLearnSmem <= 227 * 1024, "shared memory");
 
-/* Learned shading on tcgen05: a CTA shades a pair of tiles (128 pixels, one
- * per thread) as one 128-row MMA tile. Each thread builds its pixel's
- * encoded inputs as row `tid` of the A tile; one thread issues each layer's
- * MMAs into a 128 x 64 fp32 accumulator in tensor memory; each warp reads its
- * 32 lanes (rows) back, adds the bias, applies ReLU and writes the next A
- * tile, and finally its pixels' colours. 1 pixel in judgeEvery is also
- * shaded by the plain shader (FS) and its error accumulated per draw for the
- * host's judge. Every wait is bounded; on a timeout the kernel records
- * kErrSpin, releases its tensor memory and returns. */
-template <int KIND, int FS, bool MULTI>
-__global__ void __launch_bounds__(128) k_shade_learned5(const __grid_constant__ DrawParams P, uint32_t numTiles)
+template <int KIND, bool MULTI>
+__global__ void __launch_bounds__(kLearnThreads, 1) k_shade_learned5(const __grid_constant__ DrawParams P, uint32_t numTiles)
 {
 	gridDepSync();
 	extern __shared__ __align__(1024) uint8_t tsm[];
+	const int tid = threadIdx.x, warp = tid >> 5;
+	const int g = warp >> 2, gt = tid & 127;          /* group, thread within the group */
+	const uint32_t bar = 1u + (uint32_t) g;            /* the group's named barrier (0 is __syncthreads) */
 	uint8_t* sW = tsm;
-	uint8_t* sA = tsm + kTcWBytes;
-	float* sB = (float*) (sA + kTcABytes);
-	uint64_t* mbar = (uint64_t*) (sB + 208);
-	uint32_t* tslot = (uint32_t*) (mbar + 1);
-	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-	for (int i = tid; i < (int) (kTcWBytes / 16); i += 128) ((uint4*) sW)[i] = ((const uint4*) P.mlpW5)[i];
-	for (int i = tid; i < 3 * kMlpHid + kMlpOut; i += 128) sB[i] = P.mlpB[i];
-	const uint32_t mb = smemAddr(mbar);
-	if (tid == 0) mbarInit(mb, 1);
-	if (warp == 0) tcAlloc(smemAddr(tslot), kTcCols);
+	uint8_t* sA = tsm + kTcWBytes + (size_t) g * kTcABytes;
+	float* sB = (float*) (tsm + kTcWBytes + (size_t) kLearnGroups * kTcABytes);
+	uint64_t* mbars = (uint64_t*) (sB + 208);
+	uint32_t* tslot = (uint32_t*) (mbars + kLearnGroups);
+	uint32_t* sNext = tslot + 4;                       /* per group: the pair it takes next */
+	for (int i = tid; i < (int) (kTcWBytes / 16); i += kLearnThreads) ((uint4*) sW)[i] = ((const uint4*) P.mlpW5)[i];
+	for (int i = tid; i < 3 * kMlpHid + kMlpOut; i += kLearnThreads) sB[i] = P.mlpB[i];
+	const uint32_t mb = smemAddr(mbars + g);
+	if (gt == 0) {
+		mbarInit(mb, 1);
+		sNext[g] = atomicAdd(&P.ctr->learnedPairs, 1u);
+	}
+	if (warp == 0) tcAlloc(smemAddr(tslot), kLearnCols);
 	fenceProxyAsync();
 	tcFenceBefore();
 	__syncthreads();
 	tcFenceAfter();
-	const uint32_t tmem = *tslot;
-	const uint32_t laneBase = tmem + ((uint32_t) (warp * 32) << 16);
+	const uint32_t tmemAll = *tslot;
+	const uint32_t tmem = tmemAll + (uint32_t) (g * 64);
+	const uint32_t laneBase = tmem + ((uint32_t) ((warp & 3) * 32) << 16);
 	const uint32_t aAddr = smemAddr(sA), wAddr = smemAddr(sW);
-	const int half = tid >> 6, q = tid & 63;
+	const int half = gt >> 6, q = gt & 63;
 	uint32_t phase = 0;
 	bool ok = P.ctr->abort == 0;
 	const uint32_t pairs = (numTiles + 1) / 2;
-	for (uint32_t pr = blockIdx.x; ok && pr < pairs; pr += gridDim.x) {
+	for (uint32_t pr = sNext[g]; ok && pr < pairs; pr = sNext[g]) {
+		/* sNext[g] is rewritten only after the group's next barrier, once every thread has read it */
 		const uint32_t tile = 2 * pr + (uint32_t) half;
 		const bool have = tile < numTiles && P.tileStart[tile] < P.tileEnd[tile];
 		TileCtx c = {};
-		int gx = 0, gy = 0;
 		size_t idx = 0;
 		int32_t win = -1;
 		float x9[9] = { 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f };
 		if (have) {
 			c = tileCtx<MULTI>(P, tile);
-			gx = c.x0 + (q & 7);
-			gy = c.y0 + (q >> 3);
+			const int gx = c.x0 + (q & 7), gy = c.y0 + (q >> 3);
 			if (gx < c.W && gy < c.H) {
 				idx = (size_t) gy * c.W + gx;
 				win = c.winner[idx];
@@ -834,7 +844,15 @@ __global__ void __launch_bounds__(128) k_shade_learned5(const __grid_constant__ 
 				learnedInputs(c.uniform, words, x9);
 			}
 		}
-		if (!__syncthreads_or(win >= 0)) continue;
+		const bool any = namedSyncOr(bar, 128, win >= 0);
+		uint32_t next = 0;
+		if (gt == 0) next = atomicAdd(&P.ctr->learnedPairs, 1u);
+		if (!any) {
+			if (gt == 0) sNext[g] = next;
+			namedSync(bar, 128);
+			continue;
+		}
+#pragma unroll
 		for (int f = 0; f < kMlpInPad; f += 2) {
 			uint32_t v = 0;
 			if (f < kMlpIn) {
@@ -842,33 +860,35 @@ __global__ void __launch_bounds__(128) k_shade_learned5(const __grid_constant__ 
 				__sincosf(mlpBandScale((f % 12) / 2) * x9[f / 12], &sn, &cs);
 				v = packBf16(sn, cs);
 			}
-			*(uint32_t*) (sA + tcOffset(tid, f, kMlpInPad)) = v;
+			*(uint32_t*) (sA + tcOffset(gt, f, kMlpInPad)) = v;
 		}
 		fenceProxyAsync();
 		tcFenceBefore();
-		__syncthreads();
+		namedSync(bar, 128);
 		float rgb[3] = { 0.f, 0.f, 0.f };
 		for (int layer = 0; layer < 4; ++layer) {
-			if (tid == 0) {
+			if (gt == 0) {
 				tcFenceAfter();
 				const int K = layer == 0 ? kMlpInPad : 64;
 				const uint32_t w = wAddr + (layer == 0 ? kTcW1 : layer == 1 ? kTcW2 : layer == 2 ? kTcW3 : kTcW4);
 				tcLayer(tmem, aAddr, w, K, layer < 3 ? 64 : 16);
 				tcCommit(mb);
+				/* the counter's answer is awaited here, beside the first layer's MMAs */
+				if (layer == 0) sNext[g] = next;
 			}
 			const bool got = mbarWait(mb, phase);
 			phase ^= 1u;
-			if (!__syncthreads_and(got)) { ok = false; break; }
+			if (!namedSyncAnd(bar, 128, got)) { ok = false; break; }
 			tcFenceAfter();
 			if (layer < 3) {
-				const float* b = sB + 64 * layer;
+				const float* bias = sB + 64 * layer;
 				for (int col = 0; col < 64; col += 16) {
 					float v[16];
 					tcLoad16(laneBase + (uint32_t) col, v);
 #pragma unroll
 					for (int i = 0; i < 16; i += 2) {
-						const float x0 = fmaxf(v[i] + b[col + i], 0.0f), x1 = fmaxf(v[i + 1] + b[col + i + 1], 0.0f);
-						*(uint32_t*) (sA + tcOffset(tid, col + i, 64)) = packBf16(x0, x1);
+						const float x0 = fmaxf(v[i] + bias[col + i], 0.0f), x1 = fmaxf(v[i + 1] + bias[col + i + 1], 0.0f);
+						*(uint32_t*) (sA + tcOffset(gt, col + i, 64)) = packBf16(x0, x1);
 					}
 				}
 				fenceProxyAsync();
@@ -878,42 +898,67 @@ __global__ void __launch_bounds__(128) k_shade_learned5(const __grid_constant__ 
 				for (int k = 0; k < 3; ++k) rgb[k] = clamp01f(v[k] + sB[3 * kMlpHid + k]);
 			}
 			tcFenceBefore();
-			__syncthreads();
+			namedSync(bar, 128);
 		}
 		if (!ok) break;
-		double err = 0.0, chans = 0.0;
-		float worst = 0.0f;
 		if (win >= 0) {
-			float col[4] = { rgb[0], rgb[1], rgb[2], 1.0f };
+			const float col[4] = { rgb[0], rgb[1], rgb[2], 1.0f };
 			c.color[idx] = packColor(col);
-			if (pixelSampled(gx, gy, P.sampleSeed + c.d, P.judgeEvery)) {
-				SRPFragmentShaderOut ref;
-				judgeShade<KIND, FS>(P, c.uniform, c.primBase, (uint32_t) win, gx, gy, ref);
-				for (int k = 0; k < 3; ++k) {
-					const float dlt = col[k] - ref.color[k];
-					err += (double) dlt * dlt;
-					worst = fmaxf(worst, fabsf(dlt));
-				}
-				chans = 3.0;
-			}
-		}
-		/* a warp's 32 pixels lie in one tile, so in one draw */
-		for (int o = 16; o; o >>= 1) {
-			err += __shfl_xor_sync(0xFFFFFFFFu, err, o);
-			chans += __shfl_xor_sync(0xFFFFFFFFu, chans, o);
-			worst = fmaxf(worst, __shfl_xor_sync(0xFFFFFFFFu, worst, o));
-		}
-		if (lane == 0 && chans > 0.0) {
-			atomicAdd(&P.judge[2 * c.d], err);
-			atomicAdd(&P.judge[2 * c.d + 1], chans);
-			atomicMax(&P.judgeMax[c.d], __float_as_uint(worst));
 		}
 	}
-	if (!ok && P.ctr->abort == 0 && tid == 0) atomicOr(&P.ctr->errors, kErrSpin);
+	if (!ok && P.ctr->abort == 0 && gt == 0) atomicOr(&P.ctr->errors, kErrSpin);
 	tcFenceBefore();
 	__syncthreads();
 	tcFenceAfter();
-	if (warp == 0) tcDealloc(tmem, kTcCols);
+	if (warp == 0) tcDealloc(tmemAll, kLearnCols);
+}
+
+/* The judge of learned shading, a pass of its own after k_shade_learned5:
+ * 1 pixel in judgeEvery is shaded again by the plain shader (FS), and per
+ * draw the squared difference between the network's stored colour and the
+ * shader's (both as the 8-bit channels the framebuffer holds, in [0, 1]
+ * units) and the largest channel difference are accumulated. Run at the
+ * deferred-shading pass's occupancy, so that the few judged pixels do not
+ * hold up the tensor-core kernel's tile pairs. */
+template <int KIND, int FS, bool MULTI>
+__global__ void __launch_bounds__(kShadeTiles * 64) k_judge_learned(const __grid_constant__ DrawParams P, uint32_t numTiles)
+{
+	gridDepSync();
+	const uint32_t tile = blockIdx.x * kShadeTiles + (threadIdx.x >> 6);
+	const int q = threadIdx.x & 63;
+	/* tile-level exits are uniform over each warp: a warp's 32 pixels lie in one tile */
+	if (tile >= numTiles || P.ctr->abort) return;
+	if (P.tileStart[tile] >= P.tileEnd[tile]) return;
+	const TileCtx c = tileCtx<MULTI>(P, tile);
+	const int gx = c.x0 + (q & 7), gy = c.y0 + (q >> 3);
+	double err = 0.0, chans = 0.0;
+	float worst = 0.0f;
+	if (gx < c.W && gy < c.H && pixelSampled(gx, gy, P.sampleSeed + c.d, P.judgeEvery)) {
+		const size_t idx = (size_t) gy * c.W + gx;
+		const int32_t w = c.winner[idx];
+		if (w >= 0) {
+			SRPFragmentShaderOut ref;
+			shadeItem<KIND, FS>(P, c.uniform, c.primBase, (uint32_t) w, gx, gy, ref);
+			const uint32_t net = c.color[idx], plain = packColor(ref.color);
+			for (int k = 0; k < 3; ++k) {
+				const int sh = 24 - 8 * k;
+				const float dlt = (float) ((int) ((net >> sh) & 0xFFu) - (int) ((plain >> sh) & 0xFFu)) / 255.0f;
+				err += (double) dlt * dlt;
+				worst = fmaxf(worst, fabsf(dlt));
+			}
+			chans = 3.0;
+		}
+	}
+	for (int o = 16; o; o >>= 1) {
+		err += __shfl_xor_sync(0xFFFFFFFFu, err, o);
+		chans += __shfl_xor_sync(0xFFFFFFFFu, chans, o);
+		worst = fmaxf(worst, __shfl_xor_sync(0xFFFFFFFFu, worst, o));
+	}
+	if ((threadIdx.x & 31) == 0 && chans > 0.0) {
+		atomicAdd(&P.judge[2 * c.d], err);
+		atomicAdd(&P.judge[2 * c.d + 1], chans);
+		atomicMax(&P.judgeMax[c.d], __float_as_uint(worst));
+	}
 }
 
 /* ------------------------------------------------------------ launchers */
@@ -985,12 +1030,13 @@ static void shadeKind(const DrawParams& P, uint32_t numTiles, cudaStream_t s)
 	case SRP_GPU_FS_FLAT_INT: pdlLaunch(k_shade<KIND, SRP_GPU_FS_FLAT_INT, MULTI>, b, t, 0, s, P, numTiles); break;
 	case kFsLearned:
 		if constexpr (KIND == kKindTri) {
-			/* a CTA per pair of tiles, a few CTAs per SM looping over the pairs */
+			/* one CTA per SM, its groups looping over the tile pairs */
 			const unsigned pairs = (numTiles + 1) / 2;
-			const unsigned blocks = pairs < 152u * 3u ? (pairs ? pairs : 1u) : 152u * 3u;
-			cudaFuncSetAttribute(k_shade_learned5<KIND, SRP_GPU_FS_MARBLE, MULTI>,
-			                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int) kTcSmem);
-			pdlLaunch(k_shade_learned5<KIND, SRP_GPU_FS_MARBLE, MULTI>, blocks, 128, kTcSmem, s, P, numTiles);
+			const unsigned need = (pairs + kLearnGroups - 1) / kLearnGroups;
+			const unsigned blocks = need < 152u ? (need ? need : 1u) : 152u;
+			cudaFuncSetAttribute(k_shade_learned5<KIND, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) kLearnSmem);
+			pdlLaunch(k_shade_learned5<KIND, MULTI>, blocks, kLearnThreads, kLearnSmem, s, P, numTiles);
+			pdlLaunch(k_judge_learned<KIND, SRP_GPU_FS_MARBLE, MULTI>, b, t, 0, s, P, numTiles);
 		}
 		break;
 	default: break;

@@ -100,6 +100,37 @@ __device__ __forceinline__ bool mbarWait(uint32_t addr, uint32_t parity)
 	return false;
 }
 
+/* Named barrier `id` over `threads` threads (a multiple of 32): plain, and
+ * with an OR or AND of a predicate over the participants. */
+__device__ __forceinline__ void namedSync(uint32_t id, uint32_t threads)
+{
+	asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+
+__device__ __forceinline__ bool namedSyncOr(uint32_t id, uint32_t threads, bool p)
+{
+	uint32_t r;
+	asm volatile(
+	    "{\n\t.reg .pred a, b;\n\tsetp.ne.u32 a, %1, 0;\n\tbar.red.or.pred b, %2, %3, a;\n\t"
+	    "selp.u32 %0, 1, 0, b;\n\t}\n"
+	    : "=r"(r)
+	    : "r"((uint32_t) p), "r"(id), "r"(threads)
+	    : "memory");
+	return r != 0;
+}
+
+__device__ __forceinline__ bool namedSyncAnd(uint32_t id, uint32_t threads, bool p)
+{
+	uint32_t r;
+	asm volatile(
+	    "{\n\t.reg .pred a, b;\n\tsetp.ne.u32 a, %1, 0;\n\tbar.red.and.pred b, %2, %3, a;\n\t"
+	    "selp.u32 %0, 1, 0, b;\n\t}\n"
+	    : "=r"(r)
+	    : "r"((uint32_t) p), "r"(id), "r"(threads)
+	    : "memory");
+	return r != 0;
+}
+
 /* 16 consecutive fp32 columns of this thread's TMEM lane. */
 __device__ __forceinline__ void tcLoad16(uint32_t taddr, float v[16])
 {

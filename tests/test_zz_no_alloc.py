@@ -130,6 +130,8 @@ class Api:
         for free, p in reversed(self.owned):
             free(p)
         self.owned = []
+        # the ctypes thunk dies with this object: the library must not keep it
+        self.L.srpSetMessageCallback(self.srp.SRPMessageCallback())
 
 
 @pytest.fixture()
