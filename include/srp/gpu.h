@@ -172,7 +172,8 @@ float srpGpuMlpTrain(SRPGpuMlp* mlp, int steps, int batch, float learningRate);
 
 /** Draws whose fragment shader is `target` are shaded by mlp. 1 pixel in
  *  judgeEvery is also shaded by `target`; a draw whose PSNR over those
- *  pixels is below minPsnrDb is shaded again by `target` alone. mlp NULL
+ *  pixels (between the two images' stored 8-bit colour channels, scaled to
+ *  [0, 1]) is below minPsnrDb is shaded again by `target` alone. mlp NULL
  *  turns learned shading off. */
 void srpGpuSetLearnedShading(void (*target)(SRPFragmentShaderIn*, SRPFragmentShaderOut*), SRPGpuMlp* mlp,
                              float minPsnrDb, uint32_t judgeEvery);
