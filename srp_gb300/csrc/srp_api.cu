@@ -92,9 +92,14 @@ struct Registry {
 /* What one draw's resolve and shading read, written by its front stages:
  * two sets alternate between consecutive single draws, so that the front of
  * draw N+1 can run while draw N resolves and shades. A set's next front
- * waits for rasterDone, recorded after the back of the draw that used it. */
+ * waits for rasterDone, recorded after the back of the draw that used it.
+ * The winner plane is per set too, so that draw N+1's resolve can run
+ * while draw N's shading still reads draw N's winners. */
 struct DrawSet {
-	DeviceBuffer ctr, tileStart, tileEnd, heavy, vary, triR, triA, points, lines, frags, table;
+	DeviceBuffer ctr, tileStart, tileEnd, heavy, vary, triR, triA, points, lines, frags, table, winner;
+	/* the big-primitive list: written by setup, read by the binning and by
+	 * the lambda tables, which run on another stream than the next front */
+	DeviceBuffer big;
 	DeviceBuffer keys, vals, keys2, vals2;
 	/* multi-draw passes: descriptors, prefix sums, primitive bases, winners */
 	DeviceBuffer passDesc, passPrefix, passPrimPrefix, passWinner;
@@ -103,6 +108,7 @@ struct DrawSet {
 	cudaEvent_t headDone = nullptr;    /* vertex and setup done (front stream) */
 	cudaEvent_t binDone = nullptr;     /* front stages done (front stream) */
 	cudaEvent_t rasterDone = nullptr;  /* resolve and shade done (`stream`) */
+	cudaEvent_t resolved = nullptr;    /* resolve done (resolve stream) */
 };
 
 struct Lib {
@@ -115,6 +121,15 @@ struct Lib {
 	/* a draw's vertex, setup and binning run on frontStream, its resolve and
 	 * shading on `stream`, so that the next draw's front overlaps them */
 	cudaStream_t frontStream = nullptr;
+	/* with overlap, a single draw's lambda tables and resolve run on
+	 * resolveStream and its shading on `stream`: draw N+1's resolve then runs
+	 * beside draw N's shading (the resolve never reads colour, the shading
+	 * writes nothing else). rsDirty: `stream` holds framebuffer work queued
+	 * outside a draw's shading (clear, fill, copies, passes, fixed-scratch and
+	 * late-depth draws), which the next resolve on resolveStream must wait for. */
+	cudaStream_t resolveStream = nullptr;
+	bool rsDirty = true;
+	cudaEvent_t rsEvent = nullptr;
 	bool overlap = true;
 	bool graphs = true;               /* replay repeated draws from captured CUDA graphs */
 	SRPGpuTuning tune = { 96, 3 };    /* heavy-tile threshold, heavy-tile CTAs per SM */
@@ -122,8 +137,7 @@ struct Lib {
 	Registry reg;
 	/* scratch pools, grown on demand */
 	/* used by the front stages only (and by multi-draw passes) */
-	DeviceBuffer clip, vset0, vset1, codes, big, lookback, hist, partials, minmax, clipSlot, clipPolys;
-	DeviceBuffer winner;        /* resolve and shade, always on `stream` */
+	DeviceBuffer clip, vset0, vset1, codes, lookback, hist, partials, minmax, clipSlot, clipPolys;
 	DeviceBuffer fillTargets;   /* srpGpuFramebufferFillBatch */
 	DrawSet sets[2];            /* alternating between consecutive single draws */
 	int setNext = 0;
@@ -161,12 +175,15 @@ bool ensureInit(const char* fn)
 	if (!cudaOk(cudaStreamCreateWithPriority(&g.auxStream, cudaStreamNonBlocking, hiPri), fn, "cudaStreamCreate") ||
 	    !cudaOk(cudaEventCreateWithFlags(&g.forkEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 	    !cudaOk(cudaEventCreateWithFlags(&g.joinEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
-	    !cudaOk(cudaStreamCreateWithFlags(&g.frontStream, cudaStreamNonBlocking), fn, "cudaStreamCreate")) return false;
+	    !cudaOk(cudaStreamCreateWithFlags(&g.frontStream, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
+	    !cudaOk(cudaStreamCreateWithFlags(&g.resolveStream, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
+	    !cudaOk(cudaEventCreateWithFlags(&g.rsEvent, cudaEventDisableTiming), fn, "cudaEventCreate")) return false;
 	for (DrawSet& S : g.sets) {
 		if (!cudaOk(cudaEventCreateWithFlags(&S.ctrEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 		    !cudaOk(cudaEventCreateWithFlags(&S.headDone, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 		    !cudaOk(cudaEventCreateWithFlags(&S.binDone, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 		    !cudaOk(cudaEventCreateWithFlags(&S.rasterDone, cudaEventDisableTiming), fn, "cudaEventCreate") ||
+		    !cudaOk(cudaEventCreateWithFlags(&S.resolved, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 		    !cudaOk(cudaMallocHost((void**) &S.hostCtr, sizeof(DeviceCounters)), fn, "cudaMallocHost") ||
 		    !S.ctr.reserve(sizeof(DeviceCounters), fn)) return false;
 		memset(S.hostCtr, 0, sizeof(DeviceCounters));
@@ -213,7 +230,7 @@ constexpr size_t kGraphCache = 64;
 
 struct GraphEntry {
 	std::vector<unsigned char> key;
-	cudaGraphExec_t head = nullptr, head2 = nullptr, mid = nullptr, bin = nullptr, back = nullptr;
+	cudaGraphExec_t head = nullptr, head2 = nullptr, mid = nullptr, bin = nullptr, resolve = nullptr, shade = nullptr;
 };
 
 std::vector<GraphEntry> graphCache;
@@ -241,22 +258,27 @@ template <class F> cudaGraphExec_t captureGraph(cudaStream_t s, F&& enqueue)
 	return exec;
 }
 
-/* Runs a draw as five sequences:
+/* Runs a draw as six sequences:
  * - head and head2: reset up to the check kernel, on the front stream `fs`,
  *   split so that `between` (an upload the second part needs) can be waited
  *   for in the middle;
  * - mid: work that needs the head but not the binning (the lambda tables),
- *   on the library's stream, beside the bin;
+ *   on the resolve stream `rs`, beside the bin;
  * - bin: binning and sort, on `fs`;
- * - back: resolve and shade, on the library's stream.
- * With fs != stream, mid waits for the head through the set's headDone event
- * and back for the bin through binDone; back records rasterDone. Between
- * head and bin the counters are copied to the set's host mirror. Each
- * sequence replays its captured CUDA graph when graphs are on and stage
- * profiling is off (profiling records fresh events per draw). */
-template <class H, class H2, class M, class B, class K>
-void runDrawSeq(const std::vector<unsigned char>& key, DrawSet& S, cudaStream_t fs, H&& head, cudaEvent_t between,
-                H2&& head2, bool hasMid, M&& mid, B&& bin, K&& back)
+ * - resolve, on `rs`;
+ * - shade, on the library's stream (absent for late-depth draws, whose
+ *   resolve runs the shaders).
+ * With fs != rs, mid waits for the head through the set's headDone event and
+ * resolve for the bin through binDone; with rs != stream, shade waits for the
+ * resolve through the set's resolved event, and the first work on rs waits
+ * for framebuffer work queued on the library's stream since (rsDirty). The
+ * shade records rasterDone. Between head and bin the counters are copied to
+ * the set's host mirror. Each sequence replays its captured CUDA graph when
+ * graphs are on and stage profiling is off (profiling records fresh events
+ * per draw, and keeps every sequence on the library's stream). */
+template <class H, class H2, class M, class B, class R, class SH>
+void runDrawSeq(const std::vector<unsigned char>& key, DrawSet& S, cudaStream_t fs, cudaStream_t rs, H&& head,
+                cudaEvent_t between, H2&& head2, bool hasMid, M&& mid, B&& bin, R&& resolve, bool hasShade, SH&& shade)
 {
 	GraphEntry* e = nullptr;
 	if (g.graphs && !g.profiling) {
@@ -266,19 +288,21 @@ void runDrawSeq(const std::vector<unsigned char>& key, DrawSet& S, cudaStream_t 
 			fresh.key = key;
 			fresh.head = captureGraph(fs, head);
 			fresh.head2 = fresh.head ? captureGraph(fs, head2) : nullptr;
-			fresh.mid = fresh.head2 && hasMid ? captureGraph(g.stream, mid) : nullptr;
+			fresh.mid = fresh.head2 && hasMid ? captureGraph(rs, mid) : nullptr;
 			fresh.bin = fresh.head2 && (fresh.mid || !hasMid) ? captureGraph(fs, bin) : nullptr;
-			fresh.back = fresh.bin ? captureGraph(g.stream, back) : nullptr;
+			fresh.resolve = fresh.bin ? captureGraph(rs, resolve) : nullptr;
+			fresh.shade = fresh.resolve && hasShade ? captureGraph(g.stream, shade) : nullptr;
 			if (graphCache.size() < kGraphCache) graphCache.push_back(std::move(fresh));
 			else {
 				GraphEntry& old = graphCache[graphNext++ % kGraphCache];
-				for (cudaGraphExec_t x : { old.head, old.head2, old.mid, old.bin, old.back })
+				for (cudaGraphExec_t x : { old.head, old.head2, old.mid, old.bin, old.resolve, old.shade })
 					if (x) cudaGraphExecDestroy(x);
 				old = std::move(fresh);
 			}
 			e = graphFind(key);
 		}
-		if (e && !(e->head && e->head2 && (e->mid || !hasMid) && e->bin && e->back)) e = nullptr;
+		if (e && !(e->head && e->head2 && (e->mid || !hasMid) && e->bin && e->resolve && (e->shade || !hasShade)))
+			e = nullptr;
 	}
 	if (e) cudaGraphLaunch(e->head, fs);
 	else head();
@@ -288,22 +312,38 @@ void runDrawSeq(const std::vector<unsigned char>& key, DrawSet& S, cudaStream_t 
 	else head2();
 	cudaMemcpyAsync(S.hostCtr, S.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, fs);
 	cudaEventRecord(S.ctrEvent, fs);
+	if (rs != g.stream && g.rsDirty) {
+		cudaEventRecord(g.rsEvent, g.stream);
+		cudaStreamWaitEvent(rs, g.rsEvent, 0);
+		g.rsDirty = false;
+	}
 	if (hasMid) {
-		if (fs != g.stream) {
+		if (fs != rs) {
 			cudaEventRecord(S.headDone, fs);
-			cudaStreamWaitEvent(g.stream, S.headDone, 0);
+			cudaStreamWaitEvent(rs, S.headDone, 0);
 		}
-		if (e) cudaGraphLaunch(e->mid, g.stream);
+		if (e) cudaGraphLaunch(e->mid, rs);
 		else mid();
 	}
 	if (e) cudaGraphLaunch(e->bin, fs);
 	else bin();
-	if (fs != g.stream) {
+	if (fs != rs) {
 		cudaEventRecord(S.binDone, fs);
-		cudaStreamWaitEvent(g.stream, S.binDone, 0);
+		cudaStreamWaitEvent(rs, S.binDone, 0);
 	}
-	if (e) cudaGraphLaunch(e->back, g.stream);
-	else back();
+	if (e) cudaGraphLaunch(e->resolve, rs);
+	else resolve();
+	if (rs != g.stream) {
+		cudaEventRecord(S.resolved, rs);
+		cudaStreamWaitEvent(g.stream, S.resolved, 0);
+	} else {
+		/* the depth and stencil planes were written on the library's stream */
+		g.rsDirty = true;
+	}
+	if (hasShade) {
+		if (e) cudaGraphLaunch(e->shade, g.stream);
+		else shade();
+	}
 	if (fs != g.stream) cudaEventRecord(S.rasterDone, g.stream);
 }
 
@@ -644,6 +684,7 @@ static bool fbContiguous(const SRPFramebuffer* fb)
 
 static void fbUpload(const SRPFramebuffer* fb, FbExtra* x)
 {
+	g.rsDirty = true;
 	if (fbContiguous(fb)) {
 		cudaMemcpyAsync(x->color, fb->color, 9 * fb->size, cudaMemcpyHostToDevice, g.stream);
 		return;
@@ -655,6 +696,7 @@ static void fbUpload(const SRPFramebuffer* fb, FbExtra* x)
 
 static void fbDownloadAsync(const SRPFramebuffer* fb, FbExtra* x)
 {
+	g.rsDirty = true;
 	if (fbContiguous(fb)) {
 		cudaMemcpyAsync(fb->color, x->color, 9 * fb->size, cudaMemcpyDeviceToHost, g.stream);
 		return;
@@ -696,6 +738,7 @@ SRPFramebuffer* srpNewFramebuffer(size_t w, size_t h)
 	x.depth = (float*) (dev + 4 * n);
 	x.stencil = dev + 8 * n;
 	cudaMemsetAsync(dev, 0, 9 * n, g.stream);
+	g.rsDirty = true;
 	fbTable[fb] = x;
 	return fb;
 }
@@ -703,6 +746,10 @@ SRPFramebuffer* srpNewFramebuffer(size_t w, size_t h)
 void srpFreeFramebuffer(SRPFramebuffer* fb)
 {
 	if (!fb) return;
+	if (g.init) {
+		cudaStreamSynchronize(g.frontStream);
+		cudaStreamSynchronize(g.resolveStream);
+	}
 	cudaStreamSynchronize(g.stream);
 	auto it = fbTable.find(fb);
 	if (it != fbTable.end()) {
@@ -717,6 +764,7 @@ void srpFramebufferClear(const SRPFramebuffer* fb)
 {
 	FbExtra* x = fbFind(fb);
 	if (!x) return;
+	g.rsDirty = true;
 	cudaMemsetAsync(x->color, 0, 4 * fb->size, g.stream);
 	fill32((uint32_t*) x->depth, 0xBF800000u /* -1.0f */, fb->size);
 	if (g.fbMode == SRP_GPU_FB_COHERENT) {
@@ -779,6 +827,7 @@ void srpGpuFramebufferFillBatch(const SRPFramebuffer* const* fbs, size_t n, uint
 		t.push_back(FillTarget{ x->color, (uint32_t*) x->depth, x->stencil, fbs[i]->size });
 	}
 	if (!g.fillTargets.reserve(n * sizeof(FillTarget), FN)) return;
+	g.rsDirty = true;
 	/* from pageable memory: returns once the host vector has been read */
 	if (!cudaOk(cudaMemcpyAsync(g.fillTargets.ptr, t.data(), n * sizeof(FillTarget), cudaMemcpyHostToDevice, g.stream),
 	            FN, "cudaMemcpyAsync")) return;
@@ -806,6 +855,7 @@ void srpGpuFramebufferFill(const SRPFramebuffer* fb, uint32_t color, float depth
 {
 	FbExtra* x = fbFind(fb);
 	if (!x) return;
+	g.rsDirty = true;
 	uint32_t dbits;
 	memcpy(&dbits, &depth, 4);
 	if (planes & SRP_GPU_FILL_COLOR) fill32(x->color, color, fb->size);
@@ -1068,6 +1118,7 @@ static uint32_t bitsFor(uint32_t n)
 static unsigned long long readCounters()
 {
 	cudaStreamSynchronize(g.frontStream);
+	cudaStreamSynchronize(g.resolveStream);
 	for (DrawSet& S : g.sets)
 		cudaMemcpyAsync(S.hostCtr, S.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, g.stream);
 	if (!cudaOk(cudaStreamSynchronize(g.stream), "srpDraw", "kernel execution")) return 0;
@@ -1181,6 +1232,9 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 	const uint32_t keyBits = bitsFor(numTiles);
 	const bool late = sp->fs->mayOverwriteDepth && shadeSupportsLateDepth(fsId);
 	const bool learned = learnedPrepare(P, kind, late, 1, g.stream);
+	/* the resolve runs beside the previous draw's shading, except for
+	 * late-depth draws, whose resolve writes colour */
+	const cudaStream_t rs = fs != g.stream && !late ? g.resolveStream : g.stream;
 	bool drawn = false;
 	for (int attempt = 0; attempt < 4 && !drawn; ++attempt) {
 		/* long lines are queued in the big-job buffer: room for every line */
@@ -1195,11 +1249,11 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		          S.keys.reserve((size_t) entryCap * 4, FN) && S.vals.reserve((size_t) entryCap * 4, FN) &&
 		          S.keys2.reserve((size_t) entryCap * 4, FN) && S.vals2.reserve((size_t) entryCap * 4, FN) &&
 		          g.hist.reserve(sortHistWords(entryCap) * 4, FN) && g.partials.reserve(sortPartialWords(entryCap) * 4 + 64, FN) &&
-		          g.big.reserve((size_t) g.bigCap * 16, FN) && S.table.reserve((size_t) g.tableCap * 4, FN) &&
+		          S.big.reserve((size_t) g.bigCap * 16, FN) && S.table.reserve((size_t) g.tableCap * 4, FN) &&
 		          g.clipSlot.reserve((size_t) nIn * 4 + 4, FN) &&
 		          g.clipPolys.reserve((size_t) g.clipPolyCap * (1 + kMaxPoly) * 4, FN) &&
 		          S.tileStart.reserve((size_t) (numTiles + 1) * 4, FN) && S.tileEnd.reserve((size_t) (numTiles + 1) * 4, FN) &&
-		          g.winner.reserve(fb->size * 4 + 4, FN) && S.heavy.reserve((size_t) (numTiles + 1) * 4, FN);
+		          S.winner.reserve(fb->size * 4 + 4, FN) && S.heavy.reserve((size_t) (numTiles + 1) * 4, FN);
 		if (kind == kKindTri) ok = ok && S.triR.reserve((size_t) primCap * sizeof(TriRaster), FN) &&
 		                           S.triA.reserve((size_t) primCap * sizeof(TriAttr), FN);
 		else if (kind == kKindPoint) ok = ok && S.points.reserve((size_t) primCap * sizeof(PointRec), FN);
@@ -1223,7 +1277,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		P.keys = S.keys.as<uint32_t>();
 		P.vals = S.vals.as<uint32_t>();
 		P.entryCap = entryCap;
-		P.bigJobs = g.big.as<uint4>();
+		P.bigJobs = S.big.as<uint4>();
 		P.bigCap = g.bigCap;
 		P.table = S.table.as<float>();
 		P.clipSlot = g.clipSlot.as<uint32_t>();
@@ -1233,7 +1287,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		P.lookback = g.lookback.as<unsigned long long>();
 		P.tileStart = S.tileStart.as<uint32_t>();
 		P.tileEnd = S.tileEnd.as<uint32_t>();
-		P.winner = g.winner.as<int32_t>();
+		P.winner = S.winner.as<int32_t>();
 
 		/* the whole draw is enqueued before the host looks at any count */
 		uint32_t* sk = nullptr;
@@ -1255,10 +1309,10 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			stageEnd(SRP_GPU_STAGE_SETUP, isTri(prim) ? 3 : 2);
 		};
 		/* lambda tables (triangles only): needed by the resolve, not by the
-		 * binning, so they run on the library's stream beside the bin */
+		 * binning, so they run on the resolve stream beside the bin */
 		auto mid = [&]() {
 			stageBegin();
-			launchLambdaTables(P, g.bigJobsSeen[kind], g.stream);
+			launchLambdaTables(P, g.bigJobsSeen[kind], rs);
 			stageEnd(SRP_GPU_STAGE_BIN, 1);
 		};
 		auto bin = [&]() {
@@ -1272,20 +1326,16 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			launchTileRanges(P, sk, numTiles, fs);
 			stageEnd(SRP_GPU_STAGE_BIN, 2 + 1 + (int) (keyBits / 8) + 1);
 		};
-		auto back = [&]() {
-			if (late) {
-				stageBegin();
-				launchResolveLate(P, kind, sv, numTiles, g.stream);
-				stageEnd(SRP_GPU_STAGE_RESOLVE, 1);
-			} else {
-				stageBegin();
-				launchResolve(P, kind, sv, numTiles, S.heavy.as<uint32_t>(), g.stream, g.auxStream, g.forkEvent,
-				              g.joinEvent);
-				stageEnd(SRP_GPU_STAGE_RESOLVE, 3);
-				stageBegin();
-				launchShade(P, kind, numTiles, g.stream);
-				stageEnd(SRP_GPU_STAGE_SHADE, 1);
-			}
+		auto resolve = [&]() {
+			stageBegin();
+			if (late) launchResolveLate(P, kind, sv, numTiles, rs);
+			else launchResolve(P, kind, sv, numTiles, S.heavy.as<uint32_t>(), rs, g.auxStream, g.forkEvent, g.joinEvent);
+			stageEnd(SRP_GPU_STAGE_RESOLVE, late ? 1 : 3);
+		};
+		auto shade = [&]() {
+			stageBegin();
+			launchShade(P, kind, numTiles, g.stream);
+			stageEnd(SRP_GPU_STAGE_SHADE, 1);
 		};
 		/* the front waits for the last back that used this set, and for the
 		 * uploads of the buffers it reads (both on the library's stream); when
@@ -1299,8 +1349,8 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		}
 		runDrawSeq(graphKey(P, { (unsigned long long) kind, late, ib != nullptr, start, count, vb->nVertices, blocks,
 		                         keyBits, numTiles, g.bigJobsSeen[kind], (unsigned long long) (uintptr_t) g.stream,
-		                         (unsigned long long) (uintptr_t) fs }),
-		           S, fs, head, lateIb ? ib->ready : nullptr, head2, kind == kKindTri, mid, bin, back);
+		                         (unsigned long long) (uintptr_t) fs, (unsigned long long) (uintptr_t) rs }),
+		           S, fs, rs, head, lateIb ? ib->ready : nullptr, head2, kind == kKindTri, mid, bin, resolve, !late, shade);
 		g.launches += 4 + (ib && !P.shadeAll ? 1 : 0) + (isTri(prim) ? 1 : 0) + (kind == kKindPoint ? 1 : 2) + 1 +
 		              keyBits / 8 + 1 +
 		              (late ? 1 : 4);
@@ -1593,6 +1643,8 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 
 	const bool learned = learnedPrepare(P, kKindTri, false, (uint32_t) n, g.stream);
 	const cudaStream_t fs = (g.overlap && !g.profiling && !learned) ? g.frontStream : g.stream;
+	/* the pass's resolve runs beside the previous pass's shading */
+	const cudaStream_t rs = fs != g.stream ? g.resolveStream : g.stream;
 	if (fs != g.stream) {
 		/* the front waits for the last back that used this set and for the
 		 * uploads of the draws' buffers since a front last waited for them (one
@@ -1636,7 +1688,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		          S.keys.reserve((size_t) entryCap * 4, FN) && S.vals.reserve((size_t) entryCap * 4, FN) &&
 		          S.keys2.reserve((size_t) entryCap * 4, FN) && S.vals2.reserve((size_t) entryCap * 4, FN) &&
 		          g.hist.reserve(sortHistWords(entryCap) * 4, FN) && g.partials.reserve(sortPartialWords(entryCap) * 4 + 64, FN) &&
-		          g.big.reserve((size_t) g.bigCap * 16, FN) && S.table.reserve((size_t) g.tableCap * 4, FN) &&
+		          S.big.reserve((size_t) g.bigCap * 16, FN) && S.table.reserve((size_t) g.tableCap * 4, FN) &&
 		          g.clipSlot.reserve((size_t) nIn * 4 + 4, FN) &&
 		          g.clipPolys.reserve((size_t) g.clipPolyCap * (1 + kMaxPoly) * 4, FN) &&
 		          S.triR.reserve((size_t) primCap * sizeof(TriRaster), FN) &&
@@ -1657,7 +1709,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		P.keys = S.keys.as<uint32_t>();
 		P.vals = S.vals.as<uint32_t>();
 		P.entryCap = entryCap;
-		P.bigJobs = g.big.as<uint4>();
+		P.bigJobs = S.big.as<uint4>();
 		P.bigCap = g.bigCap;
 		P.table = S.table.as<float>();
 		P.tableCap = g.tableCap;
@@ -1695,18 +1747,20 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 			launchTileRanges(P, sk, numTiles, fs);
 			stageEnd(SRP_GPU_STAGE_BIN, 2 + 1 + (int) (keyBits / 8) + 1);
 		};
-		auto back = [&]() {
+		auto resolve = [&]() {
 			stageBegin();
-			launchResolveMulti(P, sv, numTiles, S.heavy.as<uint32_t>(), g.stream, g.auxStream, g.forkEvent, g.joinEvent);
+			launchResolveMulti(P, sv, numTiles, S.heavy.as<uint32_t>(), rs, g.auxStream, g.forkEvent, g.joinEvent);
 			stageEnd(SRP_GPU_STAGE_RESOLVE, 3);
+		};
+		auto shade = [&]() {
 			stageBegin();
 			launchShadeMulti(P, numTiles, g.stream);
 			stageEnd(SRP_GPU_STAGE_SHADE, 1);
 		};
 		runDrawSeq(graphKey(P, { vBlocks, (unsigned long long) maxStride, blocks, keyBits, numTiles,
 		                         g.bigJobsSeen[kKindTri], (unsigned long long) (uintptr_t) g.stream,
-		                         (unsigned long long) (uintptr_t) fs }),
-		           S, fs, head, nullptr, head2, false, [] {}, bin, back);
+		                         (unsigned long long) (uintptr_t) fs, (unsigned long long) (uintptr_t) rs }),
+		           S, fs, rs, head, nullptr, head2, false, [] {}, bin, resolve, true, shade);
 		if (fs == g.stream) markPassDone();
 		g.launches += 5 + 2 + 1 + keyBits / 8 + 1 + 4;
 		if (!cudaOk(cudaGetLastError(), FN, "launch")) return false;
@@ -1840,8 +1894,10 @@ void srpGpuSetStream(void* stream)
 {
 	if (!ensureInit("srpGpuSetStream")) return;
 	cudaStreamSynchronize(g.frontStream);
+	cudaStreamSynchronize(g.resolveStream);
 	cudaStreamSynchronize(g.stream);
 	g.stream = stream ? (cudaStream_t) stream : g.ownStream;
+	g.rsDirty = true;
 }
 
 void* srpGpuGetStream(void) { return ensureInit("srpGpuGetStream") ? (void*) g.stream : nullptr; }
@@ -1849,6 +1905,7 @@ void* srpGpuGetStream(void) { return ensureInit("srpGpuGetStream") ? (void*) g.s
 int srpGpuSynchronize(void)
 {
 	if (!g.init) return 0;
+	cudaStreamSynchronize(g.resolveStream);
 	return cudaOk(cudaStreamSynchronize(g.stream), "srpGpuSynchronize", "kernel execution") ? 0 : 1;
 }
 
@@ -1865,6 +1922,7 @@ void srpGpuResetStats(void)
 {
 	if (!g.init) return;
 	cudaStreamSynchronize(g.frontStream);
+	cudaStreamSynchronize(g.resolveStream);
 	cudaStreamSynchronize(g.stream);
 	for (DrawSet& S : g.sets) cudaMemset(S.ctr.ptr, 0, sizeof(DeviceCounters));
 	g.stats = SRPGpuStats();
@@ -1879,6 +1937,7 @@ void srpGpuSetDrawOverlap(int enable)
 {
 	if (!ensureInit("srpGpuSetDrawOverlap")) return;
 	cudaStreamSynchronize(g.frontStream);
+	cudaStreamSynchronize(g.resolveStream);
 	g.overlap = enable != 0;
 }
 
@@ -2129,6 +2188,7 @@ int fixedDrawPrepare(DrawParams& P, const SRPIndexBuffer* ib, const SRPVertexBuf
 	P.stencil = fx->stencil;
 	const int mode = isTri(prim) ? st.polygonMode : (isLine(prim) ? SRP_POLYGON_MODE_LINE : SRP_POLYGON_MODE_POINT);
 	info.stream = g.stream;
+	g.rsDirty = true;  /* its resolve writes the planes on the library's stream */
 	info.nIn = nIn;
 	info.outPer = isTri(prim) && mode != SRP_POLYGON_MODE_FILL ? 3 : 1;
 	info.numTiles = (uint32_t) st.tilesX * (uint32_t) st.tilesY;

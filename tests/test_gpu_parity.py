@@ -93,6 +93,15 @@ def test_overlapped_draws_match_serial_draws(built_library, scene, scale):
             sc.prepare()
             sc.render()
             frames.append(sc.planes())
+        # frames back to back, with no wait in between: each draw's resolve
+        # and lambda tables may queue behind the previous draw's work while
+        # the next fronts already run
+        for graphs in (0, 1):
+            L.srpGpuSetDrawGraphs(graphs)
+            for _ in range(4):
+                sc.prepare()
+                sc.render()
+            frames.append(sc.planes())
         assert L.srpGpuSynchronize() == 0
         for f in frames[1:]:
             for a, b in zip(f, frames[0]):
