@@ -315,8 +315,10 @@ typedef struct SRPGpuProfile
 void srpGpuSetDrawGraphs(int enable);
 /** Overlap of consecutive draws (default on): a draw's vertex, setup and
  *  binning stages run on a second stream of the library, beside the previous
- *  draw's resolve and shading, which stay in submission order on the
- *  library's stream. Results are identical either way. */
+ *  draw's resolve and shading, and its resolve on a third, beside the
+ *  previous draw's shading. Resolves stay in submission order among
+ *  themselves, and so do shadings, which run on the library's stream.
+ *  Results are identical either way. */
 void srpGpuSetDrawOverlap(int enable);
 
 /** Record CUDA events around every stage of every draw (off by default). */
