@@ -72,7 +72,9 @@ void srpGpuFramebufferFillBatch(const SRPFramebuffer* const* fbs, size_t n, uint
  * from page-locked memory the copies then run at the host link's speed
  * without a round trip per call. None has a counterpart in the reference. */
 
-/** srpVertexBufferCopyData without waiting for the copy. */
+/** srpVertexBufferCopyData without waiting for the copy. Copies run in
+ *  order on a copy stream of the library; a draw that reads the buffer waits
+ *  for its copy, and nothing else does. */
 void srpGpuVertexBufferCopyDataAsync(SRPVertexBuffer* buffer, size_t stride, size_t nBytes, const void* data);
 /** srpIndexBufferCopyData without waiting for the copy. */
 void srpGpuIndexBufferCopyDataAsync(SRPIndexBuffer* buffer, SRPType type, size_t nBytes, const void* data);
@@ -234,7 +236,8 @@ int srpGpuMlpGradients(SRPGpuMlp* mlp, const float* samples, size_t n, float* gr
  *  holds the array) and keeps it for later calls. Make that first call before
  *  any stream capture begins. Vertex and index buffers must already be in
  *  device memory, as srpVertexBufferCopyData / srpIndexBufferCopyData leave
- *  them when a GPU is present.
+ *  them when a GPU is present. Outside a stream capture, the draw also waits
+ *  for copies queued by the Async variants.
  *
  *  Limits. The parts of the scratch sized by the vertex buffer (about 64
  *  bytes and 4 per varying word per vertex), by the primitives (up to 96

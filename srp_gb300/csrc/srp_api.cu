@@ -130,6 +130,15 @@ struct Lib {
 	cudaStream_t resolveStream = nullptr;
 	bool rsDirty = true;
 	cudaEvent_t rsEvent = nullptr;
+	/* vertex and index uploads run on copyStream, so that neither the
+	 * resolves nor the shading wait for uploads of later draws. A stage that
+	 * reads a buffer waits for the buffer's upload event. Before an upload
+	 * the copy stream waits for the draws queued since it last did
+	 * (frontReads: on the front stream, streamReads: on `stream`). */
+	cudaStream_t copyStream = nullptr;
+	cudaEvent_t copyGateFront = nullptr, copyGateStream = nullptr;
+	bool frontReads = false, streamReads = false;
+	unsigned long long uploadSeq = 0;
 	bool overlap = true;
 	bool graphs = true;               /* replay repeated draws from captured CUDA graphs */
 	SRPGpuTuning tune = { 96, 3 };    /* heavy-tile threshold, heavy-tile CTAs per SM */
@@ -177,7 +186,10 @@ bool ensureInit(const char* fn)
 	    !cudaOk(cudaEventCreateWithFlags(&g.joinEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 	    !cudaOk(cudaStreamCreateWithFlags(&g.frontStream, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
 	    !cudaOk(cudaStreamCreateWithFlags(&g.resolveStream, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
-	    !cudaOk(cudaEventCreateWithFlags(&g.rsEvent, cudaEventDisableTiming), fn, "cudaEventCreate")) return false;
+	    !cudaOk(cudaEventCreateWithFlags(&g.rsEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
+	    !cudaOk(cudaStreamCreateWithFlags(&g.copyStream, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
+	    !cudaOk(cudaEventCreateWithFlags(&g.copyGateFront, cudaEventDisableTiming), fn, "cudaEventCreate") ||
+	    !cudaOk(cudaEventCreateWithFlags(&g.copyGateStream, cudaEventDisableTiming), fn, "cudaEventCreate")) return false;
 	for (DrawSet& S : g.sets) {
 		if (!cudaOk(cudaEventCreateWithFlags(&S.ctrEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 		    !cudaOk(cudaEventCreateWithFlags(&S.headDone, cudaEventDisableTiming), fn, "cudaEventCreate") ||
@@ -307,7 +319,7 @@ void runDrawSeq(const std::vector<unsigned char>& key, DrawSet& S, cudaStream_t 
 	if (e) cudaGraphLaunch(e->head, fs);
 	else head();
 	/* an input the second part of the head needs, uploaded meanwhile */
-	if (between && fs != g.stream) cudaStreamWaitEvent(fs, between, 0);
+	if (between) cudaStreamWaitEvent(fs, between, 0);
 	if (e) cudaGraphLaunch(e->head2, fs);
 	else head2();
 	cudaMemcpyAsync(S.hostCtr, S.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, fs);
@@ -449,8 +461,9 @@ struct SRPVertexBuffer {
 	unsigned char* host = nullptr;    /* staging copy made by CopyData */
 	DeviceBuffer dev;
 	bool dirty = false;
-	cudaEvent_t ready = nullptr;      /* recorded after the last upload (library stream) */
+	cudaEvent_t ready = nullptr;      /* recorded after the last upload (copy stream) */
 	bool pending = false;             /* uploaded since a pass's front last waited for it */
+	unsigned long long seq = 0;       /* upload number of the last upload */
 };
 
 struct SRPIndexBuffer {
@@ -461,19 +474,39 @@ struct SRPIndexBuffer {
 	bool dirty = false;
 	cudaEvent_t ready = nullptr;
 	bool pending = false;
+	unsigned long long seq = 0;
 };
 
-/* Marks the end of an upload into a buffer: the front stream of a later
- * draw waits for it. */
-static void markUpload(cudaEvent_t& ready, bool& pending)
+/* Marks the end of an upload into a buffer: the stage of a later draw that
+ * reads the buffer waits for it. Uploads are numbered in the order of the
+ * copy stream, on which they complete in that order. */
+static void markUpload(cudaEvent_t& ready, bool& pending, unsigned long long& seq)
 {
 	if (!ready && cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) != cudaSuccess) {
 		cudaGetLastError();
 		ready = nullptr;
 		return;
 	}
-	cudaEventRecord(ready, g.stream);
+	cudaEventRecord(ready, g.copyStream);
 	pending = true;
+	seq = ++g.uploadSeq;
+}
+
+/* The copy stream, made to wait first for the draws queued since it last
+ * did, which may still read the buffers it is about to overwrite. */
+static cudaStream_t copyStreamReady()
+{
+	if (g.frontReads) {
+		cudaEventRecord(g.copyGateFront, g.frontStream);
+		cudaStreamWaitEvent(g.copyStream, g.copyGateFront, 0);
+		g.frontReads = false;
+	}
+	if (g.streamReads) {
+		cudaEventRecord(g.copyGateStream, g.stream);
+		cudaStreamWaitEvent(g.copyStream, g.copyGateStream, 0);
+		g.streamReads = false;
+	}
+	return g.copyStream;
 }
 
 static size_t indexTypeSize(SRPType t)
@@ -501,30 +534,27 @@ static bool gpuPresent()
 	return present == 1;
 }
 
-/* CopyData on a machine with a GPU: the bytes go straight to HBM. From
- * pageable memory cudaMemcpyAsync returns once the source has been read; from
- * page-locked memory the copy is asynchronous, so it is waited for before
- * returning (the caller may reuse its buffer at once, as with the
- * reference's memcpy). */
+/* CopyData on a machine with a GPU: the bytes go straight to HBM, on the
+ * library's copy stream, and the copy is waited for before returning (the
+ * caller may reuse its buffer at once, as with the reference's memcpy, and
+ * the buffer is in device memory for any later work). */
 static bool copyToDevice(DeviceBuffer& dev, const void* data, size_t nBytes, const char* fn)
 {
 	if (!ensureInit(fn) || !dev.reserve(nBytes + 16, fn)) return false;
 	if (!nBytes) return true;
-	if (!cudaOk(cudaMemcpyAsync(dev.ptr, data, nBytes, cudaMemcpyHostToDevice, g.stream), fn, "cudaMemcpyAsync"))
-		return false;
-	cudaPointerAttributes attr;
-	if (cudaPointerGetAttributes(&attr, data) != cudaSuccess) { cudaGetLastError(); attr.type = cudaMemoryTypeUnregistered; }
-	if (attr.type != cudaMemoryTypeUnregistered) cudaStreamSynchronize(g.stream);
-	return true;
+	const cudaStream_t cs = copyStreamReady();
+	if (!cudaOk(cudaMemcpyAsync(dev.ptr, data, nBytes, cudaMemcpyHostToDevice, cs), fn, "cudaMemcpyAsync")) return false;
+	return cudaOk(cudaStreamSynchronize(cs), fn, "cudaMemcpyAsync");
 }
 
-/* CopyData without the wait: the copy is only enqueued, and the caller keeps
- * `data` unchanged until the stream has passed it. */
+/* CopyData without the wait: the copy is only enqueued on the copy stream,
+ * and the caller keeps `data` unchanged until srpGpuSynchronize. */
 static bool copyToDeviceAsync(DeviceBuffer& dev, const void* data, size_t nBytes, const char* fn)
 {
 	if (!ensureInit(fn) || !dev.reserve(nBytes + 16, fn)) return false;
 	if (!nBytes) return true;
-	return cudaOk(cudaMemcpyAsync(dev.ptr, data, nBytes, cudaMemcpyHostToDevice, g.stream), fn, "cudaMemcpyAsync");
+	return cudaOk(cudaMemcpyAsync(dev.ptr, data, nBytes, cudaMemcpyHostToDevice, copyStreamReady()), fn,
+	              "cudaMemcpyAsync");
 }
 
 static void* pinnedRealloc(void* old, size_t n)
@@ -545,6 +575,7 @@ SRPVertexBuffer* srpNewVertexBuffer(void) { return new SRPVertexBuffer(); }
 void srpFreeVertexBuffer(SRPVertexBuffer* b)
 {
 	if (!b) return;
+	if (g.init) cudaStreamSynchronize(g.copyStream);  /* copies from b->host may be in flight */
 	if (b->ready) cudaEventDestroy(b->ready);
 	if (b->host) cudaFreeHost(b->host);
 	if (b->dev.ptr) cudaFree(b->dev.ptr);
@@ -558,7 +589,7 @@ void srpVertexBufferCopyData(SRPVertexBuffer* b, size_t stride, size_t nBytes, c
 	b->nBytes = nBytes;
 	if (gpuPresent()) {
 		b->dirty = !copyToDevice(b->dev, data, nBytes, "srpVertexBufferCopyData");
-		if (!b->dirty) { markUpload(b->ready, b->pending); return; }
+		if (!b->dirty) { markUpload(b->ready, b->pending, b->seq); return; }
 	}
 	/* no device: keep a host copy, uploaded by the first draw */
 	if (nBytes > b->cap) { b->host = (unsigned char*) pinnedRealloc(b->host, nBytes); b->cap = nBytes; }
@@ -574,7 +605,7 @@ void srpGpuVertexBufferCopyDataAsync(SRPVertexBuffer* b, size_t stride, size_t n
 	b->nBytes = nBytes;
 	b->dirty = !copyToDeviceAsync(b->dev, data, nBytes, "srpGpuVertexBufferCopyDataAsync");
 	if (b->dirty) srpVertexBufferCopyData(b, stride, nBytes, data);
-	else markUpload(b->ready, b->pending);
+	else markUpload(b->ready, b->pending, b->seq);
 }
 
 SRPIndexBuffer* srpNewIndexBuffer(void) { return new SRPIndexBuffer(); }
@@ -582,6 +613,7 @@ SRPIndexBuffer* srpNewIndexBuffer(void) { return new SRPIndexBuffer(); }
 void srpFreeIndexBuffer(SRPIndexBuffer* b)
 {
 	if (!b) return;
+	if (g.init) cudaStreamSynchronize(g.copyStream);  /* copies from b->host may be in flight */
 	if (b->ready) cudaEventDestroy(b->ready);
 	if (b->host) cudaFreeHost(b->host);
 	if (b->dev.ptr) cudaFree(b->dev.ptr);
@@ -597,7 +629,7 @@ void srpIndexBufferCopyData(SRPIndexBuffer* b, SRPType type, size_t nBytes, cons
 	b->nBytes = nBytes;
 	if (gpuPresent()) {
 		b->dirty = !copyToDevice(b->dev, data, nBytes, "srpIndexBufferCopyData");
-		if (!b->dirty) { markUpload(b->ready, b->pending); return; }
+		if (!b->dirty) { markUpload(b->ready, b->pending, b->seq); return; }
 	}
 	if (nBytes > b->cap) { b->host = (unsigned char*) pinnedRealloc(b->host, nBytes); b->cap = nBytes; }
 	if (nBytes) memcpy(b->host, data, nBytes);
@@ -613,7 +645,7 @@ void srpGpuIndexBufferCopyDataAsync(SRPIndexBuffer* b, SRPType type, size_t nByt
 	b->nBytes = nBytes;
 	b->dirty = !copyToDeviceAsync(b->dev, data, nBytes, "srpGpuIndexBufferCopyDataAsync");
 	if (b->dirty) srpIndexBufferCopyData(b, type, nBytes, data);
-	else markUpload(b->ready, b->pending);
+	else markUpload(b->ready, b->pending, b->seq);
 }
 
 }  // extern "C"
@@ -1090,9 +1122,9 @@ static bool uploadVB(SRPVertexBuffer* vb)
 {
 	if (!vb->dirty && vb->dev.ptr) return true;
 	if (!vb->dev.reserve(vb->nBytes + 16, "srpDraw")) return false;
-	if (vb->nBytes) cudaMemcpyAsync(vb->dev.ptr, vb->host, vb->nBytes, cudaMemcpyHostToDevice, g.stream);
+	if (vb->nBytes) cudaMemcpyAsync(vb->dev.ptr, vb->host, vb->nBytes, cudaMemcpyHostToDevice, copyStreamReady());
 	vb->dirty = false;
-	markUpload(vb->ready, vb->pending);
+	markUpload(vb->ready, vb->pending, vb->seq);
 	return true;
 }
 
@@ -1100,9 +1132,9 @@ static bool uploadIB(SRPIndexBuffer* ib)
 {
 	if (!ib->dirty && ib->dev.ptr) return true;
 	if (!ib->dev.reserve(ib->nBytes + 16, "srpDraw")) return false;
-	if (ib->nBytes) cudaMemcpyAsync(ib->dev.ptr, ib->host, ib->nBytes, cudaMemcpyHostToDevice, g.stream);
+	if (ib->nBytes) cudaMemcpyAsync(ib->dev.ptr, ib->host, ib->nBytes, cudaMemcpyHostToDevice, copyStreamReady());
 	ib->dirty = false;
-	markUpload(ib->ready, ib->pending);
+	markUpload(ib->ready, ib->pending, ib->seq);
 	return true;
 }
 
@@ -1337,16 +1369,17 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			launchShade(P, kind, numTiles, g.stream);
 			stageEnd(SRP_GPU_STAGE_SHADE, 1);
 		};
-		/* the front waits for the last back that used this set, and for the
-		 * uploads of the buffers it reads (both on the library's stream); when
-		 * the whole vertex buffer is shaded, the vertex stage needs no indices
-		 * and the index upload is waited for before setup only */
+		/* the front waits for the last draw that used this set (on the
+		 * library's stream) and for the uploads of the buffers it reads (on
+		 * the copy stream); when the whole vertex buffer is shaded, the vertex
+		 * stage needs no indices and the index upload is waited for before
+		 * setup only */
 		const bool lateIb = ib && P.shadeAll && ib->ready;
-		if (fs != g.stream) {
-			cudaStreamWaitEvent(fs, S.rasterDone, 0);
-			if (vb->ready) cudaStreamWaitEvent(fs, vb->ready, 0);
-			if (ib && ib->ready && !lateIb) cudaStreamWaitEvent(fs, ib->ready, 0);
-		}
+		if (fs != g.stream) cudaStreamWaitEvent(fs, S.rasterDone, 0);
+		if (vb->ready) cudaStreamWaitEvent(fs, vb->ready, 0);
+		if (ib && ib->ready && !lateIb) cudaStreamWaitEvent(fs, ib->ready, 0);
+		if (fs != g.stream) g.frontReads = true;
+		else g.streamReads = true;
 		runDrawSeq(graphKey(P, { (unsigned long long) kind, late, ib != nullptr, start, count, vb->nVertices, blocks,
 		                         keyBits, numTiles, g.bigJobsSeen[kind], (unsigned long long) (uintptr_t) g.stream,
 		                         (unsigned long long) (uintptr_t) fs, (unsigned long long) (uintptr_t) rs }),
@@ -1645,30 +1678,26 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	const cudaStream_t fs = (g.overlap && !g.profiling && !learned) ? g.frontStream : g.stream;
 	/* the pass's resolve runs beside the previous pass's shading */
 	const cudaStream_t rs = fs != g.stream ? g.resolveStream : g.stream;
-	if (fs != g.stream) {
-		/* the front waits for the last back that used this set and for the
-		 * uploads of the draws' buffers since a front last waited for them (one
-		 * event of the library's stream stands for many) */
-		cudaStreamWaitEvent(fs, S.rasterDone, 0);
-		size_t pending = 0;
-		for (size_t k = 0; k < n; ++k) {
-			const SRPGpuDraw& d = draws[idx[k]];
-			pending += ((SRPVertexBuffer*) d.vertexBuffer)->pending;
-			if (d.indexBuffer) pending += ((SRPIndexBuffer*) d.indexBuffer)->pending;
-		}
-		if (pending > 64) {
-			cudaEventRecord(S.headDone, g.stream);
-			cudaStreamWaitEvent(fs, S.headDone, 0);
-		}
+	/* the front waits for the last draw that used this set (on the library's
+	 * stream) and for the uploads of the draws' buffers since a front last
+	 * waited for them: uploads complete in order on the copy stream, so the
+	 * latest of them stands for all */
+	if (fs != g.stream) cudaStreamWaitEvent(fs, S.rasterDone, 0);
+	{
+		cudaEvent_t latest = nullptr;
+		unsigned long long latestSeq = 0;
 		for (size_t k = 0; k < n; ++k) {
 			const SRPGpuDraw& d = draws[idx[k]];
 			SRPVertexBuffer* vb = (SRPVertexBuffer*) d.vertexBuffer;
 			SRPIndexBuffer* ib = (SRPIndexBuffer*) d.indexBuffer;
-			if (vb->pending && pending <= 64) cudaStreamWaitEvent(fs, vb->ready, 0);
-			if (ib && ib->pending && pending <= 64) cudaStreamWaitEvent(fs, ib->ready, 0);
+			if (vb->pending && vb->ready && vb->seq > latestSeq) { latest = vb->ready; latestSeq = vb->seq; }
+			if (ib && ib->pending && ib->ready && ib->seq > latestSeq) { latest = ib->ready; latestSeq = ib->seq; }
 			vb->pending = false;
 			if (ib) ib->pending = false;
 		}
+		if (latest) cudaStreamWaitEvent(fs, latest, 0);
+		if (fs != g.stream) g.frontReads = true;
+		else g.streamReads = true;
 	}
 	/* descriptors and prefix sums go up on the front stream, ahead of the head */
 	cudaMemcpyAsync(S.passDesc.ptr, desc, n * sizeof(DrawDesc), cudaMemcpyHostToDevice, fs);
@@ -1893,6 +1922,7 @@ void srpGpuDrawBatch(const SRPGpuDraw* draws, size_t n)
 void srpGpuSetStream(void* stream)
 {
 	if (!ensureInit("srpGpuSetStream")) return;
+	cudaStreamSynchronize(g.copyStream);
 	cudaStreamSynchronize(g.frontStream);
 	cudaStreamSynchronize(g.resolveStream);
 	cudaStreamSynchronize(g.stream);
@@ -1905,6 +1935,8 @@ void* srpGpuGetStream(void) { return ensureInit("srpGpuGetStream") ? (void*) g.s
 int srpGpuSynchronize(void)
 {
 	if (!g.init) return 0;
+	cudaStreamSynchronize(g.copyStream);
+	cudaStreamSynchronize(g.frontStream);
 	cudaStreamSynchronize(g.resolveStream);
 	return cudaOk(cudaStreamSynchronize(g.stream), "srpGpuSynchronize", "kernel execution") ? 0 : 1;
 }
@@ -2189,6 +2221,19 @@ int fixedDrawPrepare(DrawParams& P, const SRPIndexBuffer* ib, const SRPVertexBuf
 	const int mode = isTri(prim) ? st.polygonMode : (isLine(prim) ? SRP_POLYGON_MODE_LINE : SRP_POLYGON_MODE_POINT);
 	info.stream = g.stream;
 	g.rsDirty = true;  /* its resolve writes the planes on the library's stream */
+	/* the uploads of its buffers, on the copy stream; inside a stream capture
+	 * nothing is waited for: there the buffers come from srpVertexBufferCopyData
+	 * and srpIndexBufferCopyData, which return once their copy is done */
+	cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+	if (cudaStreamIsCapturing(g.stream, &cap) != cudaSuccess) {
+		cudaGetLastError();
+		cap = cudaStreamCaptureStatusNone;
+	}
+	if (cap == cudaStreamCaptureStatusNone) {
+		if (vb->ready) cudaStreamWaitEvent(g.stream, vb->ready, 0);
+		if (ib && ib->ready) cudaStreamWaitEvent(g.stream, ib->ready, 0);
+	}
+	g.streamReads = true;
 	info.nIn = nIn;
 	info.outPer = isTri(prim) && mode != SRP_POLYGON_MODE_FILL ? 3 : 1;
 	info.numTiles = (uint32_t) st.tilesX * (uint32_t) st.tilesY;

@@ -110,3 +110,46 @@ def test_batch_with_a_bad_index_reports_and_draws_the_rest(api):
             L.srpDrawIndexBuffer(ib, vb, ref, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, cnt)
         assert_same(api.planes(fbs[i]), api.planes(ref), f"draw {i}")
     assert L.srpGpuSynchronize() == 0
+
+
+def test_framebuffer_work_between_overlapped_draws_keeps_its_place(api):
+    """A depth fill and an asynchronous download queued between draws that
+    overlap (front, resolve and shading on three streams) act at their place
+    in submission order: the second draw sees the filled depth, and the
+    download holds the planes after that draw, not after the one queued
+    behind it. Overlap on and off give the same planes."""
+    import srp_gb300
+    L = api.L
+    vp = ctypes.c_void_p
+    L.srpGpuFramebufferFill.argtypes = [vp, ctypes.c_uint32, ctypes.c_float, ctypes.c_uint8, ctypes.c_uint]
+    L.srpGpuFramebufferSyncAsync.argtypes = [vp]
+    L.srpGpuSetDrawOverlap.argtypes = [ctypes.c_int]
+    rng = np.random.default_rng(12)
+    soups = [triangle_soup(rng, 3000) for _ in range(3)]
+    results = []
+    try:
+        for overlap in (0, 1):
+            L.srpGpuSetDrawOverlap(overlap)
+            vbs = [api.vertex_buffer(t) for t in soups]
+            fb = api.framebuffer(320, 240)
+            for _ in range(2):
+                L.srpFramebufferClear(fb)
+                L.srpDrawVertexBuffer(vbs[0], fb, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, soups[0].shape[0])
+                L.srpGpuFramebufferFill(fb, 0, 0.25, 0, 2)  # depth plane only
+                L.srpDrawVertexBuffer(vbs[1], fb, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, soups[1].shape[0])
+                L.srpGpuFramebufferSyncAsync(fb)
+                L.srpDrawVertexBuffer(vbs[2], fb, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, soups[2].shape[0])
+            assert L.srpGpuSynchronize() == 0
+            mid = srp_gb300.framebuffer_arrays(fb)
+            end = api.planes(fb)
+            assert not api.errors(), api.errors()
+            results.append((mid, end))
+    finally:
+        L.srpGpuSetDrawOverlap(1)
+    (mid0, end0), (mid1, end1) = results
+    assert_same(mid1, mid0, "download between overlapped draws")
+    assert_same(end1, end0, "planes after overlapped draws")
+    # the download is not the final state: the third draw changed the image
+    assert not np.array_equal(mid0[0], end0[0])
+    # the fill took effect: pixels the second draw left alone hold its depth
+    assert np.count_nonzero(mid0[1] == np.float32(0.25)) > 0
