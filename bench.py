@@ -290,21 +290,33 @@ def run_batch(args):
     clk = clocks.stop()
     # end to end through the public API: every scene's geometry up from pinned
     # host memory and its three framebuffer planes back, with the
-    # stream-ordered transfers and one wait per step
-    e2e = []
-    for it in range(1 + max(3, args.steps)):
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        for sc in batch:
-            sc.upload_async()
-        prepare()
-        srp_gb300.render_batch(batch, fbs)
-        for sc in batch:
-            sc.sync_async()
-        if L.srpGpuSynchronize() != 0:
-            raise RuntimeError("srpGpuSynchronize failed")
-        if it:  # the first pass is an untimed warm-up
-            e2e.append(time.perf_counter() - t1)
+    # stream-ordered transfers and one wait per step: the Batch calls (gather
+    # kernels), and one call per buffer beside them
+    def e2e_steps(batch_calls):
+        out = []
+        for it in range(1 + max(3, args.steps)):
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            if batch_calls:
+                srp_gb300.upload_batch(batch)
+            else:
+                for sc in batch:
+                    sc.upload_async()
+            prepare()
+            srp_gb300.render_batch(batch, fbs)
+            if batch_calls:
+                srp_gb300.sync_batch(fbs)
+            else:
+                for sc in batch:
+                    sc.sync_async()
+            if L.srpGpuSynchronize() != 0:
+                raise RuntimeError("srpGpuSynchronize failed")
+            if it:  # the first pass is an untimed warm-up
+                out.append(time.perf_counter() - t1)
+        return out
+
+    e2e = e2e_steps(True)
+    e2e_calls = e2e_steps(False)
     L.srpGpuSetProfiling(1)
     L.srpGpuResetProfile()
     with torch.cuda.stream(stream):
@@ -330,7 +342,10 @@ def run_batch(args):
                    "l2": "flushed between steps (256 MB write)", "tuning": tuning},
         "clocks": clk,
         "e2e": {"value": round(args.scenes / e2e_s, 2), "unit": "scenes/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(pixels * 9)},
+                "d2h_bytes_per_step": int(pixels * 9),
+                "transfers": "srpGpuVertexBufferCopyDataBatchAsync / srpGpuIndexBufferCopyDataBatchAsync / "
+                             "srpGpuFramebufferSyncBatchAsync (gather kernels), one wait per step",
+                "with_per_buffer_calls": round(args.scenes / (sum(e2e_calls) / len(e2e_calls)), 2)},
         "gpu_launches": int(st.kernelLaunches),
         "roofline": {"bound": "hbm", "achieved": round(resolve_gbs, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(resolve_gbs / peak, 5), "traffic": None,

@@ -82,6 +82,23 @@ void srpGpuIndexBufferCopyDataAsync(SRPIndexBuffer* buffer, SRPType type, size_t
  *  the next srpGpuSynchronize. */
 void srpGpuFramebufferSyncAsync(const SRPFramebuffer* fb);
 
+/** Many srpGpuVertexBufferCopyDataAsync calls in one: buffer i takes
+ *  nBytes[i] bytes of stride strides[i] from data[i]. Sources the device can
+ *  reach (page-locked memory, or any host memory where the device has
+ *  pageable-memory access) are copied by one gather kernel per 256 buffers
+ *  on the copy stream, at the host link's speed and without a driver call
+ *  per buffer; other sources take the single-buffer path. */
+void srpGpuVertexBufferCopyDataBatchAsync(SRPVertexBuffer* const* buffers, const size_t* strides, const size_t* nBytes,
+                                          const void* const* data, size_t n);
+/** Many srpGpuIndexBufferCopyDataAsync calls in one, as above. */
+void srpGpuIndexBufferCopyDataBatchAsync(SRPIndexBuffer* const* buffers, const SRPType* types, const size_t* nBytes,
+                                         const void* const* data, size_t n);
+/** Many srpGpuFramebufferSyncAsync calls in one: framebuffers last written by
+ *  the same draw or batch pass come back by one gather kernel, after that
+ *  draw or pass only, beside later ones. The host arrays are current after
+ *  the next srpGpuSynchronize. */
+void srpGpuFramebufferSyncBatchAsync(const SRPFramebuffer* const* fbs, size_t n);
+
 /* ----------------------------------------------------- batched draws */
 
 /** One draw of srpGpuDrawBatch: the arguments of srpDrawIndexBuffer

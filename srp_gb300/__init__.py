@@ -219,13 +219,31 @@ def render_batch(batch, fbs):
     S.sceneBatchRender(sp, fp, n, scratch)
 
 
+def upload_batch(batch):
+    """Scene.upload_async of every scene with the Batch copies (gather
+    kernels, 256 scenes at a time): complete after srpGpuSynchronize."""
+    S = scenes()
+    n = len(batch)
+    sp = (ctypes.c_void_p * n)(*[sc.ptr for sc in batch])
+    S.sceneUploadBatchAsync(sp, ctypes.c_size_t(n))
+
+
+def sync_batch(fbs):
+    """srpGpuFramebufferSyncBatchAsync of the framebuffers: the host arrays
+    are current after srpGpuSynchronize."""
+    L = lib()
+    n = len(fbs)
+    fp = (ctypes.c_void_p * n)(*fbs)
+    L.srpGpuFramebufferSyncBatchAsync(fp, ctypes.c_size_t(n))
+
+
 def prepare_batch(batch, fbs):
     """Prepare the framebuffers of a batch in one srpGpuFramebufferFillBatch."""
     S = scenes()
     n = len(batch)
     sp = (ctypes.c_void_p * n)(*[sc.ptr for sc in batch])
     fp = (ctypes.c_void_p * n)(*fbs)
-    S.scenePrepareBatch(sp, fp, n)
+    S.scenePrepareBatch(sp, fp, ctypes.c_size_t(n))
 
 
 def autotune_batch(batch, fbs, repeats=1):

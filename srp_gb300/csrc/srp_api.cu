@@ -139,6 +139,27 @@ struct Lib {
 	cudaEvent_t copyGateFront = nullptr, copyGateStream = nullptr;
 	bool frontReads = false, streamReads = false;
 	unsigned long long uploadSeq = 0;
+	/* srpGpuFramebufferSyncAsync copies on downloadStream, after the event of
+	 * the draw or pass that last wrote the framebuffer (one of writeEvents,
+	 * recorded on `stream` after its shading, numbered by writeSeq), so that
+	 * a batch's first framebuffers come back while later passes render.
+	 * downloadsPending: framebuffer work queued later must first wait for
+	 * those copies (fbAfterDownloads). */
+	static constexpr int kWriteEvents = 64;
+	cudaStream_t downloadStream = nullptr;
+	cudaEvent_t downloadEvent = nullptr;
+	cudaEvent_t writeEvents[kWriteEvents] = {};
+	int writeNext = 0;
+	unsigned long long writeSeq = 0, downloadWaitedSeq = 0;
+	bool downloadsPending = false;
+	/* gathered transfers (the Batch calls): one kernel per group of buffers,
+	 * item lists staged in gatherUp / gatherDown; a group's uploads end at
+	 * one of gatherEvents, which its buffers borrow as their upload event */
+	static constexpr int kGatherEvents = 64;
+	cudaEvent_t gatherEvents[kGatherEvents] = {};
+	int gatherNext = 0;
+	DeviceBuffer gatherUp, gatherDown;
+	bool pageableAccess = false;      /* the device reaches any host memory */
 	bool overlap = true;
 	bool graphs = true;               /* replay repeated draws from captured CUDA graphs */
 	SRPGpuTuning tune = { 96, 3 };    /* heavy-tile threshold, heavy-tile CTAs per SM */
@@ -189,7 +210,19 @@ bool ensureInit(const char* fn)
 	    !cudaOk(cudaEventCreateWithFlags(&g.rsEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 	    !cudaOk(cudaStreamCreateWithFlags(&g.copyStream, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
 	    !cudaOk(cudaEventCreateWithFlags(&g.copyGateFront, cudaEventDisableTiming), fn, "cudaEventCreate") ||
-	    !cudaOk(cudaEventCreateWithFlags(&g.copyGateStream, cudaEventDisableTiming), fn, "cudaEventCreate")) return false;
+	    !cudaOk(cudaEventCreateWithFlags(&g.copyGateStream, cudaEventDisableTiming), fn, "cudaEventCreate") ||
+	    !cudaOk(cudaStreamCreateWithFlags(&g.downloadStream, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
+	    !cudaOk(cudaEventCreateWithFlags(&g.downloadEvent, cudaEventDisableTiming), fn, "cudaEventCreate")) return false;
+	for (cudaEvent_t& e : g.writeEvents)
+		if (!cudaOk(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), fn, "cudaEventCreate")) return false;
+	for (cudaEvent_t& e : g.gatherEvents)
+		if (!cudaOk(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), fn, "cudaEventCreate")) return false;
+	{
+		int dev = 0, pageable = 0;
+		cudaGetDevice(&dev);
+		if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) cudaGetLastError();
+		g.pageableAccess = pageable != 0;
+	}
 	for (DrawSet& S : g.sets) {
 		if (!cudaOk(cudaEventCreateWithFlags(&S.ctrEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 		    !cudaOk(cudaEventCreateWithFlags(&S.headDone, cudaEventDisableTiming), fn, "cudaEventCreate") ||
@@ -462,6 +495,7 @@ struct SRPVertexBuffer {
 	DeviceBuffer dev;
 	bool dirty = false;
 	cudaEvent_t ready = nullptr;      /* recorded after the last upload (copy stream) */
+	bool readyOwned = true;           /* false: ready is a gathered group's event */
 	bool pending = false;             /* uploaded since a pass's front last waited for it */
 	unsigned long long seq = 0;       /* upload number of the last upload */
 };
@@ -473,6 +507,7 @@ struct SRPIndexBuffer {
 	DeviceBuffer dev;
 	bool dirty = false;
 	cudaEvent_t ready = nullptr;
+	bool readyOwned = true;
 	bool pending = false;
 	unsigned long long seq = 0;
 };
@@ -480,8 +515,12 @@ struct SRPIndexBuffer {
 /* Marks the end of an upload into a buffer: the stage of a later draw that
  * reads the buffer waits for it. Uploads are numbered in the order of the
  * copy stream, on which they complete in that order. */
-static void markUpload(cudaEvent_t& ready, bool& pending, unsigned long long& seq)
+static void markUpload(cudaEvent_t& ready, bool& readyOwned, bool& pending, unsigned long long& seq)
 {
+	if (!readyOwned) {
+		ready = nullptr;
+		readyOwned = true;
+	}
 	if (!ready && cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) != cudaSuccess) {
 		cudaGetLastError();
 		ready = nullptr;
@@ -507,6 +546,80 @@ static cudaStream_t copyStreamReady()
 		g.streamReads = false;
 	}
 	return g.copyStream;
+}
+
+/* ------------------------------------------------------ gathered copies */
+
+/* One contiguous copy of a gathered transfer, cut into kGatherChunk pieces;
+ * firstChunk counts the pieces of the items before it. */
+struct GatherItem {
+	const unsigned char* src;
+	unsigned char* dst;
+	unsigned long long bytes;
+	unsigned long long firstChunk;
+};
+constexpr unsigned long long kGatherChunk = 64ull << 10;
+
+/* A block per piece, its item found by binary search over firstChunk.
+ * Sources and destinations are device memory or host memory that the device
+ * reaches (page-locked, or any host memory with pageable-memory access). */
+__global__ void k_gather(const GatherItem* items, unsigned n, unsigned long long chunks)
+{
+	for (unsigned long long c = blockIdx.x; c < chunks; c += gridDim.x) {
+		unsigned lo = 0, hi = n;
+		while (hi - lo > 1) {
+			const unsigned mid = (lo + hi) / 2;
+			if (items[mid].firstChunk <= c) lo = mid;
+			else hi = mid;
+		}
+		const GatherItem it = items[lo];
+		const unsigned long long off = (c - it.firstChunk) * kGatherChunk;
+		const unsigned long long len = it.bytes - off < kGatherChunk ? it.bytes - off : kGatherChunk;
+		const unsigned char* src = it.src + off;
+		unsigned char* dst = it.dst + off;
+		if ((((uintptr_t) src) | ((uintptr_t) dst)) % 16 == 0) {
+			const unsigned long long n16 = len / 16;
+			for (unsigned long long i = threadIdx.x; i < n16; i += blockDim.x) ((uint4*) dst)[i] = ((const uint4*) src)[i];
+			for (unsigned long long i = n16 * 16 + threadIdx.x; i < len; i += blockDim.x) dst[i] = src[i];
+		} else {
+			for (unsigned long long i = threadIdx.x; i < len; i += blockDim.x) dst[i] = src[i];
+		}
+	}
+}
+
+/* The address by which the device reaches host memory p, or null. */
+static void* deviceView(const void* p)
+{
+	if (g.pageableAccess) return (void*) p;
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+		cudaGetLastError();
+		return nullptr;
+	}
+	if (a.type == cudaMemoryTypeHost || a.type == cudaMemoryTypeManaged || a.type == cudaMemoryTypeDevice)
+		return a.devicePointer ? a.devicePointer : (void*) p;
+	return nullptr;
+}
+
+/* Enqueues the copies of items [first, last) as one kernel on stream s, its
+ * item list staged in dev at offset `slot` items (from pageable memory: the
+ * call returns once the list has been read). */
+static bool gatherLaunch(std::vector<GatherItem>& items, size_t first, size_t last, DeviceBuffer& dev, size_t slot,
+                         cudaStream_t s, const char* fn)
+{
+	if (last <= first) return true;
+	unsigned long long chunks = 0;
+	for (size_t i = first; i < last; ++i) {
+		items[i].firstChunk = chunks;
+		chunks += (items[i].bytes + kGatherChunk - 1) / kGatherChunk;
+	}
+	GatherItem* d = dev.as<GatherItem>() + slot;
+	if (!cudaOk(cudaMemcpyAsync(d, items.data() + first, (last - first) * sizeof(GatherItem), cudaMemcpyHostToDevice, s),
+	            fn, "cudaMemcpyAsync")) return false;
+	const unsigned blocks = (unsigned) std::min<unsigned long long>(chunks, 256);
+	k_gather<<<blocks, 256, 0, s>>>(d, (unsigned) (last - first), chunks);
+	++g.launches;
+	return cudaOk(cudaGetLastError(), fn, "launch");
 }
 
 static size_t indexTypeSize(SRPType t)
@@ -576,7 +689,7 @@ void srpFreeVertexBuffer(SRPVertexBuffer* b)
 {
 	if (!b) return;
 	if (g.init) cudaStreamSynchronize(g.copyStream);  /* copies from b->host may be in flight */
-	if (b->ready) cudaEventDestroy(b->ready);
+	if (b->ready && b->readyOwned) cudaEventDestroy(b->ready);
 	if (b->host) cudaFreeHost(b->host);
 	if (b->dev.ptr) cudaFree(b->dev.ptr);
 	delete b;
@@ -589,7 +702,7 @@ void srpVertexBufferCopyData(SRPVertexBuffer* b, size_t stride, size_t nBytes, c
 	b->nBytes = nBytes;
 	if (gpuPresent()) {
 		b->dirty = !copyToDevice(b->dev, data, nBytes, "srpVertexBufferCopyData");
-		if (!b->dirty) { markUpload(b->ready, b->pending, b->seq); return; }
+		if (!b->dirty) { markUpload(b->ready, b->readyOwned, b->pending, b->seq); return; }
 	}
 	/* no device: keep a host copy, uploaded by the first draw */
 	if (nBytes > b->cap) { b->host = (unsigned char*) pinnedRealloc(b->host, nBytes); b->cap = nBytes; }
@@ -605,7 +718,7 @@ void srpGpuVertexBufferCopyDataAsync(SRPVertexBuffer* b, size_t stride, size_t n
 	b->nBytes = nBytes;
 	b->dirty = !copyToDeviceAsync(b->dev, data, nBytes, "srpGpuVertexBufferCopyDataAsync");
 	if (b->dirty) srpVertexBufferCopyData(b, stride, nBytes, data);
-	else markUpload(b->ready, b->pending, b->seq);
+	else markUpload(b->ready, b->readyOwned, b->pending, b->seq);
 }
 
 SRPIndexBuffer* srpNewIndexBuffer(void) { return new SRPIndexBuffer(); }
@@ -614,7 +727,7 @@ void srpFreeIndexBuffer(SRPIndexBuffer* b)
 {
 	if (!b) return;
 	if (g.init) cudaStreamSynchronize(g.copyStream);  /* copies from b->host may be in flight */
-	if (b->ready) cudaEventDestroy(b->ready);
+	if (b->ready && b->readyOwned) cudaEventDestroy(b->ready);
 	if (b->host) cudaFreeHost(b->host);
 	if (b->dev.ptr) cudaFree(b->dev.ptr);
 	delete b;
@@ -629,7 +742,7 @@ void srpIndexBufferCopyData(SRPIndexBuffer* b, SRPType type, size_t nBytes, cons
 	b->nBytes = nBytes;
 	if (gpuPresent()) {
 		b->dirty = !copyToDevice(b->dev, data, nBytes, "srpIndexBufferCopyData");
-		if (!b->dirty) { markUpload(b->ready, b->pending, b->seq); return; }
+		if (!b->dirty) { markUpload(b->ready, b->readyOwned, b->pending, b->seq); return; }
 	}
 	if (nBytes > b->cap) { b->host = (unsigned char*) pinnedRealloc(b->host, nBytes); b->cap = nBytes; }
 	if (nBytes) memcpy(b->host, data, nBytes);
@@ -645,7 +758,105 @@ void srpGpuIndexBufferCopyDataAsync(SRPIndexBuffer* b, SRPType type, size_t nByt
 	b->nBytes = nBytes;
 	b->dirty = !copyToDeviceAsync(b->dev, data, nBytes, "srpGpuIndexBufferCopyDataAsync");
 	if (b->dirty) srpIndexBufferCopyData(b, type, nBytes, data);
-	else markUpload(b->ready, b->pending, b->seq);
+	else markUpload(b->ready, b->readyOwned, b->pending, b->seq);
+}
+
+/* An upload of a Batch call: the buffer's device memory, the source as the
+ * device reaches it, and the buffer's upload bookkeeping. */
+struct UploadTarget {
+	DeviceBuffer* dev;
+	const void* src;
+	size_t bytes;
+	cudaEvent_t* ready;
+	bool* readyOwned;
+	bool* pending;
+	unsigned long long* seq;
+	bool* dirty;
+};
+
+/* Gathered uploads, in groups of 256 buffers: one kernel per group on the
+ * copy stream, and one event, which the group's buffers borrow as their
+ * upload event. */
+static void gatherUploads(std::vector<UploadTarget>& t, const char* fn)
+{
+	if (t.empty()) return;
+	const cudaStream_t cs = copyStreamReady();
+	std::vector<GatherItem> items;
+	items.reserve(t.size());
+	for (const UploadTarget& u : t) items.push_back({ (const unsigned char*) u.src, (unsigned char*) u.dev->ptr, u.bytes, 0 });
+	if (!g.gatherUp.reserve(items.size() * sizeof(GatherItem), fn)) return;
+	constexpr size_t kGroup = 256;
+	for (size_t first = 0; first < items.size(); first += kGroup) {
+		const size_t last = std::min(items.size(), first + kGroup);
+		if (!gatherLaunch(items, first, last, g.gatherUp, first, cs, fn)) return;
+		cudaEvent_t e = g.gatherEvents[g.gatherNext];
+		g.gatherNext = (g.gatherNext + 1) % Lib::kGatherEvents;
+		cudaEventRecord(e, cs);
+		const unsigned long long seq = ++g.uploadSeq;
+		for (size_t k = first; k < last; ++k) {
+			UploadTarget& u = t[k];
+			if (*u.ready && *u.readyOwned) cudaEventDestroy(*u.ready);
+			*u.ready = e;
+			*u.readyOwned = false;
+			*u.pending = true;
+			*u.seq = seq;
+			*u.dirty = false;
+		}
+	}
+}
+
+void srpGpuVertexBufferCopyDataBatchAsync(SRPVertexBuffer* const* buffers, const size_t* strides, const size_t* nBytes,
+                                          const void* const* data, size_t n)
+{
+	const char* FN = "srpGpuVertexBufferCopyDataBatchAsync";
+	if (!n || !buffers) return;
+	if (!gpuPresent() || !ensureInit(FN)) {
+		for (size_t i = 0; i < n; ++i) srpVertexBufferCopyData(buffers[i], strides[i], nBytes[i], data[i]);
+		return;
+	}
+	std::vector<UploadTarget> t;
+	t.reserve(n);
+	for (size_t i = 0; i < n; ++i) {
+		SRPVertexBuffer* b = buffers[i];
+		const void* src = nBytes[i] ? deviceView(data[i]) : nullptr;
+		if (!src || !b->dev.reserve(nBytes[i] + 16, FN)) {
+			srpGpuVertexBufferCopyDataAsync(b, strides[i], nBytes[i], data[i]);
+			continue;
+		}
+		b->stride = strides[i];
+		b->nVertices = strides[i] ? nBytes[i] / strides[i] : 0;
+		b->nBytes = nBytes[i];
+		t.push_back({ &b->dev, src, nBytes[i], &b->ready, &b->readyOwned, &b->pending, &b->seq, &b->dirty });
+	}
+	gatherUploads(t, FN);
+}
+
+void srpGpuIndexBufferCopyDataBatchAsync(SRPIndexBuffer* const* buffers, const SRPType* types, const size_t* nBytes,
+                                         const void* const* data, size_t n)
+{
+	const char* FN = "srpGpuIndexBufferCopyDataBatchAsync";
+	if (!n || !buffers) return;
+	if (!gpuPresent() || !ensureInit(FN)) {
+		for (size_t i = 0; i < n; ++i) srpIndexBufferCopyData(buffers[i], types[i], nBytes[i], data[i]);
+		return;
+	}
+	std::vector<UploadTarget> t;
+	t.reserve(n);
+	for (size_t i = 0; i < n; ++i) {
+		SRPIndexBuffer* b = buffers[i];
+		const size_t elem = indexTypeSize(types[i]);
+		const void* src = nBytes[i] && elem ? deviceView(data[i]) : nullptr;
+		if (!src || !b->dev.reserve(nBytes[i] + 16, FN)) {
+			srpGpuIndexBufferCopyDataAsync(b, types[i], nBytes[i], data[i]);
+			continue;
+		}
+		b->type = types[i];
+		b->elemSize = elem;
+		b->nIndices = nBytes[i] / elem;
+		b->nBytes = nBytes[i];
+		t.push_back({ &b->dev, src, nBytes[i], &b->ready, &b->readyOwned, &b->pending, &b->seq, &b->dirty });
+	}
+	gatherUploads(t, FN);
 }
 
 }  // extern "C"
@@ -657,6 +868,14 @@ struct FbExtra {
 	uint32_t* color = nullptr;
 	float* depth = nullptr;
 	uint8_t* stencil = nullptr;
+	/* the draw or pass that last wrote the planes: its event and number
+	 * (null after any other write, whose end the library's stream marks) */
+	cudaEvent_t lastWrite = nullptr;
+	unsigned long long lastWriteSeq = 0;
+	/* the host block of the planes as made by srpNewFramebuffer, and the
+	 * address by which the device reaches it (null if it cannot) */
+	void* hostBase = nullptr;
+	void* hostDev = nullptr;
 };
 /* The public struct has no room for device pointers; they live in a side
  * table keyed by the framebuffer address. */
@@ -714,8 +933,40 @@ static bool fbContiguous(const SRPFramebuffer* fb)
 	       fb->stencil == (unsigned char*) fb->color + 8 * n;
 }
 
+/* Framebuffer work about to be queued on the library's stream comes after
+ * the copies queued on the download stream, which read the planes into the
+ * host arrays; the resolve stream follows through rsDirty. */
+static void fbAfterDownloads()
+{
+	if (!g.downloadsPending) return;
+	cudaEventRecord(g.downloadEvent, g.downloadStream);
+	cudaStreamWaitEvent(g.stream, g.downloadEvent, 0);
+	g.downloadsPending = false;
+	g.rsDirty = true;
+}
+
+/* A write other than a draw's: later downloads of the framebuffer wait for
+ * the library's stream. */
+static void fbOtherWrite(FbExtra* x)
+{
+	fbAfterDownloads();
+	x->lastWrite = nullptr;
+}
+
+/* The end of a draw or pass, marked on the library's stream after its
+ * shading; returns the event and its number. */
+static cudaEvent_t drawWriteEvent(unsigned long long& seq)
+{
+	cudaEvent_t e = g.writeEvents[g.writeNext];
+	g.writeNext = (g.writeNext + 1) % Lib::kWriteEvents;
+	cudaEventRecord(e, g.stream);
+	seq = ++g.writeSeq;
+	return e;
+}
+
 static void fbUpload(const SRPFramebuffer* fb, FbExtra* x)
 {
+	fbOtherWrite(x);
 	g.rsDirty = true;
 	if (fbContiguous(fb)) {
 		cudaMemcpyAsync(x->color, fb->color, 9 * fb->size, cudaMemcpyHostToDevice, g.stream);
@@ -728,6 +979,7 @@ static void fbUpload(const SRPFramebuffer* fb, FbExtra* x)
 
 static void fbDownloadAsync(const SRPFramebuffer* fb, FbExtra* x)
 {
+	fbAfterDownloads();  /* the same host arrays */
 	g.rsDirty = true;
 	if (fbContiguous(fb)) {
 		cudaMemcpyAsync(fb->color, x->color, 9 * fb->size, cudaMemcpyDeviceToHost, g.stream);
@@ -769,6 +1021,8 @@ SRPFramebuffer* srpNewFramebuffer(size_t w, size_t h)
 	x.color = (uint32_t*) dev;
 	x.depth = (float*) (dev + 4 * n);
 	x.stencil = dev + 8 * n;
+	x.hostBase = host;
+	x.hostDev = deviceView(host);
 	cudaMemsetAsync(dev, 0, 9 * n, g.stream);
 	g.rsDirty = true;
 	fbTable[fb] = x;
@@ -781,6 +1035,7 @@ void srpFreeFramebuffer(SRPFramebuffer* fb)
 	if (g.init) {
 		cudaStreamSynchronize(g.frontStream);
 		cudaStreamSynchronize(g.resolveStream);
+		cudaStreamSynchronize(g.downloadStream);  /* into the host arrays freed below */
 	}
 	cudaStreamSynchronize(g.stream);
 	auto it = fbTable.find(fb);
@@ -796,6 +1051,7 @@ void srpFramebufferClear(const SRPFramebuffer* fb)
 {
 	FbExtra* x = fbFind(fb);
 	if (!x) return;
+	fbOtherWrite(x);
 	g.rsDirty = true;
 	cudaMemsetAsync(x->color, 0, 4 * fb->size, g.stream);
 	fill32((uint32_t*) x->depth, 0xBF800000u /* -1.0f */, fb->size);
@@ -843,7 +1099,62 @@ int srpGpuSaveFramebufferPNG(const SRPFramebuffer* fb, const char* path)
 void srpGpuFramebufferSyncAsync(const SRPFramebuffer* fb)
 {
 	FbExtra* x = fbFind(fb);
-	if (x) fbDownloadAsync(fb, x);
+	if (!x) return;
+	if (!x->lastWrite || !fbContiguous(fb)) {
+		fbDownloadAsync(fb, x);
+		return;
+	}
+	/* after the draw or pass that wrote it last, beside later ones */
+	if (x->lastWriteSeq > g.downloadWaitedSeq) {
+		cudaStreamWaitEvent(g.downloadStream, x->lastWrite, 0);
+		g.downloadWaitedSeq = x->lastWriteSeq;
+	}
+	cudaMemcpyAsync(fb->color, x->color, 9 * fb->size, cudaMemcpyDeviceToHost, g.downloadStream);
+	g.downloadsPending = true;
+}
+
+void srpGpuFramebufferSyncBatchAsync(const SRPFramebuffer* const* fbs, size_t n)
+{
+	const char* FN = "srpGpuFramebufferSyncBatchAsync";
+	if (!n || !fbs) return;
+	if (!g.init || !g.gatherDown.reserve(n * sizeof(GatherItem), FN)) {
+		for (size_t i = 0; i < n; ++i) srpGpuFramebufferSyncAsync(fbs[i]);
+		return;
+	}
+	/* runs of framebuffers last written by the same draw or pass: one kernel
+	 * each on the download stream, after that draw or pass */
+	std::vector<GatherItem> items;
+	items.reserve(n);
+	size_t first = 0;
+	cudaEvent_t runEvent = nullptr;
+	unsigned long long runSeq = 0;
+	auto flush = [&]() {
+		if (items.size() > first) {
+			if (runSeq > g.downloadWaitedSeq) {
+				cudaStreamWaitEvent(g.downloadStream, runEvent, 0);
+				g.downloadWaitedSeq = runSeq;
+			}
+			gatherLaunch(items, first, items.size(), g.gatherDown, first, g.downloadStream, FN);
+			g.downloadsPending = true;
+		}
+		first = items.size();
+	};
+	for (size_t i = 0; i < n; ++i) {
+		const SRPFramebuffer* fb = fbs[i];
+		FbExtra* x = fbFind(fb);
+		if (!x) continue;
+		if (!x->lastWrite || !x->hostDev || (void*) fb->color != x->hostBase || !fbContiguous(fb) || !fb->size) {
+			srpGpuFramebufferSyncAsync(fb);
+			continue;
+		}
+		if (x->lastWriteSeq != runSeq) {
+			flush();
+			runEvent = x->lastWrite;
+			runSeq = x->lastWriteSeq;
+		}
+		items.push_back({ (const unsigned char*) x->color, (unsigned char*) x->hostDev, 9ull * fb->size, 0 });
+	}
+	flush();
 }
 
 void srpGpuFramebufferFillBatch(const SRPFramebuffer* const* fbs, size_t n, uint32_t color, float depth,
@@ -856,6 +1167,7 @@ void srpGpuFramebufferFillBatch(const SRPFramebuffer* const* fbs, size_t n, uint
 	for (size_t i = 0; i < n; ++i) {
 		FbExtra* x = fbFind(fbs[i]);
 		if (!x) { SRP_ERROR(FN, "Framebuffer %zu was not created by srpNewFramebuffer", i); return; }
+		fbOtherWrite(x);
 		t.push_back(FillTarget{ x->color, (uint32_t*) x->depth, x->stencil, fbs[i]->size });
 	}
 	if (!g.fillTargets.reserve(n * sizeof(FillTarget), FN)) return;
@@ -887,6 +1199,7 @@ void srpGpuFramebufferFill(const SRPFramebuffer* fb, uint32_t color, float depth
 {
 	FbExtra* x = fbFind(fb);
 	if (!x) return;
+	fbOtherWrite(x);
 	g.rsDirty = true;
 	uint32_t dbits;
 	memcpy(&dbits, &depth, 4);
@@ -1124,7 +1437,7 @@ static bool uploadVB(SRPVertexBuffer* vb)
 	if (!vb->dev.reserve(vb->nBytes + 16, "srpDraw")) return false;
 	if (vb->nBytes) cudaMemcpyAsync(vb->dev.ptr, vb->host, vb->nBytes, cudaMemcpyHostToDevice, copyStreamReady());
 	vb->dirty = false;
-	markUpload(vb->ready, vb->pending, vb->seq);
+	markUpload(vb->ready, vb->readyOwned, vb->pending, vb->seq);
 	return true;
 }
 
@@ -1134,7 +1447,7 @@ static bool uploadIB(SRPIndexBuffer* ib)
 	if (!ib->dev.reserve(ib->nBytes + 16, "srpDraw")) return false;
 	if (ib->nBytes) cudaMemcpyAsync(ib->dev.ptr, ib->host, ib->nBytes, cudaMemcpyHostToDevice, copyStreamReady());
 	ib->dirty = false;
-	markUpload(ib->ready, ib->pending, ib->seq);
+	markUpload(ib->ready, ib->readyOwned, ib->pending, ib->seq);
 	return true;
 }
 
@@ -1166,6 +1479,10 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 	SRPVertexBuffer* vb = (SRPVertexBuffer*) vbc;
 	FbExtra* fx = fbFind(fb);
 	if (!fx) { SRP_ERROR(FN, "Framebuffer was not created by srpNewFramebuffer"); return; }
+	/* after downloads in flight; until the draw has been queued in full,
+	 * downloads of this framebuffer go back to the library's stream */
+	fbAfterDownloads();
+	fx->lastWrite = nullptr;
 	const int vsId = lookupVS((void*) sp->vs->shader);
 	const int fsId = lookupFS((void*) sp->fs->shader);
 	if (!vsId || !fsId) {
@@ -1433,6 +1750,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		}
 	}
 	++g.stats.draws;
+	fx->lastWrite = drawWriteEvent(fx->lastWriteSeq);
 	if (g.fbMode == SRP_GPU_FB_COHERENT) fbDownload(fb, fx);
 }
 
@@ -1571,6 +1889,11 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	 * stream: such a pass runs there whole) */
 	DrawSet& S = g.sets[g.setNext];
 	g.setNext ^= 1;
+	/* after downloads in flight; until the pass has been queued in full,
+	 * downloads of its framebuffers go back to the library's stream */
+	fbAfterDownloads();
+	for (size_t k = 0; k < n; ++k)
+		if (FbExtra* x = fbFind(draws[idx[k]].framebuffer)) x->lastWrite = nullptr;
 	if (!buildLayout(sp0->vs, P.L)) return true;
 	DrawState& st = P.st;
 	st.frontFaceCW = srpContext.raster.frontFace == SRP_WINDING_CW;
@@ -1843,6 +2166,15 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		}
 	}
 	g.stats.draws += n;
+	if (drawn) {
+		unsigned long long seq = 0;
+		const cudaEvent_t e = drawWriteEvent(seq);
+		for (size_t k = 0; k < n; ++k)
+			if (FbExtra* x = fbFind(draws[idx[k]].framebuffer)) {
+				x->lastWrite = e;
+				x->lastWriteSeq = seq;
+			}
+	}
 	if (g.fbMode == SRP_GPU_FB_COHERENT)
 		for (size_t k = 0; k < n; ++k) fbDownload(draws[idx[k]].framebuffer, fbFind(draws[idx[k]].framebuffer));
 	if (fs == g.stream) markPassDone();
@@ -1922,6 +2254,8 @@ void srpGpuDrawBatch(const SRPGpuDraw* draws, size_t n)
 void srpGpuSetStream(void* stream)
 {
 	if (!ensureInit("srpGpuSetStream")) return;
+	cudaStreamSynchronize(g.downloadStream);
+	g.downloadsPending = false;
 	cudaStreamSynchronize(g.copyStream);
 	cudaStreamSynchronize(g.frontStream);
 	cudaStreamSynchronize(g.resolveStream);
@@ -1935,6 +2269,7 @@ void* srpGpuGetStream(void) { return ensureInit("srpGpuGetStream") ? (void*) g.s
 int srpGpuSynchronize(void)
 {
 	if (!g.init) return 0;
+	cudaStreamSynchronize(g.downloadStream);
 	cudaStreamSynchronize(g.copyStream);
 	cudaStreamSynchronize(g.frontStream);
 	cudaStreamSynchronize(g.resolveStream);
@@ -2220,6 +2555,7 @@ int fixedDrawPrepare(DrawParams& P, const SRPIndexBuffer* ib, const SRPVertexBuf
 	P.stencil = fx->stencil;
 	const int mode = isTri(prim) ? st.polygonMode : (isLine(prim) ? SRP_POLYGON_MODE_LINE : SRP_POLYGON_MODE_POINT);
 	info.stream = g.stream;
+	fbOtherWrite(fx);
 	g.rsDirty = true;  /* its resolve writes the planes on the library's stream */
 	/* the uploads of its buffers, on the copy stream; inside a stream capture
 	 * nothing is waited for: there the buffers come from srpVertexBufferCopyData

@@ -1465,6 +1465,39 @@ void sceneUploadAsync(Scene* s)
 	if (s->nvb == 0 && s->nib > 0) srpGpuIndexBufferCopyDataAsync(s->ib[0], s->itype[0], s->ibytes[0], s->idata[0]);
 }
 
+void sceneUploadBatchAsync(Scene** scenes, size_t n)
+{
+	size_t cap = 0;
+	for (size_t i = 0; i < n; ++i) cap += (size_t) (scenes[i]->nvb > scenes[i]->nib ? scenes[i]->nvb : scenes[i]->nib);
+	if (!cap) return;
+	SRPVertexBuffer** vb = (SRPVertexBuffer**) malloc(cap * sizeof *vb);
+	SRPIndexBuffer** ib = (SRPIndexBuffer**) malloc(cap * sizeof *ib);
+	size_t* stride = (size_t*) malloc(cap * sizeof *stride);
+	size_t* vbytes = (size_t*) malloc(cap * sizeof *vbytes);
+	size_t* ibytes = (size_t*) malloc(cap * sizeof *ibytes);
+	SRPType* itype = (SRPType*) malloc(cap * sizeof *itype);
+	const void** vsrc = (const void**) malloc(cap * sizeof *vsrc);
+	const void** isrc = (const void**) malloc(cap * sizeof *isrc);
+	for (size_t first = 0; first < n; first += 256) {
+		const size_t last = first + 256 < n ? first + 256 : n;
+		size_t nv = 0, ni = 0;
+		for (size_t i = first; i < last; ++i) {
+			const Scene* s = scenes[i];
+			for (int k = 0; k < s->nvb; ++k) {
+				vb[nv] = s->vb[k]; stride[nv] = s->vstride[k]; vbytes[nv] = s->vbytes[k]; vsrc[nv] = s->vdata[k];
+				++nv;
+			}
+			for (int k = 0; k < s->nib; ++k) {
+				ib[ni] = s->ib[k]; itype[ni] = s->itype[k]; ibytes[ni] = s->ibytes[k]; isrc[ni] = s->idata[k];
+				++ni;
+			}
+		}
+		srpGpuVertexBufferCopyDataBatchAsync(vb, stride, vbytes, vsrc, nv);
+		srpGpuIndexBufferCopyDataBatchAsync(ib, itype, ibytes, isrc, ni);
+	}
+	free(vb); free(ib); free(stride); free(vbytes); free(ibytes); free(itype); free(vsrc); free(isrc);
+}
+
 void scenePrepareBatch(Scene** scenes, SRPFramebuffer** fbs, size_t n)
 {
 	if (!n) return;

@@ -64,6 +64,10 @@ int sceneBatchAutotune(Scene** scenes, SRPFramebuffer** fbs, size_t n, SRPGpuDra
 /* sceneUpload with the asynchronous copies (srpGpu*CopyDataAsync): the
  * scene's host data must stay unchanged until srpGpuSynchronize. */
 void sceneUploadAsync(Scene* s);
+/* sceneUploadAsync of n scenes with the Batch copies, 256 scenes at a time
+ * (their vertex buffers, then their index buffers), so that the first
+ * scenes' buffers arrive first. */
+void sceneUploadBatchAsync(Scene** scenes, size_t n);
 /* scenePrepareFramebuffer of n scenes in one srpGpuFramebufferFillBatch when
  * they share their initial depth and stencil (else one by one). */
 void scenePrepareBatch(Scene** scenes, SRPFramebuffer** fbs, size_t n);

@@ -211,9 +211,11 @@ def test_frame_autotuner_ends_and_keeps_results_exact(built_library):
     assert L.srpGpuSynchronize() == 0
 
 
-def test_async_transfers_and_fill_batch_match_the_synchronous_path(built_library):
+@pytest.mark.parametrize("calls", ["per_buffer", "batch"])
+def test_async_transfers_and_fill_batch_match_the_synchronous_path(built_library, calls):
     """Stream-ordered uploads, one batched framebuffer fill and stream-ordered
-    downloads (one wait in all) give the images of the synchronous calls."""
+    downloads (one wait in all) give the images of the synchronous calls, with
+    one call per buffer and with the Batch calls (gather kernels)."""
     import srp_gb300
     L = srp_gb300.lib()
     S = srp_gb300.scenes()
@@ -234,12 +236,18 @@ def test_async_transfers_and_fill_batch_match_the_synchronous_path(built_library
             ctypes.memset(v.color, 0xAB, 4 * v.size)
             ctypes.memset(v.depth, 0xAB, 4 * v.size)
             ctypes.memset(v.stencil, 0xAB, v.size)
-        for sc in scenes:
-            sc.upload_async()
+        if calls == "batch":
+            srp_gb300.upload_batch(scenes)
+        else:
+            for sc in scenes:
+                sc.upload_async()
         srp_gb300.prepare_batch(scenes, fbs)
         srp_gb300.render_batch(scenes, fbs)
-        for sc in scenes:
-            sc.sync_async()
+        if calls == "batch":
+            srp_gb300.sync_batch(fbs)
+        else:
+            for sc in scenes:
+                sc.sync_async()
         assert L.srpGpuSynchronize() == 0
         for fb, w in zip(fbs, want):
             c, d, st = srp_gb300.framebuffer_arrays(fb)
@@ -277,6 +285,19 @@ def test_overlapped_passes_match_serial_passes(built_library):
             for i, (a, b) in enumerate(zip(got, want)):
                 for x, y in zip(a, b):
                     assert np.array_equal(x, y), i
+        # gathered downloads: one kernel per pass, each after its own pass,
+        # into host arrays scribbled over first
+        for fb in fbs:
+            v = ctypes.cast(fb, ctypes.POINTER(srp_gb300.FramebufferView)).contents
+            ctypes.memset(v.color, 0xAB, 9 * v.size)
+        srp_gb300.prepare_batch(scenes, fbs)
+        srp_gb300.render_batch(scenes, fbs)
+        srp_gb300.sync_batch(fbs)
+        assert L.srpGpuSynchronize() == 0
+        for i, (fb, b) in enumerate(zip(fbs, want)):
+            c, d, st = srp_gb300.framebuffer_arrays(fb)
+            for x, y in zip((c, d.view(np.uint32), st), b):
+                assert np.array_equal(x, y), i
     finally:
         L.srpGpuSetDrawOverlap(1)
         for sc in scenes:
