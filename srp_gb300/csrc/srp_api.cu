@@ -100,6 +100,10 @@ struct DrawSet {
 	/* the big-primitive list: written by setup, read by the binning and by
 	 * the lambda tables, which run on another stream than the next front */
 	DeviceBuffer big;
+	/* used by the front stages only, which run on the set's own front
+	 * stream: the next draw's front (other set) runs beside this one's */
+	DeviceBuffer clip, vset0, vset1, codes, lookback, hist, partials, minmax, clipSlot, clipPolys;
+	cudaStream_t front = nullptr;
 	DeviceBuffer keys, vals, keys2, vals2;
 	/* multi-draw passes: descriptors, prefix sums, primitive bases, winners */
 	DeviceBuffer passDesc, passPrefix, passPrimPrefix, passWinner;
@@ -118,9 +122,9 @@ struct Lib {
 	/* heavy-tile resolve runs here, beside the light tiles on `stream` */
 	cudaStream_t auxStream = nullptr;
 	cudaEvent_t forkEvent = nullptr, joinEvent = nullptr;
-	/* a draw's vertex, setup and binning run on frontStream, its resolve and
-	 * shading on `stream`, so that the next draw's front overlaps them */
-	cudaStream_t frontStream = nullptr;
+	/* a draw's vertex, setup and binning run on its scratch set's front
+	 * stream, so that the next draw's front (other set) runs beside them and
+	 * beside this draw's resolve and shading */
 	/* with overlap, a single draw's lambda tables and resolve run on
 	 * resolveStream and its shading on `stream`: draw N+1's resolve then runs
 	 * beside draw N's shading (the resolve never reads colour, the shading
@@ -134,7 +138,7 @@ struct Lib {
 	 * resolves nor the shading wait for uploads of later draws. A stage that
 	 * reads a buffer waits for the buffer's upload event. Before an upload
 	 * the copy stream waits for the draws queued since it last did
-	 * (frontReads: on the front stream, streamReads: on `stream`). */
+	 * (frontReads: on the sets' front streams, streamReads: on `stream`). */
 	cudaStream_t copyStream = nullptr;
 	cudaEvent_t copyGateFront = nullptr, copyGateStream = nullptr;
 	bool frontReads = false, streamReads = false;
@@ -166,8 +170,7 @@ struct Lib {
 	SRPGpuFramebufferMode fbMode = SRP_GPU_FB_COHERENT;
 	Registry reg;
 	/* scratch pools, grown on demand */
-	/* used by the front stages only (and by multi-draw passes) */
-	DeviceBuffer clip, vset0, vset1, codes, lookback, hist, partials, minmax, clipSlot, clipPolys;
+
 	DeviceBuffer fillTargets;   /* srpGpuFramebufferFillBatch */
 	DrawSet sets[2];            /* alternating between consecutive single draws */
 	int setNext = 0;
@@ -195,6 +198,12 @@ struct Lib {
 
 Lib g;
 
+static void syncFronts()
+{
+	for (DrawSet& S : g.sets)
+		if (S.front) cudaStreamSynchronize(S.front);
+}
+
 bool ensureInit(const char* fn)
 {
 	if (g.init) return true;
@@ -205,7 +214,8 @@ bool ensureInit(const char* fn)
 	if (!cudaOk(cudaStreamCreateWithPriority(&g.auxStream, cudaStreamNonBlocking, hiPri), fn, "cudaStreamCreate") ||
 	    !cudaOk(cudaEventCreateWithFlags(&g.forkEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 	    !cudaOk(cudaEventCreateWithFlags(&g.joinEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
-	    !cudaOk(cudaStreamCreateWithFlags(&g.frontStream, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
+	    !cudaOk(cudaStreamCreateWithFlags(&g.sets[0].front, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
+	    !cudaOk(cudaStreamCreateWithFlags(&g.sets[1].front, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
 	    !cudaOk(cudaStreamCreateWithFlags(&g.resolveStream, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
 	    !cudaOk(cudaEventCreateWithFlags(&g.rsEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 	    !cudaOk(cudaStreamCreateWithFlags(&g.copyStream, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
@@ -234,7 +244,8 @@ bool ensureInit(const char* fn)
 		memset(S.hostCtr, 0, sizeof(DeviceCounters));
 		cudaMemset(S.ctr.ptr, 0, sizeof(DeviceCounters));
 	}
-	if (!g.minmax.reserve(16, fn)) return false;
+	for (DrawSet& S : g.sets)
+		if (!S.minmax.reserve(16, fn)) return false;
 	g.init = true;
 	return true;
 }
@@ -536,8 +547,10 @@ static void markUpload(cudaEvent_t& ready, bool& readyOwned, bool& pending, unsi
 static cudaStream_t copyStreamReady()
 {
 	if (g.frontReads) {
-		cudaEventRecord(g.copyGateFront, g.frontStream);
-		cudaStreamWaitEvent(g.copyStream, g.copyGateFront, 0);
+		for (DrawSet& S : g.sets) {
+			cudaEventRecord(g.copyGateFront, S.front);
+			cudaStreamWaitEvent(g.copyStream, g.copyGateFront, 0);
+		}
 		g.frontReads = false;
 	}
 	if (g.streamReads) {
@@ -1033,7 +1046,7 @@ void srpFreeFramebuffer(SRPFramebuffer* fb)
 {
 	if (!fb) return;
 	if (g.init) {
-		cudaStreamSynchronize(g.frontStream);
+		syncFronts();
 		cudaStreamSynchronize(g.resolveStream);
 		cudaStreamSynchronize(g.downloadStream);  /* into the host arrays freed below */
 	}
@@ -1462,7 +1475,7 @@ static uint32_t bitsFor(uint32_t n)
  * returns the fragments counted by all draws. */
 static unsigned long long readCounters()
 {
-	cudaStreamSynchronize(g.frontStream);
+	syncFronts();
 	cudaStreamSynchronize(g.resolveStream);
 	for (DrawSet& S : g.sets)
 		cudaMemcpyAsync(S.hostCtr, S.ctr.ptr, sizeof(DeviceCounters), cudaMemcpyDeviceToHost, g.stream);
@@ -1500,7 +1513,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 	/* this draw's scratch set and front stream */
 	DrawSet& S = g.sets[g.setNext];
 	g.setNext ^= 1;
-	const cudaStream_t fs = (g.overlap && !g.profiling) ? g.frontStream : g.stream;
+	const cudaStream_t fs = (g.overlap && !g.profiling) ? S.front : g.stream;
 	/* state snapshot */
 	DrawState& st = P.st;
 	st.W = (int) fb->width; st.H = (int) fb->height;
@@ -1566,7 +1579,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			return;
 		}
 	}
-	P.minmax = g.minmax.as<unsigned long long>();
+	P.minmax = S.minmax.as<unsigned long long>();
 	P.ctr = S.ctr.as<DeviceCounters>();
 	P.color = fx->color;
 	P.depth = fx->depth;
@@ -1591,16 +1604,16 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		const uint32_t rows = (uint32_t) vb->nVertices + g.clipRows;
 		const size_t nw = (size_t) std::max(P.L.nWords, 1);
 		const uint32_t blocks = (uint32_t) ((nIn + kSetupThreads - 1) / kSetupThreads);
-		bool ok = g.clip.reserve((size_t) rows * 16, FN) && S.vary.reserve((size_t) rows * nw * 4, FN) &&
-		          g.vset0.reserve((size_t) vb->nVertices * 16 + 16, FN) && g.vset1.reserve((size_t) vb->nVertices * 16 + 16, FN) &&
-		          g.codes.reserve((size_t) vb->nVertices + 16, FN) &&
-		          g.lookback.reserve((size_t) std::max(blocks, 1u) * 8, FN) &&
+		bool ok = S.clip.reserve((size_t) rows * 16, FN) && S.vary.reserve((size_t) rows * nw * 4, FN) &&
+		          S.vset0.reserve((size_t) vb->nVertices * 16 + 16, FN) && S.vset1.reserve((size_t) vb->nVertices * 16 + 16, FN) &&
+		          S.codes.reserve((size_t) vb->nVertices + 16, FN) &&
+		          S.lookback.reserve((size_t) std::max(blocks, 1u) * 8, FN) &&
 		          S.keys.reserve((size_t) entryCap * 4, FN) && S.vals.reserve((size_t) entryCap * 4, FN) &&
 		          S.keys2.reserve((size_t) entryCap * 4, FN) && S.vals2.reserve((size_t) entryCap * 4, FN) &&
-		          g.hist.reserve(sortHistWords(entryCap) * 4, FN) && g.partials.reserve(sortPartialWords(entryCap) * 4 + 64, FN) &&
+		          S.hist.reserve(sortHistWords(entryCap) * 4, FN) && S.partials.reserve(sortPartialWords(entryCap) * 4 + 64, FN) &&
 		          S.big.reserve((size_t) g.bigCap * 16, FN) && S.table.reserve((size_t) g.tableCap * 4, FN) &&
-		          g.clipSlot.reserve((size_t) nIn * 4 + 4, FN) &&
-		          g.clipPolys.reserve((size_t) g.clipPolyCap * (1 + kMaxPoly) * 4, FN) &&
+		          S.clipSlot.reserve((size_t) nIn * 4 + 4, FN) &&
+		          S.clipPolys.reserve((size_t) g.clipPolyCap * (1 + kMaxPoly) * 4, FN) &&
 		          S.tileStart.reserve((size_t) (numTiles + 1) * 4, FN) && S.tileEnd.reserve((size_t) (numTiles + 1) * 4, FN) &&
 		          S.winner.reserve(fb->size * 4 + 4, FN) && S.heavy.reserve((size_t) (numTiles + 1) * 4, FN);
 		if (kind == kKindTri) ok = ok && S.triR.reserve((size_t) primCap * sizeof(TriRaster), FN) &&
@@ -1609,10 +1622,10 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		else ok = ok && S.lines.reserve((size_t) primCap * sizeof(LineRec), FN) &&
 		          S.frags.reserve((size_t) entryCap * sizeof(LineFrag), FN);
 		if (!ok) return;
-		P.clip = g.clip.as<float4>();
-		P.vset0 = g.vset0.as<float4>();
-		P.vset1 = g.vset1.as<float4>();
-		P.codes = g.codes.as<uint8_t>();
+		P.clip = S.clip.as<float4>();
+		P.vset0 = S.vset0.as<float4>();
+		P.vset1 = S.vset1.as<float4>();
+		P.codes = S.codes.as<uint8_t>();
 		P.vary = S.vary.as<uint32_t>();
 		P.clipBase = (uint32_t) vb->nVertices;
 		P.clipCap = g.clipRows;
@@ -1629,11 +1642,11 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		P.bigJobs = S.big.as<uint4>();
 		P.bigCap = g.bigCap;
 		P.table = S.table.as<float>();
-		P.clipSlot = g.clipSlot.as<uint32_t>();
-		P.clipPolys = g.clipPolys.as<uint32_t>();
+		P.clipSlot = S.clipSlot.as<uint32_t>();
+		P.clipPolys = S.clipPolys.as<uint32_t>();
 		P.clipPolyCap = g.clipPolyCap;
 		P.tableCap = g.tableCap;
-		P.lookback = g.lookback.as<unsigned long long>();
+		P.lookback = S.lookback.as<unsigned long long>();
 		P.tileStart = S.tileStart.as<uint32_t>();
 		P.tileEnd = S.tileEnd.as<uint32_t>();
 		P.winner = S.winner.as<int32_t>();
@@ -1668,8 +1681,8 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			stageBegin();
 			if (kind == kKindLineFrag) launchLineFrags(P, fs);
 			else launchBigEntries(P, g.bigJobsSeen[kind], fs);
-			sortEntries(P, keyBits, S.keys2.as<uint32_t>(), S.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
-			            g.partials.as<uint32_t>(), &sk, &sv, fs);
+			sortEntries(P, keyBits, S.keys2.as<uint32_t>(), S.vals2.as<uint32_t>(), S.hist.as<uint32_t>(),
+			            S.partials.as<uint32_t>(), &sk, &sv, fs);
 			cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, fs);
 			cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, fs);
 			launchTileRanges(P, sk, numTiles, fs);
@@ -1992,13 +2005,13 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	P.primPrefix = S.passPrimPrefix.as<uint32_t>();
 	P.nIn = (int) nIn;
 	P.nVertices = vRows;
-	P.minmax = g.minmax.as<unsigned long long>();
+	P.minmax = S.minmax.as<unsigned long long>();
 	P.ctr = S.ctr.as<DeviceCounters>();
 	if (g.fbMode == SRP_GPU_FB_COHERENT)
 		for (size_t k = 0; k < n; ++k) fbUpload(draws[idx[k]].framebuffer, fbFind(draws[idx[k]].framebuffer));
 
 	const bool learned = learnedPrepare(P, kKindTri, false, (uint32_t) n, g.stream);
-	const cudaStream_t fs = (g.overlap && !g.profiling && !learned) ? g.frontStream : g.stream;
+	const cudaStream_t fs = (g.overlap && !g.profiling && !learned) ? S.front : g.stream;
 	/* the pass's resolve runs beside the previous pass's shading */
 	const cudaStream_t rs = fs != g.stream ? g.resolveStream : g.stream;
 	/* the front waits for the last draw that used this set (on the library's
@@ -2033,25 +2046,25 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		const unsigned long long rows = (unsigned long long) vRows + g.clipRows;
 		const size_t nw = (size_t) std::max(P.L.nWords, 1);
 		const uint32_t blocks = (nIn + kSetupThreads - 1) / kSetupThreads;
-		bool ok = g.clip.reserve(rows * 16, FN) && S.vary.reserve(rows * nw * 4, FN) &&
-		          g.vset0.reserve((size_t) vRows * 16 + 16, FN) && g.vset1.reserve((size_t) vRows * 16 + 16, FN) &&
-		          g.codes.reserve((size_t) vRows + 16, FN) &&
-		          g.lookback.reserve((size_t) std::max(blocks, 1u) * 8, FN) &&
+		bool ok = S.clip.reserve(rows * 16, FN) && S.vary.reserve(rows * nw * 4, FN) &&
+		          S.vset0.reserve((size_t) vRows * 16 + 16, FN) && S.vset1.reserve((size_t) vRows * 16 + 16, FN) &&
+		          S.codes.reserve((size_t) vRows + 16, FN) &&
+		          S.lookback.reserve((size_t) std::max(blocks, 1u) * 8, FN) &&
 		          S.keys.reserve((size_t) entryCap * 4, FN) && S.vals.reserve((size_t) entryCap * 4, FN) &&
 		          S.keys2.reserve((size_t) entryCap * 4, FN) && S.vals2.reserve((size_t) entryCap * 4, FN) &&
-		          g.hist.reserve(sortHistWords(entryCap) * 4, FN) && g.partials.reserve(sortPartialWords(entryCap) * 4 + 64, FN) &&
+		          S.hist.reserve(sortHistWords(entryCap) * 4, FN) && S.partials.reserve(sortPartialWords(entryCap) * 4 + 64, FN) &&
 		          S.big.reserve((size_t) g.bigCap * 16, FN) && S.table.reserve((size_t) g.tableCap * 4, FN) &&
-		          g.clipSlot.reserve((size_t) nIn * 4 + 4, FN) &&
-		          g.clipPolys.reserve((size_t) g.clipPolyCap * (1 + kMaxPoly) * 4, FN) &&
+		          S.clipSlot.reserve((size_t) nIn * 4 + 4, FN) &&
+		          S.clipPolys.reserve((size_t) g.clipPolyCap * (1 + kMaxPoly) * 4, FN) &&
 		          S.triR.reserve((size_t) primCap * sizeof(TriRaster), FN) &&
 		          S.triA.reserve((size_t) primCap * sizeof(TriAttr), FN) &&
 		          S.tileStart.reserve((size_t) (numTiles + 1) * 4, FN) && S.tileEnd.reserve((size_t) (numTiles + 1) * 4, FN) &&
 		          S.heavy.reserve((size_t) (numTiles + 1) * 4, FN);
 		if (!ok) return false;
-		P.clip = g.clip.as<float4>();
-		P.vset0 = g.vset0.as<float4>();
-		P.vset1 = g.vset1.as<float4>();
-		P.codes = g.codes.as<uint8_t>();
+		P.clip = S.clip.as<float4>();
+		P.vset0 = S.vset0.as<float4>();
+		P.vset1 = S.vset1.as<float4>();
+		P.codes = S.codes.as<uint8_t>();
 		P.vary = S.vary.as<uint32_t>();
 		P.clipBase = vRows;
 		P.clipCap = g.clipRows;
@@ -2065,10 +2078,10 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		P.bigCap = g.bigCap;
 		P.table = S.table.as<float>();
 		P.tableCap = g.tableCap;
-		P.clipSlot = g.clipSlot.as<uint32_t>();
-		P.clipPolys = g.clipPolys.as<uint32_t>();
+		P.clipSlot = S.clipSlot.as<uint32_t>();
+		P.clipPolys = S.clipPolys.as<uint32_t>();
 		P.clipPolyCap = g.clipPolyCap;
-		P.lookback = g.lookback.as<unsigned long long>();
+		P.lookback = S.lookback.as<unsigned long long>();
 		P.tileStart = S.tileStart.as<uint32_t>();
 		P.tileEnd = S.tileEnd.as<uint32_t>();
 
@@ -2092,8 +2105,8 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 			stageBegin();
 			launchLambdaTablesMulti(P, g.bigJobsSeen[kKindTri], fs);
 			launchBigEntriesMulti(P, g.bigJobsSeen[kKindTri], fs);
-			sortEntries(P, keyBits, S.keys2.as<uint32_t>(), S.vals2.as<uint32_t>(), g.hist.as<uint32_t>(),
-			            g.partials.as<uint32_t>(), &sk, &sv, fs);
+			sortEntries(P, keyBits, S.keys2.as<uint32_t>(), S.vals2.as<uint32_t>(), S.hist.as<uint32_t>(),
+			            S.partials.as<uint32_t>(), &sk, &sv, fs);
 			cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, fs);
 			cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, fs);
 			launchTileRanges(P, sk, numTiles, fs);
@@ -2257,7 +2270,7 @@ void srpGpuSetStream(void* stream)
 	cudaStreamSynchronize(g.downloadStream);
 	g.downloadsPending = false;
 	cudaStreamSynchronize(g.copyStream);
-	cudaStreamSynchronize(g.frontStream);
+	syncFronts();
 	cudaStreamSynchronize(g.resolveStream);
 	cudaStreamSynchronize(g.stream);
 	g.stream = stream ? (cudaStream_t) stream : g.ownStream;
@@ -2271,7 +2284,7 @@ int srpGpuSynchronize(void)
 	if (!g.init) return 0;
 	cudaStreamSynchronize(g.downloadStream);
 	cudaStreamSynchronize(g.copyStream);
-	cudaStreamSynchronize(g.frontStream);
+	syncFronts();
 	cudaStreamSynchronize(g.resolveStream);
 	return cudaOk(cudaStreamSynchronize(g.stream), "srpGpuSynchronize", "kernel execution") ? 0 : 1;
 }
@@ -2288,7 +2301,7 @@ void srpGpuGetStats(SRPGpuStats* s)
 void srpGpuResetStats(void)
 {
 	if (!g.init) return;
-	cudaStreamSynchronize(g.frontStream);
+	syncFronts();
 	cudaStreamSynchronize(g.resolveStream);
 	cudaStreamSynchronize(g.stream);
 	for (DrawSet& S : g.sets) cudaMemset(S.ctr.ptr, 0, sizeof(DeviceCounters));
@@ -2303,7 +2316,7 @@ void srpGpuSetDrawGraphs(int enable) { g.graphs = enable != 0; }
 void srpGpuSetDrawOverlap(int enable)
 {
 	if (!ensureInit("srpGpuSetDrawOverlap")) return;
-	cudaStreamSynchronize(g.frontStream);
+	syncFronts();
 	cudaStreamSynchronize(g.resolveStream);
 	g.overlap = enable != 0;
 }

@@ -248,6 +248,10 @@ def test_async_transfers_and_fill_batch_match_the_synchronous_path(built_library
         else:
             for sc in scenes:
                 sc.sync_async()
+        # framebuffer work queued right behind the downloads waits for them
+        for fb in fbs:
+            S.srpGpuFramebufferFill(ctypes.c_void_p(fb), ctypes.c_uint32(0x12345678), ctypes.c_float(0.25),
+                                    ctypes.c_uint8(7), 7)
         assert L.srpGpuSynchronize() == 0
         for fb, w in zip(fbs, want):
             c, d, st = srp_gb300.framebuffer_arrays(fb)
