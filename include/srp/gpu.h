@@ -329,13 +329,15 @@ typedef struct SRPGpuProfile
 
 /** Replay repeated draws from CUDA graphs (on by default). A draw's work
  *  after its host-side preparation is captured once per distinct set of
- *  draw parameters and launch sizes, and relaunched as two graphs when the
- *  same draw comes again (the host reads the draw's counters between them).
+ *  draw parameters and launch sizes, and relaunched as graphs, one per
+ *  sequence of the draw on each of its streams, when the same draw comes
+ *  again (the host reads the draw's counters between them).
  *  Stage profiling launches directly. */
 void srpGpuSetDrawGraphs(int enable);
 /** Overlap of consecutive draws (default on): a draw's vertex, setup and
- *  binning stages run on a second stream of the library, beside the previous
- *  draw's resolve and shading, and its resolve on a third, beside the
+ *  binning stages run on a front stream of the library (one per scratch set,
+ *  the sets alternating between draws), beside the previous draw's front,
+ *  resolve and shading, and its resolve on another stream, beside the
  *  previous draw's shading. Resolves stay in submission order among
  *  themselves, and so do shadings, which run on the library's stream.
  *  Results are identical either way. */
