@@ -147,15 +147,17 @@ struct Lib {
 	 * the draw or pass that last wrote the framebuffer (one of writeEvents,
 	 * recorded on `stream` after its shading, numbered by writeSeq), so that
 	 * a batch's first framebuffers come back while later passes render.
-	 * downloadsPending: framebuffer work queued later must first wait for
-	 * those copies (fbAfterDownloads). */
+	 * Each download is marked by one of downloadEvents (numbered by
+	 * downloadSeq); work queued later on `stream` that touches the same
+	 * framebuffer first waits for its download (fbAfterDownloads), work on
+	 * other framebuffers does not. streamDownloadSeq: the downloads `stream`
+	 * has waited for, in order. */
 	static constexpr int kWriteEvents = 64;
 	cudaStream_t downloadStream = nullptr;
-	cudaEvent_t downloadEvent = nullptr;
 	cudaEvent_t writeEvents[kWriteEvents] = {};
-	int writeNext = 0;
-	unsigned long long writeSeq = 0, downloadWaitedSeq = 0;
-	bool downloadsPending = false;
+	cudaEvent_t downloadEvents[kWriteEvents] = {};
+	int writeNext = 0, downloadNext = 0;
+	unsigned long long writeSeq = 0, downloadWaitedSeq = 0, downloadSeq = 0, streamDownloadSeq = 0;
 	/* gathered transfers (the Batch calls): one kernel per group of buffers,
 	 * item lists staged in gatherUp / gatherDown; a group's uploads end at
 	 * one of gatherEvents, which its buffers borrow as their upload event */
@@ -221,9 +223,10 @@ bool ensureInit(const char* fn)
 	    !cudaOk(cudaStreamCreateWithFlags(&g.copyStream, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
 	    !cudaOk(cudaEventCreateWithFlags(&g.copyGateFront, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 	    !cudaOk(cudaEventCreateWithFlags(&g.copyGateStream, cudaEventDisableTiming), fn, "cudaEventCreate") ||
-	    !cudaOk(cudaStreamCreateWithFlags(&g.downloadStream, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
-	    !cudaOk(cudaEventCreateWithFlags(&g.downloadEvent, cudaEventDisableTiming), fn, "cudaEventCreate")) return false;
+	    !cudaOk(cudaStreamCreateWithFlags(&g.downloadStream, cudaStreamNonBlocking), fn, "cudaStreamCreate")) return false;
 	for (cudaEvent_t& e : g.writeEvents)
+		if (!cudaOk(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), fn, "cudaEventCreate")) return false;
+	for (cudaEvent_t& e : g.downloadEvents)
 		if (!cudaOk(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), fn, "cudaEventCreate")) return false;
 	for (cudaEvent_t& e : g.gatherEvents)
 		if (!cudaOk(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), fn, "cudaEventCreate")) return false;
@@ -885,6 +888,9 @@ struct FbExtra {
 	 * (null after any other write, whose end the library's stream marks) */
 	cudaEvent_t lastWrite = nullptr;
 	unsigned long long lastWriteSeq = 0;
+	/* its last download on the download stream: the event and number */
+	cudaEvent_t download = nullptr;
+	unsigned long long downloadSeq = 0;
 	/* the host block of the planes as made by srpNewFramebuffer, and the
 	 * address by which the device reaches it (null if it cannot) */
 	void* hostBase = nullptr;
@@ -946,23 +952,34 @@ static bool fbContiguous(const SRPFramebuffer* fb)
 	       fb->stencil == (unsigned char*) fb->color + 8 * n;
 }
 
-/* Framebuffer work about to be queued on the library's stream comes after
- * the copies queued on the download stream, which read the planes into the
- * host arrays; the resolve stream follows through rsDirty. */
-static void fbAfterDownloads()
+/* Work on framebuffer x about to be queued on the library's stream comes
+ * after x's download on the download stream, which reads the planes into
+ * the host arrays; the resolve stream follows through rsDirty. Downloads
+ * complete in order, so waiting for one covers every earlier one. */
+static void fbAfterDownloads(FbExtra* x)
 {
-	if (!g.downloadsPending) return;
-	cudaEventRecord(g.downloadEvent, g.downloadStream);
-	cudaStreamWaitEvent(g.stream, g.downloadEvent, 0);
-	g.downloadsPending = false;
+	if (x->downloadSeq <= g.streamDownloadSeq) return;
+	cudaStreamWaitEvent(g.stream, x->download, 0);
+	g.streamDownloadSeq = x->downloadSeq;
 	g.rsDirty = true;
+}
+
+/* Marks the downloads just queued on the download stream; returns the event
+ * and its number. */
+static cudaEvent_t downloadMark(unsigned long long& seq)
+{
+	cudaEvent_t e = g.downloadEvents[g.downloadNext];
+	g.downloadNext = (g.downloadNext + 1) % Lib::kWriteEvents;
+	cudaEventRecord(e, g.downloadStream);
+	seq = ++g.downloadSeq;
+	return e;
 }
 
 /* A write other than a draw's: later downloads of the framebuffer wait for
  * the library's stream. */
 static void fbOtherWrite(FbExtra* x)
 {
-	fbAfterDownloads();
+	fbAfterDownloads(x);
 	x->lastWrite = nullptr;
 }
 
@@ -992,7 +1009,7 @@ static void fbUpload(const SRPFramebuffer* fb, FbExtra* x)
 
 static void fbDownloadAsync(const SRPFramebuffer* fb, FbExtra* x)
 {
-	fbAfterDownloads();  /* the same host arrays */
+	fbAfterDownloads(x);  /* the same host arrays */
 	g.rsDirty = true;
 	if (fbContiguous(fb)) {
 		cudaMemcpyAsync(fb->color, x->color, 9 * fb->size, cudaMemcpyDeviceToHost, g.stream);
@@ -1123,7 +1140,7 @@ void srpGpuFramebufferSyncAsync(const SRPFramebuffer* fb)
 		g.downloadWaitedSeq = x->lastWriteSeq;
 	}
 	cudaMemcpyAsync(fb->color, x->color, 9 * fb->size, cudaMemcpyDeviceToHost, g.downloadStream);
-	g.downloadsPending = true;
+	x->download = downloadMark(x->downloadSeq);
 }
 
 void srpGpuFramebufferSyncBatchAsync(const SRPFramebuffer* const* fbs, size_t n)
@@ -1137,7 +1154,9 @@ void srpGpuFramebufferSyncBatchAsync(const SRPFramebuffer* const* fbs, size_t n)
 	/* runs of framebuffers last written by the same draw or pass: one kernel
 	 * each on the download stream, after that draw or pass */
 	std::vector<GatherItem> items;
+	std::vector<FbExtra*> owners;
 	items.reserve(n);
+	owners.reserve(n);
 	size_t first = 0;
 	cudaEvent_t runEvent = nullptr;
 	unsigned long long runSeq = 0;
@@ -1148,7 +1167,12 @@ void srpGpuFramebufferSyncBatchAsync(const SRPFramebuffer* const* fbs, size_t n)
 				g.downloadWaitedSeq = runSeq;
 			}
 			gatherLaunch(items, first, items.size(), g.gatherDown, first, g.downloadStream, FN);
-			g.downloadsPending = true;
+			unsigned long long seq = 0;
+			const cudaEvent_t e = downloadMark(seq);
+			for (size_t k = first; k < items.size(); ++k) {
+				owners[k]->download = e;
+				owners[k]->downloadSeq = seq;
+			}
 		}
 		first = items.size();
 	};
@@ -1166,6 +1190,7 @@ void srpGpuFramebufferSyncBatchAsync(const SRPFramebuffer* const* fbs, size_t n)
 			runSeq = x->lastWriteSeq;
 		}
 		items.push_back({ (const unsigned char*) x->color, (unsigned char*) x->hostDev, 9ull * fb->size, 0 });
+		owners.push_back(x);
 	}
 	flush();
 }
@@ -1492,9 +1517,9 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 	SRPVertexBuffer* vb = (SRPVertexBuffer*) vbc;
 	FbExtra* fx = fbFind(fb);
 	if (!fx) { SRP_ERROR(FN, "Framebuffer was not created by srpNewFramebuffer"); return; }
-	/* after downloads in flight; until the draw has been queued in full,
+	/* after its download in flight; until the draw has been queued in full,
 	 * downloads of this framebuffer go back to the library's stream */
-	fbAfterDownloads();
+	fbAfterDownloads(fx);
 	fx->lastWrite = nullptr;
 	const int vsId = lookupVS((void*) sp->vs->shader);
 	const int fsId = lookupFS((void*) sp->fs->shader);
@@ -1902,11 +1927,13 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	 * stream: such a pass runs there whole) */
 	DrawSet& S = g.sets[g.setNext];
 	g.setNext ^= 1;
-	/* after downloads in flight; until the pass has been queued in full,
-	 * downloads of its framebuffers go back to the library's stream */
-	fbAfterDownloads();
+	/* after their downloads in flight; until the pass has been queued in
+	 * full, downloads of its framebuffers go back to the library's stream */
 	for (size_t k = 0; k < n; ++k)
-		if (FbExtra* x = fbFind(draws[idx[k]].framebuffer)) x->lastWrite = nullptr;
+		if (FbExtra* x = fbFind(draws[idx[k]].framebuffer)) {
+			fbAfterDownloads(x);
+			x->lastWrite = nullptr;
+		}
 	if (!buildLayout(sp0->vs, P.L)) return true;
 	DrawState& st = P.st;
 	st.frontFaceCW = srpContext.raster.frontFace == SRP_WINDING_CW;
@@ -2268,7 +2295,6 @@ void srpGpuSetStream(void* stream)
 {
 	if (!ensureInit("srpGpuSetStream")) return;
 	cudaStreamSynchronize(g.downloadStream);
-	g.downloadsPending = false;
 	cudaStreamSynchronize(g.copyStream);
 	syncFronts();
 	cudaStreamSynchronize(g.resolveStream);
