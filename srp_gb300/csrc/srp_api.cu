@@ -830,10 +830,14 @@ void srpGpuVertexBufferCopyDataBatchAsync(SRPVertexBuffer* const* buffers, const
 		for (size_t i = 0; i < n; ++i) srpVertexBufferCopyData(buffers[i], strides[i], nBytes[i], data[i]);
 		return;
 	}
+	/* a buffer given more than once keeps its last copy, as n single calls
+	 * would leave it */
 	std::vector<UploadTarget> t;
 	t.reserve(n);
-	for (size_t i = 0; i < n; ++i) {
+	std::unordered_set<const SRPVertexBuffer*> seen;
+	for (size_t i = n; i-- > 0;) {
 		SRPVertexBuffer* b = buffers[i];
+		if (!seen.insert(b).second) continue;
 		const void* src = nBytes[i] ? deviceView(data[i]) : nullptr;
 		if (!src || !b->dev.reserve(nBytes[i] + 16, FN)) {
 			srpGpuVertexBufferCopyDataAsync(b, strides[i], nBytes[i], data[i]);
@@ -844,6 +848,7 @@ void srpGpuVertexBufferCopyDataBatchAsync(SRPVertexBuffer* const* buffers, const
 		b->nBytes = nBytes[i];
 		t.push_back({ &b->dev, src, nBytes[i], &b->ready, &b->readyOwned, &b->pending, &b->seq, &b->dirty });
 	}
+	std::reverse(t.begin(), t.end());
 	gatherUploads(t, FN);
 }
 
@@ -858,8 +863,10 @@ void srpGpuIndexBufferCopyDataBatchAsync(SRPIndexBuffer* const* buffers, const S
 	}
 	std::vector<UploadTarget> t;
 	t.reserve(n);
-	for (size_t i = 0; i < n; ++i) {
+	std::unordered_set<const SRPIndexBuffer*> seen;
+	for (size_t i = n; i-- > 0;) {
 		SRPIndexBuffer* b = buffers[i];
+		if (!seen.insert(b).second) continue;
 		const size_t elem = indexTypeSize(types[i]);
 		const void* src = nBytes[i] && elem ? deviceView(data[i]) : nullptr;
 		if (!src || !b->dev.reserve(nBytes[i] + 16, FN)) {
@@ -872,6 +879,7 @@ void srpGpuIndexBufferCopyDataBatchAsync(SRPIndexBuffer* const* buffers, const S
 		b->nBytes = nBytes[i];
 		t.push_back({ &b->dev, src, nBytes[i], &b->ready, &b->readyOwned, &b->pending, &b->seq, &b->dirty });
 	}
+	std::reverse(t.begin(), t.end());
 	gatherUploads(t, FN);
 }
 

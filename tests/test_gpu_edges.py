@@ -153,3 +153,31 @@ def test_framebuffer_work_between_overlapped_draws_keeps_its_place(api):
     assert not np.array_equal(mid0[0], end0[0])
     # the fill took effect: pixels the second draw left alone hold its depth
     assert np.count_nonzero(mid0[1] == np.float32(0.25)) > 0
+
+
+def test_batch_upload_of_a_repeated_buffer_keeps_the_last_copy(api):
+    """srpGpuVertexBufferCopyDataBatchAsync given one buffer twice leaves it
+    as two single calls would: holding the second copy."""
+    L = api.L
+    vp = ctypes.c_void_p
+    L.srpGpuVertexBufferCopyDataBatchAsync.argtypes = [vp, vp, vp, vp, ctypes.c_size_t]
+    rng = np.random.default_rng(14)
+    a = np.ascontiguousarray(triangle_soup(rng, 800), dtype=np.float32)
+    b = np.ascontiguousarray(triangle_soup(rng, 500), dtype=np.float32)
+    vb = api.vertex_buffer(a)
+    ref_vb = api.vertex_buffer(b)
+    bufs = (vp * 2)(vb, vb)
+    strides = (ctypes.c_size_t * 2)(a.shape[1] * 4, b.shape[1] * 4)
+    sizes = (ctypes.c_size_t * 2)(a.nbytes, b.nbytes)
+    datas = (vp * 2)(a.ctypes.data, b.ctypes.data)
+    L.srpGpuVertexBufferCopyDataBatchAsync(ctypes.addressof(bufs), ctypes.addressof(strides), ctypes.addressof(sizes),
+                                           ctypes.addressof(datas), 2)
+    fb = api.framebuffer(256, 192)
+    ref = api.framebuffer(256, 192)
+    L.srpDrawVertexBuffer(vb, fb, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, b.shape[0])
+    L.srpDrawVertexBuffer(ref_vb, ref, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, b.shape[0])
+    got, want = api.planes(fb), api.planes(ref)
+    assert not api.errors(), api.errors()
+    assert_same(got, want, "repeated buffer in a batch upload")
+    assert int(np.count_nonzero(want[0])) > 100
+    assert L.srpGpuSynchronize() == 0
