@@ -79,3 +79,37 @@ def test_host_validation_reports_like_the_reference(built_library):
     assert any("drawBuffer" in m and "Unknown primitive type: 42" in m for m in msgs), msgs
     assert any("srpSizeofType" in m for m in msgs), msgs
     assert len(msgs) == 3, msgs
+
+
+NO_GPU_SCRIPT = r"""
+import ctypes, sys
+sys.path.insert(0, sys.argv[1])
+import srp_gb300 as s
+L = s.lib()
+msgs = []
+@s.MESSAGE_CALLBACK
+def cb(t, sev, fn, msg, user):
+    msgs.append((t, sev, fn.decode(), msg.decode()))
+ctx = ctypes.c_void_p.in_dll(L, "srpContext")
+L.srpNewContext.argtypes = [ctypes.c_void_p]
+L.srpNewContext(ctypes.addressof(ctx))
+L.srpSetMessageCallback(s.SRPMessageCallback(cb, None))
+L.srpNewFramebuffer.restype = ctypes.c_void_p
+L.srpNewFramebuffer.argtypes = [ctypes.c_size_t, ctypes.c_size_t]
+fb = L.srpNewFramebuffer(64, 48)
+print("FB", fb)
+for m in msgs:
+    print("MSG", m)
+"""
+
+
+def test_without_a_gpu_the_library_reports_instead_of_falling_back(built_library):
+    """No CPU fallback: where no GPU can be used, creating a framebuffer
+    reports the CUDA error through the message callback and returns NULL."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    out = subprocess.check_output([sys.executable, "-c", NO_GPU_SCRIPT, ROOT], cwd=ROOT).decode()
+    assert "FB None" in out, out
+    msgs = [l for l in out.splitlines() if l.startswith("MSG")]
+    assert any("srpNewFramebuffer" in m and "CUDA error" in m for m in msgs), msgs
