@@ -250,11 +250,17 @@ int srpGpuMlpGradients(SRPGpuMlp* mlp, const float* samples, size_t n, float* gr
  *
  *  The first call on a device looks up the array's address (with that device
  *  current; the lookup loads the part of the library's device image that
- *  holds the array) and keeps it for later calls. Make that first call before
- *  any stream capture begins. Vertex and index buffers must already be in
- *  device memory, as srpVertexBufferCopyData / srpIndexBufferCopyData leave
- *  them when a GPU is present. Outside a stream capture, the draw also waits
- *  for copies queued by the Async variants.
+ *  holds the array) and keeps it for later calls. No call may be made while
+ *  the library's stream is being captured into a CUDA graph: partway through
+ *  the draw the host waits for the counters of its setup stage, so such a
+ *  call is rejected (-1 and a message) before anything is queued. Vertex and
+ *  index buffers must already be in device memory, as
+ *  srpVertexBufferCopyData / srpIndexBufferCopyData leave them when a GPU is
+ *  present; the draw waits for copies queued by the Async variants.
+ *
+ *  Learned shading (srpGpuSetLearnedShading) and fragment capture
+ *  (srpGpuMlpCapture) do not apply to these draws: they always run the
+ *  program's own fragment shader, as if neither were set.
  *
  *  Limits. The parts of the scratch sized by the vertex buffer (about 64
  *  bytes and 4 per varying word per vertex), by the primitives (up to 96
@@ -263,7 +269,8 @@ int srpGpuMlpGradients(SRPGpuMlp* mlp, const float* samples, size_t n, float* gr
  *  the draw produces is checked once the setup stage has counted it: tile
  *  entries (about 16 bytes each, 32 for lines) in three quarters of what is
  *  left, barycentric tables of large triangles in the other quarter, at most
- *  16384 vertices created by clipping and 4096 triangles that need clipping.
+ *  16384 vertices created by clipping and 4096 triangles that need clipping
+ *  (whose extra triangles are counted in the primitive part).
  *  A draw beyond a limit is rejected: it returns -1, says which size was too
  *  large through the message callback and leaves the framebuffer unchanged.
  *

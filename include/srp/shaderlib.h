@@ -20,6 +20,11 @@
 #define SRP_STD_MAX_LIGHTS 16
 #define SRP_STD_MAX_PASS   16
 
+/** Packed mixed-type varying block read by srpFsMixed, at byte
+ *  4*varyingOffset: +0 int8, +1 double[2], +17 uint16, +19 float[2],
+ *  +27 int16, +29 uint64 (37 bytes, every member but the first unaligned). */
+#define SRP_MIXED_BLOCK_BYTES 37
+
 /** Uniform block read by all built-in shaders. Vertex layouts are described
  *  in 32-bit words: the position is always words 0..2 of the vertex. */
 typedef struct SRPStdUniform
@@ -39,8 +44,10 @@ typedef struct SRPStdUniform
 	float depthBias;
 	uint32_t nLights;
 	uint32_t marbleOctaves;
-	uint32_t passOffset;     /* srpVsTransform: first vertex word copied to varyings */
-	uint32_t passCount;      /* srpVsTransform: number of words copied (<= 16) */
+	uint32_t passOffset;     /* srpVsTransform: first vertex word copied to varyings;
+	                            srpVsBytes: first vertex byte (< 64) */
+	uint32_t passCount;      /* srpVsTransform: number of words copied (<= 16);
+	                            srpVsBytes: number of bytes copied (<= 64) */
 	uint32_t normalOffset;   /* srpVsWorld: vertex word offset of the normal */
 	uint32_t uvOffset;       /* srpVsWorld: vertex word offset of the uv */
 	uint32_t extraOffset;    /* srpVsWorld: first extra word appended to varyings */
@@ -56,6 +63,7 @@ typedef enum SRPGpuVertexShaderId
 	SRP_GPU_VS_NONE = 0,
 	SRP_GPU_VS_TRANSFORM = 1,  /* clip = P*(V*(M*pos)); varyings = passthrough words */
 	SRP_GPU_VS_WORLD = 2,      /* varyings = world pos, world normal, uv, extras */
+	SRP_GPU_VS_BYTES = 3,      /* clip as TRANSFORM; varyings = passCount raw vertex bytes from byte passOffset */
 	SRP_GPU_VS_COUNT
 } SRPGpuVertexShaderId;
 
@@ -72,6 +80,9 @@ typedef enum SRPGpuFragmentShaderId
 	SRP_GPU_FS_DEPTH_OVERWRITE = 8, /* colour from varyings, writes fragDepth (late Z) */
 	SRP_GPU_FS_FRAGCOORD = 9,       /* colour from fragCoord and frontFacing */
 	SRP_GPU_FS_FLAT_INT = 10,       /* palette colour from an int32 varying at word o */
+	SRP_GPU_FS_MIXED = 11,          /* colour from the packed mixed-type block at word o (srpFsMixed) */
+	SRP_GPU_FS_BYTE_PALETTE = 12,   /* 0 red, 1 green, 2 blue, else hashed: uint8 varying at byte 4*o */
+	SRP_GPU_FS_PRIMITIVE_MOD = 13,  /* ((id*97, id*57, id*23) mod 255) / 255 / colour[0] */
 	SRP_GPU_FS_COUNT
 } SRPGpuFragmentShaderId;
 
@@ -82,6 +93,7 @@ extern "C" {
 /* Host entry points of the built-in shaders. */
 void srpVsTransform(SRPVertexShaderIn* in, SRPVertexShaderOut* out);
 void srpVsWorld(SRPVertexShaderIn* in, SRPVertexShaderOut* out);
+void srpVsBytes(SRPVertexShaderIn* in, SRPVertexShaderOut* out);
 void srpFsVaryingColor(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out);
 void srpFsSolid(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out);
 void srpFsPrimitiveId(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out);
@@ -92,6 +104,9 @@ void srpFsMarble(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out);
 void srpFsDepthOverwrite(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out);
 void srpFsFragCoord(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out);
 void srpFsFlatInt(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out);
+void srpFsMixed(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out);
+void srpFsBytePalette(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out);
+void srpFsPrimitiveMod(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out);
 
 #ifdef __cplusplus
 }

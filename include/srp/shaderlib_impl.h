@@ -119,7 +119,71 @@ SRP_SHADER_FN void srpslVsWorld(SRPVertexShaderIn* in, SRPVertexShaderOut* out)
 			srpslStoreU(out->varyings, 8 + w, srpslLoadU(vtx, u->extraOffset + w));
 }
 
+/* Clip position as srpVsTransform; the varyings are `passCount` raw bytes of
+ * the vertex starting at byte `passOffset` (both clamped to 64), so that a
+ * program can hand any packed varying block (sub-word integers, doubles,
+ * unaligned members) straight from its vertex layout to the interpolator. */
+SRP_SHADER_FN void srpslVsBytes(SRPVertexShaderIn* in, SRPVertexShaderOut* out)
+{
+	const SRPStdUniform* u = (const SRPStdUniform*) in->uniform;
+	const unsigned char* vtx = (const unsigned char*) in->vertex;
+	float p[4] = { srpslLoadF(vtx, 0), srpslLoadF(vtx, 1), srpslLoadF(vtx, 2), 1.0f };
+	float a[4], b[4];
+	srpslMatVec(&u->model, p, a);
+	srpslMatVec(&u->view, a, b);
+	srpslMatVec(&u->projection, b, out->clipPosition);
+	const uint32_t off = u->passOffset < 64u ? u->passOffset : 64u;
+	const uint32_t n = u->passCount < 64u ? u->passCount : 64u;
+	memcpy((unsigned char*) out->varyings, vtx + off, n);
+}
+
 /* -------------------------------------------------------------- fragment */
+
+SRP_SHADER_FN void srpslFsMixed(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out)
+{
+	const SRPStdUniform* u = (const SRPStdUniform*) in->uniform;
+	const unsigned char* v = (const unsigned char*) in->varyings + 4u * u->varyingOffset;
+	int8_t a; double d[2]; uint16_t b; float f[2]; int16_t c; uint64_t e;
+	memcpy(&a, v, 1); memcpy(d, v + 1, 16); memcpy(&b, v + 17, 2);
+	memcpy(f, v + 19, 8); memcpy(&c, v + 27, 2); memcpy(&e, v + 29, 8);
+	const uint32_t k = ((uint32_t) (int32_t) a * 7u + (uint32_t) b * 13u + (uint32_t) (int32_t) c * 3u + (uint32_t) e) & 15u;
+	out->color[0] = (float) (d[0] - floor(d[0]));
+	out->color[1] = 0.25f + 0.5f * (f[0] - floorf(f[0]));
+	out->color[2] = 0.5f * (float) (d[1] - floor(d[1])) + 0.25f * (f[1] - floorf(f[1])) + (float) k * (0.25f / 15.0f);
+	out->color[3] = 1.0f;
+}
+
+/* Colour of a uint8 varying at byte 4*varyingOffset: 0 red, 1 green, 2 blue
+ * (the palette of the reference's flat-interpolation test scene), other
+ * values hashed. */
+SRP_SHADER_FN void srpslFsBytePalette(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out)
+{
+	const SRPStdUniform* u = (const SRPStdUniform*) in->uniform;
+	uint8_t k;
+	memcpy(&k, (const unsigned char*) in->varyings + 4u * u->varyingOffset, 1);
+	if (k < 3u) {
+		for (int i = 0; i < 3; ++i) out->color[i] = (uint32_t) i == k ? 1.0f : 0.0f;
+	} else {
+		out->color[0] = (float) ((k * 37u) & 255u) / 255.0f;
+		out->color[1] = (float) ((k * 101u) & 255u) / 255.0f;
+		out->color[2] = (float) ((k * 193u) & 255u) / 255.0f;
+	}
+	out->color[3] = 1.0f;
+}
+
+/* ((id*97, id*57, id*23) mod 255) / 255 / colour[0] in double, then rounded to
+ * float: the primitive-ID colouring of the reference's clipping, polygon-mode
+ * and primitive test scenes (colour[0] = 1, or 2 for the darker variant). */
+SRP_SHADER_FN void srpslFsPrimitiveMod(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out)
+{
+	const SRPStdUniform* u = (const SRPStdUniform*) in->uniform;
+	const uint32_t id = (uint32_t) in->primitiveID;
+	const double div = (double) u->color[0];
+	out->color[0] = (float) ((double) ((id * 97u) % 255u) / 255. / div);
+	out->color[1] = (float) ((double) ((id * 57u) % 255u) / 255. / div);
+	out->color[2] = (float) ((double) ((id * 23u) % 255u) / 255. / div);
+	out->color[3] = 1.0f;
+}
 
 SRP_SHADER_FN void srpslFsVaryingColor(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out)
 {

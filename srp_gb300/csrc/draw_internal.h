@@ -9,6 +9,16 @@
 
 namespace srpg {
 
+/* Width of the radix-sort key for tile numbers below n, in whole 8-bit
+ * digits: the ordinary and the fixed-scratch draw sort with the same key, so
+ * that their per-tile item orders, and therefore their images, are equal. */
+inline uint32_t sortKeyBits(uint32_t n)
+{
+	uint32_t b = 0;
+	while ((1ull << b) < (unsigned long long) n + 1ull) ++b;
+	return (b + 7) / 8 * 8;
+}
+
 struct FixedDrawInfo {
 	cudaStream_t stream;   /* the library's stream */
 	size_t nIn;            /* input primitives of the draw */

@@ -221,6 +221,7 @@ __device__ __forceinline__ void runVS(SRPVertexShaderIn* in, SRPVertexShaderOut*
 {
 	if (VS == SRP_GPU_VS_TRANSFORM) srpslVsTransform(in, out);
 	else if (VS == SRP_GPU_VS_WORLD) srpslVsWorld(in, out);
+	else if (VS == SRP_GPU_VS_BYTES) srpslVsBytes(in, out);
 }
 
 /* One thread per vertex of [lo, hi]: the block's vertex records (a
@@ -1411,6 +1412,10 @@ void launchVertex(const DrawParams& P, unsigned long long first, unsigned long l
 		cudaFuncSetAttribute(k_vertex<SRP_GPU_VS_WORLD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
 		pdlLaunch(k_vertex<SRP_GPU_VS_WORLD>, blocks, kVertexThreads, smem, s, P, first, n);
 		break;
+	case SRP_GPU_VS_BYTES:
+		cudaFuncSetAttribute(k_vertex<SRP_GPU_VS_BYTES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+		pdlLaunch(k_vertex<SRP_GPU_VS_BYTES>, blocks, kVertexThreads, smem, s, P, first, n);
+		break;
 	default:
 		cudaFuncSetAttribute(k_vertex<SRP_GPU_VS_TRANSFORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
 		pdlLaunch(k_vertex<SRP_GPU_VS_TRANSFORM>, blocks, kVertexThreads, smem, s, P, first, n);
@@ -1468,6 +1473,10 @@ void launchVertexMulti(const DrawParams& P, uint32_t blocks, int maxStride, cuda
 	case SRP_GPU_VS_WORLD:
 		cudaFuncSetAttribute(k_vertex_multi<SRP_GPU_VS_WORLD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
 		pdlLaunch(k_vertex_multi<SRP_GPU_VS_WORLD>, blocks, kVertexThreads, smem, s, P);
+		break;
+	case SRP_GPU_VS_BYTES:
+		cudaFuncSetAttribute(k_vertex_multi<SRP_GPU_VS_BYTES>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
+		pdlLaunch(k_vertex_multi<SRP_GPU_VS_BYTES>, blocks, kVertexThreads, smem, s, P);
 		break;
 	default:
 		cudaFuncSetAttribute(k_vertex_multi<SRP_GPU_VS_TRANSFORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);

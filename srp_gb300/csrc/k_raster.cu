@@ -65,6 +65,9 @@ __device__ __forceinline__ void runFS(SRPFragmentShaderIn* in, SRPFragmentShader
 	case SRP_GPU_FS_DEPTH_OVERWRITE: srpslFsDepthOverwrite(in, out); break;
 	case SRP_GPU_FS_FRAGCOORD: srpslFsFragCoord(in, out); break;
 	case SRP_GPU_FS_FLAT_INT: srpslFsFlatInt(in, out); break;
+	case SRP_GPU_FS_MIXED: srpslFsMixed(in, out); break;
+	case SRP_GPU_FS_BYTE_PALETTE: srpslFsBytePalette(in, out); break;
+	case SRP_GPU_FS_PRIMITIVE_MOD: srpslFsPrimitiveMod(in, out); break;
 	default: break;
 	}
 }
@@ -1028,6 +1031,9 @@ static void shadeKind(const DrawParams& P, uint32_t numTiles, cudaStream_t s)
 	case SRP_GPU_FS_DEPTH_OVERWRITE: pdlLaunch(k_shade<KIND, SRP_GPU_FS_DEPTH_OVERWRITE, MULTI>, b, t, 0, s, P, numTiles); break;
 	case SRP_GPU_FS_FRAGCOORD: pdlLaunch(k_shade<KIND, SRP_GPU_FS_FRAGCOORD, MULTI>, b, t, 0, s, P, numTiles); break;
 	case SRP_GPU_FS_FLAT_INT: pdlLaunch(k_shade<KIND, SRP_GPU_FS_FLAT_INT, MULTI>, b, t, 0, s, P, numTiles); break;
+	case SRP_GPU_FS_MIXED: pdlLaunch(k_shade<KIND, SRP_GPU_FS_MIXED, MULTI>, b, t, 0, s, P, numTiles); break;
+	case SRP_GPU_FS_BYTE_PALETTE: pdlLaunch(k_shade<KIND, SRP_GPU_FS_BYTE_PALETTE, MULTI>, b, t, 0, s, P, numTiles); break;
+	case SRP_GPU_FS_PRIMITIVE_MOD: pdlLaunch(k_shade<KIND, SRP_GPU_FS_PRIMITIVE_MOD, MULTI>, b, t, 0, s, P, numTiles); break;
 	case kFsLearned:
 		if constexpr (KIND == kKindTri) {
 			/* one CTA per SM, its groups looping over the tile pairs */

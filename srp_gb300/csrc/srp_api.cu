@@ -31,6 +31,7 @@
 #include "gpu_types.h"
 #include "imageio.h"
 #include "kernels.h"
+#include "draw_internal.h"
 #include "learned_internal.h"
 
 /* The reference requires the user program to define `SRPContext srpContext`.
@@ -1399,6 +1400,7 @@ static int lookupVS(void* fn)
 {
 	if (fn == (void*) srpVsTransform) return SRP_GPU_VS_TRANSFORM;
 	if (fn == (void*) srpVsWorld) return SRP_GPU_VS_WORLD;
+	if (fn == (void*) srpVsBytes) return SRP_GPU_VS_BYTES;
 	for (auto& e : g.reg.vs) if (e.first == fn) return e.second;
 	return 0;
 }
@@ -1411,6 +1413,8 @@ static int lookupFS(void* fn)
 		{ (void*) srpFsTextureModulate, SRP_GPU_FS_TEXTURE_MODULATE }, { (void*) srpFsBlinnPhong, SRP_GPU_FS_BLINN_PHONG },
 		{ (void*) srpFsMarble, SRP_GPU_FS_MARBLE }, { (void*) srpFsDepthOverwrite, SRP_GPU_FS_DEPTH_OVERWRITE },
 		{ (void*) srpFsFragCoord, SRP_GPU_FS_FRAGCOORD }, { (void*) srpFsFlatInt, SRP_GPU_FS_FLAT_INT },
+		{ (void*) srpFsMixed, SRP_GPU_FS_MIXED }, { (void*) srpFsBytePalette, SRP_GPU_FS_BYTE_PALETTE },
+		{ (void*) srpFsPrimitiveMod, SRP_GPU_FS_PRIMITIVE_MOD },
 	};
 	for (auto& b : builtin) if (b.f == fn) return b.id;
 	for (auto& e : g.reg.fs) if (e.first == fn) return e.second;
@@ -1495,13 +1499,6 @@ static bool uploadIB(SRPIndexBuffer* ib)
 	ib->dirty = false;
 	markUpload(ib->ready, ib->readyOwned, ib->pending, ib->seq);
 	return true;
-}
-
-static uint32_t bitsFor(uint32_t n)
-{
-	uint32_t b = 0;
-	while ((1ull << b) < (unsigned long long) n + 1ull) ++b;
-	return (b + 7) / 8 * 8;
 }
 
 /* Copies both sets' counters to their host mirrors (waits for the GPU) and
@@ -1624,7 +1621,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 
 	uint32_t primCap = (uint32_t) std::min<size_t>(nIn * outPer + 4096, 0x3FFFFFFFu);
 	uint32_t entryCap = (uint32_t) std::min<double>((double) (nIn * outPer) * g.entryRatio[kind] + 4096, 4.0e9);
-	const uint32_t keyBits = bitsFor(numTiles);
+	const uint32_t keyBits = sortKeyBits(numTiles);
 	const bool late = sp->fs->mayOverwriteDepth && shadeSupportsLateDepth(fsId);
 	const bool learned = learnedPrepare(P, kind, late, 1, g.stream);
 	/* the resolve runs beside the previous draw's shading, except for
@@ -2075,7 +2072,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	cudaMemcpyAsync(S.passPrefix.ptr, passPrefix.data(), passPrefix.size() * 4, cudaMemcpyHostToDevice, fs);
 	uint32_t primCap = (uint32_t) std::min<unsigned long long>((unsigned long long) nIn + 4096, 0x3FFFFFFFu);
 	uint32_t entryCap = (uint32_t) std::min<double>((double) nIn * g.entryRatio[kKindTri] + 4096, 4.0e9);
-	const uint32_t keyBits = bitsFor(numTiles);
+	const uint32_t keyBits = sortKeyBits(numTiles);
 	bool drawn = false;
 	for (int attempt = 0; attempt < 4 && !drawn; ++attempt) {
 		const unsigned long long rows = (unsigned long long) vRows + g.clipRows;
@@ -2476,8 +2473,6 @@ void srpGpuSetTileSize(int tileSize)
 
 /* ------------------------------------------- for the fixed-scratch draw */
 
-#include "draw_internal.h"
-
 namespace srpg {
 
 int fixedDrawPrepare(DrawParams& P, const SRPIndexBuffer* ib, const SRPVertexBuffer* vb, const SRPFramebuffer* fb,
@@ -2518,6 +2513,16 @@ int fixedDrawPrepare(DrawParams& P, const SRPIndexBuffer* ib, const SRPVertexBuf
 	if (nIn > 0x7FFFFFFFull) { SRP_ERROR(FN, "Draw too large for the GPU path (%zu primitives)", nIn); return -1; }
 	/* what the ordinary draw would set up by allocating */
 	if (!g.init) { SRP_ERROR(FN, "The library is not initialised: create the framebuffer with srpNewFramebuffer first"); return -1; }
+	/* the draw reads its counters back to the host partway through, which no
+	 * stream capture allows: reject it before anything is queued or changed */
+	cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+	const cudaError_t ce = cudaStreamIsCapturing(g.stream, &cap);
+	if (ce != cudaSuccess) cudaGetLastError();
+	if (ce != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+		SRP_ERROR(FN, "Called while the library's stream is being captured: a fixed-scratch draw waits for its "
+		              "counters mid-draw, so no call can be part of a CUDA graph capture");
+		return -1;
+	}
 	FbExtra* fx = fbFind(fb);
 	if (!fx) { SRP_ERROR(FN, "Framebuffer was not created by srpNewFramebuffer"); return -1; }
 	if (vb->dirty || (!vb->dev.ptr && vb->nBytes)) {
@@ -2604,18 +2609,9 @@ int fixedDrawPrepare(DrawParams& P, const SRPIndexBuffer* ib, const SRPVertexBuf
 	info.stream = g.stream;
 	fbOtherWrite(fx);
 	g.rsDirty = true;  /* its resolve writes the planes on the library's stream */
-	/* the uploads of its buffers, on the copy stream; inside a stream capture
-	 * nothing is waited for: there the buffers come from srpVertexBufferCopyData
-	 * and srpIndexBufferCopyData, which return once their copy is done */
-	cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-	if (cudaStreamIsCapturing(g.stream, &cap) != cudaSuccess) {
-		cudaGetLastError();
-		cap = cudaStreamCaptureStatusNone;
-	}
-	if (cap == cudaStreamCaptureStatusNone) {
-		if (vb->ready) cudaStreamWaitEvent(g.stream, vb->ready, 0);
-		if (ib && ib->ready) cudaStreamWaitEvent(g.stream, ib->ready, 0);
-	}
+	/* the uploads of its buffers, on the copy stream */
+	if (vb->ready) cudaStreamWaitEvent(g.stream, vb->ready, 0);
+	if (ib && ib->ready) cudaStreamWaitEvent(g.stream, ib->ready, 0);
 	g.streamReads = true;
 	info.nIn = nIn;
 	info.outPer = isTri(prim) && mode != SRP_POLYGON_MODE_FILL ? 3 : 1;

@@ -99,13 +99,6 @@ size_t binBytes(size_t E, bool lineFrags)
 	       round256(sortHistWords((uint32_t) e) * 4) + round256(sortPartialWords((uint32_t) e) * 4 + 64);
 }
 
-uint32_t keyBitsFor(uint32_t n)
-{
-	uint32_t b = 0;
-	while ((1ull << b) < (unsigned long long) n + 1ull) ++b;
-	return (b + 7) / 8 * 8;
-}
-
 bool launchedOk(const char* what)
 {
 	const cudaError_t e = cudaGetLastError();
@@ -131,7 +124,9 @@ extern "C" int srpGpuDrawFixedScratch(const SRPIndexBuffer* ib, const SRPVertexB
 	const size_t rows = nV + kClipRows;
 	const size_t nw = (size_t) std::max(P.L.nWords, 1);
 	const size_t blocks = std::max<size_t>((info.nIn + kSetupThreads - 1) / kSetupThreads, 1);
-	const size_t primCap = std::min<size_t>(info.nIn * info.outPer + 4096, 0x3FFFFFFFu);
+	/* every input primitive once, plus the extra triangles of clipping: each
+	 * of the kClipPolys clipped triangles fans out into up to kMaxPoly - 2 */
+	const size_t primCap = std::min<size_t>((info.nIn + kClipPolys * (kMaxPoly - 3)) * info.outPer, 0x3FFFFFFFu);
 	Carver cv;
 	const size_t oCtr = cv.take(sizeof(DeviceCounters));
 	const size_t oMinmax = cv.take(16);
@@ -272,7 +267,7 @@ extern "C" int srpGpuDrawFixedScratch(const SRPIndexBuffer* ib, const SRPVertexB
 		launches += 2;
 	}
 	if (E) {
-		const uint32_t keyBits = keyBitsFor(info.numTiles);
+		const uint32_t keyBits = sortKeyBits(info.numTiles);
 		uint32_t* sk;
 		uint32_t* sv;
 		sortEntries(P, keyBits, (uint32_t*) (base + oKeys2), (uint32_t*) (base + oVals2), (uint32_t*) (base + oHist),

@@ -142,7 +142,7 @@ struct Scene {
 	size_t texBytes;
 	int nprog;
 	SRPStdUniform uni[MAX_PROG];
-	SRPVaryingInfo vinfo[MAX_PROG][4];
+	SRPVaryingInfo vinfo[MAX_PROG][8];
 	SRPVertexShader vs[MAX_PROG];
 	SRPFragmentShader fs[MAX_PROG];
 	SRPShaderProgram sp[MAX_PROG];
@@ -261,13 +261,33 @@ static SRPVaryingInfo vi(size_t n, SRPType t, SRPInterpolationMode m)
 	return v;
 }
 
+#ifdef SCENES_GPU
+/* With the switch on, every draw of a scene goes through
+ * srpGpuDrawFixedScratch instead; rejected draws are counted. */
+static int gFixedScratch, gFixedRejected;
+void sceneUseFixedScratch(int on) { gFixedScratch = on; gFixedRejected = 0; }
+int sceneFixedScratchRejected(void) { return gFixedRejected; }
+#endif
+
 static void drawI(Scene* s, int ib, int vb, SRPFramebuffer* fb, int prog, SRPPrimitive p, size_t start, size_t count)
 {
+#ifdef SCENES_GPU
+	if (gFixedScratch) {
+		gFixedRejected += srpGpuDrawFixedScratch(s->ib[ib], s->vb[vb], fb, &s->sp[prog], p, start, count) != 0;
+		return;
+	}
+#endif
 	srpDrawIndexBuffer(s->ib[ib], s->vb[vb], fb, &s->sp[prog], p, start, count);
 }
 
 static void drawV(Scene* s, int vb, SRPFramebuffer* fb, int prog, SRPPrimitive p, size_t start, size_t count)
 {
+#ifdef SCENES_GPU
+	if (gFixedScratch) {
+		gFixedRejected += srpGpuDrawFixedScratch(NULL, s->vb[vb], fb, &s->sp[prog], p, start, count) != 0;
+		return;
+	}
+#endif
 	srpDrawVertexBuffer(s->vb[vb], fb, &s->sp[prog], p, start, count);
 }
 
@@ -1318,6 +1338,118 @@ static void buildBMScene(Scene* s, Rng* rng)
 	program(s, 0, srpVsWorld, srpFsMarble, 0, 3, v0);
 }
 
+/* ------------------------------------------------- packed varying layouts */
+
+#define PACK13_BYTES 13   /* position (12 B) + uint8 palette index */
+#define PACK49_BYTES (12 + SRP_MIXED_BLOCK_BYTES)
+
+static void renderVaryings(Scene* s, SRPFramebuffer* fb)
+{
+	const size_t half = s->param[0], nTri = s->param[1];
+	srpDepthTest(true);
+	srpDepthCompareOp(SRP_COMPARE_LESS);
+	srpRasterCullFace(SRP_FACE_NONE);
+	/* 13-byte vertices, one uint8 flat varying: first, then last provoking vertex */
+	srpProvokingVertexMode(SRP_PROVOKING_VERTEX_FIRST);
+	drawV(s, 0, fb, 0, SRP_PRIM_TRIANGLES, 0, 3 * half);
+	srpProvokingVertexMode(SRP_PROVOKING_VERTEX_LAST);
+	drawV(s, 0, fb, 0, SRP_PRIM_TRIANGLES, 3 * half, 3 * half);
+	/* 49-byte vertices, the 37-byte mixed block: perspective, affine, flat */
+	const size_t third = nTri / 3;
+	drawI(s, 0, 1, fb, 1, SRP_PRIM_TRIANGLES, 0, 3 * third);
+	srpProvokingVertexMode(SRP_PROVOKING_VERTEX_FIRST);
+	drawI(s, 0, 1, fb, 2, SRP_PRIM_TRIANGLES, 3 * third, 3 * third);
+	srpProvokingVertexMode(SRP_PROVOKING_VERTEX_LAST);
+	drawI(s, 0, 1, fb, 3, SRP_PRIM_TRIANGLES, 6 * third, 3 * (nTri - 2 * third));
+	/* the same block on lines (two-vertex interpolation) and points (raw) */
+	srpDepthCompareOp(SRP_COMPARE_LEQUAL);
+	drawI(s, 0, 1, fb, 4, SRP_PRIM_LINE_STRIP, 0, 3 * third);
+	srpRasterPointSize(3.f);
+	drawV(s, 1, fb, 5, SRP_PRIM_POINTS, 0, 3 * nTri);
+}
+
+static void packMixed(Rng* rng, unsigned char* blk)
+{
+	int8_t a = (int8_t) (rngNext(rng) >> 56);
+	double d[2] = { rngRange(rng, -4, 4), rngRange(rng, -3, 3) };
+	uint16_t b = (uint16_t) (rngNext(rng) >> 48);
+	float f[2] = { (float) rngRange(rng, -2, 2), (float) rngRange(rng, -2, 2) };
+	int16_t c = (int16_t) (rngNext(rng) >> 48);
+	uint64_t e = rngNext(rng);
+	memcpy(blk, &a, 1); memcpy(blk + 1, d, 16); memcpy(blk + 17, &b, 2);
+	memcpy(blk + 19, f, 8); memcpy(blk + 27, &c, 2); memcpy(blk + 29, &e, 8);
+}
+
+/* Every varying element type the reference interpolates
+ * (src/pipeline/interpolation.c:63-163) in byte-packed layouts:
+ * - 13-byte vertices (position + a uint8, as in the reference's own flat
+ *   interpolation test scene, tests/scenes/interpolation/flat.c:8-17), the
+ *   uint8 declared as one UINT8 flat varying, with both provoking vertices;
+ * - 49-byte vertices whose 37-byte varying block holds int8, 2 doubles,
+ *   uint16, 2 floats, int16 and uint64 at odd offsets, drawn with every
+ *   floating attribute perspective, affine and flat, then as a line strip and
+ *   as points. Triangles straddle the near plane, so clipping interpolates the
+ *   doubles and copies the integers from the pair's provoking vertex. */
+static void buildVaryings(Scene* s, Rng* rng)
+{
+	featureSize(s);
+	const double sc = s->scale < 1 ? s->scale : 1;
+	const size_t nTri0 = (size_t) (120 * sc) + 8, nTri = (size_t) (240 * sc) + 12;
+	s->param[0] = (int) (nTri0 / 2);
+	s->param[1] = (int) nTri;
+	float* tmp = (float*) malloc(nTri * 3 * 8 * sizeof(float));
+	/* 13-byte vertices */
+	randomTris(rng, tmp, nTri0, 3.0, 0.2, 11.0, 8);
+	unsigned char* v13 = (unsigned char*) malloc(nTri0 * 3 * PACK13_BYTES);
+	for (size_t i = 0; i < nTri0 * 3; ++i) {
+		memcpy(v13 + i * PACK13_BYTES, tmp + i * 8, 12);
+		v13[i * PACK13_BYTES + 12] = (unsigned char) (i % 5 == 4 ? (rngNext(rng) >> 56) : (rngNext(rng) % 3));
+	}
+	addVB(s, v13, PACK13_BYTES, nTri0 * 3 * PACK13_BYTES);
+	free(v13);
+	/* 49-byte vertices */
+	randomTris(rng, tmp, nTri, 3.0, -1.0, 12.0, 8);
+	unsigned char* v49 = (unsigned char*) malloc(nTri * 3 * PACK49_BYTES);
+	for (size_t i = 0; i < nTri * 3; ++i) {
+		memcpy(v49 + i * PACK49_BYTES, tmp + i * 8, 12);
+		packMixed(rng, v49 + i * PACK49_BYTES + 12);
+	}
+	addVB(s, v49, PACK49_BYTES, nTri * 3 * PACK49_BYTES);
+	free(v49);
+	free(tmp);
+	const size_t nv = nTri * 3;
+	uint16_t* idx = (uint16_t*) malloc(nv * sizeof(uint16_t));
+	for (size_t i = 0; i < nv; ++i) idx[i] = (uint16_t) ((i * 7919) % nv);
+	addIB(s, SRP_UINT16, idx, nv * 2);
+	free(idx);
+	for (int k = 0; k < 6; ++k) {
+		SRPStdUniform* u = &s->uni[k];
+		baseUniform(u);
+		u->model = rotation(0.05 * k, 0.1, 0.02);
+		u->projection = perspective60((float) s->W / (float) s->H, 0.5f, 12.f);
+		u->passOffset = 12;
+		u->passCount = k == 0 ? 1 : SRP_MIXED_BLOCK_BYTES;
+	}
+	SRPVaryingInfo v8[1] = { vi(1, SRP_UINT8, SRP_INTERPOLATION_MODE_FLAT) };
+	program(s, 0, srpVsBytes, srpFsBytePalette, 0, 1, v8);
+	const SRPInterpolationMode modes[5] = { SRP_INTERPOLATION_MODE_PERSPECTIVE, SRP_INTERPOLATION_MODE_AFFINE,
+	                                        SRP_INTERPOLATION_MODE_FLAT, SRP_INTERPOLATION_MODE_PERSPECTIVE,
+	                                        SRP_INTERPOLATION_MODE_AFFINE };
+	for (int k = 0; k < 5; ++k) {
+		const SRPInterpolationMode m = modes[k];
+		/* integer members are flat whatever mode they are given */
+		SRPVaryingInfo mix[6] = { vi(1, SRP_INT8, m), vi(2, SRP_DOUBLE, m), vi(1, SRP_UINT16, m),
+		                          vi(2, SRP_FLOAT, m), vi(1, SRP_INT16, m), vi(1, SRP_UINT64, m) };
+		program(s, 1 + k, srpVsBytes, srpFsMixed, 0, 6, mix);
+	}
+	s->nTris = nTri0 + nTri;
+	s->nLines = 3 * (nTri / 3) - 1;
+	s->nPoints = 3 * nTri;
+	s->depthInit = 1.0f;
+	s->render = renderVaryings;
+	s->draws = 7;
+}
+
 /* ------------------------------------------------------------- registry */
 
 typedef struct SceneDef { const char* name; void (*build)(Scene*, Rng*); } SceneDef;
@@ -1337,6 +1469,7 @@ static const SceneDef DEFS[] = {
 	{ "topologies", buildTopologies },
 	{ "late_z", buildLateZ },
 	{ "lit", buildLit },
+	{ "varyings", buildVaryings },
 	{ "bscene", buildBScene },
 	{ "msoup", buildMSoup },
 	{ "bmscene", buildBMScene },

@@ -71,6 +71,11 @@ void sceneUploadBatchAsync(Scene** scenes, size_t n);
 /* scenePrepareFramebuffer of n scenes in one srpGpuFramebufferFillBatch when
  * they share their initial depth and stencil (else one by one). */
 void scenePrepareBatch(Scene** scenes, SRPFramebuffer** fbs, size_t n);
+/* Draw every scene through srpGpuDrawFixedScratch (on) or the ordinary draw
+ * calls (off, the default); the count of fixed-scratch draws rejected since
+ * the switch was last set. */
+void sceneUseFixedScratch(int on);
+int sceneFixedScratchRejected(void);
 #endif
 
 /* Convenience: create a framebuffer of the scene's size, prepare, render, copy

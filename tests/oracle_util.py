@@ -17,6 +17,20 @@ def manifest():
         return json.load(f)
 
 
+def hash_cases():
+    """Reference frames too large to store, kept as SHA-256 digests of their
+    planes (tests/golden/hashes.json, written by make_golden.py)."""
+    with open(os.path.join(GOLDEN, "hashes.json")) as f:
+        return json.load(f)
+
+
+def plane_digests(d):
+    """SHA-256 of the colour, depth-bit and stencil planes, little-endian."""
+    import hashlib
+    return {k: hashlib.sha256(np.ascontiguousarray(d[k]).astype(d[k].dtype.newbyteorder("<")).tobytes()).hexdigest()
+            for k in ("color", "depth_bits", "stencil")}
+
+
 def load_golden(case):
     z = np.load(os.path.join(GOLDEN, case["name"] + ".npz"))
     return {"color": z["color"], "depth_bits": z["depth_bits"], "stencil": z["stencil"]}

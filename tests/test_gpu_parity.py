@@ -5,7 +5,7 @@ channel. Every call goes through the srp C API of libsrp_gb300.so."""
 import numpy as np
 import pytest
 
-from oracle_util import manifest, load_golden, oracle_render, compare_planes
+from oracle_util import manifest, load_golden, oracle_render, compare_planes, hash_cases, plane_digests
 
 pytestmark = pytest.mark.gpu
 
@@ -28,7 +28,8 @@ def test_gpu_matches_reference_fixture(built_library, case):
 SEEDED = [(n, seed, scale) for n, scale in [
     ("sphere", 0.5), ("soup", 0.02), ("clip_tris", 1.0), ("clip_lines", 1.0), ("points", 1.0),
     ("interp", 1.0), ("depth_ops", 1.0), ("raster_rules", 1.0), ("scissor", 1.0), ("stencil", 1.0),
-    ("poly_modes", 1.0), ("topologies", 1.0), ("late_z", 1.0), ("lit", 1.0)] for seed in (2, 5)]
+    ("poly_modes", 1.0), ("topologies", 1.0), ("late_z", 1.0), ("lit", 1.0), ("varyings", 1.0)]
+    for seed in (2, 5)]
 
 
 @pytest.mark.parametrize("scene,seed,scale", SEEDED)
@@ -48,6 +49,23 @@ def test_full_size_configs_match_oracle(built_library, oracle_exe, scene, seed):
     got = gpu_render(scene, seed, 1.0)
     compare_planes(got, want, f"{scene} full size")
     assert got["fragments"] == want["fragments"]
+
+
+@pytest.mark.parametrize("case", hash_cases(), ids=lambda c: c["name"])
+def test_full_size_bench_frame_matches_reference_digests(built_library, oracle_exe, case):
+    """The frame bench.py times, against digests of the reference's own
+    rendering: depth and stencil hash to the reference's planes; colour is
+    within 1/255 of the oracle, whose colour plane hashes to the reference's."""
+    got = gpu_render(case["scene"], case["seed"], case["scale"])
+    assert str(got["hash"]) == case["input_hash"], "scene inputs differ from the reference's"
+    dg = plane_digests(got)
+    assert dg["depth_bits"] == case["sha256"]["depth_bits"], "depth differs from the reference's"
+    assert dg["stencil"] == case["sha256"]["stencil"], "stencil differs from the reference's"
+    assert got["fragments"] == case["fragments"]
+    if dg["color"] != case["sha256"]["color"]:
+        want = oracle_render(oracle_exe, case["scene"], case["seed"], case["scale"])
+        assert plane_digests(want)["color"] == case["sha256"]["color"]
+        compare_planes(got, want, case["name"])
 
 
 @pytest.mark.parametrize("scene,scale", [("soup", 0.02), ("lit", 1.0), ("stencil", 1.0)])

@@ -8,7 +8,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from oracle_util import manifest, load_golden, oracle_render, compare_planes
+from oracle_util import manifest, load_golden, oracle_render, compare_planes, hash_cases, plane_digests
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 REF = "/root/reference"
@@ -21,6 +21,15 @@ def test_oracle_matches_reference_fixtures(oracle_exe, case):
     want = load_golden(case)
     for k in ("color", "depth_bits", "stencil"):
         assert np.array_equal(got[k], want[k]), f"{case['name']}: {k} differs from the reference"
+    assert got["fragments"] == case["fragments"]
+
+
+@pytest.mark.parametrize("case", hash_cases(), ids=lambda c: c["name"])
+def test_oracle_matches_reference_digests(oracle_exe, case):
+    """The full-size bench frame: the oracle's planes hash to the reference's."""
+    got = oracle_render(oracle_exe, case["scene"], case["seed"], case["scale"])
+    assert str(got["hash"]) == case["input_hash"], "scene inputs differ from the reference's"
+    assert plane_digests(got) == case["sha256"]
     assert got["fragments"] == case["fragments"]
 
 

@@ -5,8 +5,14 @@ through the C ABI of libsrp_gb300.so.
 The file is named so that pytest collects it last: it has to pass both on its
 own in a fresh process (the first call then does the per-device set-up) and
 after every other GPU test in the same process. Images must be bit-identical
-to those of srpDrawIndexBuffer / srpDrawVertexBuffer."""
+to those of srpDrawIndexBuffer / srpDrawVertexBuffer, and the seeded scenes
+drawn through it must match the reference's fixtures and the CPU oracle.
+Callers that need it cannot have device memory allocated mid-frame, so one
+test also checks that repeated calls leave the device's free memory as it
+was."""
 import ctypes
+import glob
+import os
 
 import numpy as np
 import pytest
@@ -278,4 +284,221 @@ def test_fixed_scratch_between_overlapped_draws(api):
     assert not api.errors(), api.errors()
     assert_same(got, want, "overlapped sequence")
     assert_same(got2, want, "overlapped sequence, graphs replayed")
+    assert L.srpGpuSynchronize() == 0
+
+
+# ------------------------------------------------- seeded scenes, oracle
+
+
+def render_fixed(name, seed, scale):
+    """One frame of a seeded scene with every draw through
+    srpGpuDrawFixedScratch; returns the planes and the rejected-draw count."""
+    import srp_gb300
+    L, S = srp_gb300.lib(), srp_gb300.scenes()
+    S.sceneUseFixedScratch.argtypes = [ctypes.c_int]
+    S.sceneFixedScratchRejected.restype = ctypes.c_int
+    L.srpGpuSetFramebufferMode(srp_gb300.SRP_GPU_FB_DEVICE)
+    sc = srp_gb300.Scene(name, seed, scale)
+    try:
+        sc.prepare()
+        S.sceneUseFixedScratch(1)
+        try:
+            sc.render()
+            rejected = S.sceneFixedScratchRejected()
+        finally:
+            S.sceneUseFixedScratch(0)
+        c, d, st = sc.planes()
+        assert L.srpGpuSynchronize() == 0
+        return {"color": c, "depth_bits": d.view(np.uint32), "stencil": st, "hash": int(sc.input_hash)}, rejected
+    finally:
+        sc.close()
+
+
+# points, wireframe and point polygon modes, the late-depth resolve, large
+# triangles with barycentric tables, every varying type, strips and fans
+FIXED_SCENES = ["varyings", "poly_modes", "late_z", "points", "clip_tris", "raster_rules", "interp", "stencil",
+                "topologies", "sphere"]
+# draws a scene makes on purpose out of range, which both draws reject
+EXPECTED_REJECTIONS = {"topologies": 1}
+
+
+@pytest.mark.parametrize("scene", FIXED_SCENES)
+def test_fixed_scratch_matches_reference_fixtures(built_library, scene):
+    """Scenes whose every draw is a fixed-scratch draw equal the reference's
+    own renderings (depth and stencil bit-exact, colour within 1/255)."""
+    from oracle_util import manifest, load_golden, compare_planes
+    cases = [c for c in manifest() if c["scene"] == scene]
+    assert cases
+    for case in cases:
+        got, rejected = render_fixed(case["scene"], case["seed"], case["scale"])
+        assert rejected == EXPECTED_REJECTIONS.get(scene, 0)
+        assert str(got["hash"]) == case["input_hash"]
+        compare_planes(got, load_golden(case), case["name"] + " (fixed scratch)")
+
+
+@pytest.mark.parametrize("scene,scale", [("varyings", 1.0), ("poly_modes", 1.0), ("late_z", 1.0), ("clip_lines", 1.0),
+                                         ("soup", 0.03)])
+def test_fixed_scratch_matches_oracle(built_library, oracle_exe, scene, scale):
+    from oracle_util import oracle_render, compare_planes
+    want = oracle_render(oracle_exe, scene, 4, scale)
+    got, rejected = render_fixed(scene, 4, scale)
+    assert rejected == 0
+    assert got["hash"] == want["hash"]
+    compare_planes(got, want, f"{scene} seed 4 (fixed scratch)")
+
+
+def cudart():
+    """The CUDA runtime as a shared library, for cudaMemGetInfo and stream
+    capture (the GPU library links its own static copy)."""
+    cands = ["libcudart.so.13", "/usr/local/cuda/lib64/libcudart.so.13", "/usr/local/cuda/lib64/libcudart.so"]
+    cands += glob.glob("/usr/local/lib/python3*/dist-packages/nvidia/cu13/lib/libcudart.so.13")
+    for c in cands:
+        try:
+            return ctypes.CDLL(c)
+        except OSError:
+            continue
+    pytest.fail("no libcudart shared library found")
+
+
+def free_device_bytes(rt):
+    free, total = ctypes.c_size_t(), ctypes.c_size_t()
+    assert rt.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0
+    return free.value
+
+
+def test_fixed_scratch_allocates_nothing(built_library):
+    """After a first pass (which loads the array's device image), further
+    fixed-scratch frames of several scenes leave the device's free memory
+    exactly as it was: no call allocates or frees device memory."""
+    import srp_gb300
+    L, S = srp_gb300.lib(), srp_gb300.scenes()
+    S.sceneUseFixedScratch.argtypes = [ctypes.c_int]
+    S.sceneFixedScratchRejected.restype = ctypes.c_int
+    rt = cudart()
+    L.srpGpuSetFramebufferMode(srp_gb300.SRP_GPU_FB_DEVICE)
+    scs = [srp_gb300.Scene(n, 6, x) for n, x in (("varyings", 1.0), ("poly_modes", 1.0), ("late_z", 1.0),
+                                                   ("soup", 0.03), ("clip_lines", 1.0))]
+    try:
+        frees = []
+        for rep in range(3):
+            for sc in scs:
+                sc.prepare()
+            assert L.srpGpuSynchronize() == 0
+            frees.append(free_device_bytes(rt))
+            S.sceneUseFixedScratch(1)
+            try:
+                for sc in scs:
+                    sc.render()
+                assert S.sceneFixedScratchRejected() == 0
+            finally:
+                S.sceneUseFixedScratch(0)
+            assert L.srpGpuSynchronize() == 0
+            frees.append(free_device_bytes(rt))
+        # the first pass may load the array's device image; none after it moves memory
+        assert len(set(frees[1:])) == 1, frees
+    finally:
+        for sc in scs:
+            sc.close()
+
+
+def test_fixed_scratch_large_triangles(api):
+    """A few triangles covering the whole framebuffer go through the
+    barycentric-table path of large primitives; the images equal the
+    ordinary draw's."""
+    L = api.L
+    L.srpGpuSetFramebufferMode(1)
+    rng = np.random.default_rng(31)
+    W, H = 640, 480
+    n = 12
+    pos = rng.uniform(-3.0, 3.0, size=(3 * n, 2))
+    z = np.repeat(rng.uniform(-0.9, 0.9, size=n), 3)[:, None] + rng.uniform(-0.05, 0.05, size=(3 * n, 1))
+    verts = np.concatenate([pos, z, rng.uniform(0, 1, size=(3 * n, 3))], axis=1)
+    vb = api.vertex_buffer(verts)
+    ordinary, fixed = api.framebuffer(W, H), api.framebuffer(W, H)
+    L.srpDrawVertexBuffer(vb, ordinary, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, 3 * n)
+    assert L.srpGpuDrawFixedScratch(None, vb, fixed, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, 3 * n) == 0
+    want, got = api.planes(ordinary), api.planes(fixed)
+    assert not api.errors(), api.errors()
+    assert int(np.count_nonzero(want[1] != np.float32(-1.0).view(np.uint32))) > W * H // 2
+    assert_same(got, want, "full-screen triangles")
+
+
+def test_fixed_scratch_ignores_learned_shading(built_library):
+    """With learned shading set, the ordinary draw shades with the network,
+    while the fixed-scratch draw runs the program's own shader: its image is
+    the plain draw's."""
+    import srp_gb300
+    L, S = srp_gb300.lib(), srp_gb300.scenes()
+    vp = ctypes.c_void_p
+    L.srpGpuMlpCreate.restype = vp
+    L.srpGpuMlpCreate.argtypes = [ctypes.c_uint64, ctypes.c_size_t]
+    L.srpGpuMlpFree.argtypes = [vp]
+    L.srpGpuSetLearnedShading.argtypes = [vp, vp, ctypes.c_float, ctypes.c_uint32]
+    S.sceneUseFixedScratch.argtypes = [ctypes.c_int]
+    S.sceneFixedScratchRejected.restype = ctypes.c_int
+    L.srpGpuSetFramebufferMode(srp_gb300.SRP_GPU_FB_DEVICE)
+    marble = ctypes.cast(L.srpFsMarble, vp)
+    net = L.srpGpuMlpCreate(3, 1 << 10)
+    sc = srp_gb300.Scene("msoup", 12, 0.03)
+    try:
+        sc.prepare()
+        sc.render()
+        plain = [a.copy() for a in sc.planes()]
+        L.srpGpuSetLearnedShading(marble, net, 0.0, 16)
+        sc.prepare()
+        sc.render()
+        learned = sc.planes()
+        sc.prepare()
+        S.sceneUseFixedScratch(1)
+        try:
+            sc.render()
+            assert S.sceneFixedScratchRejected() == 0
+        finally:
+            S.sceneUseFixedScratch(0)
+        fixed = sc.planes()
+    finally:
+        L.srpGpuSetLearnedShading(None, None, 0.0, 0)
+        sc.close()
+        L.srpGpuMlpFree(net)
+    assert L.srpGpuSynchronize() == 0
+    assert (learned[0] != plain[0]).any(), "the untrained network should change the colours"
+    for a, b in zip(fixed, plain):
+        assert np.array_equal(a, b)
+
+
+def test_fixed_scratch_refuses_stream_capture(api):
+    """A call while the library's stream is being captured is rejected before
+    anything is queued: the capture ends with an empty graph and stays valid,
+    and the framebuffer is unchanged."""
+    L = api.L
+    rt = cudart()
+    L.srpGpuSetFramebufferMode(1)
+    rng = np.random.default_rng(5)
+    vb = api.vertex_buffer(triangle_soup(rng, 200))
+    fb = api.framebuffer(256, 192)
+    before = api.planes(fb)
+    stream = ctypes.c_void_p()
+    assert rt.cudaStreamCreateWithFlags(ctypes.byref(stream), 1) == 0  # cudaStreamNonBlocking
+    graph = ctypes.c_void_p()
+    nodes = ctypes.c_size_t(1)
+    try:
+        L.srpGpuSetStream(stream)
+        assert rt.cudaStreamBeginCapture(stream, 2) == 0  # cudaStreamCaptureModeRelaxed
+        rc = L.srpGpuDrawFixedScratch(None, vb, fb, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, 600)
+        assert rt.cudaStreamEndCapture(stream, ctypes.byref(graph)) == 0
+        assert rt.cudaGraphGetNodes(graph, None, ctypes.byref(nodes)) == 0
+    finally:
+        if graph.value:
+            rt.cudaGraphDestroy(graph)
+        L.srpGpuSetStream(None)
+        rt.cudaStreamSynchronize(stream)
+        rt.cudaStreamDestroy(stream)
+    errs = api.errors()
+    assert rc == -1 and errs and "captured" in errs[-1][2], errs
+    assert nodes.value == 0
+    assert_same(api.planes(fb), before, "rejected during capture")
+    # the next call outside a capture draws as usual
+    api.messages.clear()
+    assert L.srpGpuDrawFixedScratch(None, vb, fb, ctypes.byref(api.prog), SRP_PRIM_TRIANGLES, 0, 600) == 0
+    assert not api.errors(), api.errors()
     assert L.srpGpuSynchronize() == 0
