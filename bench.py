@@ -16,6 +16,19 @@ followed by 100k lines and 100k points -- three srp draw calls.
 A fragment is a pixel that passed coverage and the scissor test (before depth
 and stencil), counted the same way by the CPU oracle.
 
+  roofline  the frame's algorithmic bytes (vertex and index bytes, the three
+            framebuffer planes read and written once, the texture once) over
+            the frame time, against the measured HBM copy bandwidth;
+            stage_roofline splits them by stage, with the resolve stage's
+            intermediate bytes and measured DRAM traffic beside its share.
+
+At N = 1 the line also carries the other configurations, each measured after
+the frame on its own scenes (--frame-only leaves them out):
+  batch          4096 independent scenes through srpGpuDrawBatch (scenes/s)
+  learned        the frame shaded by the marble shader, plain against its
+                 learned MLP stand-in, alone and with the 40 dB judge
+  batch_learned  the batch with the marble shader and its stand-in
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 --impl reference times the reference's algorithm on the host cores: the CPU
@@ -67,6 +80,23 @@ def replica_throughput(local_ms, local_units, world, device):
 
 
 TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "resolve_soup_1080p.md")
+FRAME_TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "frame_traffic_soup.md")
+
+
+def frame_traffic(scale):
+    """DRAM bytes (read + write) of all the frame's kernels per full-size
+    frame, from the committed ncu capture; None for any other size or when
+    no capture is committed."""
+    if scale != 1.0:
+        return None
+    try:
+        with open(FRAME_TRAFFIC_PROFILE) as f:
+            for line in f:
+                if line.startswith("traffic_bytes_per_frame:"):
+                    return int(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
 
 
 def resolve_traffic(scale):
@@ -165,18 +195,24 @@ def run_reference(args):
     cores = os.cpu_count() or 1
     frames = max(1, args.warmup + args.steps)
     t0 = time.perf_counter()
+    # every core renders the same frame (seed and size of the GPU line)
     with cf.ThreadPoolExecutor(max_workers=cores) as ex:
-        res = list(ex.map(lambda i: cpu_frame(1.0, frames, SEED + i % 4), range(cores)))
+        res = list(ex.map(lambda i: cpu_frame(args.scale, frames, SEED), range(cores)))
     wall = time.perf_counter() - t0
     # throughput over the timed frames: each worker reports its mean frame time
-    frags = sum(r["fragments"] for r in res) / cores
+    frags = res[0]["fragments"]
     per_core_fps = [1.0 / r["mean_s"] for r in res]
     value = frags * sum(per_core_fps) / 1e6
+    mean_s = sum(r["mean_s"] for r in res) / cores
     line = {"impl": "reference", "metric": "Mfrag/s", "value": round(value, 3), "unit": "Mfrag/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(1000.0 * sum(r["mean_s"] for r in res) / cores, 3),
+            "ms_per_step": round(1000.0 * mean_s / cores, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "seed": SEED},
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "seed": SEED, "width": res[0]["width"], "height": res[0]["height"],
+                       "triangles": res[0]["triangles"], "lines": res[0]["lines"], "points": res[0]["points"],
+                       "fragments_per_frame": frags, "frames_per_s": round(sum(per_core_fps), 2),
+                       "mtri_per_s": round(res[0]["triangles"] * sum(per_core_fps) / 1e6, 2)},
             "cpu_baseline": {"value": round(value, 3), "unit": "Mfrag/s", "cores": cores, "kind": "port",
                              "host": host_cpu(),
                              "sample": f"{frames} full frames per core, {cores} processes, wall {wall:.1f}s"},
@@ -231,9 +267,9 @@ def run_reference_batch(args):
     print(json.dumps(line))
 
 
-def run_batch(args):
+def run_batch(args, emit=True):
     """The batched-scenes workload: all scenes drawn by one srpGpuDrawBatch
-    call per step (multi-draw passes)."""
+    call per step (multi-draw passes). Returns the line; prints it if emit."""
     import ctypes
     import torch
     import srp_gb300
@@ -329,8 +365,11 @@ def run_batch(args):
     total_ms = sum(times)
     step_s = total_ms / args.steps / 1000.0
     peak, peak_kind = peaks()
-    resolve_bytes = prof.resolveItems * 68 + pixels * 14
-    resolve_gbs = resolve_bytes / (stage_ms["resolve"] / 1000.0) / 1e9 if stage_ms["resolve"] > 0 else 0.0
+    tex = sum(sc.info.textureBytes for sc in batch)
+    # algorithmic bytes of a step: every scene's vertex and index bytes, its
+    # colour and depth planes read and written, its texture once
+    algo_bytes = h2d + pixels * 8 * 2 + tex
+    step_gbs = algo_bytes / step_s / 1e9
     e2e_s = sum(e2e) / len(e2e)
     line = {
         "metric": "scenes/s", "value": round(args.scenes / step_s, 2), "unit": "scenes/s", "n_gpus": 1,
@@ -347,10 +386,12 @@ def run_batch(args):
                              "srpGpuFramebufferSyncBatchAsync (gather kernels), one wait per step",
                 "with_per_buffer_calls": round(args.scenes / (sum(e2e_calls) / len(e2e_calls)), 2)},
         "gpu_launches": int(st.kernelLaunches),
-        "roofline": {"bound": "hbm", "achieved": round(resolve_gbs, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(resolve_gbs / peak, 5), "traffic": None,
-                     "kernel": "resolve stage (k_tile_classify + k_resolve + k_resolve_heavy, multi-draw)",
-                     "algorithmic_bytes_per_step": int(resolve_bytes), "ms_per_step": round(stage_ms["resolve"], 3),
+        "roofline": {"bound": "hbm", "achieved": round(step_gbs, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(step_gbs / peak, 5), "traffic": None,
+                     "kernel": "the whole batch: every kernel of srpGpuDrawBatch, timed as one step",
+                     "algorithmic_bytes_per_step": int(algo_bytes),
+                     "basis": "vertex + index bytes + colour and depth planes read and written + textures",
+                     "resolve_intermediate_bytes_per_step": int(prof.resolveItems * 68 + pixels * 14),
                      "note": f"peak {peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
         "stages_ms_per_step": {k: round(v, 3) for k, v in stage_ms.items()},
     }
@@ -361,9 +402,11 @@ def run_batch(args):
         line["cpu_baseline"] = {"value": round(cnt / secs, 3), "unit": "scenes/s", "cores": 1, "kind": "port",
                                 "sample": f"scenes 0..{cnt - 1} of the batch on 1 host core, "
                                           f"{round(cfr / secs / 1e6, 2)} Mfrag/s"}
-    print(json.dumps(line))
+    if emit:
+        print(json.dumps(line))
     for sc in batch:
         sc.close()
+    return line
 
 
 LEARNED_WORKLOAD = ("learned: 2.0M-triangle geodesic-sphere soup at 1920x1080 shaded by 8-octave value-noise "
@@ -378,11 +421,23 @@ class LearnedStats(ctypes.Structure):
                 ("psnrHistogram", ctypes.c_uint64 * 6)]
 
 
-def run_learned(args):
+MLP_FLOPS_PER_FRAGMENT = 2 * (108 * 64 + 64 * 64 + 64 * 64 + 64 * 3)
+
+
+def tensor_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
+def run_learned(args, emit=True):
     """Train the learned stand-in of the marble shader on fragments of 32
     training scenes, then time a held-out full-size frame shaded by the
     shader, by the network alone, and by the network with the judge's
-    40 dB fallback."""
+    40 dB fallback. Returns the line; prints it if emit."""
     import ctypes
     import torch
     import srp_gb300
@@ -441,10 +496,13 @@ def run_learned(args):
     torch.cuda.synchronize()
     L.srpGpuResetStats()
     sc.prepare()
+    depth_before = sc.planes()[1]
     sc.render()
     st = srp_gb300.SRPGpuStats()
     L.srpGpuGetStats(ctypes.byref(st))
     frags = st.fragments
+    # pixels the shading stage colours: those whose depth the draw wrote
+    shaded = int((sc.planes()[1] != depth_before).sum())
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
     plain_ms, plain_shade = timed(args.steps)
@@ -485,9 +543,19 @@ def run_learned(args):
         "clocks": clk,
         "gpu_launches": int(st.kernelLaunches),
     }
-    print(json.dumps(line))
+    if shaded and mlp_shade > 0:
+        tpk, tkind = tensor_peak()
+        tflops = shaded * MLP_FLOPS_PER_FRAGMENT / (mlp_shade / 1000.0) / 1e12
+        line["roofline"] = {"bound": "tensor", "achieved": round(tflops, 2), "peak": tpk, "unit": "TFLOP/s",
+                            "frac": round(tflops / tpk, 5), "traffic": None,
+                            "kernel": "learned shading stage (k_shade_learned5), network alone",
+                            "flops_per_frame": shaded * MLP_FLOPS_PER_FRAGMENT, "shaded_pixels": shaded,
+                            "note": f"peak {tkind} (MEASURED_PEAKS.json bf16_tflops)"}
+    if emit:
+        print(json.dumps(line))
     sc.close()
     L.srpGpuMlpFree(net)
+    return line
 
 
 BATCH_LEARNED_WORKLOAD = ("batch-learned: the 4096-scene batch shaded by 8-octave value-noise marble with 16 point "
@@ -509,10 +577,10 @@ def learned_api(L):
     return ctypes.cast(L.srpFsMarble, vp)
 
 
-def run_batch_learned(args):
+def run_batch_learned(args, emit=True):
     """The batch of run_batch with the marble shader: trained on fragments of
     512 other scenes, then timed plain, learned, and learned with the 40 dB
-    per-draw fallback."""
+    per-draw fallback. Returns the line; prints it if emit."""
     import torch
     import srp_gb300
 
@@ -603,10 +671,12 @@ def run_batch_learned(args):
                                         fallback_rate=round(lj.fallbacks / max(lj.draws, 1), 4)),
         "clocks": clk,
     }
-    print(json.dumps(line))
+    if emit:
+        print(json.dumps(line))
     for sc in batchs:
         sc.close()
     L.srpGpuMlpFree(net)
+    return line
 
 
 def main():
@@ -625,6 +695,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default resolve tuning (--workload frame, batch)")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch every kernel directly instead of replaying captured CUDA graphs (srpGpuSetDrawGraphs(0))")
+    ap.add_argument("--frame-only", action="store_true",
+                    help="--workload frame without the batch, learned and batch-learned summaries added to its line")
     args = ap.parse_args()
     if args.workload == "batch":
         return run_reference_batch(args) if args.impl == "reference" else run_batch(args)
@@ -752,17 +824,26 @@ def main():
     h2d = info.vertexBytes + info.indexBytes
     d2h = info.width * info.height * 9
     peak, peak_kind = peaks()
-    # whole frame: vertex + index bytes, framebuffer planes read and written,
-    # texture once (B of the design notes)
-    algo_bytes = (info.vertexBytes + info.indexBytes + info.width * info.height * 9 * 2 + info.textureBytes)
+    # algorithmic bytes of the frame: every vertex and index byte read once,
+    # the colour, depth and stencil planes read and written once (the API
+    # keeps them across draws), the texture read once
+    px = info.width * info.height
+    algo_bytes = info.vertexBytes + info.indexBytes + px * 9 * 2 + info.textureBytes
     frame_gbs = algo_bytes / (total_ms / args.steps / 1000.0) / 1e9
-    # dominant kernel: the resolve stage (per-tile coverage/stencil/depth);
-    # algorithmic bytes per frame = each (tile, item) pair's index and record
-    # (4 + 64 B) + depth and stencil planes read and written + winner plane
-    items = prof.resolveItems / nprof
-    resolve_bytes = items * 68 + info.width * info.height * (5 * 2 + 4)
+    # each stage's share of those bytes; binning moves only intermediate data
+    share = {"vertex": info.vertexBytes, "setup": info.indexBytes, "bin": 0,
+             "resolve": px * 5 * 2, "shade": px * 4 * 2 + info.textureBytes}
     dom = max(stage_ms, key=stage_ms.get)
-    resolve_gbs = resolve_bytes / (stage_ms["resolve"] / 1000.0) / 1e9 if stage_ms["resolve"] > 0 else 0.0
+    items = prof.resolveItems / nprof
+    stage_roof = {}
+    for k, ms in stage_ms.items():
+        gbs = share[k] / (ms / 1000.0) / 1e9 if ms > 0 else 0.0
+        stage_roof[k] = {"ms": round(ms, 4), "algorithmic_bytes": int(share[k]), "achieved": round(gbs, 1),
+                         "frac": round(gbs / peak, 5)}
+    # what the resolve reads and writes beyond its share: a (tile, item)
+    # pair's index and record (4 + 64 B), the winner plane
+    stage_roof["resolve"]["intermediate_bytes"] = int(items * 68 + px * 4)
+    stage_roof["resolve"]["traffic"] = resolve_traffic(args.scale)
     line = {
         "metric": "Mfrag/s", "value": round(value, 3), "unit": "Mfrag/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
@@ -780,16 +861,16 @@ def main():
                 "uploads": "srpGpuVertexBufferCopyDataAsync / srpGpuIndexBufferCopyDataAsync, one wait per frame",
                 "with_reference_copy_calls": round(frags_per_frame / (sum(e2e_sync_times) / len(e2e_sync_times)) / 1e6, 3)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "achieved": round(resolve_gbs, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(resolve_gbs / peak, 5), "traffic": resolve_traffic(args.scale),
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, "
-                                       "profiles/resolve_soup_1080p.md",
-                     "kernel": "k_resolve (all three draws of the frame)",
-                     "algorithmic_bytes_per_frame": int(resolve_bytes),
-                     "ms_per_frame": round(stage_ms["resolve"], 4),
-                     "note": f"peak {peak_kind} (MEASURED_PEAKS.json hbm_gbs); dominant stage this run: {dom}"},
-        "frame_roofline": {"achieved": round(frame_gbs, 1), "unit": "GB/s", "frac": round(frame_gbs / peak, 5),
-                           "algorithmic_bytes": int(algo_bytes)},
+        "roofline": {"bound": "hbm", "achieved": round(frame_gbs, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(frame_gbs / peak, 5), "traffic": frame_traffic(args.scale),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum summed over the frame's "
+                                       "kernels, " + os.path.relpath(FRAME_TRAFFIC_PROFILE, ROOT),
+                     "kernel": "the frame's draw path: every kernel of its three draws, timed as one frame",
+                     "algorithmic_bytes_per_frame": int(algo_bytes),
+                     "basis": "vertex + index bytes + colour/depth/stencil planes read and written + texture",
+                     "dominant_stage": dom,
+                     "note": f"peak {peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+        "stage_roofline": stage_roof,
         "stages_ms_per_frame": {k: round(v, 4) for k, v in stage_ms.items()},
         "stage_launches_per_frame": stage_launches,
     }
@@ -800,9 +881,18 @@ def main():
         line["cpu_baseline"] = {"value": round(r["fragments"] / r["mean_s"] / 1e6, 3), "unit": "Mfrag/s",
                                 "cores": 1, "kind": "port", "host": host_cpu(),
                                 "sample": "5 full frames of the same workload on 1 host core (mean frame time)"}
+    sc.close()
+    if rank == 0 and world == 1 and not args.frame_only:
+        # the other configurations, each on its own scenes, after the frame
+        sub = argparse.Namespace(**vars(args))
+        sub.steps, sub.warmup, sub.scale = min(args.steps, 5), max(args.warmup, 3), 1.0
+        for key, fn in (("batch", run_batch), ("learned", run_learned), ("batch_learned", run_batch_learned)):
+            try:
+                line[key] = fn(sub, emit=False)
+            except Exception as e:  # a failed summary must not hide the frame's line
+                line[key] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0:
         print(json.dumps(line))
-    sc.close()
     if world > 1:
         dist.destroy_process_group()
 

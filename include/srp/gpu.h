@@ -305,6 +305,7 @@ typedef struct SRPGpuStats
 	uint64_t clipOverflows;      /* clipped polygons with more than 6 vertices */
 	uint64_t draws;
 	uint64_t kernelLaunches;     /* kernels launched by the library */
+	uint64_t drawRetries;        /* draws run again after their scratch buffers grew */
 } SRPGpuStats;
 
 /** Read the counters accumulated since the last reset (waits for the GPU). */
@@ -313,6 +314,35 @@ void srpGpuResetStats(void);
 
 /** Tile edge in pixels used by the binning and raster stages (8 or 16). */
 void srpGpuSetTileSize(int tileSize);
+
+/* ----------------------------------------- failure-detection tests */
+
+/* Every wait of a kernel on another block or on the tensor cores (the
+ * look-back of the ordered setup, the mbarrier waits of learned shading) is
+ * bounded: when it runs out, the kernel records a timeout, the draw stops or
+ * falls back, and the error is reported through the message callback. These
+ * calls make that path run, for tests; none has a counterpart in the
+ * reference. */
+
+/** Polls after which a bounded device wait gives up, for the draws issued
+ *  from now on; 0 restores the default (2^24). */
+void srpGpuSetWaitLimit(uint32_t iterations);
+
+#define SRP_GPU_WAIT_TEST_SETUP   1u  /* the ordered setup's first block never publishes its prefix: the
+                                         draw reports "Ordered-compaction wait timed out" and draws nothing */
+#define SRP_GPU_WAIT_TEST_LEARNED 2u  /* learned shading issues no MMAs for its second layer: the draw
+                                         reports the timeout and is shaded again by its own shader */
+/** Withhold the selected signals (SRP_GPU_WAIT_TEST_*) from the draws issued
+ *  from now on, so that the waits depending on them run out; 0 turns it off.
+ *  Combine with a small srpGpuSetWaitLimit to keep the wait short. */
+void srpGpuSetWaitTest(uint32_t flags);
+
+/** The estimate of (tile, primitive) pairs per input primitive with which
+ *  the next draw of each kind sizes its pair buffers; each draw replaces it
+ *  with what it counted. A draw whose pairs exceed the estimate stops before
+ *  its resolve, grows the buffers and runs again (srpGpuStats.drawRetries);
+ *  0 forces that path on the next draw. */
+void srpGpuSetEntryEstimate(double entriesPerPrimitive);
 
 /* ---------------------------------------------------------- profiling */
 

@@ -23,7 +23,7 @@ SRP_GPU_FB_DEVICE = 1
 
 class SRPGpuStats(ctypes.Structure):
     _fields_ = [(n, ctypes.c_uint64) for n in
-                ("fragments", "primitives", "binEntries", "clipOverflows", "draws", "kernelLaunches")]
+                ("fragments", "primitives", "binEntries", "clipOverflows", "draws", "kernelLaunches", "drawRetries")]
 
 
 class SRPGpuDraw(ctypes.Structure):

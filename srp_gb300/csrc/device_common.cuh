@@ -254,8 +254,10 @@ __device__ __forceinline__ float triRecip(const float iw[3], const float l[3])
 	return __fdiv_rn(1.0f, __fadd_rn(__fadd_rn(__fmul_rn(iw[0], l[0]), __fmul_rn(iw[1], l[1])), __fmul_rn(iw[2], l[2])));
 }
 
-/* Bounded spin budget for waits on other blocks. */
+/* Bounded spin budget for waits on other blocks; a draw may set a smaller
+ * one (DrawParams::spinLimit, 0 = this default). */
 constexpr unsigned kSpinLimit = 1u << 24;
+__device__ __forceinline__ unsigned spinBudget(uint32_t limit) { return limit ? limit : kSpinLimit; }
 
 /* Decoupled look-back over a status array whose words hold a 2-bit flag in
  * the top bits (0 not yet published, 1 block aggregate, 2 inclusive prefix)
@@ -266,7 +268,8 @@ constexpr unsigned kSpinLimit = 1u << 24;
  * load latencies. A predecessor that has not published yet is re-read with
  * a bounded spin; on timeout the error bit is set and the walk ends. */
 template <typename T, int W>
-__device__ __forceinline__ T lookBack(const T* status, long long j, int flagShift, T valueMask, unsigned* errors)
+__device__ __forceinline__ T lookBack(const T* status, long long j, int flagShift, T valueMask, unsigned* errors,
+                                      unsigned limit = kSpinLimit)
 {
 	T acc = 0;
 	unsigned spins = 0;
@@ -278,7 +281,7 @@ __device__ __forceinline__ T lookBack(const T* status, long long j, int flagShif
 #pragma unroll
 		for (int k = 0; k < W; ++k) {
 			while ((v[k] >> flagShift) == 0) {
-				if (++spins > kSpinLimit) { atomicOr(errors, kErrSpin); return acc; }
+				if (++spins > limit) { atomicOr(errors, kErrSpin); return acc; }
 				__nanosleep(32);
 				v[k] = *((volatile const T*) (status + (j - k)));
 			}

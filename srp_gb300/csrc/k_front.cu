@@ -721,13 +721,15 @@ __device__ __forceinline__ unsigned long long orderedOffset(const DrawParams& P,
 		const uint32_t aggP = (uint32_t) (blockTotal >> 32), aggE = (uint32_t) blockTotal;
 		unsigned long long prefix = 0;
 		if (bid == 0) {
-			atomicExch(&P.lookback[0], packStatus(2, aggP, aggE));
+			/* a failure-detection test withholds the first prefix: every
+			 * later block's look-back then runs out (kErrSpin) */
+			if (!(P.waitTest & kWaitTestSetup)) atomicExch(&P.lookback[0], packStatus(2, aggP, aggE));
 		} else {
 			atomicExch(&P.lookback[bid], packStatus(1, aggP, aggE));
 			/* prims (bits 32..61) and entries (bits 0..31) summed as one word:
 			 * the entry total stays below 2^32 (checked by the host) */
 			const unsigned long long acc = lookBack<unsigned long long, 16>(
-				P.lookback, (long long) bid - 1, 62, 0x3FFFFFFFFFFFFFFFull, &P.ctr->errors);
+				P.lookback, (long long) bid - 1, 62, 0x3FFFFFFFFFFFFFFFull, &P.ctr->errors, spinBudget(P.spinLimit));
 			const unsigned long long accP = acc >> 32, accE = acc & 0xFFFFFFFFull;
 			if (accE + aggE > 0xFFFFFFFFull || accP + aggP > 0x3FFFFFFFull) atomicOr(&P.ctr->errors, kErrCapacity);
 			atomicExch(&P.lookback[bid], packStatus(2, (uint32_t) (accP + aggP), (uint32_t) (accE + aggE)));

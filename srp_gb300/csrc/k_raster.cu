@@ -870,7 +870,9 @@ __global__ void __launch_bounds__(kLearnThreads, 1) k_shade_learned5(const __gri
 		namedSync(bar, 128);
 		float rgb[3] = { 0.f, 0.f, 0.f };
 		for (int layer = 0; layer < 4; ++layer) {
-			if (gt == 0) {
+			/* a failure-detection test issues nothing for layer 1: its wait
+			 * runs out with no MMA in flight */
+			if (gt == 0 && !(layer == 1 && (P.waitTest & kWaitTestLearned))) {
 				tcFenceAfter();
 				const int K = layer == 0 ? kMlpInPad : 64;
 				const uint32_t w = wAddr + (layer == 0 ? kTcW1 : layer == 1 ? kTcW2 : layer == 2 ? kTcW3 : kTcW4);
@@ -879,7 +881,7 @@ __global__ void __launch_bounds__(kLearnThreads, 1) k_shade_learned5(const __gri
 				/* the counter's answer is awaited here, beside the first layer's MMAs */
 				if (layer == 0) sNext[g] = next;
 			}
-			const bool got = mbarWait(mb, phase);
+			const bool got = mbarWait(mb, phase, P.spinLimit);
 			phase ^= 1u;
 			if (!namedSyncAnd(bar, 128, got)) { ok = false; break; }
 			tcFenceAfter();

@@ -98,8 +98,16 @@ struct DrawParams {
 	float* capture;
 	unsigned long long* captureCount;
 	uint32_t captureCap, captureEvery;
+	/* bounded device waits: polls before a wait gives up (0: the default),
+	 * and the kWaitTest* signals withheld so that a wait runs out (tests of
+	 * failure detection only) */
+	uint32_t spinLimit, waitTest;
 	alignas(16) unsigned char uniform[kMaxUniformBytes];
 };
+
+/* Signals a test can withhold (srpGpuSetWaitTest). */
+constexpr uint32_t kWaitTestSetup = 1u;    /* block 0 of the ordered setup never publishes its prefix */
+constexpr uint32_t kWaitTestLearned = 2u;  /* learned shading issues no MMAs (and no commit) for layer 1 */
 
 /* Fragment-shader id of learned shading (not a user shader). */
 constexpr int kFsLearned = 100;

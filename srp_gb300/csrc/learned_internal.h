@@ -16,8 +16,11 @@ bool learnedPrepare(DrawParams& P, int kind, bool late, uint32_t nDraws, cudaStr
 /* After a learned-shaded draw or pass has been enqueued: waits for the
  * judge, records the statistics and sets redo[d] for every draw whose PSNR
  * is below the threshold (and, with redoDev, a device copy of redo).
- * Returns the number of such draws. */
-uint32_t learnedJudge(uint32_t nDraws, uint8_t* redo, const uint8_t** redoDev, cudaStream_t s);
+ * When the network's kernel ran out of a bounded wait (kErrSpin in ctr's
+ * errors), it reports that and marks every draw for redo. Returns the number
+ * of draws marked. */
+uint32_t learnedJudge(uint32_t nDraws, uint8_t* redo, const uint8_t** redoDev, cudaStream_t s,
+                      const DeviceCounters* ctr);
 
 /* srp_api.cu: error message through the user's callback, and the device id of
  * a host fragment shader (0 if it has none). */

@@ -197,6 +197,9 @@ struct Lib {
 	 * draw of that kind, whose count the host does not wait for */
 	double entryRatio[3] = { 4.0, 64.0, 4.0 };
 	uint32_t bigJobsSeen[3] = { 1024, 0, 1024 };   /* big primitives of the last draw, per kind */
+	/* failure-detection tests: polls before a bounded device wait gives up
+	 * (0 = the kernels' default) and the signals withheld from them */
+	uint32_t spinLimit = 0, waitTest = 0;
 };
 
 Lib g;
@@ -1587,6 +1590,8 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 	P.vsId = vsId;
 	P.fsId = fsId;
 	P.heavyItems = g.tune.heavyItems;
+	P.spinLimit = g.spinLimit;
+	P.waitTest = g.waitTest;
 	P.heavyCtasPerSM = g.tune.heavyCtasPerSM;
 	P.prim = prim;
 	P.start = start;
@@ -1768,6 +1773,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			if (c.clipTris > g.clipPolyCap) { g.clipPolyCap = (uint32_t) std::min<unsigned long long>(c.clipTris * 2, 1u << 30); grew = true; }
 			if (c.tableWords > g.tableCap) { g.tableCap = std::min<unsigned long long>(c.tableWords * 5 / 4 + 1024, 0xFFFFFFFFull); grew = true; }
 			if (!grew) { SRP_ERROR(FN, "Scratch capacity exceeded"); return; }
+			++g.stats.drawRetries;
 			continue;
 		}
 		g.entryRatio[kind] = std::max(0.25, std::min(4096.0, (double) c.entries / (double) (nIn * outPer) * 1.25));
@@ -1783,7 +1789,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 	if (learned) {
 		/* the judge found the network too far from the shader: shade again */
 		uint8_t redo = 0;
-		if (learnedJudge(1, &redo, nullptr, g.stream)) {
+		if (learnedJudge(1, &redo, nullptr, g.stream, P.ctr)) {
 			P.fsId = P.judgeFs;
 			stageBegin();
 			launchShade(P, kind, numTiles, g.stream);
@@ -1965,6 +1971,8 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	P.vsId = lookupVS((void*) sp0->vs->shader);
 	P.fsId = lookupFS((void*) sp0->fs->shader);
 	P.heavyItems = g.tune.heavyItems;
+	P.spinLimit = g.spinLimit;
+	P.waitTest = g.waitTest;
 	P.heavyCtasPerSM = g.tune.heavyCtasPerSM;
 	P.prim = SRP_PRIM_TRIANGLES;
 
@@ -2185,6 +2193,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 			if (c.clipTris > g.clipPolyCap) { g.clipPolyCap = (uint32_t) std::min<unsigned long long>(c.clipTris * 2, 1u << 30); grew = true; }
 			if (c.tableWords > g.tableCap) { g.tableCap = std::min<unsigned long long>(c.tableWords * 5 / 4 + 1024, 0xFFFFFFFFull); grew = true; }
 			if (!grew) { SRP_ERROR(FN, "Scratch capacity exceeded"); return false; }
+			++g.stats.drawRetries;
 			continue;
 		}
 		g.entryRatio[kKindTri] = std::max(0.25, std::min(4096.0, (double) c.entries / (double) nIn * 1.25));
@@ -2200,7 +2209,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 	if (drawn && learned) {
 		std::vector<uint8_t> redo(n);
 		const uint8_t* redoDev = nullptr;
-		if (learnedJudge((uint32_t) n, redo.data(), &redoDev, g.stream)) {
+		if (learnedJudge((uint32_t) n, redo.data(), &redoDev, g.stream, P.ctr)) {
 			P.fsId = P.judgeFs;
 			P.redo = redoDev;
 			stageBegin();
@@ -2469,6 +2478,16 @@ void srpGpuSetTileSize(int tileSize)
 	if (tileSize != kTile) SRP_ERROR("srpGpuSetTileSize", "Only %d-pixel tiles are built into this library", kTile);
 }
 
+void srpGpuSetWaitLimit(uint32_t iterations) { g.spinLimit = iterations; }
+
+void srpGpuSetWaitTest(uint32_t flags) { g.waitTest = flags & (kWaitTestSetup | kWaitTestLearned); }
+
+void srpGpuSetEntryEstimate(double entriesPerPrimitive)
+{
+	const double r = entriesPerPrimitive < 0.0 ? 0.0 : std::min(entriesPerPrimitive, 4096.0);
+	for (double& e : g.entryRatio) e = r;
+}
+
 }  // extern "C"
 
 /* ------------------------------------------- for the fixed-scratch draw */
@@ -2586,6 +2605,8 @@ int fixedDrawPrepare(DrawParams& P, const SRPIndexBuffer* ib, const SRPVertexBuf
 	P.vsId = vsId;
 	P.fsId = fsId;
 	P.heavyItems = g.tune.heavyItems;
+	P.spinLimit = g.spinLimit;
+	P.waitTest = g.waitTest;
 	P.heavyCtasPerSM = g.tune.heavyCtasPerSM;
 	P.prim = prim;
 	P.start = start;

@@ -163,13 +163,29 @@ bool learnedPrepare(DrawParams& P, int kind, bool late, uint32_t nDraws, cudaStr
 	return true;
 }
 
-uint32_t learnedJudge(uint32_t nDraws, uint8_t* redo, const uint8_t** redoDev, cudaStream_t s)
+uint32_t learnedJudge(uint32_t nDraws, uint8_t* redo, const uint8_t** redoDev, cudaStream_t s,
+                      const DeviceCounters* ctr)
 {
 	L.hostJudge.resize(2 * (size_t) nDraws);
 	L.hostMax.resize(nDraws);
+	unsigned int errors = 0;
 	cudaMemcpyAsync(L.hostJudge.data(), L.judge, 2 * sizeof(double) * nDraws, cudaMemcpyDeviceToHost, s);
 	cudaMemcpyAsync(L.hostMax.data(), L.judgeMax, sizeof(unsigned int) * nDraws, cudaMemcpyDeviceToHost, s);
+	cudaMemcpyAsync(&errors, &ctr->errors, sizeof errors, cudaMemcpyDeviceToHost, s);
 	if (!ok(cudaStreamSynchronize(s), "learned shading judge")) return 0;
+	if (errors & kErrSpin) {
+		/* the network's colours are incomplete: every draw is shaded again */
+		learnedError("a tensor-core wait of the learned shading kernel timed out; the draw%s shaded again by "
+		             "its own fragment shader", nDraws > 1 ? "s are" : " is");
+		for (uint32_t d = 0; d < nDraws; ++d) redo[d] = 1;
+		L.stats.draws += nDraws;
+		L.stats.fallbacks += nDraws;
+		if (redoDev) {
+			cudaMemcpyAsync(L.redoDev, redo, nDraws, cudaMemcpyHostToDevice, s);
+			*redoDev = L.redoDev;
+		}
+		return nDraws;
+	}
 	uint32_t nRedo = 0;
 	for (uint32_t d = 0; d < nDraws; ++d) {
 		const double sse = L.hostJudge[2 * d], chans = L.hostJudge[2 * d + 1];

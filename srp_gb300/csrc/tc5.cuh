@@ -84,10 +84,12 @@ __device__ __forceinline__ void mbarInit(uint32_t addr, uint32_t count)
 	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(count) : "memory");
 }
 
-/* Bounded wait for the phase with the given parity to complete. */
-__device__ __forceinline__ bool mbarWait(uint32_t addr, uint32_t parity)
+/* Bounded wait for the phase with the given parity to complete: at most
+ * `limit` polls (0 = kTcSpinLimit). */
+__device__ __forceinline__ bool mbarWait(uint32_t addr, uint32_t parity, uint32_t limit = 0)
 {
-	for (unsigned i = 0; i < kTcSpinLimit; ++i) {
+	const unsigned polls = limit ? limit : kTcSpinLimit;
+	for (unsigned i = 0; i < polls; ++i) {
 		uint32_t done;
 		asm volatile(
 		    "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
