@@ -99,11 +99,18 @@ def build(verbose=False, ptxas_info=False):
     return so
 
 
+def reference_dir():
+    """Where the reference's sources are read from (test infrastructure only):
+    $SRP_REFERENCE, else the read-only checkout of the build machine."""
+    return os.environ.get("SRP_REFERENCE", "/root/reference")
+
+
 def build_oracle():
     """CPU oracle (always) and the reference build (only where its sources are)."""
     _run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "port"])
-    if os.path.isdir("/root/reference/src"):
-        _run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"])
+    ref = reference_dir()
+    if os.path.isdir(os.path.join(ref, "src")):
+        _run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF={ref}"])
 
 
 if __name__ == "__main__":

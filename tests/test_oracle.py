@@ -11,7 +11,7 @@ import pytest
 from oracle_util import manifest, load_golden, oracle_render, compare_planes, hash_cases, plane_digests
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference"
+REF = os.environ.get("SRP_REFERENCE", "/root/reference")
 
 
 @pytest.mark.parametrize("case", manifest(), ids=lambda c: c["name"])
@@ -49,7 +49,7 @@ def test_reference_golden_images(tmp_path):
     against the oracle; the reference matches its golden PNGs within the
     tolerance of its tests (1/255), the oracle matches the reference exactly."""
     from pngio import read_png
-    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "refscenes"])
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "refscenes", f"REF={REF}"])
     d = os.path.join(ROOT, "oracle", "_ref", "refscenes")
     goldens = sorted(glob.glob(os.path.join(REF, "tests", "references", "*", "*.png")))
     assert len(goldens) == 18
