@@ -399,6 +399,85 @@ __device__ __forceinline__ uint32_t tileCount(int minX, int minY, int maxXex, in
 	return (uint32_t) ((maxXex - 1) / kTile - minX / kTile + 1) * (uint32_t) ((maxYex - 1) / kTile - minY / kTile + 1);
 }
 
+/* The inclusive pixel box [x0, x1] x [y0, y1] (x0, y0 >= 0) cut to the
+ * scissor rectangle: a pixel outside it fails the scissor test before any
+ * other test or write (src/raster/fragment.c:63-75), so tiles outside it need
+ * no (tile, item) pair. Returns false when nothing is left. */
+__device__ __forceinline__ bool scissorBox(const DrawState& st, int& x0, int& y0, int& x1, int& y1)
+{
+	if (x1 < x0 || y1 < y0) return false;
+	if (!st.scissorEnabled) return true;
+	if (st.sx1 <= st.sx0 || st.sy1 <= st.sy0) return false;
+	const uint64_t lx = max((uint64_t) x0, st.sx0), hx = min((uint64_t) x1, st.sx1 - 1);
+	const uint64_t ly = max((uint64_t) y0, st.sy0), hy = min((uint64_t) y1, st.sy1 - 1);
+	if (lx > hx || ly > hy) return false;
+	x0 = (int) lx; x1 = (int) hx; y0 = (int) ly; y1 = (int) hy;
+	return true;
+}
+
+/* Bounding boxes of at most this many pixels a side are tested pixel by
+ * pixel at setup. */
+constexpr int kTinyTri = 3;
+
+/* A triangle's bounding box cut to the scissor rectangle. */
+__device__ __forceinline__ bool triScissorBox(const DrawState& st, const TriRaster& R, int& x0, int& y0, int& x1, int& y1)
+{
+	x0 = R.minX; y0 = R.minY; x1 = (int) R.maxX - 1; y1 = (int) R.maxY - 1;
+	return scissorBox(st, x0, y0, x1, y1);
+}
+
+/* Whether a pixel centre of [x0, x1] x [y0, y1] (inside the bounding box)
+ * passes the inside test, walking the box from its first pixel as the
+ * reference does (src/raster/triangle.c:73-111): the same serial fp32 adds
+ * the resolve's exact chain reproduces, so the answer is the resolve's. */
+__device__ __forceinline__ bool triCoversBox(const TriRaster& R, int x0, int y0, int x1, int y1)
+{
+	float row[3] = { R.l0[0], R.l0[1], R.l0[2] };
+	for (int y = (int) R.minY; y <= y1; ++y) {
+		if (y >= y0) {
+			float l[3] = { row[0], row[1], row[2] };
+			for (int x = (int) R.minX; x <= x1; ++x) {
+				if (x >= x0 && insideTri(l, R.flags)) return true;
+#pragma unroll
+				for (int i = 0; i < 3; ++i) l[i] = __fadd_rn(l[i], R.dx[i]);
+			}
+		}
+#pragma unroll
+		for (int i = 0; i < 3; ++i) row[i] = __fadd_rn(row[i], R.dy[i]);
+	}
+	return false;
+}
+
+/* Tiles that get a (tile, triangle) pair: those of the bounding box cut to the
+ * scissor, or none when the triangle covers no pixel centre there. Most
+ * triangles of a dense mesh seen from afar are smaller than a pixel; for a
+ * bounding box of at most kTinyTri x kTinyTri pixels every pixel centre is
+ * tested, so a triangle is dropped only when the resolve would find no
+ * fragment in it either. It keeps its primitive number. Writers emit over
+ * triScissorBox when this count is not zero. */
+__device__ __forceinline__ uint32_t triPairTiles(const DrawState& st, const TriRaster& R)
+{
+	int x0, y0, x1, y1;
+	if (!triScissorBox(st, R, x0, y0, x1, y1)) return 0u;
+	if ((int) R.maxX - (int) R.minX <= kTinyTri && (int) R.maxY - (int) R.minY <= kTinyTri &&
+	    !triCoversBox(R, x0, y0, x1, y1))
+		return 0u;
+	return tileCount(x0, y0, x1 + 1, y1 + 1);
+}
+
+/* Pixel box of a point's pairs: its raster bounds cut to the scissor. */
+__device__ __forceinline__ bool pointPairBox(const DrawState& st, const PointRec& R, int& x0, int& y0, int& x1, int& y1)
+{
+	x0 = R.x0; y0 = R.y0; x1 = R.x1; y1 = R.y1;
+	return scissorBox(st, x0, y0, x1, y1);
+}
+
+__device__ __forceinline__ uint32_t pointPairTiles(const DrawState& st, const PointRec& R)
+{
+	int x0, y0, x1, y1;
+	return pointPairBox(st, R, x0, y0, x1, y1) ? tileCount(x0, y0, x1 + 1, y1 + 1) : 0u;
+}
+
 /* Triangle setup (src/raster/triangle.c:113-238). Returns false if the
  * triangle is culled or degenerate. */
 __device__ bool setupTriangle(const DrawState& st, int W, int H, const SV& v0, const SV& v1, const SV& v2, TriRaster& R,
@@ -577,7 +656,8 @@ __device__ __forceinline__ void writeTri(const DrawParams& P, TriRaster& R, TriA
 				A.id = prim;
 				P.triR[prim] = R;
 				P.triA[prim] = A;
-				emitEntries(P, kKindTri, prim, entry, R.minX, R.minY, (int) R.maxX - 1, (int) R.maxY - 1);
+				int x0, y0, x1, y1;
+				if (nt && triScissorBox(P.st, R, x0, y0, x1, y1)) emitEntries(P, kKindTri, prim, entry, x0, y0, x1, y1);
 			} else atomicOr(&P.ctr->errors, kErrCapacity);
 }
 
@@ -589,7 +669,7 @@ __device__ __forceinline__ void handleTriangle(const DrawParams& P, const SV& a,
 		TriRaster R;
 		TriAttr A;
 		if (!setupTriangle(P.st, P.st.W, P.st.H, a, b, c, R, A)) return;
-		const uint32_t nt = tileCount(R.minX, R.minY, R.maxX, R.maxY);
+		const uint32_t nt = triPairTiles(P.st, R);
 		if (write) writeTri(P, R, A, nt, prim, entry);
 		prim += 1;
 		entry += nt;
@@ -612,12 +692,13 @@ __device__ __forceinline__ void handleTriangle(const DrawParams& P, const SV& a,
 		for (int j = 0; j < 3; ++j) {
 			PointRec R;
 			setupPoint(P.st, *vv[j], R);
-			const uint32_t nt = tileCount(R.x0, R.y0, R.x1 + 1, R.y1 + 1);
+			const uint32_t nt = pointPairTiles(P.st, R);
 			if (write) {
 				if (prim < P.primCap) {
 					R.id = prim;
 					P.points[prim] = R;
-					emitEntries(P, kKindPoint, prim, entry, R.x0, R.y0, R.x1, R.y1);
+					int x0, y0, x1, y1;
+					if (pointPairBox(P.st, R, x0, y0, x1, y1)) emitEntries(P, kKindPoint, prim, entry, x0, y0, x1, y1);
 				} else atomicOr(&P.ctr->errors, kErrCapacity);
 			}
 			prim += 1;
@@ -827,7 +908,7 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup(cons
 			PointRec R;
 			setupPoint(P.st, as.sv[0], R);
 			nPrim = 1;
-			nEnt = tileCount(R.x0, R.y0, R.x1 + 1, R.y1 + 1);
+			nEnt = pointPairTiles(P.st, R);
 		} else if (MODE == kLines) {
 			LineRec L;
 			setupLine(P.st, as.sv[0], as.sv[1], L);
@@ -840,7 +921,7 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup(cons
 				fOk = setupTriangle(P.st, P.st.W, P.st.H, as.sv[0], as.sv[1], as.sv[2], fR, fA);
 				if (fOk) {
 					nPrim = 1;
-					nEnt = tileCount(fR.minX, fR.minY, fR.maxX, fR.maxY);
+					nEnt = triPairTiles(P.st, fR);
 					sR[tid] = fR;
 					sA[tid] = fA;
 				}
@@ -865,7 +946,8 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup(cons
 		if (primBase < P.primCap) {
 			R.id = primBase;
 			P.points[primBase] = R;
-			emitEntries(P, kKindPoint, primBase, entBase, R.x0, R.y0, R.x1, R.y1);
+			int x0, y0, x1, y1;
+			if (pointPairBox(P.st, R, x0, y0, x1, y1)) emitEntries(P, kKindPoint, primBase, entBase, x0, y0, x1, y1);
 		} else atomicOr(&P.ctr->errors, kErrCapacity);
 	} else if (MODE == kLines) {
 		LineRec L;
@@ -960,14 +1042,10 @@ __global__ void k_big_entries(const __grid_constant__ DrawParams P)
 	const uint32_t nJobs = (uint32_t) min(P.ctr->bigJobs, (unsigned long long) P.bigCap);
 	for (uint32_t j = blockIdx.x; j < nJobs; j += gridDim.x) {
 		const uint4 job = P.bigJobs[j];
-		int x0, y0, x1;
-		if (job.z == kKindTri) {
-			const TriRaster& R = P.triR[job.x];
-			x0 = R.minX; y0 = R.minY; x1 = (int) R.maxX - 1;
-		} else {
-			const PointRec& R = P.points[job.x];
-			x0 = R.x0; y0 = R.y0; x1 = R.x1;
-		}
+		/* the pixel box setup counted the job's pairs over */
+		int x0, y0, x1, y1;
+		if (job.z == kKindTri) triScissorBox(P.st, P.triR[job.x], x0, y0, x1, y1);
+		else pointPairBox(P.st, P.points[job.x], x0, y0, x1, y1);
 		const int tx0 = x0 / kTile, ty0 = y0 / kTile, ntx = x1 / kTile - tx0 + 1;
 		for (uint32_t i = threadIdx.x; i < job.w; i += blockDim.x) {
 			const uint32_t e = job.y + i;
