@@ -695,6 +695,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default resolve tuning (--workload frame, batch)")
     ap.add_argument("--no-graphs", action="store_true",
                     help="launch every kernel directly instead of replaying captured CUDA graphs (srpGpuSetDrawGraphs(0))")
+    ap.add_argument("--tile-copies", type=int, default=None,
+                    help="SRP_GPU_TILE_COPY_* bits for srpGpuSetTileCopies (default: the library's)")
     ap.add_argument("--frame-only", action="store_true",
                     help="--workload frame without the batch, learned and batch-learned summaries added to its line")
     args = ap.parse_args()
@@ -723,6 +725,9 @@ def main():
     L.srpGpuSetFramebufferMode(srp_gb300.SRP_GPU_FB_DEVICE)
     if args.no_graphs:
         L.srpGpuSetDrawGraphs(0)
+    if args.tile_copies is not None:
+        L.srpGpuSetTileCopies.argtypes = [ctypes.c_uint]
+        L.srpGpuSetTileCopies(args.tile_copies)
     stream = torch.cuda.Stream()
     L.srpGpuSetStream(ctypes.c_void_p(stream.cuda_stream))
     sc = srp_gb300.Scene(SCENE, SEED + rank, args.scale)
@@ -849,7 +854,7 @@ def main():
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "seed": SEED, "width": info.width, "height": info.height,
-                   "graphs": not args.no_graphs,
+                   "graphs": not args.no_graphs, "tile_copies": args.tile_copies,
                    "triangles": info.inputTriangles, "lines": info.inputLines, "points": info.inputPoints,
                    "fragments_per_frame": frags_per_frame, "l2": "flushed between frames (256 MB write)",
                    "tuning": tuning,

@@ -315,6 +315,16 @@ void srpGpuResetStats(void);
 /** Tile edge in pixels used by the binning and raster stages (8 or 16). */
 void srpGpuSetTileSize(int tileSize);
 
+/** Parts of a single draw (into a framebuffer whose width is a multiple of
+ *  4) whose 8 x 8 framebuffer tiles move between global and shared memory by
+ *  2-D tensor copies of the tensor-memory-access unit (TMA): */
+#define SRP_GPU_TILE_COPY_RESOLVE_LOAD  1u  /* the light-tile resolve loads its depth tile */
+#define SRP_GPU_TILE_COPY_RESOLVE_STORE 2u  /* and stores its depth and winning-fragment tiles */
+#define SRP_GPU_TILE_COPY_SHADE         4u  /* the shading loads, updates and stores its colour tile */
+/** Select them (0, the default: every kernel reads and writes the pixels
+ *  directly). The images are the same whatever the selection. */
+void srpGpuSetTileCopies(unsigned parts);
+
 /* ----------------------------------------- failure-detection tests */
 
 /* Every wait of a kernel on another block or on the tensor cores (the

@@ -20,7 +20,13 @@ LIB = os.path.join(PKG, "lib")
 OBJ = os.path.join(PKG, "_build")
 INC = os.path.join(ROOT, "include")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
-CU_SOURCES = ["k_front.cu", "k_bin.cu", "k_raster.cu", "k_mlp.cu", "srp_api.cu", "srp_fixed.cu", "srp_learned.cu"]
+CU_SOURCES = ["k_front.cu", "k_bin.cu", "k_raster.cu", "k_shade.cu", "k_mlp.cu", "srp_api.cu", "srp_fixed.cu",
+              "srp_learned.cu"]
+# Units whose device arithmetic must round exactly as the reference's fp32
+# code (vertex transform, setup, barycentrics, depth): no multiply-add
+# contraction there. Shading (colour, held to 1/255) and the network's
+# training and inference kernels may contract.
+CONTRACTED = {"k_shade.cu", "k_mlp.cu"}
 C_SOURCES = ["srp_math.c", "imageio.c"]
 
 
@@ -67,7 +73,8 @@ def build(verbose=False, ptxas_info=False):
         s = os.path.join(CSRC, src)
         o = os.path.join(OBJ, src + ".o")
         if _stale(o, [s] + hdrs):
-            cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC",
+            fmad = [] if src in CONTRACTED else ["-fmad=false"]
+            cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", *fmad, "-Xcompiler", "-fPIC",
                    "-I", INC, "-I", CSRC, *zdef, "-c", s, "-o", o]
             if ptxas_info:
                 cmd.insert(2, "-Xptxas=-v")

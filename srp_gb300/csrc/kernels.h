@@ -3,6 +3,7 @@
  * the host-side launch wrappers of each kernel translation unit. */
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "gpu_types.h"
@@ -102,8 +103,21 @@ struct DrawParams {
 	 * and the kWaitTest* signals withheld so that a wait runs out (tests of
 	 * failure detection only) */
 	uint32_t spinLimit, waitTest;
+	/* tile copies by TMA (a single draw into a framebuffer whose width is a
+	 * multiple of 4; tma = 0 otherwise): tensor maps of the depth, winner and
+	 * colour planes, in 8 x 8 boxes of 32-bit pixels. kTmaResolveLoad: the
+	 * light-tile resolve loads its depth tile through them; kTmaResolveStore:
+	 * it stores its depth and winner tiles; kTmaShade: the deferred shading
+	 * loads, updates and stores its colour tile. */
+	uint32_t tma;
+	alignas(64) CUtensorMap tmDepth;
+	alignas(64) CUtensorMap tmWinner;
+	alignas(64) CUtensorMap tmColor;
 	alignas(16) unsigned char uniform[kMaxUniformBytes];
 };
+
+/* Parts of a draw whose framebuffer tiles move by TMA (DrawParams::tma). */
+constexpr uint32_t kTmaResolveLoad = 1u, kTmaResolveStore = 2u, kTmaShade = 4u;
 
 /* Signals a test can withhold (srpGpuSetWaitTest). */
 constexpr uint32_t kWaitTestSetup = 1u;    /* block 0 of the ordered setup never publishes its prefix */

@@ -200,6 +200,11 @@ struct Lib {
 	/* failure-detection tests: polls before a bounded device wait gives up
 	 * (0 = the kernels' default) and the signals withheld from them */
 	uint32_t spinLimit = 0, waitTest = 0;
+	/* the parts of a draw whose framebuffer tiles move by TMA (kTma* bits),
+	 * where the planes allow it; none by default: on the 1080p soup frame
+	 * every selection measured slower than direct access (8 x 8 tiles are
+	 * small copies, and the resolve's staging lowers its occupancy) */
+	uint32_t tma = 0;
 };
 
 Lib g;
@@ -408,6 +413,44 @@ void runDrawSeq(const std::vector<unsigned char>& key, DrawSet& S, cudaStream_t 
 		else shade();
 	}
 	if (fs != g.stream) cudaEventRecord(S.rasterDone, g.stream);
+}
+
+/* cuTensorMapEncodeTiled, taken from the driver through the runtime (the
+ * library does not link the driver library itself); null if unavailable. */
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encodeTiledFn()
+{
+	static EncodeTiledFn fn = nullptr;
+	static bool looked = false;
+	if (!looked) {
+		looked = true;
+		void* p = nullptr;
+		cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+		    q == cudaDriverEntryPointSuccess)
+			fn = (EncodeTiledFn) p;
+		else
+			cudaGetLastError();
+	}
+	return fn;
+}
+
+/* Tensor map of a W x H plane of 32-bit pixels with rows of W pixels, in
+ * 8 x 8 boxes: the tile copies of the resolve and the shading. The plane
+ * must start on 16 bytes and W be a multiple of 4 (16-byte row pitch). */
+bool encodeTileMap(CUtensorMap* m, void* plane, int W, int H, CUtensorMapDataType type)
+{
+	const EncodeTiledFn fn = encodeTiledFn();
+	if (!fn || !plane || W <= 0 || H <= 0 || (W & 3) || ((uintptr_t) plane & 15)) return false;
+	const cuuint64_t dims[2] = { (cuuint64_t) W, (cuuint64_t) H };
+	const cuuint64_t strides[1] = { (cuuint64_t) W * 4 };
+	const cuuint32_t box[2] = { (cuuint32_t) kTile, (cuuint32_t) kTile };
+	const cuuint32_t elem[2] = { 1, 1 };
+	return fn(m, type, 2, plane, dims, strides, box, elem, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+	          CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 /* The key of a draw: its parameters and the host-side launch sizes. */
@@ -1685,6 +1728,10 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		P.tileStart = S.tileStart.as<uint32_t>();
 		P.tileEnd = S.tileEnd.as<uint32_t>();
 		P.winner = S.winner.as<int32_t>();
+		/* framebuffer tiles by TMA where the planes allow it */
+		P.tma = g.tma && encodeTileMap(&P.tmDepth, P.depth, st.W, st.H, CU_TENSOR_MAP_DATA_TYPE_FLOAT32) &&
+		        encodeTileMap(&P.tmWinner, P.winner, st.W, st.H, CU_TENSOR_MAP_DATA_TYPE_INT32) &&
+		        encodeTileMap(&P.tmColor, P.color, st.W, st.H, CU_TENSOR_MAP_DATA_TYPE_UINT32) ? g.tma : 0u;
 
 		/* the whole draw is enqueued before the host looks at any count */
 		uint32_t* sk = nullptr;
@@ -2479,6 +2526,11 @@ void srpGpuSetTileSize(int tileSize)
 }
 
 void srpGpuSetWaitLimit(uint32_t iterations) { g.spinLimit = iterations; }
+
+void srpGpuSetTileCopies(unsigned parts)
+{
+	g.tma = parts & (SRP_GPU_TILE_COPY_RESOLVE_LOAD | SRP_GPU_TILE_COPY_RESOLVE_STORE | SRP_GPU_TILE_COPY_SHADE);
+}
 
 void srpGpuSetWaitTest(uint32_t flags) { g.waitTest = flags & (kWaitTestSetup | kWaitTestLearned); }
 

@@ -128,3 +128,93 @@ def test_overlapped_draws_match_serial_draws(built_library, scene, scale):
         L.srpGpuSetDrawOverlap(1)
         L.srpGpuSetDrawGraphs(1)
         sc.close()
+
+
+TILE_COPY_DEFAULT = 0  # the library's default: no tile copies
+
+
+@pytest.mark.parametrize("scene,scale", [("soup", 0.1), ("stencil", 1.0), ("points", 1.0), ("varyings", 1.0),
+                                         ("sphere", 1.0), ("interp", 1.0)])
+def test_tma_tile_copies_match_direct_access(built_library, scene, scale):
+    """With the tile copies by TMA (the default) the light-tile resolve and
+    the shading move their tiles through shared memory with 2-D tensor
+    copies; with them off they read and write the pixels directly. The
+    images are identical, including framebuffers whose edge tiles reach past
+    the planes (sides not multiples of 8)."""
+    import ctypes
+    import srp_gb300
+    L = srp_gb300.lib()
+    L.srpGpuSetTileCopies.argtypes = [ctypes.c_uint]
+    L.srpGpuSetFramebufferMode(srp_gb300.SRP_GPU_FB_DEVICE)
+    sc = srp_gb300.Scene(scene, 23, scale)
+    try:
+        frames = []
+        for on in (0, 7, 7, 1, 3, 4):
+            L.srpGpuSetTileCopies(on)
+            sc.prepare()
+            sc.render()
+            frames.append([a.copy() for a in sc.planes()])
+        assert L.srpGpuSynchronize() == 0
+        for f in frames[1:]:
+            for a, b in zip(f, frames[0]):
+                assert np.array_equal(a, b)
+    finally:
+        L.srpGpuSetTileCopies(TILE_COPY_DEFAULT)
+        sc.close()
+
+
+def test_tma_tile_copies_on_ragged_framebuffer(built_library):
+    """A 300 x 203 framebuffer (width a multiple of 4 but not of 8, height not
+    a multiple of 8): the right and bottom tiles' TMA boxes reach past the
+    planes. Random triangles with depth test, drawn with and without the
+    tile copies, give the same planes, and the oracle's."""
+    import ctypes
+    import os
+    import subprocess
+    import srp_gb300
+    import srpapi as A
+    L = srp_gb300.lib()
+    L.srpGpuSetTileCopies.argtypes = [ctypes.c_uint]
+    L.srpGpuSetFramebufferMode(srp_gb300.SRP_GPU_FB_COHERENT)
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    subprocess.check_call(["make", "-s", "-C", os.path.join(root, "oracle"), "portlib"])
+    rng = np.random.default_rng(41)
+    n = 3000
+    centre = rng.uniform(-1.2, 1.2, size=(n, 1, 3))
+    verts = np.concatenate([(centre + rng.uniform(-0.08, 0.08, size=(n, 3, 3))).reshape(-1, 3),
+                            rng.uniform(0, 1, size=(3 * n, 3))], axis=1).astype(np.float32)
+
+    def render(srp):
+        srp.new_context()
+        srp.srpDepthTest(True)
+        u = A.StdUniform()
+        u.model = u.view = u.projection = srp.mat4ConstructIdentity()
+        u.passOffset, u.passCount = 3, 3
+        sp = srp.program(u, "srpVsTransform", "srpFsVaryingColor", [(3, A.FLOAT, A.INTERP_PERSPECTIVE)], 12)
+        fb = srp.srpNewFramebuffer(300, 203)
+        vb = srp.vertex_buffer(verts)
+        srp.srpFramebufferClear(fb)
+        srp.srpDrawVertexBuffer(vb, fb, ctypes.byref(sp), A.PRIM_TRIANGLES, 0, 3 * n)
+        planes = srp.planes(fb)
+        srp.srpFreeVertexBuffer(vb)
+        srp.srpFreeFramebuffer(fb)
+        return planes
+
+    gpu = A.Srp(srp_gb300.library_path())
+    port = A.Srp(os.path.join(root, "oracle", "_build", "libsrp_port.so"))
+    try:
+        got = []
+        for on in (7, 0):
+            L.srpGpuSetTileCopies(on)
+            got.append(render(gpu))
+        want = render(port)
+        assert not gpu.errors() and not port.errors()
+    finally:
+        L.srpGpuSetTileCopies(TILE_COPY_DEFAULT)
+        gpu.close()
+        port.close()
+    for a, b in zip(got[0], got[1]):
+        assert np.array_equal(a, b)
+    assert int((want[1] != np.float32(-1.0)).sum()) > 10000
+    compare_planes({"color": got[0][0], "depth_bits": got[0][1].view(np.uint32), "stencil": got[0][2]},
+                   {"color": want[0], "depth_bits": want[1].view(np.uint32), "stencil": want[2]}, "300x203")
