@@ -79,39 +79,33 @@ def replica_throughput(local_ms, local_units, world, device):
     return local_units / (local_ms / 1000.0), local_ms
 
 
-TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "resolve_soup_1080p.md")
 FRAME_TRAFFIC_PROFILE = os.path.join(ROOT, "profiles", "frame_traffic_soup.md")
 
 
-def frame_traffic(scale):
-    """DRAM bytes (read + write) of all the frame's kernels per full-size
-    frame, from the committed ncu capture; None for any other size or when
-    no capture is committed."""
+def profile_figure(key, scale):
+    """A per-frame DRAM byte count of the full-size frame from the committed
+    ncu summary (cold-cache bytes of each kernel captured on the half-size
+    frame, scaled); None for any other size or when it is missing."""
     if scale != 1.0:
         return None
     try:
         with open(FRAME_TRAFFIC_PROFILE) as f:
             for line in f:
-                if line.startswith("traffic_bytes_per_frame:"):
-                    return int(line.split(":", 1)[1])
+                if line.startswith(key + ":"):
+                    return int(float(line.split(":", 1)[1]))
     except OSError:
         pass
     return None
+
+
+def frame_traffic(scale):
+    """DRAM bytes (read + write) of all the frame's kernels per frame."""
+    return profile_figure("traffic_bytes_per_frame", scale)
 
 
 def resolve_traffic(scale):
-    """DRAM bytes (read + write) of the resolve stage per full-size frame, from
-    the committed ncu capture; None for any other size."""
-    if scale != 1.0:
-        return None
-    try:
-        with open(TRAFFIC_PROFILE) as f:
-            for line in f:
-                if line.startswith("traffic_bytes_per_frame:"):
-                    return int(line.split(":", 1)[1])
-    except OSError:
-        pass
-    return None
+    """DRAM bytes (read + write) of the resolve stage's kernels per frame."""
+    return profile_figure("resolve_traffic_bytes_per_frame", scale)
 
 
 class ClockSampler:
@@ -411,6 +405,77 @@ def run_batch(args, emit=True):
 
 LEARNED_WORKLOAD = ("learned: 2.0M-triangle geodesic-sphere soup at 1920x1080 shaded by 8-octave value-noise "
                     "marble with 16 point lights (srpFsMarble), against its learned MLP stand-in")
+# the 32 training scenes' size: about 4M shaded fragments in all
+LEARNED_CAPTURE_SCALE = 0.24
+
+
+def capture(L, net, marble, scenes, scale):
+    """Every pixel the marble shader shades in `scenes` training scenes
+    (seeds 1000 on, none of them the held-out frame's) becomes a sample of
+    `net`."""
+    import srp_gb300
+    L.srpGpuMlpCapture(net, marble, 1)
+    for i in range(scenes):
+        sc = srp_gb300.Scene("msoup", 1000 + i, scale)
+        sc.prepare()
+        sc.render()
+        sc.close()
+    L.srpGpuMlpCapture(None, None, 0)
+
+
+def covered_psnr(img, ref, covered):
+    """PSNR (dB) over the covered pixels of packed RGBA8 planes, channels in [0, 1]."""
+    import numpy as np
+    def rgb(c):
+        c = c[covered].astype(np.int64)
+        return np.stack([(c >> 24) & 255, (c >> 16) & 255, (c >> 8) & 255], -1) / 255.0
+    mse = float(((rgb(img) - rgb(ref)) ** 2).mean())
+    return round(10.0 * math.log10(1.0 / mse), 2) if mse > 0 else None
+
+
+def learned_quality(L, marble, net, scale):
+    """PSNR of the held-out frame over its covered pixels against the 8-octave
+    marble shader's own image: for the trained network (no fallback), for no
+    network (every pixel the reference's mean colour), for the one-octave
+    level of detail of the shader (msoup_lod), and for networks trained on
+    fewer steps or fewer fragments."""
+    import numpy as np
+    import srp_gb300
+
+    def frame(name, learned_net):
+        sc = srp_gb300.Scene(name, SEED, scale)
+        try:
+            if learned_net:
+                L.srpGpuSetLearnedShading(marble, learned_net, 0.0, 64)
+            sc.prepare()
+            sc.render()
+            return [a.copy() for a in sc.planes()]
+        finally:
+            L.srpGpuSetLearnedShading(None, None, 0.0, 0)
+            sc.close()
+
+    ref = frame("msoup", None)
+    covered = ref[1] != ref[1][0]
+    c = ref[0][covered].astype(np.int64)
+    mean = [int(round(float(((c >> s) & 255).mean()))) for s in (24, 16, 8)]
+    const = np.full_like(ref[0], (mean[0] << 24) | (mean[1] << 16) | (mean[2] << 8) | 255)
+    out = {"covered_pixels": int(covered.sum()),
+           "network": covered_psnr(frame("msoup", net)[0], ref[0], covered),
+           "constant_colour": covered_psnr(const, ref[0], covered),
+           "one_octave_shader": covered_psnr(frame("msoup_lod", None)[0], ref[0], covered)}
+    sweep = []
+    for scenes, steps in ((32, 500), (32, 1500), (32, 6000), (8, 3000), (16, 3000)):
+        n2 = L.srpGpuMlpCreate(11, 4 << 20)
+        try:
+            capture(L, n2, marble, scenes, LEARNED_CAPTURE_SCALE)
+            samples = L.srpGpuMlpSampleCount(n2)
+            L.srpGpuMlpTrain(n2, steps, 16384, 2e-3)
+            sweep.append({"scenes": scenes, "samples": samples, "steps": steps,
+                          "psnr_db": covered_psnr(frame("msoup", n2)[0], ref[0], covered)})
+        finally:
+            L.srpGpuMlpFree(n2)
+    out["network_sweep"] = sweep
+    return out
 
 
 class LearnedStats(ctypes.Structure):
@@ -450,15 +515,10 @@ def run_learned(args, emit=True):
     stream = torch.cuda.Stream()
     L.srpGpuSetStream(ctypes.c_void_p(stream.cuda_stream))
     net = L.srpGpuMlpCreate(7, 4 << 20)
-    # training data: every shaded pixel of 32 smaller scenes (other seeds)
+    # training data: every shaded pixel of 32 smaller scenes (other seeds),
+    # about 4M fragments
     t0 = time.perf_counter()
-    L.srpGpuMlpCapture(net, marble, 1)
-    for i in range(32):
-        sc = srp_gb300.Scene("msoup", 1000 + i, 0.12)
-        sc.prepare()
-        sc.render()
-        sc.close()
-    L.srpGpuMlpCapture(None, None, 0)
+    capture(L, net, marble, 32, LEARNED_CAPTURE_SCALE)
     samples = L.srpGpuMlpSampleCount(net)
     capture_s = time.perf_counter() - t0
     steps, batch = args.train_steps, 16384
@@ -528,7 +588,8 @@ def run_learned(args, emit=True):
         "warmup": args.warmup, "ms_per_step": round(judged_ms, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16 (network), f32 (rest)", "data": "synthetic",
         "config": {"workload": LEARNED_WORKLOAD, "seed": SEED, "fragments_per_frame": frags,
-                   "training": {"scenes": 32, "samples": samples, "capture_s": round(capture_s, 2),
+                   "training": {"scenes": 32, "scene_scale": LEARNED_CAPTURE_SCALE, "samples": samples,
+                                "capture_s": round(capture_s, 2),
                                 "steps": steps, "batch": batch, "train_s": round(train_s, 2),
                                 "final_batch_mse": round(final_mse, 6)}},
         "plain": {"ms_per_frame": round(plain_ms, 4), "Mfrag_per_s": mfr(plain_ms), "shade_ms": round(plain_shade, 4)},
@@ -543,6 +604,7 @@ def run_learned(args, emit=True):
         "clocks": clk,
         "gpu_launches": int(st.kernelLaunches),
     }
+    line["quality_psnr_db"] = learned_quality(L, marble, net, args.scale)
     if shaded and mlp_shade > 0:
         tpk, tkind = tensor_peak()
         tflops = shaded * MLP_FLOPS_PER_FRAGMENT / (mlp_shade / 1000.0) / 1e12

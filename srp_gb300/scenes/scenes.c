@@ -1218,6 +1218,16 @@ static void buildMSoup(Scene* s, Rng* rng)
 	s->draws = 1;
 }
 
+/* The marble soup with the marble's noise cut to its first octave: the
+ * same geometry, camera and lights for a given seed, shaded by the cheap
+ * level of detail of the same procedural shader. The baseline that the
+ * learned stand-in of the 8-octave shader is measured against. */
+static void buildMSoupLod(Scene* s, Rng* rng)
+{
+	buildMSoup(s, rng);
+	s->uni[0].marbleOctaves = 1;
+}
+
 /* One scene of the batched workload: a single mesh of random triangles
  * (log-uniform 12 to 200k of them) in its own framebuffer (each side
  * log-uniform 64 to 1024), random camera, textured Blinn-Phong with one
@@ -1472,6 +1482,7 @@ static const SceneDef DEFS[] = {
 	{ "varyings", buildVaryings },
 	{ "bscene", buildBScene },
 	{ "msoup", buildMSoup },
+	{ "msoup_lod", buildMSoupLod },
 	{ "bmscene", buildBMScene },
 };
 

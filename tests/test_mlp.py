@@ -304,3 +304,70 @@ def test_learned_shading_in_a_batch(built_library):
             sc.close()
         net.close()
     assert L.srpGpuSynchronize() == 0
+
+
+def covered_psnr(img, ref, covered):
+    """PSNR (dB) over the covered pixels of two packed RGBA8 colour planes,
+    channels in [0, 1]."""
+    def rgb(c):
+        c = c[covered].astype(np.int64)
+        return np.stack([(c >> 24) & 255, (c >> 16) & 255, (c >> 8) & 255], -1) / 255.0
+    mse = float(((rgb(img) - rgb(ref)) ** 2).mean())
+    return 10.0 * np.log10(1.0 / mse) if mse > 0 else float("inf")
+
+
+@pytest.mark.gpu
+def test_trained_network_gain_over_the_method_without_it(built_library):
+    """What the trained network gains. On a held-out scene the image of the
+    8-octave marble shader is the reference; PSNR is taken over the covered
+    pixels for three stand-ins of the shader: the trained network; no
+    network, every pixel the reference's mean colour (the best constant);
+    and the cheap level of detail, the same shader with one noise octave.
+    The network must beat the constant clearly. It does not beat the
+    one-octave shader: a 3 x 64 network over 6 encoding bands cannot follow
+    8 octaves of noise, which is why the judge sends such draws back."""
+    import srp_gb300
+    L, S = srp_gb300.lib(), srp_gb300.scenes()
+    L.srpGpuSetFramebufferMode(1)
+    vp = ctypes.c_void_p
+    L.srpGpuMlpCapture.argtypes = [vp, vp, ctypes.c_uint32]
+    L.srpGpuSetLearnedShading.argtypes = [vp, vp, ctypes.c_float, ctypes.c_uint32]
+    marble = ctypes.cast(L.srpFsMarble, vp)
+    net = Net(capacity=3 << 20)
+    try:
+        L.srpGpuMlpCapture(net.m, marble, 1)
+        for seed in range(1000, 1016):
+            sc = srp_gb300.Scene("msoup", seed, 0.24)
+            sc.prepare()
+            sc.render()
+            sc.close()
+        L.srpGpuMlpCapture(None, None, 0)
+        assert net.L.srpGpuMlpSampleCount(net.m) > 2000000
+        assert net.L.srpGpuMlpTrain(net.m, 3000, 16384, 2e-3) >= 0
+        images = {}
+        for name, learned in (("msoup", False), ("msoup", True), ("msoup_lod", False)):
+            sc = srp_gb300.Scene(name, 1, 0.25)
+            try:
+                if learned:
+                    L.srpGpuSetLearnedShading(marble, net.m, 0.0, 64)
+                sc.prepare()
+                sc.render()
+                images[(name, learned)] = sync_planes(S, sc.fb)
+            finally:
+                L.srpGpuSetLearnedShading(None, None, 0.0, 0)
+                sc.close()
+    finally:
+        net.close()
+    assert L.srpGpuSynchronize() == 0
+    ref = images[("msoup", False)]
+    covered = ref[1] != ref[1][0]
+    assert covered.sum() > 200000
+    c = ref[0][covered].astype(np.int64)
+    mean = [int(round(float(((c >> s) & 255).mean()))) for s in (24, 16, 8)]
+    const = np.full_like(ref[0], (mean[0] << 24) | (mean[1] << 16) | (mean[2] << 8) | 255)
+    psnr_net = covered_psnr(images[("msoup", True)][0], ref[0], covered)
+    psnr_const = covered_psnr(const, ref[0], covered)
+    psnr_lod = covered_psnr(images[("msoup_lod", False)][0], ref[0], covered)
+    print(f"held-out PSNR: network {psnr_net:.2f} dB, constant {psnr_const:.2f} dB, one octave {psnr_lod:.2f} dB")
+    assert psnr_net > psnr_const + 3.0, (psnr_net, psnr_const, psnr_lod)
+    assert psnr_lod > psnr_net, (psnr_net, psnr_const, psnr_lod)
