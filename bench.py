@@ -9,10 +9,13 @@ followed by 100k lines and 100k points -- three srp draw calls.
           draws are timed with CUDA events on the library's stream, the L2 is
           flushed and the framebuffer re-initialised between frames, outside
           the events.
-  e2e     the same frame through the public API from host memory: the vertex
-          and index bytes are copied in with srpVertexBufferCopyData /
-          srpIndexBufferCopyData (uploaded by the draw), and the framebuffer
-          planes are read back to the host, all inside the timed region.
+  e2e     the same frame through the public API from host memory, frames
+          back to back: each frame copies its vertex and index bytes in with
+          srpGpuVertexBufferCopyDataAsync / srpGpuIndexBufferCopyDataAsync and
+          reads its framebuffer planes back with srpGpuFramebufferSyncAsync,
+          all inside the timed region, which ends with srpGpuSynchronize.
+          Beside it: one wait per frame, and the reference's own copy calls
+          (srpVertexBufferCopyData / srpIndexBufferCopyData).
 A fragment is a pixel that passed coverage and the scissor test (before depth
 and stencil), counted the same way by the CPU oracle.
 
@@ -108,52 +111,141 @@ def resolve_traffic(scale):
     return profile_figure("resolve_traffic_bytes_per_frame", scale)
 
 
+# NVML clock-event reason bits (nvml.h, nvmlClocksEventReason*)
+NVML_REASONS = [(0x8, "hw_slowdown"), (0x40, "hw_thermal_slowdown"), (0x20, "sw_thermal_slowdown"),
+                (0x4, "sw_power_cap"), (0x80, "hw_power_brake_slowdown")]
+
+
+def clock_sampler_main(argv):
+    """The clock-sampling child process: reads the SM clock, its maximum and
+    the clock-event reasons of one GPU through NVML (read-only queries) every
+    `period` seconds and prints `monotonic_s,sm_mhz,max_mhz,reasons,power_mw`
+    lines until killed. Exits 3 when NVML cannot be used."""
+    bus, index, period = argv[0], int(argv[1]), float(argv[2])
+    try:
+        nvml = ctypes.CDLL("libnvidia-ml.so.1")
+        if nvml.nvmlInit_v2() != 0:
+            sys.exit(3)
+        h = ctypes.c_void_p()
+        if not bus or nvml.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(h)) != 0:
+            if nvml.nvmlDeviceGetHandleByIndex_v2(index, ctypes.byref(h)) != 0:
+                sys.exit(3)
+        reasons_fn = getattr(nvml, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nvml.nvmlDeviceGetCurrentClocksThrottleReasons
+    except (OSError, AttributeError):
+        sys.exit(3)
+    sm, mx, rs, pw = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong(), ctypes.c_uint()
+    i = 0
+    while True:
+        t = time.monotonic()
+        ok = nvml.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(sm)) == 0  # NVML_CLOCK_SM
+        ok = ok and nvml.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0
+        ok = ok and reasons_fn(h, ctypes.byref(rs)) == 0
+        if i % 20 == 0 and nvml.nvmlDeviceGetPowerUsage(h, ctypes.byref(pw)) != 0:
+            pw.value = 0
+        if ok:
+            sys.stdout.write(f"{t:.6f},{sm.value},{mx.value},{rs.value},{pw.value}\n")
+            sys.stdout.flush()
+        i += 1
+        time.sleep(period)
+
+
 class ClockSampler:
-    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+    """Samples the SM clock and the throttle reasons of the GPU while the
+    bench runs: a child process polls NVML every millisecond (nvidia-smi's
+    100 ms loop where NVML cannot be loaded). start() returns once the first
+    sample is in; begin() and end() mark the timed region, and stop() reports
+    the samples taken inside it."""
 
     def __init__(self, index):
         self.index, self.samples, self.proc = index, [], None
+        self.t0 = self.t1 = None
+        self.source = None
+        self.first = threading.Event()
+
+    def _bus_id(self):
+        try:
+            import torch
+            p = torch.cuda.get_device_properties(self.index)
+            return f"{p.pci_domain_id:08X}:{p.pci_bus_id:02X}:{p.pci_device_id:02X}.0"
+        except Exception:
+            return ""
 
     def start(self):
+        cmd = [sys.executable, os.path.abspath(__file__), "--clock-sampler", self._bus_id(), str(self.index), "0.001"]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.source = "nvml"
+            self.thread = threading.Thread(target=self._read_nvml, daemon=True)
+            self.thread.start()
+            self.first.wait(timeout=10)
+            if self.proc.poll() is not None:
+                self._start_smi()
+                self.first.wait(timeout=10)
+        except Exception:
+            self.proc, self.source = None, None
+
+    def _start_smi(self):
         q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
-        try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
-                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
-            self.thread.start()
-        except Exception:
-            self.proc = None
+        self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                      "--format=csv,noheader,nounits", "-lms", "100"],
+                                     stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        self.source = "nvidia-smi"
+        self.thread = threading.Thread(target=self._read_smi, daemon=True)
+        self.thread.start()
 
-    def _read(self):
+    def _read_nvml(self):
         for line in self.proc.stdout:
-            self.samples.append([x.strip() for x in line.split(",")])
+            try:
+                t, sm, mx, rs, pw = line.strip().split(",")
+                bits = int(rs)
+                self.samples.append((float(t), float(sm), float(mx),
+                                     [n for b, n in NVML_REASONS if bits & b], float(pw) / 1000.0))
+                self.first.set()
+            except ValueError:
+                pass
+
+    def _read_smi(self):
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.proc.stdout:
+            s = [x.strip() for x in line.split(",")]
+            try:
+                self.samples.append((time.monotonic(), float(s[0]), float(s[1]),
+                                     [n for n, v in zip(names, s[3:7]) if v.lower().startswith("active")],
+                                     float(s[2])))
+                self.first.set()
+            except (ValueError, IndexError):
+                pass
+
+    def begin(self):
+        self.t0 = time.monotonic()
+
+    def end(self):
+        self.t1 = time.monotonic()
 
     def stop(self):
+        if self.t1 is None:
+            self.end()
         if self.proc:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except Exception:
                 self.proc.kill()
-        sm = []
-        mx = 0.0
-        reasons = set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for s in self.samples:
-            try:
-                sm.append(float(s[0]))
-                mx = max(mx, float(s[1]))
-                for n, v in zip(names, s[3:7]):
-                    if v.lower().startswith("active"):
-                        reasons.add(n)
-            except Exception:
-                pass
-        sm.sort()
-        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx or None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+            self.thread.join(timeout=5)
+        t0 = self.t0 if self.t0 is not None else float("-inf")
+        inside = [x for x in list(self.samples) if t0 <= x[0] <= self.t1]
+        sm = sorted(x[1] for x in inside)
+        power = sorted(x[4] for x in inside if x[4] > 0)
+        reasons = sorted({r for x in inside for r in x[3]})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None,
+                "sm_max_mhz": max((x[2] for x in inside), default=None),
+                "sm_min_mhz": sm[0] if sm else None,
+                "power_w": power[len(power) // 2] if power else None,
+                "reasons": reasons, "samples": len(sm), "source": self.source,
+                "window_ms": round((self.t1 - self.t0) * 1e3, 2) if self.t0 is not None else None}
 
 
 def host_cpu():
@@ -303,6 +395,7 @@ def run_batch(args, emit=True):
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
     times = []
+    clocks.begin()
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
             flush.fill_(1.0)
@@ -314,6 +407,7 @@ def run_batch(args, emit=True):
             e1.record(stream)
         stream.synchronize()
         times.append(e0.elapsed_time(e1))
+    clocks.end()
     st = srp_gb300.SRPGpuStats()
     L.srpGpuGetStats(ctypes.byref(st))
     frags = st.fragments / max(args.steps, 1)
@@ -565,6 +659,7 @@ def run_learned(args, emit=True):
     shaded = int((sc.planes()[1] != depth_before).sum())
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
+    clocks.begin()
     plain_ms, plain_shade = timed(args.steps)
     L.srpGpuSetLearnedShading(marble, net, 0.0, 64)
     for _ in range(2):
@@ -702,6 +797,7 @@ def run_batch_learned(args, emit=True):
     frags = st.fragments
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
+    clocks.begin()
     plain_ms = timed()
     L.srpGpuSetLearnedShading(marble, net, 0.0, 64)
     L.srpGpuResetLearnedStats()
@@ -830,6 +926,7 @@ def main():
     torch.cuda.synchronize()
     clocks.start()
     times = []
+    clocks.begin()
     t_wall0 = time.perf_counter()
     for _ in range(args.steps):
         with torch.cuda.stream(stream):
@@ -848,6 +945,7 @@ def main():
         times.append(e0.elapsed_time(e1))
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall0
+    clocks.end()
     L.srpGpuGetStats(ctypes.byref(st0))
     frags_per_frame = st0.fragments / max(args.steps, 1)
     launches = st0.kernelLaunches
@@ -871,6 +969,26 @@ def main():
         return ts
     e2e_times = e2e_frames(sc.upload_async)
     e2e_sync_times = e2e_frames(sc.upload)
+
+    # Frames back to back through the same calls with one srpGpuSynchronize at
+    # the end (the headline e2e): every frame still uploads its vertex and
+    # index buffers from host memory and downloads its framebuffer, but frame
+    # n+1's uploads and front stages run beside frame n's resolve, shading and
+    # download.
+    def e2e_stream(nframes):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(nframes):
+            sc.upload_async()
+            sc.prepare()
+            frame()
+            sc.sync_async()
+        if L.srpGpuSynchronize() != 0:
+            raise RuntimeError("srpGpuSynchronize failed after the streamed frames")
+        return time.perf_counter() - t0
+    e2e_stream(2)  # untimed warm-up
+    n_stream = max(10, args.steps)
+    e2e_stream_s = e2e_stream(n_stream) / n_stream
     # per-stage device time (CUDA events inside the library) on separate frames
     L.srpGpuSetProfiling(1)
     L.srpGpuResetProfile()
@@ -923,9 +1041,13 @@ def main():
                    "frames_per_s": round(args.steps / (total_ms / 1000.0), 2),
                    "mtri_per_s": round(info.inputTriangles * args.steps / (total_ms / 1000.0) / 1e6, 2)},
         "clocks": clk,
-        "e2e": {"value": round(frags_per_frame / e2e_s / 1e6, 3), "unit": "Mfrag/s",
+        "e2e": {"value": round(frags_per_frame / e2e_stream_s / 1e6, 3), "unit": "Mfrag/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "uploads": "srpGpuVertexBufferCopyDataAsync / srpGpuIndexBufferCopyDataAsync, one wait per frame",
+                "frames": n_stream,
+                "calls": "per frame srpGpuVertexBufferCopyDataAsync / srpGpuIndexBufferCopyDataAsync, "
+                         "framebuffer fill, draws, srpGpuFramebufferSyncAsync; one srpGpuSynchronize after all frames",
+                "one_wait_per_frame": round(frags_per_frame / e2e_s / 1e6, 3),
+                "one_wait_per_frame_ms": round(e2e_s * 1e3, 3),
                 "with_reference_copy_calls": round(frags_per_frame / (sum(e2e_sync_times) / len(e2e_sync_times)) / 1e6, 3)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": round(frame_gbs, 1), "peak": peak, "unit": "GB/s",
@@ -965,4 +1087,7 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "--clock-sampler":
+        clock_sampler_main(sys.argv[2:])
+    else:
+        main()

@@ -137,12 +137,9 @@ struct Lib {
 	cudaEvent_t rsEvent = nullptr;
 	/* vertex and index uploads run on copyStream, so that neither the
 	 * resolves nor the shading wait for uploads of later draws. A stage that
-	 * reads a buffer waits for the buffer's upload event. Before an upload
-	 * the copy stream waits for the draws queued since it last did
-	 * (frontReads: on the sets' front streams, streamReads: on `stream`). */
+	 * reads a buffer waits for the buffer's upload event. An upload itself
+	 * waits for nothing (copyStreamReady). */
 	cudaStream_t copyStream = nullptr;
-	cudaEvent_t copyGateFront = nullptr, copyGateStream = nullptr;
-	bool frontReads = false, streamReads = false;
 	unsigned long long uploadSeq = 0;
 	/* srpGpuFramebufferSyncAsync copies on downloadStream, after the event of
 	 * the draw or pass that last wrote the framebuffer (one of writeEvents,
@@ -230,8 +227,6 @@ bool ensureInit(const char* fn)
 	    !cudaOk(cudaStreamCreateWithFlags(&g.resolveStream, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
 	    !cudaOk(cudaEventCreateWithFlags(&g.rsEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 	    !cudaOk(cudaStreamCreateWithFlags(&g.copyStream, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
-	    !cudaOk(cudaEventCreateWithFlags(&g.copyGateFront, cudaEventDisableTiming), fn, "cudaEventCreate") ||
-	    !cudaOk(cudaEventCreateWithFlags(&g.copyGateStream, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 	    !cudaOk(cudaStreamCreateWithFlags(&g.downloadStream, cudaStreamNonBlocking), fn, "cudaStreamCreate")) return false;
 	for (cudaEvent_t& e : g.writeEvents)
 		if (!cudaOk(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), fn, "cudaEventCreate")) return false;
@@ -592,24 +587,15 @@ static void markUpload(cudaEvent_t& ready, bool& readyOwned, bool& pending, unsi
 	seq = ++g.uploadSeq;
 }
 
-/* The copy stream, made to wait first for the draws queued since it last
- * did, which may still read the buffers it is about to overwrite. */
-static cudaStream_t copyStreamReady()
-{
-	if (g.frontReads) {
-		for (DrawSet& S : g.sets) {
-			cudaEventRecord(g.copyGateFront, S.front);
-			cudaStreamWaitEvent(g.copyStream, g.copyGateFront, 0);
-		}
-		g.frontReads = false;
-	}
-	if (g.streamReads) {
-		cudaEventRecord(g.copyGateStream, g.stream);
-		cudaStreamWaitEvent(g.copyStream, g.copyGateStream, 0);
-		g.streamReads = false;
-	}
-	return g.copyStream;
-}
+/* The stream of vertex and index uploads. An upload need not wait for the
+ * draws queued before it: only the index-range, vertex, clip pre-pass and
+ * setup kernels read those buffers, all of them before the draw's setup
+ * counters are copied, and every draw call (single draws, multi-draw passes,
+ * the fixed-scratch draw) waits on the host for those counters before it
+ * returns. So when an upload is issued no earlier draw still reads the
+ * buffer, and the next frame's uploads run beside this frame's resolve and
+ * shading. */
+static cudaStream_t copyStreamReady() { return g.copyStream; }
 
 /* ------------------------------------------------------ gathered copies */
 
@@ -1790,8 +1776,6 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		if (fs != g.stream) cudaStreamWaitEvent(fs, S.rasterDone, 0);
 		if (vb->ready) cudaStreamWaitEvent(fs, vb->ready, 0);
 		if (ib && ib->ready && !lateIb) cudaStreamWaitEvent(fs, ib->ready, 0);
-		if (fs != g.stream) g.frontReads = true;
-		else g.streamReads = true;
 		runDrawSeq(graphKey(P, { (unsigned long long) kind, late, ib != nullptr, start, count, vb->nVertices, blocks,
 		                         keyBits, numTiles, g.bigJobsSeen[kind], (unsigned long long) (uintptr_t) g.stream,
 		                         (unsigned long long) (uintptr_t) fs, (unsigned long long) (uintptr_t) rs }),
@@ -2119,8 +2103,6 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 			if (ib) ib->pending = false;
 		}
 		if (latest) cudaStreamWaitEvent(fs, latest, 0);
-		if (fs != g.stream) g.frontReads = true;
-		else g.streamReads = true;
 	}
 	/* descriptors and prefix sums go up on the front stream, ahead of the head */
 	cudaMemcpyAsync(S.passDesc.ptr, desc, n * sizeof(DrawDesc), cudaMemcpyHostToDevice, fs);
@@ -2685,7 +2667,6 @@ int fixedDrawPrepare(DrawParams& P, const SRPIndexBuffer* ib, const SRPVertexBuf
 	/* the uploads of its buffers, on the copy stream */
 	if (vb->ready) cudaStreamWaitEvent(g.stream, vb->ready, 0);
 	if (ib && ib->ready) cudaStreamWaitEvent(g.stream, ib->ready, 0);
-	g.streamReads = true;
 	info.nIn = nIn;
 	info.outPer = isTri(prim) && mode != SRP_POLYGON_MODE_FILL ? 3 : 1;
 	info.numTiles = (uint32_t) st.tilesX * (uint32_t) st.tilesY;

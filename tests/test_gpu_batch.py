@@ -307,3 +307,71 @@ def test_overlapped_passes_match_serial_passes(built_library):
         for sc in scenes:
             sc.close()
     assert L.srpGpuSynchronize() == 0
+
+
+def test_async_uploads_into_buffers_earlier_draws_read(built_library):
+    """Stream-ordered uploads do not wait for earlier draws: every draw call
+    returns only after its setup has read the vertex and index buffers. Three
+    frames drawn from one vertex buffer and one index buffer, each refilled
+    with srpGpu*CopyDataAsync before its draw, with one srpGpuSynchronize at
+    the end, give the images of the synchronous calls."""
+    import srp_gb300
+    import srpapi as A
+    L = srp_gb300.lib()
+    L.srpGpuVertexBufferCopyDataAsync.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_void_p]
+    L.srpGpuIndexBufferCopyDataAsync.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p]
+    L.srpGpuFramebufferSyncAsync.argtypes = [ctypes.c_void_p]
+    L.srpGpuFramebufferSync.argtypes = [ctypes.c_void_p]
+    rng = np.random.default_rng(77)
+    n, W, H = 20000, 640, 360
+    frames = []
+    for _ in range(3):
+        centre = rng.uniform(-1.1, 1.1, size=(n, 1, 3))
+        verts = np.concatenate([(centre + rng.uniform(-0.06, 0.06, size=(n, 3, 3))).reshape(-1, 3),
+                                rng.uniform(0, 1, size=(3 * n, 3))], axis=1).astype(np.float32)
+        frames.append((verts, rng.permutation(3 * n).astype(np.uint32)))
+    srp = A.Srp(srp_gb300.library_path())
+    L.srpGpuSetFramebufferMode(srp_gb300.SRP_GPU_FB_DEVICE)
+    try:
+        srp.srpDepthTest(True)
+        u = A.StdUniform()
+        u.model = u.view = u.projection = srp.mat4ConstructIdentity()
+        u.passOffset, u.passCount = 3, 3
+        sp = srp.program(u, "srpVsTransform", "srpFsVaryingColor", [(3, A.FLOAT, A.INTERP_PERSPECTIVE)], 12)
+        fbs = [srp.srpNewFramebuffer(W, H) for _ in frames]
+        vb = srp.srpNewVertexBuffer()
+        ib = srp.srpNewIndexBuffer()
+
+        def draw(k):
+            srp.srpFramebufferClear(fbs[k])
+            srp.srpDrawIndexBuffer(ib, vb, fbs[k], ctypes.byref(sp), A.PRIM_TRIANGLES, 0, 3 * n)
+
+        want = []
+        for k, (verts, idx) in enumerate(frames):
+            srp.srpVertexBufferCopyData(vb, 24, verts.nbytes, verts.ctypes.data)
+            srp.srpIndexBufferCopyData(ib, A.UINT32, idx.nbytes, idx.ctypes.data)
+            draw(k)
+            L.srpGpuFramebufferSync(fbs[k])
+            want.append(srp.planes(fbs[k]))
+        for fb in fbs:
+            srp.srpFramebufferClear(fb)
+            L.srpGpuFramebufferSync(fb)
+        for k, (verts, idx) in enumerate(frames):
+            L.srpGpuVertexBufferCopyDataAsync(vb, 24, verts.nbytes, verts.ctypes.data)
+            L.srpGpuIndexBufferCopyDataAsync(ib, A.UINT32, idx.nbytes, idx.ctypes.data)
+            draw(k)
+            L.srpGpuFramebufferSyncAsync(fbs[k])
+        assert L.srpGpuSynchronize() == 0
+        got = [srp.planes(fb) for fb in fbs]
+        assert not srp.errors()
+        srp.srpFreeVertexBuffer(vb)
+        srp.srpFreeIndexBuffer(ib)
+        for fb in fbs:
+            srp.srpFreeFramebuffer(fb)
+    finally:
+        srp.close()
+    for k, (a, b) in enumerate(zip(got, want)):
+        assert int((b[1] != np.float32(-1.0)).sum()) > 20000, k
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y), k
+    assert not np.array_equal(want[0][0], want[1][0])
