@@ -441,6 +441,44 @@ def run_batch(args, emit=True):
 
     e2e = e2e_steps(True)
     e2e_calls = e2e_steps(False)
+
+    # Steps back to back with the Batch calls and one srpGpuSynchronize at
+    # the end: with one copy of the batch (step n+1's uploads follow step n's
+    # draws), and with two (a second batch of the same seeds; step n+1's
+    # uploads are issued before step n's draws, and run beside them).
+    def e2e_stream(batches, nsteps):
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        if len(batches) > 1:
+            srp_gb300.upload_batch(batches[0])
+        for i in range(nsteps):
+            cur = batches[i % len(batches)]
+            if len(batches) == 1:
+                srp_gb300.upload_batch(cur)
+            elif i + 1 < nsteps:
+                srp_gb300.upload_batch(batches[(i + 1) % len(batches)])
+            cur_fbs = [sc.fb for sc in cur]
+            srp_gb300.prepare_batch(cur, cur_fbs)
+            srp_gb300.render_batch(cur, cur_fbs)
+            srp_gb300.sync_batch(cur_fbs)
+        if L.srpGpuSynchronize() != 0:
+            raise RuntimeError("srpGpuSynchronize failed after the streamed steps")
+        return (time.perf_counter() - t1) / nsteps
+
+    n_stream = max(4, args.steps)
+    e2e_stream((batch,), 2)  # untimed warm-up
+    e2e_one_copy = e2e_stream((batch,), n_stream)
+    batch_b = [srp_gb300.Scene("bscene", srp_gb300.batch_seed(BATCH_BASE, i), args.scale) for i in range(args.scenes)]
+    e2e_stream((batch, batch_b), 2)  # untimed warm-up
+    e2e_prefetch = e2e_stream((batch, batch_b), n_stream)
+    # both copies hold the same scenes: spot-check that their images agree
+    for i in list(range(32)) + list(range(args.scenes - 32, args.scenes)):
+        for x, y in zip(srp_gb300.framebuffer_arrays(batch[i].fb), srp_gb300.framebuffer_arrays(batch_b[i].fb)):
+            if x.tobytes() != y.tobytes():
+                raise RuntimeError(f"the double-buffered batches differ at scene {i}")
+    for sc in batch_b:
+        sc.close()
+    del batch_b
     L.srpGpuSetProfiling(1)
     L.srpGpuResetProfile()
     with torch.cuda.stream(stream):
@@ -468,11 +506,15 @@ def run_batch(args, emit=True):
                    "mtri_per_s": round(tris / step_s / 1e6, 1), "generation_s": round(gen_s, 1),
                    "l2": "flushed between steps (256 MB write)", "tuning": tuning},
         "clocks": clk,
-        "e2e": {"value": round(args.scenes / e2e_s, 2), "unit": "scenes/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(pixels * 9),
+        "e2e": {"value": round(args.scenes / e2e_prefetch, 2), "unit": "scenes/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(pixels * 9), "steps": n_stream,
+                "ms_per_step": round(e2e_prefetch * 1e3, 3),
                 "transfers": "srpGpuVertexBufferCopyDataBatchAsync / srpGpuIndexBufferCopyDataBatchAsync / "
-                             "srpGpuFramebufferSyncBatchAsync (gather kernels), one wait per step",
-                "with_per_buffer_calls": round(args.scenes / (sum(e2e_calls) / len(e2e_calls)), 2)},
+                             "srpGpuFramebufferSyncBatchAsync (gather kernels); one srpGpuSynchronize after all steps",
+                "prefetch": "two copies of the batch (same seeds): step n+1's uploads are issued before step n's draws",
+                "one_copy": round(args.scenes / e2e_one_copy, 2),
+                "one_wait_per_step": round(args.scenes / e2e_s, 2),
+                "one_wait_per_step_per_buffer_calls": round(args.scenes / (sum(e2e_calls) / len(e2e_calls)), 2)},
         "gpu_launches": int(st.kernelLaunches),
         "roofline": {"bound": "hbm", "achieved": round(step_gbs, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(step_gbs / peak, 5), "traffic": None,
@@ -989,6 +1031,36 @@ def main():
     e2e_stream(2)  # untimed warm-up
     n_stream = max(10, args.steps)
     e2e_stream_s = e2e_stream(n_stream) / n_stream
+
+    # The same with the frame's buffers double-buffered (a second Scene of the
+    # same seed): frame i+1's uploads are issued before frame i's draws, so
+    # they run on the copy engine beside frame i instead of after it. Every
+    # frame still uploads its 83.6 MB and downloads its planes inside the
+    # timed region, which starts before the first upload.
+    sc_b = srp_gb300.Scene(SCENE, SEED + rank, args.scale)
+
+    def e2e_prefetch(nframes):
+        pair = (sc, sc_b)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pair[0].upload_async()
+        for i in range(nframes):
+            cur = pair[i % 2]
+            if i + 1 < nframes:
+                pair[(i + 1) % 2].upload_async()
+            cur.prepare()
+            cur.render()
+            cur.sync_async()
+        if L.srpGpuSynchronize() != 0:
+            raise RuntimeError("srpGpuSynchronize failed after the prefetched frames")
+        return time.perf_counter() - t0
+    e2e_prefetch(4)  # untimed warm-up
+    e2e_prefetch_s = e2e_prefetch(n_stream) / n_stream
+    # both copies hold the same frame: their host planes must agree
+    for x, y in zip(srp_gb300.framebuffer_arrays(sc.fb), srp_gb300.framebuffer_arrays(sc_b.fb)):
+        if x.tobytes() != y.tobytes():
+            raise RuntimeError("the double-buffered frames differ")
+    sc_b.close()
     # per-stage device time (CUDA events inside the library) on separate frames
     L.srpGpuSetProfiling(1)
     L.srpGpuResetProfile()
@@ -1041,11 +1113,15 @@ def main():
                    "frames_per_s": round(args.steps / (total_ms / 1000.0), 2),
                    "mtri_per_s": round(info.inputTriangles * args.steps / (total_ms / 1000.0) / 1e6, 2)},
         "clocks": clk,
-        "e2e": {"value": round(frags_per_frame / e2e_stream_s / 1e6, 3), "unit": "Mfrag/s",
+        "e2e": {"value": round(frags_per_frame / e2e_prefetch_s / 1e6, 3), "unit": "Mfrag/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "frames": n_stream,
+                "ms_per_frame": round(e2e_prefetch_s * 1e3, 4),
                 "calls": "per frame srpGpuVertexBufferCopyDataAsync / srpGpuIndexBufferCopyDataAsync, "
                          "framebuffer fill, draws, srpGpuFramebufferSyncAsync; one srpGpuSynchronize after all frames",
+                "prefetch": "two copies of the frame's buffers and framebuffer (same seed): frame i+1's uploads "
+                            "are issued before frame i's draws",
+                "one_copy": round(frags_per_frame / e2e_stream_s / 1e6, 3),
                 "one_wait_per_frame": round(frags_per_frame / e2e_s / 1e6, 3),
                 "one_wait_per_frame_ms": round(e2e_s * 1e3, 3),
                 "with_reference_copy_calls": round(frags_per_frame / (sum(e2e_sync_times) / len(e2e_sync_times)) / 1e6, 3)},
