@@ -196,28 +196,41 @@ class ClockSampler:
         self.thread = threading.Thread(target=self._read_smi, daemon=True)
         self.thread.start()
 
+    @staticmethod
+    def parse_nvml(line):
+        """(time, sm_mhz, max_mhz, reasons, power_w) of a line of the NVML
+        child, or None if it does not parse."""
+        try:
+            t, sm, mx, rs, pw = line.strip().split(",")
+            bits = int(rs)
+            return (float(t), float(sm), float(mx), [n for b, n in NVML_REASONS if bits & b], float(pw) / 1000.0)
+        except ValueError:
+            return None
+
+    @staticmethod
+    def parse_smi(line, t):
+        """The same for a csv line of nvidia-smi, taken at time t."""
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        s = [x.strip() for x in line.split(",")]
+        try:
+            return (t, float(s[0]), float(s[1]), [n for n, v in zip(names, s[3:7]) if v.lower().startswith("active")],
+                    float(s[2]))
+        except (ValueError, IndexError):
+            return None
+
     def _read_nvml(self):
         for line in self.proc.stdout:
-            try:
-                t, sm, mx, rs, pw = line.strip().split(",")
-                bits = int(rs)
-                self.samples.append((float(t), float(sm), float(mx),
-                                     [n for b, n in NVML_REASONS if bits & b], float(pw) / 1000.0))
+            x = self.parse_nvml(line)
+            if x:
+                self.samples.append(x)
                 self.first.set()
-            except ValueError:
-                pass
 
     def _read_smi(self):
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in self.proc.stdout:
-            s = [x.strip() for x in line.split(",")]
-            try:
-                self.samples.append((time.monotonic(), float(s[0]), float(s[1]),
-                                     [n for n, v in zip(names, s[3:7]) if v.lower().startswith("active")],
-                                     float(s[2])))
+            x = self.parse_smi(line, time.monotonic())
+            if x:
+                self.samples.append(x)
                 self.first.set()
-            except (ValueError, IndexError):
-                pass
 
     def begin(self):
         self.t0 = time.monotonic()

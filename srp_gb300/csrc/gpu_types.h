@@ -15,6 +15,8 @@ constexpr int kMaxVaryingWords = 32;
 constexpr int kMaxVaryings = 16;
 /* Vertices a Sutherland-Hodgman polygon can reach (3 + one per plane). */
 constexpr int kMaxPoly = 9;
+/* Triangles of the fan of such a polygon. */
+constexpr int kClipFan = kMaxPoly - 2;
 
 enum VaryingMode : uint8_t { kPerspective = 0, kAffine = 1, kFlat = 2 };
 

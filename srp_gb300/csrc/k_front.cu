@@ -637,8 +637,11 @@ template <int MODE>
 struct Assembly {
 	int nPoly;
 	bool clipped;
+	uint32_t slot;       /* clipped, filled: the pre-pass's slot of its fan */
 	SV sv[3];            /* unclipped: per-vertex setup data from k_vertex */
-	PV poly[kMaxPoly];   /* clipped: polygon in clip space */
+	/* clipped, lines or points: polygon in clip space (filled triangles read
+	 * their fan, set up by the pre-pass, instead) */
+	PV poly[MODE == kTriFill ? 1 : kMaxPoly];
 };
 
 /* Write a set-up triangle as primitive `prim` with its pairs at `entry`. */
@@ -704,6 +707,48 @@ __device__ __forceinline__ void handleTriangle(const DrawParams& P, const SV& a,
 			prim += 1;
 			entry += nt;
 		}
+	}
+}
+
+/* The fan of a clipped filled triangle (src/pipeline/clipping.c:139-183 then
+ * triangle setup of each fan triangle, in fan order), set up by the clip
+ * pre-pass into its slot: the triangles that survive setup, their records,
+ * and their pair counts (tile pairs in a pass; the pair box otherwise).
+ * The ordered setup then only copies them to their places. */
+template <bool MULTI>
+__device__ __noinline__ void setupClipFan(const DrawParams& P, uint32_t slot, const PV* poly, int n, int W, int H)
+{
+	uint32_t nP = 0, nE = 0;
+	if (n >= 3) {
+		const SV p0 = fromClip(W, H, poly[0]);
+		for (int f = 1; f + 1 < n; ++f) {
+			TriRaster R;
+			TriAttr A;
+			if (!setupTriangle(P.st, W, H, p0, fromClip(W, H, poly[f]), fromClip(W, H, poly[f + 1]), R, A)) continue;
+			const uint32_t nt = MULTI ? tileCount(R.minX, R.minY, R.maxX, R.maxY) : triPairTiles(P.st, R);
+			A.pad = nt;
+			const size_t at = (size_t) slot * kClipFan + nP;
+			P.clipR[at] = R;
+			P.clipA[at] = A;
+			nP += 1;
+			nE += nt;
+		}
+	}
+	P.clipFan[slot] = make_uint2(nP, nE);
+}
+
+/* Copies the fan of slot to primitives prim.. and pairs entry.. */
+__device__ __forceinline__ void writeClipFan(const DrawParams& P, uint32_t slot, uint32_t nPrim, uint32_t prim,
+                                             uint32_t entry)
+{
+	for (uint32_t j = 0; j < nPrim; ++j) {
+		const size_t at = (size_t) slot * kClipFan + j;
+		TriRaster R = P.clipR[at];
+		TriAttr A = P.clipA[at];
+		const uint32_t nt = A.pad;
+		A.pad = 0;
+		writeTri(P, R, A, nt, prim + j, entry);
+		entry += nt;
 	}
 }
 
@@ -886,11 +931,13 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup(cons
 #pragma unroll
 					for (int i = 0; i < 3; ++i) as.sv[i] = loadSV(P, vi[i]);
 				} else {
-					/* clipped by k_clip_prepass: read back its polygon */
+					/* clipped by k_clip_prepass: read back its fan or its polygon */
 					as.clipped = true;
 					const uint32_t slot = P.clipSlot[k];
 					if (slot >= P.clipPolyCap) { live = false; }
-					else {
+					else if constexpr (MODE == kTriFill) {
+						as.slot = slot;
+					} else {
 						const uint32_t* poly = P.clipPolys + (size_t) slot * (1 + kMaxPoly);
 						as.nPoly = (int) poly[0];
 						for (int i = 0; i < as.nPoly && i < kMaxPoly; ++i) as.poly[i] = loadPV(P, poly[1 + i]);
@@ -928,6 +975,10 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup(cons
 			} else {
 				handleTriangle<MODE>(P, as.sv[0], as.sv[1], as.sv[2], false, nPrim, nEnt);
 			}
+		} else if constexpr (MODE == kTriFill) {
+			const uint2 fan = P.clipFan[as.slot];
+			nPrim = fan.x;
+			nEnt = fan.y;
 		} else {
 			const SV p0 = fromClip(P.st, as.poly[0]);
 			for (int f = 1; f + 1 < as.nPoly; ++f)
@@ -967,6 +1018,8 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup(cons
 		} else {
 			handleTriangle<MODE>(P, as.sv[0], as.sv[1], as.sv[2], true, primBase, entBase);
 		}
+	} else if constexpr (MODE == kTriFill) {
+		writeClipFan(P, as.slot, nPrim, primBase, entBase);
 	} else {
 		const SV p0 = fromClip(P.st, as.poly[0]);
 		for (int f = 1; f + 1 < as.nPoly; ++f)
@@ -978,7 +1031,9 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup(cons
  * ordered setup: no ordering is needed to clip, so the long, divergent
  * Sutherland-Hodgman path runs here instead of inside the scan-coupled setup
  * blocks. The polygon (vertex count and vertex rows, new vertices included)
- * goes to a slot that k_setup reads back. */
+ * goes to a slot that k_setup reads back; for filled triangles the fan is
+ * set up here as well, so that k_setup<kTriFill> only copies its records
+ * (and carries no polygon, no stack frame and no spills). */
 __global__ void __launch_bounds__(kSetupThreads, 16) k_clip_prepass(const __grid_constant__ DrawParams P)
 {
 	gridDepSync();
@@ -998,6 +1053,7 @@ __global__ void __launch_bounds__(kSetupThreads, 16) k_clip_prepass(const __grid
 	uint32_t* out = P.clipPolys + (size_t) slot * (1 + kMaxPoly);
 	out[0] = (uint32_t) n;
 	for (int i = 0; i < n; ++i) out[1 + i] = poly[i].ref;
+	if (P.st.polygonMode == SRP_POLYGON_MODE_FILL) setupClipFan<false>(P, (uint32_t) slot, poly, n, P.st.W, P.st.H);
 	P.clipSlot[k] = (uint32_t) slot;
 }
 
@@ -1293,6 +1349,8 @@ __global__ void __launch_bounds__(kSetupThreads, 16) k_clip_prepass_multi(const 
 	uint32_t* out = P.clipPolys + (size_t) slot * (1 + kMaxPoly);
 	out[0] = (uint32_t) n;
 	for (int i = 0; i < n; ++i) out[1 + i] = poly[i].ref;
+	const DrawDesc& D = P.draws[d];
+	setupClipFan<true>(P, (uint32_t) slot, poly, n, D.W, D.H);
 	P.clipSlot[k] = (uint32_t) slot;
 }
 
@@ -1356,8 +1414,7 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup_mult
 	int W = 0, H = 0, tilesX = 0;
 	uint32_t tileBase = 0;
 	SV sv[3];
-	int nPoly = 0;
-	PV poly[kMaxPoly];
+	uint32_t slot = 0;
 	if (live) {
 		uint32_t vi[3];
 		unsigned long long local;
@@ -1373,15 +1430,10 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup_mult
 #pragma unroll
 				for (int i = 0; i < 3; ++i) sv[i] = loadSV(P, vi[i]);
 			} else {
+				/* clipped: its fan was set up by k_clip_prepass_multi */
 				clipped = true;
-				const uint32_t slot = P.clipSlot[k];
+				slot = P.clipSlot[k];
 				if (slot >= P.clipPolyCap) live = false;
-				else {
-					const uint32_t* pp = P.clipPolys + (size_t) slot * (1 + kMaxPoly);
-					nPoly = (int) pp[0];
-					for (int i = 0; i < nPoly && i < kMaxPoly; ++i) poly[i] = loadPV(P, pp[1 + i]);
-					if (nPoly < 3) live = false;
-				}
 			}
 		}
 	}
@@ -1399,14 +1451,9 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup_mult
 				sA[tid] = fA;
 			}
 		} else {
-			const SV p0 = fromClip(W, H, poly[0]);
-			for (int f = 1; f + 1 < nPoly; ++f) {
-				TriRaster R;
-				TriAttr A;
-				if (!setupTriangle(P.st, W, H, p0, fromClip(W, H, poly[f]), fromClip(W, H, poly[f + 1]), R, A)) continue;
-				nPrim += 1;
-				nEnt += tileCount(R.minX, R.minY, R.maxX, R.maxY);
-			}
+			const uint2 fan = P.clipFan[slot];
+			nPrim = fan.x;
+			nEnt = fan.y;
 		}
 	}
 	const unsigned long long base = orderedOffset(P, bid, nPrim, nEnt, sWarp, sPrefix);
@@ -1420,14 +1467,13 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup_mult
 			writeTriMulti(P, d, tilesX, tileBase, fR, fA, nEnt, primBase, entBase);
 		}
 	} else {
-		const SV p0 = fromClip(W, H, poly[0]);
-		for (int f = 1; f + 1 < nPoly; ++f) {
-			TriRaster R;
-			TriAttr A;
-			if (!setupTriangle(P.st, W, H, p0, fromClip(W, H, poly[f]), fromClip(W, H, poly[f + 1]), R, A)) continue;
-			const uint32_t nt = tileCount(R.minX, R.minY, R.maxX, R.maxY);
-			writeTriMulti(P, d, tilesX, tileBase, R, A, nt, primBase, entBase);
-			primBase += 1;
+		for (uint32_t j = 0; j < nPrim; ++j) {
+			const size_t at = (size_t) slot * kClipFan + j;
+			TriRaster R = P.clipR[at];
+			TriAttr A = P.clipA[at];
+			const uint32_t nt = A.pad;
+			A.pad = 0;
+			writeTriMulti(P, d, tilesX, tileBase, R, A, nt, primBase + j, entBase);
 			entBase += nt;
 		}
 	}

@@ -50,6 +50,12 @@ struct DrawParams {
 	uint32_t* clipSlot;            /* [nIn], written only for clipped triangles */
 	uint32_t* clipPolys;           /* [clipPolyCap][1 + kMaxPoly] */
 	uint32_t clipPolyCap;
+	/* filled triangles: each clipped triangle's fan, set up by the clip
+	 * pre-pass, [clipPolyCap]: (triangles, pairs), and its triangles'
+	 * records, [clipPolyCap][kClipFan] (TriAttr.pad = the triangle's pairs) */
+	uint2* clipFan;
+	TriRaster* clipR;
+	TriAttr* clipA;
 	uint4* bigJobs;                /* primitives covering many tiles */
 	uint32_t bigCap;
 	/* exact barycentrics of big triangles at every (row, tile column) start:

@@ -104,6 +104,8 @@ struct DrawSet {
 	/* used by the front stages only, which run on the set's own front
 	 * stream: the next draw's front (other set) runs beside this one's */
 	DeviceBuffer clip, vset0, vset1, codes, lookback, hist, partials, minmax, clipSlot, clipPolys;
+	/* filled triangles: the fans set up by the clip pre-pass, read by setup */
+	DeviceBuffer clipFan, clipR, clipA;
 	cudaStream_t front = nullptr;
 	DeviceBuffer keys, vals, keys2, vals2;
 	/* multi-draw passes: descriptors, prefix sums, primitive bases, winners */
@@ -1545,6 +1547,22 @@ static unsigned long long readCounters()
 	return g.sets[0].hostCtr->fragments + g.sets[1].hostCtr->fragments;
 }
 
+/* Room for the clip pre-pass's fans of filled triangles: g.clipPolyCap
+ * slots of kClipFan records each. */
+static bool reserveClipFans(DrawSet& S, const char* fn)
+{
+	const size_t slots = g.clipPolyCap;
+	return S.clipFan.reserve(slots * sizeof(uint2), fn) && S.clipR.reserve(slots * kClipFan * sizeof(TriRaster), fn) &&
+	       S.clipA.reserve(slots * kClipFan * sizeof(TriAttr), fn);
+}
+
+static void setClipFans(DrawParams& P, DrawSet& S)
+{
+	P.clipFan = S.clipFan.as<uint2>();
+	P.clipR = S.clipR.as<TriRaster>();
+	P.clipA = S.clipA.as<TriAttr>();
+}
+
 /* The GPU pipeline for one draw call. */
 static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const SRPFramebuffer* fb,
                     const SRPShaderProgram* sp, SRPPrimitive prim, size_t start, size_t count, size_t nIn)
@@ -1681,7 +1699,8 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		          S.tileStart.reserve((size_t) (numTiles + 1) * 4, FN) && S.tileEnd.reserve((size_t) (numTiles + 1) * 4, FN) &&
 		          S.winner.reserve(fb->size * 4 + 4, FN) && S.heavy.reserve((size_t) (numTiles + 1) * 4, FN);
 		if (kind == kKindTri) ok = ok && S.triR.reserve((size_t) primCap * sizeof(TriRaster), FN) &&
-		                           S.triA.reserve((size_t) primCap * sizeof(TriAttr), FN);
+		                           S.triA.reserve((size_t) primCap * sizeof(TriAttr), FN) &&
+		                           reserveClipFans(S, FN);
 		else if (kind == kKindPoint) ok = ok && S.points.reserve((size_t) primCap * sizeof(PointRec), FN);
 		else ok = ok && S.lines.reserve((size_t) primCap * sizeof(LineRec), FN) &&
 		          S.frags.reserve((size_t) entryCap * sizeof(LineFrag), FN);
@@ -1709,6 +1728,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		P.clipSlot = S.clipSlot.as<uint32_t>();
 		P.clipPolys = S.clipPolys.as<uint32_t>();
 		P.clipPolyCap = g.clipPolyCap;
+		setClipFans(P, S);
 		P.tableCap = g.tableCap;
 		P.lookback = S.lookback.as<unsigned long long>();
 		P.tileStart = S.tileStart.as<uint32_t>();
@@ -2126,7 +2146,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		          S.clipSlot.reserve((size_t) nIn * 4 + 4, FN) &&
 		          S.clipPolys.reserve((size_t) g.clipPolyCap * (1 + kMaxPoly) * 4, FN) &&
 		          S.triR.reserve((size_t) primCap * sizeof(TriRaster), FN) &&
-		          S.triA.reserve((size_t) primCap * sizeof(TriAttr), FN) &&
+		          S.triA.reserve((size_t) primCap * sizeof(TriAttr), FN) && reserveClipFans(S, FN) &&
 		          S.tileStart.reserve((size_t) (numTiles + 1) * 4, FN) && S.tileEnd.reserve((size_t) (numTiles + 1) * 4, FN) &&
 		          S.heavy.reserve((size_t) (numTiles + 1) * 4, FN);
 		if (!ok) return false;
@@ -2150,6 +2170,7 @@ static bool runPass(const SRPGpuDraw* draws, const std::vector<size_t>& idx, con
 		P.clipSlot = S.clipSlot.as<uint32_t>();
 		P.clipPolys = S.clipPolys.as<uint32_t>();
 		P.clipPolyCap = g.clipPolyCap;
+		setClipFans(P, S);
 		P.lookback = S.lookback.as<unsigned long long>();
 		P.tileStart = S.tileStart.as<uint32_t>();
 		P.tileEnd = S.tileEnd.as<uint32_t>();

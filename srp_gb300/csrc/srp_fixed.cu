@@ -138,10 +138,13 @@ extern "C" int srpGpuDrawFixedScratch(const SRPIndexBuffer* ib, const SRPVertexB
 	const size_t oVary = cv.take(rows * nw * 4);
 	const size_t oSlot = cv.take(info.nIn * 4 + 4);
 	const size_t oPolys = cv.take(kClipPolys * (1 + kMaxPoly) * 4);
-	size_t oPrimA = 0, oPrimB = 0;
+	size_t oPrimA = 0, oPrimB = 0, oFan = 0, oFanR = 0, oFanA = 0;
 	if (info.kind == kKindTri) {
 		oPrimA = cv.take(primCap * sizeof(TriRaster));
 		oPrimB = cv.take(primCap * sizeof(TriAttr));
+		oFan = cv.take(kClipPolys * sizeof(uint2));
+		oFanR = cv.take(kClipPolys * kClipFan * sizeof(TriRaster));
+		oFanA = cv.take(kClipPolys * kClipFan * sizeof(TriAttr));
 	} else {
 		oPrimA = cv.take(primCap * (info.kind == kKindPoint ? sizeof(PointRec) : sizeof(LineRec)));
 	}
@@ -195,6 +198,9 @@ extern "C" int srpGpuDrawFixedScratch(const SRPIndexBuffer* ib, const SRPVertexB
 	if (info.kind == kKindTri) {
 		P.triR = (TriRaster*) (base + oPrimA);
 		P.triA = (TriAttr*) (base + oPrimB);
+		P.clipFan = (uint2*) (base + oFan);
+		P.clipR = (TriRaster*) (base + oFanR);
+		P.clipA = (TriAttr*) (base + oFanA);
 	} else if (info.kind == kKindPoint) {
 		P.points = (PointRec*) (base + oPrimA);
 	} else {

@@ -13,23 +13,36 @@ import bench  # noqa: E402
 
 def test_clock_summary_reports_median_max_and_active_reasons():
     c = bench.ClockSampler(0)
-    # clocks.sm, clocks.max.sm, power.draw, hw_slowdown, hw_thermal_slowdown,
-    # sw_thermal_slowdown, sw_power_cap (nvidia-smi csv, no units)
-    c.samples = [
-        ["2070", "2070", "900.1", "Not Active", "Not Active", "Not Active", "Active"],
-        ["1980", "2070", "950.0", "Active", "Not Active", "Not Active", "Not Active"],
-        ["2070", "2070", "910.4", "Not Active", "Not Active", "Not Active", "Not Active"],
-        ["[N/A]", "2070", "0", "Not Active", "Not Active", "Not Active", "Not Active"],  # unreadable row
-    ]
+    # NVML child lines: monotonic s, SM MHz, max MHz, clock-event reason bits, power mW
+    lines = ["10.000,2070,2070,4,900100",      # sw_power_cap
+             "10.010,1980,2070,8,950000",      # hw_slowdown
+             "10.020,2070,2070,0,910400",
+             "10.030,2070,2070,64,0",          # hw_thermal_slowdown, outside the window
+             "garbage"]
+    c.samples = [x for x in map(bench.ClockSampler.parse_nvml, lines) if x]
+    assert len(c.samples) == 4
+    c.t0, c.t1 = 9.99, 10.025
     s = c.stop()
-    assert s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0
+    assert s["sm_mhz"] == 2070.0 and s["sm_max_mhz"] == 2070.0 and s["sm_min_mhz"] == 1980.0
     assert s["reasons"] == ["hw_slowdown", "sw_power_cap"]
     assert s["samples"] == 3
+    assert s["power_w"] == 910.4
+
+
+def test_clock_summary_of_nvidia_smi_lines():
+    # clocks.sm, clocks.max.sm, power.draw, hw_slowdown, hw_thermal_slowdown,
+    # sw_thermal_slowdown, sw_power_cap (csv, no units)
+    rows = ["2070, 2070, 900.1, Not Active, Not Active, Not Active, Active",
+            "1980, 2070, 950.0, Active, Not Active, Not Active, Not Active",
+            "[N/A], 2070, 0, Not Active, Not Active, Not Active, Not Active"]  # unreadable row
+    got = [bench.ClockSampler.parse_smi(r, 1.0) for r in rows]
+    assert got[2] is None
+    assert got[0][3] == ["sw_power_cap"] and got[1][3] == ["hw_slowdown"] and got[1][1] == 1980.0
 
 
 def test_clock_summary_without_samples():
     s = bench.ClockSampler(0).stop()
-    assert s == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+    assert s["sm_mhz"] is None and s["sm_max_mhz"] is None and s["reasons"] == [] and s["samples"] == 0
 
 
 def test_peaks_measured_file_and_fallback(tmp_path, monkeypatch):
