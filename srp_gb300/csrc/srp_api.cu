@@ -226,7 +226,9 @@ bool ensureInit(const char* fn)
 	    !cudaOk(cudaEventCreateWithFlags(&g.joinEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 	    !cudaOk(cudaStreamCreateWithFlags(&g.sets[0].front, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
 	    !cudaOk(cudaStreamCreateWithFlags(&g.sets[1].front, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
-	    !cudaOk(cudaStreamCreateWithFlags(&g.resolveStream, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
+	    /* high priority: when frames are queued back to back, a frame's
+	     * resolve goes ahead of the next frame's front stages */
+	    !cudaOk(cudaStreamCreateWithPriority(&g.resolveStream, cudaStreamNonBlocking, hiPri), fn, "cudaStreamCreate") ||
 	    !cudaOk(cudaEventCreateWithFlags(&g.rsEvent, cudaEventDisableTiming), fn, "cudaEventCreate") ||
 	    !cudaOk(cudaStreamCreateWithFlags(&g.copyStream, cudaStreamNonBlocking), fn, "cudaStreamCreate") ||
 	    !cudaOk(cudaStreamCreateWithFlags(&g.downloadStream, cudaStreamNonBlocking), fn, "cudaStreamCreate")) return false;
