@@ -102,9 +102,18 @@ struct __align__(16) LineRec {
 	float invW[2];
 	uint32_t vref[2];
 	uint32_t id;
-	uint32_t fragBase;   /* first fragment slot */
-	uint32_t pad[2];
+	uint32_t fragBase;   /* first pair slot of its runs */
+	uint32_t slots;      /* pair slots of its runs; bit 31: every step lands in the framebuffer */
+	uint32_t endPix;     /* pixel one step past the last (x | y << 16, 16 bits each) */
 };
+
+/* Line draws bin runs of fragments (k_front.cu): a run's pair value is its
+ * slot k | count << kRunCountShift, its fragments' records are at
+ * k * kRunFrags + j (a run has at most kRunMaxCount fragments, and slots
+ * stay below 2^kRunCountShift). */
+constexpr uint32_t kRunFrags = 16;
+constexpr uint32_t kRunCountShift = 28;
+constexpr uint32_t kRunMaxCount = 15;
 
 /* One line fragment (16 bytes). */
 struct __align__(16) LineFrag {

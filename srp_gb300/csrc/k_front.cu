@@ -583,6 +583,66 @@ __device__ void setupLine(const DrawState& st, const SV& a, const SV& b, LineRec
 	L.vref[0] = a.ref; L.vref[1] = b.ref;
 }
 
+/* Line draws are binned as runs: a run is a maximal sequence of consecutive
+ * DDA steps that pass the scissor test, land in the framebuffer and fall in
+ * one tile. A line gets slots for its runs in the (tile, item) arrays; the
+ * run in slot k keeps its fragments' records at k * kRunFrags + j, and its
+ * pair carries k | count << kRunCountShift. */
+
+constexpr uint32_t kShortLine = 48;   /* steps one thread walks on its own */
+
+constexpr uint32_t kLineInside = 0x80000000u;
+
+/* Tile distance (columns + rows) between two pixels with coordinates >= 0. */
+__device__ __forceinline__ uint32_t tileDistance(int ax, int ay, int bx, int by)
+{
+	return (uint32_t) abs(ax / kTile - bx / kTile) + (uint32_t) abs(ay / kTile - by / kTile);
+}
+
+/* The far end of a coordinate's DDA: a value at least as far along the
+ * line's direction as the accumulator after n steps. Each of the n fp32
+ * additions rounds by at most half an ulp of the larger magnitude, i.e.
+ * 2^-24 * max |value|, so the accumulated value lies within
+ * n * 2^-24 * max |value| of the exact sum v0 + n * inc; twice that, plus a
+ * little, bounds it. */
+__device__ __forceinline__ int farPixel(float v0, float inc, uint32_t n)
+{
+	const double e = (double) v0 + (double) n * (double) inc;
+	const double m = (double) n * fmax(fabs((double) v0), fabs(e)) * 0x1p-23 + 0x1p-10;
+	const double f = inc >= 0.0f ? e + m : e - m;
+	/* rounding half away from zero, as the walker rounds */
+	return (int) fmax(fmin(round(f), 2.0e9), -2.0e9);
+}
+
+/* Pair slots for the runs of a line (L.slots, L.endPix), set after setupLine.
+ * The DDA's pixel coordinates are monotone along the line. With its first
+ * pixel and a pixel E at or beyond the one past its last step (farPixel) in
+ * the framebuffer, every step lands in it; the steps that pass the scissor
+ * rectangle are then consecutive (a monotone path through a rectangle), and
+ * a walker visiting steps [a, b) finds at most tileDistance(pixel a,
+ * pixel b) + 1 runs, E standing in for the pixel one past the end. A short
+ * line has one walker; a long one has 32 (a warp's lanes, on consecutive
+ * segments, the last one ending at E), whose bounds add up to
+ * tileDistance(first pixel, E) + 32. Elsewhere a run may be a single step,
+ * and the line gets a slot per step. */
+__device__ __forceinline__ void lineRunInfo(const DrawState& st, LineRec& L)
+{
+	const uint32_t total = (uint32_t) L.steps + 1u;
+	const int ax = (int) roundf(L.x0), ay = (int) roundf(L.y0);
+	const int bx = farPixel(L.x0, L.xInc, total), by = farPixel(L.y0, L.yInc, total);
+	const bool inside = ax >= 0 && ay >= 0 && bx >= 0 && by >= 0 && ax < st.W && bx < st.W && ay < st.H && by < st.H;
+	uint32_t slots = total;
+	if (inside) {
+		const uint32_t walkers = total <= kShortLine ? 1u : 32u;
+		const uint32_t d = tileDistance(ax, ay, bx, by) + walkers;
+		if (d < slots) slots = d;
+	}
+	L.slots = slots | (inside ? kLineInside : 0u);
+	L.endPix = ((uint32_t) bx & 0xFFFFu) | ((uint32_t) by << 16);
+}
+
+__device__ __forceinline__ uint32_t lineSlots(const LineRec& L) { return L.slots & ~kLineInside; }
+
 /* Point setup: divide, screen space, coverage square and raster bounds
  * (src/raster/point.c:32-79, 121-163). */
 __device__ void setupPoint(const DrawState& st, const SV& v, PointRec& R)
@@ -639,9 +699,9 @@ struct Assembly {
 	bool clipped;
 	uint32_t slot;       /* clipped, filled: the pre-pass's slot of its fan */
 	SV sv[3];            /* unclipped: per-vertex setup data from k_vertex */
-	/* clipped, lines or points: polygon in clip space (filled triangles read
-	 * their fan, set up by the pre-pass, instead) */
-	PV poly[MODE == kTriFill ? 1 : kMaxPoly];
+	/* clipped triangles drawn as lines or points: polygon in clip space
+	 * (filled triangles read their fan, set up by the pre-pass, instead) */
+	PV poly[(MODE == kTriLine || MODE == kTriPoint) ? kMaxPoly : 1];
 };
 
 /* Write a set-up triangle as primitive `prim` with its pairs at `entry`. */
@@ -682,12 +742,13 @@ __device__ __forceinline__ void handleTriangle(const DrawParams& P, const SV& a,
 		for (int j = 0; j < 3; ++j) {
 			LineRec L;
 			setupLine(P.st, *vv[j], *vv[(j + 1) % 3], L);
+			lineRunInfo(P.st, L);
 			if (write) {
 				if (prim < P.primCap) { L.id = prim; L.fragBase = entry; P.lines[prim] = L; }
 				else atomicOr(&P.ctr->errors, kErrCapacity);
 			}
 			prim += 1;
-			entry += (uint32_t) L.steps + 1u;
+			entry += lineSlots(L);
 		}
 	} else if (MODE == kTriPoint) {
 		const SV* vv[3] = { &a, &b, &c };
@@ -950,6 +1011,8 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup(cons
 	uint32_t nPrim = 0, nEnt = 0;
 	/* unclipped filled triangle: set up once, kept in shared memory across the scan */
 	bool fOk = false;
+	/* a line's run slots, kept across the scan */
+	uint32_t lSlots = 0, lEnd = 0;
 	if (live) {
 		if (MODE == kPoints) {
 			PointRec R;
@@ -959,8 +1022,11 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup(cons
 		} else if (MODE == kLines) {
 			LineRec L;
 			setupLine(P.st, as.sv[0], as.sv[1], L);
+			lineRunInfo(P.st, L);
 			nPrim = 1;
-			nEnt = (uint32_t) L.steps + 1u;
+			nEnt = lineSlots(L);
+			lSlots = L.slots;
+			lEnd = L.endPix;
 		} else if (!as.clipped) {
 			if (MODE == kTriFill) {
 				TriRaster fR;
@@ -1003,6 +1069,8 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup(cons
 	} else if (MODE == kLines) {
 		LineRec L;
 		setupLine(P.st, as.sv[0], as.sv[1], L);
+		L.slots = lSlots;
+		L.endPix = lEnd;
 		if (primBase < P.primCap) {
 			L.id = primBase;
 			L.fragBase = entBase;
@@ -1128,27 +1196,36 @@ __global__ void k_lambda_tables(const __grid_constant__ DrawParams P)
 }
 
 /* Steps [s0, s1) of line i's DDA, exactly as the reference walks them
- * (fp32 accumulators, round half away from zero; src/raster/line.c:34-77):
- * the accumulators are entered at s0 with the exact jump-ahead (chain.h),
- * then stepped serially. Each step writes one record and one (tile,
- * fragment) pair; steps whose pixel fails the scissor test or falls outside
- * the framebuffer get the key one past the last tile, which sorts them out
- * (src/raster/fragment.c:63-75). Returns the steps that passed the scissor. */
-__device__ unsigned long long walkLine(const DrawParams& P, const LineRec& L, uint32_t i, uint32_t s0, uint32_t s1)
+ * (fp32 accumulators, round half away from zero; src/raster/line.c:34-77),
+ * from the accumulators (x, y, t) at step s0. Steps whose pixel fails the
+ * scissor test or falls outside the framebuffer are dropped
+ * (src/raster/fragment.c:63-75); the others form runs (see lineRunInfo),
+ * written to slots slot0.. of the pair arrays, at most nSlots of them; the
+ * slots left over get the key one past the last tile, which sorts them out.
+ * Returns the steps that passed the scissor test. */
+__device__ unsigned long long walkLineRuns(const DrawParams& P, const LineRec& L, uint32_t i, uint32_t s0, uint32_t s1,
+                                           float x, float y, float t, uint32_t slot0, uint32_t nSlots)
 {
 	unsigned long long passed = 0;
 	const uint32_t invalid = (uint32_t) (P.st.tilesX * P.st.tilesY);
-	float x = srpChainAdd(L.x0, L.xInc, s0), y = srpChainAdd(L.y0, L.yInc, s0);
-	float t = srpChainAdd(0.0f, L.tInc, s0);
 	const unsigned long long size = (unsigned long long) P.st.W * (unsigned long long) P.st.H;
+	uint32_t used = 0, runKey = invalid, runN = 0;
+	auto flush = [&]() {
+		if (runN) {
+			const uint32_t k = slot0 + used;
+			if (used < nSlots && k < P.entryCap) {
+				P.keys[k] = runKey;
+				P.vals[k] = k | (runN << kRunCountShift);
+			}
+			++used;
+		}
+		runN = 0;
+	};
 	for (uint32_t s = s0; s < s1; ++s) {
 		const int px = (int) roundf(x), py = (int) roundf(y);
-		const float w0 = __fsub_rn(1.0f, t);
-		const float depth = __fadd_rn(__fmul_rn(L.c[0], w0), __fmul_rn(L.c[1], t));
-		const uint32_t e = L.fragBase + s;
 		uint32_t key = invalid;
 		if (scissorPass(P.st, px, py)) {
-			++passed;
+			++passed;  /* counted as the reference's fragments are, before the framebuffer bound */
 			const unsigned long long idx = (unsigned long long) (long long) py * (unsigned long long) P.st.W
 			                             + (unsigned long long) (long long) px;
 			if (idx < size) {
@@ -1157,21 +1234,34 @@ __device__ unsigned long long walkLine(const DrawParams& P, const LineRec& L, ui
 				key = (gy / kTile) * (uint32_t) P.st.tilesX + gx / kTile;
 			}
 		}
-		if (e < P.fragCap && e < P.entryCap) {
-			LineFrag F;
-			F.depth = depth; F.t = t; F.line = i; F.px = (int16_t) px; F.py = (int16_t) py;
-			P.frags[e] = F;
-			P.keys[e] = key;
-			P.vals[e] = e;
+		if (key != runKey || runN == kRunMaxCount) {
+			flush();
+			runKey = key;
+		}
+		if (key != invalid) {
+			const uint32_t k = slot0 + used;
+			if (used < nSlots && k < P.entryCap) {
+				const unsigned long long rec = (unsigned long long) k * kRunFrags + runN;
+				if (rec < P.fragCap) {
+					LineFrag F;
+					F.depth = __fadd_rn(__fmul_rn(L.c[0], __fsub_rn(1.0f, t)), __fmul_rn(L.c[1], t));
+					F.t = t; F.line = i; F.px = (int16_t) px; F.py = (int16_t) py;
+					P.frags[rec] = F;
+				}
+			}
+			++runN;
 		}
 		x = __fadd_rn(x, L.xInc);
 		y = __fadd_rn(y, L.yInc);
 		t = __fadd_rn(t, L.tInc);
 	}
+	flush();
+	for (uint32_t u = used; u < nSlots; ++u) {
+		const uint32_t k = slot0 + u;
+		if (k < P.entryCap) { P.keys[k] = invalid; P.vals[k] = 0; }
+	}
 	return passed;
 }
-
-constexpr uint32_t kShortLine = 48;   /* steps one thread walks on its own */
 
 /* One thread per line; lines longer than kShortLine steps are queued for
  * k_line_frags_long. */
@@ -1189,14 +1279,20 @@ __global__ void k_line_frags(const __grid_constant__ DrawParams P)
 			const unsigned long long j = atomicAdd(&P.ctr->lineFrags, 1ull);
 			if (j < P.bigCap) P.bigJobs[j].x = i;
 		} else {
-			passed = walkLine(P, L, i, 0, total);
+			passed = walkLineRuns(P, L, i, 0, total, L.x0, L.y0, 0.0f, L.fragBase, lineSlots(L));
 		}
 	}
 	for (int o = 16; o; o >>= 1) passed += __shfl_xor_sync(0xFFFFFFFFu, passed, o);
 	if ((threadIdx.x & 31) == 0 && passed) atomicAdd(&P.ctr->fragments, passed);
 }
 
-/* Long lines: one warp per line, lane l walks a contiguous run of steps. */
+/* Long lines: one warp per line, lane l walks a contiguous segment of steps
+ * into its share of the line's slots. A lane's share is bounded by the tile
+ * distance from its first pixel to the next lane's first pixel (the far
+ * pixel E of lineRunInfo for the last lane), + 1, or by its step count
+ * when not every step of the line lands in the framebuffer (lineRunInfo);
+ * an exclusive scan of the shares places them, and the last lane clears
+ * the slots beyond them. */
 __global__ void k_line_frags_long(const __grid_constant__ DrawParams P)
 {
 	gridDepSync();
@@ -1210,9 +1306,140 @@ __global__ void k_line_frags_long(const __grid_constant__ DrawParams P)
 		const uint32_t total = (uint32_t) L.steps + 1u;
 		const uint32_t seg = (total + 31u) / 32u;
 		const uint32_t s0 = min(lane * seg, total), s1 = min(s0 + seg, total);
-		unsigned long long passed = walkLine(P, L, i, s0, s1);
+		const float x = srpChainAdd(L.x0, L.xInc, s0), y = srpChainAdd(L.y0, L.yInc, s0);
+		const float t = srpChainAdd(0.0f, L.tInc, s0);
+		const int px = (int) roundf(x), py = (int) roundf(y);
+		int nx = __shfl_down_sync(0xFFFFFFFFu, px, 1), ny = __shfl_down_sync(0xFFFFFFFFu, py, 1);
+		if (lane == 31) { nx = (int) (int16_t) (L.endPix & 0xFFFFu); ny = (int) (int16_t) (L.endPix >> 16); }
+		uint32_t mine = s1 - s0;
+		if ((L.slots & kLineInside) && mine) {
+			const uint32_t d = tileDistance(px, py, nx, ny) + 1u;
+			if (d < mine) mine = d;
+		}
+		uint32_t incl = mine;
+#pragma unroll
+		for (int o = 1; o < 32; o <<= 1) {
+			const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+			if (lane >= (uint32_t) o) incl += v;
+		}
+		unsigned long long passed = walkLineRuns(P, L, i, s0, s1, x, y, t, L.fragBase + incl - mine, mine);
+		if (lane == 31) {
+			const uint32_t invalid = (uint32_t) (P.st.tilesX * P.st.tilesY);
+			for (uint32_t u = incl; u < lineSlots(L); ++u) {
+				const uint32_t k = L.fragBase + u;
+				if (k < P.entryCap) { P.keys[k] = invalid; P.vals[k] = 0; }
+			}
+		}
 		for (int o = 16; o; o >>= 1) passed += __shfl_xor_sync(0xFFFFFFFFu, passed, o);
 		if (lane == 0 && passed) atomicAdd(&P.ctr->fragments, passed);
+	}
+}
+
+/* Runs back to fragments, after the sort: the fragment counts of the sorted
+ * runs are scanned (per block of kRunBlock, then over the blocks), every run
+ * writes its fragments' record numbers to fragVals in sorted order, and the
+ * tile ranges are moved from runs to fragments, so that the resolve and
+ * shading kernels see one item per fragment in (tile, line, step) order. */
+constexpr int kRunBlock = 1024;
+
+__device__ __forceinline__ uint32_t runCount(uint32_t v) { return v >> kRunCountShift; }
+
+__global__ void __launch_bounds__(kRunBlock) k_run_sums(const __grid_constant__ DrawParams P, const uint32_t* vals)
+{
+	gridDepSync();
+	__shared__ uint32_t sw[kRunBlock / 32];
+	const uint32_t n = (uint32_t) min(P.ctr->entries, (unsigned long long) P.entryCap);
+	const uint32_t i = blockIdx.x * kRunBlock + threadIdx.x;
+	uint32_t c = (i < n && !P.ctr->abort) ? runCount(vals[i]) : 0u;
+	for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
+	if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = c;
+	__syncthreads();
+	if (threadIdx.x < 32) {
+		uint32_t v = sw[threadIdx.x];
+		for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+		if (threadIdx.x == 0) P.runSums[blockIdx.x] = v;
+	}
+}
+
+/* Exclusive scan of the nb block sums in place; runSums[nb] = the total. */
+__global__ void __launch_bounds__(kRunBlock) k_run_scan(const __grid_constant__ DrawParams P, uint32_t nb)
+{
+	gridDepSync();
+	__shared__ uint32_t sw[kRunBlock / 32];
+	__shared__ uint32_t carry;
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	if (threadIdx.x == 0) carry = 0;
+	__syncthreads();
+	for (uint32_t b0 = 0; b0 < nb; b0 += kRunBlock) {
+		const uint32_t b = b0 + threadIdx.x;
+		const uint32_t v = b < nb ? P.runSums[b] : 0u;
+		uint32_t incl = v;
+		for (int o = 1; o < 32; o <<= 1) {
+			const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+			if (lane >= o) incl += y;
+		}
+		if (lane == 31) sw[warp] = incl;
+		__syncthreads();
+		if (warp == 0) {
+			uint32_t w = sw[lane];
+			for (int o = 1; o < 32; o <<= 1) {
+				const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+				if (lane >= o) w += y;
+			}
+			sw[lane] = w;
+		}
+		__syncthreads();
+		const uint32_t excl = carry + (warp ? sw[warp - 1] : 0u) + incl - v;
+		if (b < nb) P.runSums[b] = excl;
+		__syncthreads();
+		if (threadIdx.x == kRunBlock - 1) carry = excl + v;
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) P.runSums[nb] = carry;
+}
+
+__global__ void __launch_bounds__(kRunBlock) k_run_expand(const __grid_constant__ DrawParams P, const uint32_t* vals)
+{
+	gridDepSync();
+	__shared__ uint32_t sw[kRunBlock / 32];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const uint32_t n = (uint32_t) min(P.ctr->entries, (unsigned long long) P.entryCap);
+	const uint32_t i = blockIdx.x * kRunBlock + threadIdx.x;
+	const uint32_t v = (i < n && !P.ctr->abort) ? vals[i] : 0u;
+	const uint32_t c = runCount(v);
+	uint32_t incl = c;
+	for (int o = 1; o < 32; o <<= 1) {
+		const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+		if (lane >= o) incl += y;
+	}
+	if (lane == 31) sw[warp] = incl;
+	__syncthreads();
+	if (warp == 0) {
+		uint32_t w = sw[lane];
+		for (int o = 1; o < 32; o <<= 1) {
+			const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+			if (lane >= o) w += y;
+		}
+		sw[lane] = w;
+	}
+	__syncthreads();
+	const uint32_t off = P.runSums[blockIdx.x] + (warp ? sw[warp - 1] : 0u) + incl - c;
+	if (i < n) P.fragOff[i] = off;
+	if (i == n) P.fragOff[n] = off;
+	const uint32_t k = v & ((1u << kRunCountShift) - 1u);
+	for (uint32_t j = 0; j < c; ++j)
+		if (off + j < P.fragCap) P.fragVals[off + j] = k * kRunFrags + j;
+}
+
+__global__ void k_run_tiles(const __grid_constant__ DrawParams P, uint32_t numTiles)
+{
+	gridDepSync();
+	const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= numTiles || P.ctr->abort) return;
+	const uint32_t a = P.tileStart[t], b = P.tileEnd[t];
+	if (b > a) {
+		P.tileStart[t] = P.fragOff[a];
+		P.tileEnd[t] = P.fragOff[b];
 	}
 }
 
@@ -1589,6 +1816,19 @@ void launchLineFrags(const DrawParams& P, cudaStream_t s)
 	if (!P.primCap) return;
 	pdlLaunch(k_line_frags, (P.primCap + 127) / 128, 128, 0, s, P);
 	pdlLaunch(k_line_frags_long, 152 * 8, 128, 0, s, P);
+}
+
+uint32_t runSumWords(uint32_t entryCap) { return (entryCap + kRunBlock - 1) / kRunBlock + 2; }
+
+void launchRunExpand(const DrawParams& P, const uint32_t* vals, uint32_t numTiles, cudaStream_t s)
+{
+	if (!P.entryCap) return;
+	/* one block more than the runs need, so that fragOff[n] is written even when n fills the last block */
+	const uint32_t nb = (P.entryCap + 1 + kRunBlock - 1) / kRunBlock;
+	pdlLaunch(k_run_sums, nb, kRunBlock, 0, s, P, vals);
+	pdlLaunch(k_run_scan, 1, kRunBlock, 0, s, P, nb);
+	pdlLaunch(k_run_expand, nb, kRunBlock, 0, s, P, vals);
+	pdlLaunch(k_run_tiles, (numTiles + 255) / 256, 256, 0, s, P, numTiles);
 }
 
 void launchVertexMulti(const DrawParams& P, uint32_t blocks, int maxStride, cudaStream_t s)

@@ -39,8 +39,15 @@ struct DrawParams {
 	TriAttr* triA;
 	LineRec* lines;
 	PointRec* points;
-	LineFrag* frags;
-	uint32_t primCap, fragCap;
+	LineFrag* frags;               /* line draws: kRunFrags records per pair slot */
+	uint32_t primCap;
+	unsigned long long fragCap;    /* records in frags */
+	/* line draws, after the sort: fragment offsets of the sorted runs
+	 * [entryCap + 1], the runs' block sums [runSumWords], and the record
+	 * numbers of the fragments in sorted order [fragCap] */
+	uint32_t* fragOff;
+	uint32_t* runSums;
+	uint32_t* fragVals;
 	/* (tile, item) pairs */
 	uint32_t* keys;
 	uint32_t* vals;
@@ -157,6 +164,13 @@ void launchBigEntries(const DrawParams& P, uint32_t jobsHint, cudaStream_t s);
 /* lambda tables of the big triangles (triangle draws) */
 void launchLambdaTables(const DrawParams& P, uint32_t jobsHint, cudaStream_t s);
 void launchLineFrags(const DrawParams& P, cudaStream_t s);
+/* Line draws: turns the sorted runs back into fragments (fragVals, and the
+ * tile ranges over them). */
+void launchRunExpand(const DrawParams& P, const uint32_t* vals, uint32_t numTiles, cudaStream_t s);
+uint32_t runSumWords(uint32_t entryCap);
+/* Largest pair capacity of a line draw (a run's slot shares its value word
+ * with its fragment count). */
+constexpr uint32_t kMaxLineEntries = (1u << kRunCountShift) - 1u;
 /* k_front.cu, multi-draw pass */
 void launchVertexMulti(const DrawParams& P, uint32_t blocks, int maxStride, cudaStream_t s);
 void launchClipPrepassMulti(const DrawParams& P, cudaStream_t s);

@@ -98,6 +98,9 @@ struct Registry {
  * while draw N's shading still reads draw N's winners. */
 struct DrawSet {
 	DeviceBuffer ctr, tileStart, tileEnd, heavy, vary, triR, triA, points, lines, frags, table, winner;
+	/* line draws: the runs' fragment offsets and block sums, and the
+	 * fragments in sorted order */
+	DeviceBuffer fragOff, runSums, fragVals;
 	/* the big-primitive list: written by setup, read by the binning and by
 	 * the lambda tables, which run on another stream than the next front */
 	DeviceBuffer big;
@@ -1675,6 +1678,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 
 	uint32_t primCap = (uint32_t) std::min<size_t>(nIn * outPer + 4096, 0x3FFFFFFFu);
 	uint32_t entryCap = (uint32_t) std::min<double>((double) (nIn * outPer) * g.entryRatio[kind] + 4096, 4.0e9);
+	if (kind == kKindLineFrag) entryCap = std::min(entryCap, kMaxLineEntries);
 	const uint32_t keyBits = sortKeyBits(numTiles);
 	const bool late = sp->fs->mayOverwriteDepth && shadeSupportsLateDepth(fsId);
 	const bool learned = learnedPrepare(P, kind, late, 1, g.stream);
@@ -1705,7 +1709,9 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		                           reserveClipFans(S, FN);
 		else if (kind == kKindPoint) ok = ok && S.points.reserve((size_t) primCap * sizeof(PointRec), FN);
 		else ok = ok && S.lines.reserve((size_t) primCap * sizeof(LineRec), FN) &&
-		          S.frags.reserve((size_t) entryCap * sizeof(LineFrag), FN);
+		          S.frags.reserve((size_t) entryCap * kRunFrags * sizeof(LineFrag), FN) &&
+		          S.fragVals.reserve((size_t) entryCap * kRunFrags * 4, FN) &&
+		          S.fragOff.reserve(((size_t) entryCap + 2) * 4, FN) && S.runSums.reserve((size_t) runSumWords(entryCap) * 4, FN);
 		if (!ok) return;
 		P.clip = S.clip.as<float4>();
 		P.vset0 = S.vset0.as<float4>();
@@ -1720,7 +1726,10 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		P.points = S.points.as<PointRec>();
 		P.frags = S.frags.as<LineFrag>();
 		P.primCap = primCap;
-		P.fragCap = kind == kKindLineFrag ? entryCap : 0;
+		P.fragCap = kind == kKindLineFrag ? (unsigned long long) entryCap * kRunFrags : 0;
+		P.fragVals = S.fragVals.as<uint32_t>();
+		P.fragOff = S.fragOff.as<uint32_t>();
+		P.runSums = S.runSums.as<uint32_t>();
 		P.keys = S.keys.as<uint32_t>();
 		P.vals = S.vals.as<uint32_t>();
 		P.entryCap = entryCap;
@@ -1776,7 +1785,12 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, fs);
 			cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, fs);
 			launchTileRanges(P, sk, numTiles, fs);
-			stageEnd(SRP_GPU_STAGE_BIN, 2 + 1 + (int) (keyBits / 8) + 1);
+			if (kind == kKindLineFrag) {
+				/* the sorted runs back to fragments: the resolve takes one item per fragment */
+				launchRunExpand(P, sv, numTiles, fs);
+				sv = P.fragVals;
+			}
+			stageEnd(SRP_GPU_STAGE_BIN, 2 + 1 + (int) (keyBits / 8) + 1 + (kind == kKindLineFrag ? 4 : 0));
 		};
 		auto resolve = [&]() {
 			stageBegin();
@@ -1803,7 +1817,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		                         (unsigned long long) (uintptr_t) fs, (unsigned long long) (uintptr_t) rs }),
 		           S, fs, rs, head, lateIb ? ib->ready : nullptr, head2, kind == kKindTri, mid, bin, resolve, !late, shade);
 		g.launches += 4 + (ib && !P.shadeAll ? 1 : 0) + (isTri(prim) ? 1 : 0) + (kind == kKindPoint ? 1 : 2) + 1 +
-		              keyBits / 8 + 1 +
+		              keyBits / 8 + 1 + (kind == kKindLineFrag ? 4 : 0) +
 		              (late ? 1 : 4);
 		if (!cudaOk(cudaGetLastError(), FN, "launch")) return;
 		/* wait for the setup counters only; the rest of the draw runs on */
@@ -1821,7 +1835,11 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			bool grew = false;
 			if (c.clipVerts > g.clipRows) { g.clipRows = (uint32_t) std::min<unsigned long long>(c.clipVerts * 2, 0x7FFFFFFF); grew = true; }
 			if (c.prims > primCap) { primCap = (uint32_t) std::min<unsigned long long>(c.prims + 1024, 0x3FFFFFFF); grew = true; }
-			if (c.entries > entryCap) { entryCap = (uint32_t) std::min<double>(c.entries * 1.25 + 1024, 4.0e9); grew = true; }
+			if (c.entries > entryCap) {
+				const double cap = kind == kKindLineFrag ? (double) kMaxLineEntries : 4.0e9;
+				const uint32_t want = (uint32_t) std::min<double>(c.entries * 1.25 + 1024, cap);
+				if (want > entryCap) { entryCap = want; grew = true; }
+			}
 			if (c.bigJobs > g.bigCap) { g.bigCap = (uint32_t) std::min<unsigned long long>(c.bigJobs * 2, 1u << 30); grew = true; }
 			if (c.clipTris > g.clipPolyCap) { g.clipPolyCap = (uint32_t) std::min<unsigned long long>(c.clipTris * 2, 1u << 30); grew = true; }
 			if (c.tableWords > g.tableCap) { g.tableCap = std::min<unsigned long long>(c.tableWords * 5 / 4 + 1024, 0xFFFFFFFFull); grew = true; }

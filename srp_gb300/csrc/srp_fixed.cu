@@ -95,7 +95,12 @@ size_t round256(size_t b) { return (b + 255) & ~(size_t) 255; }
 size_t binBytes(size_t E, bool lineFrags)
 {
 	const size_t e = E ? E : 1;
-	return 4 * round256(e * 4) + (lineFrags ? round256(e * sizeof(LineFrag)) : 0) +
+	/* line draws: kRunFrags records and fragment numbers per pair slot, the
+	 * runs' fragment offsets and their block sums */
+	const size_t lines = lineFrags ? round256(e * kRunFrags * sizeof(LineFrag)) + round256(e * kRunFrags * 4) +
+	                                     round256((e + 2) * 4) + round256((size_t) runSumWords((uint32_t) e) * 4)
+	                               : 0;
+	return 4 * round256(e * 4) + lines +
 	       round256(sortHistWords((uint32_t) e) * 4) + round256(sortPartialWords((uint32_t) e) * 4 + 64);
 }
 
@@ -168,13 +173,17 @@ extern "C" int srpGpuDrawFixedScratch(const SRPIndexBuffer* ib, const SRPVertexB
 	const size_t oTable = cv.take(tableBytes);
 	const size_t binRoom = (size_t) SRP_GPU_FIXED_SCRATCH_BYTES - cv.used;
 	const bool lineFrags = info.kind == kKindLineFrag;
-	size_t entryCap = std::min<size_t>(binRoom / (16 + (lineFrags ? sizeof(LineFrag) : 0) + 2), 0xF0000000u);
+	size_t entryCap = std::min<size_t>(binRoom / (16 + (lineFrags ? kRunFrags * (sizeof(LineFrag) + 4) + 4 : 0) + 2),
+	                                   lineFrags ? (size_t) kMaxLineEntries : (size_t) 0xF0000000u);
 	while (entryCap > 0 && binBytes(entryCap, lineFrags) > binRoom) entryCap -= entryCap / 64 + 1;
 	const size_t oKeys = cv.take(entryCap * 4);
 	const size_t oVals = cv.take(entryCap * 4);
 	const size_t oKeys2 = cv.take(entryCap * 4);
 	const size_t oVals2 = cv.take(entryCap * 4);
-	const size_t oFrags = lineFrags ? cv.take(entryCap * sizeof(LineFrag)) : 0;
+	const size_t oFrags = lineFrags ? cv.take(entryCap * kRunFrags * sizeof(LineFrag)) : 0;
+	const size_t oFragVals = lineFrags ? cv.take(entryCap * kRunFrags * 4) : 0;
+	const size_t oFragOff = lineFrags ? cv.take((entryCap + 2) * 4) : 0;
+	const size_t oRunSums = lineFrags ? cv.take((size_t) runSumWords((uint32_t) entryCap) * 4) : 0;
 	const size_t oHist = cv.take(sortHistWords((uint32_t) std::max<size_t>(entryCap, 1)) * 4);
 	const size_t oPartials = cv.take(sortPartialWords((uint32_t) std::max<size_t>(entryCap, 1)) * 4 + 64);
 	if (cv.used > (size_t) SRP_GPU_FIXED_SCRATCH_BYTES) {
@@ -208,7 +217,12 @@ extern "C" int srpGpuDrawFixedScratch(const SRPIndexBuffer* ib, const SRPVertexB
 		P.frags = (LineFrag*) (base + oFrags);
 	}
 	P.primCap = (uint32_t) primCap;
-	P.fragCap = lineFrags ? (uint32_t) entryCap : 0;
+	P.fragCap = lineFrags ? (unsigned long long) entryCap * kRunFrags : 0;
+	if (lineFrags) {
+		P.fragVals = (uint32_t*) (base + oFragVals);
+		P.fragOff = (uint32_t*) (base + oFragOff);
+		P.runSums = (uint32_t*) (base + oRunSums);
+	}
 	P.bigJobs = (uint4*) (base + oBig);
 	P.bigCap = (uint32_t) bigCap;
 	P.table = (float*) (base + oTable);
@@ -282,6 +296,12 @@ extern "C" int srpGpuDrawFixedScratch(const SRPIndexBuffer* ib, const SRPVertexB
 		cudaMemsetAsync(P.tileStart, 0, (size_t) info.numTiles * 4, s);
 		cudaMemsetAsync(P.tileEnd, 0, (size_t) info.numTiles * 4, s);
 		launchTileRanges(P, sk, info.numTiles, s);
+		if (lineFrags) {
+			/* the sorted runs back to fragments */
+			launchRunExpand(P, sv, info.numTiles, s);
+			sv = P.fragVals;
+			launches += 4;
+		}
 		if (info.late) {
 			launchResolveLate(P, info.kind, sv, info.numTiles, s);
 			launches += 2;
