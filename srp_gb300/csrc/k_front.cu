@@ -1336,10 +1336,11 @@ __global__ void k_line_frags_long(const __grid_constant__ DrawParams P)
 }
 
 /* Runs back to fragments, after the sort: the fragment counts of the sorted
- * runs are scanned (per block of kRunBlock, then over the blocks), every run
- * writes its fragments' record numbers to fragVals in sorted order, and the
- * tile ranges are moved from runs to fragments, so that the resolve and
- * shading kernels see one item per fragment in (tile, line, step) order. */
+ * runs are scanned (per block of kRunBlock, then over the blocks), and every
+ * run writes its fragments' record numbers to fragVals in sorted order and,
+ * if it is the first or last run of its tile, the tile's fragment range, so
+ * that the resolve and shading kernels see one item per fragment in (tile,
+ * line, step) order. */
 constexpr int kRunBlock = 1024;
 
 __device__ __forceinline__ uint32_t runCount(uint32_t v) { return v >> kRunCountShift; }
@@ -1398,7 +1399,8 @@ __global__ void __launch_bounds__(kRunBlock) k_run_scan(const __grid_constant__ 
 	if (threadIdx.x == 0) P.runSums[nb] = carry;
 }
 
-__global__ void __launch_bounds__(kRunBlock) k_run_expand(const __grid_constant__ DrawParams P, const uint32_t* vals)
+__global__ void __launch_bounds__(kRunBlock) k_run_expand(const __grid_constant__ DrawParams P, const uint32_t* keys,
+                                                          const uint32_t* vals, uint32_t numTiles)
 {
 	gridDepSync();
 	__shared__ uint32_t sw[kRunBlock / 32];
@@ -1424,23 +1426,14 @@ __global__ void __launch_bounds__(kRunBlock) k_run_expand(const __grid_constant_
 	}
 	__syncthreads();
 	const uint32_t off = P.runSums[blockIdx.x] + (warp ? sw[warp - 1] : 0u) + incl - c;
-	if (i < n) P.fragOff[i] = off;
-	if (i == n) P.fragOff[n] = off;
+	if (c == 0) return;
 	const uint32_t k = v & ((1u << kRunCountShift) - 1u);
 	for (uint32_t j = 0; j < c; ++j)
 		if (off + j < P.fragCap) P.fragVals[off + j] = k * kRunFrags + j;
-}
-
-__global__ void k_run_tiles(const __grid_constant__ DrawParams P, uint32_t numTiles)
-{
-	gridDepSync();
-	const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-	if (t >= numTiles || P.ctr->abort) return;
-	const uint32_t a = P.tileStart[t], b = P.tileEnd[t];
-	if (b > a) {
-		P.tileStart[t] = P.fragOff[a];
-		P.tileEnd[t] = P.fragOff[b];
-	}
+	const uint32_t key = keys[i];
+	if (key >= numTiles) return;
+	if (i == 0 || keys[i - 1] != key) P.tileStart[key] = off;
+	if (i + 1 == n || keys[i + 1] != key) P.tileEnd[key] = off + c;
 }
 
 /* ============================================================ multi-draw */
@@ -1820,15 +1813,13 @@ void launchLineFrags(const DrawParams& P, cudaStream_t s)
 
 uint32_t runSumWords(uint32_t entryCap) { return (entryCap + kRunBlock - 1) / kRunBlock + 2; }
 
-void launchRunExpand(const DrawParams& P, const uint32_t* vals, uint32_t numTiles, cudaStream_t s)
+void launchRunExpand(const DrawParams& P, const uint32_t* keys, const uint32_t* vals, uint32_t numTiles, cudaStream_t s)
 {
 	if (!P.entryCap) return;
-	/* one block more than the runs need, so that fragOff[n] is written even when n fills the last block */
-	const uint32_t nb = (P.entryCap + 1 + kRunBlock - 1) / kRunBlock;
+	const uint32_t nb = (P.entryCap + kRunBlock - 1) / kRunBlock;
 	pdlLaunch(k_run_sums, nb, kRunBlock, 0, s, P, vals);
 	pdlLaunch(k_run_scan, 1, kRunBlock, 0, s, P, nb);
-	pdlLaunch(k_run_expand, nb, kRunBlock, 0, s, P, vals);
-	pdlLaunch(k_run_tiles, (numTiles + 255) / 256, 256, 0, s, P, numTiles);
+	pdlLaunch(k_run_expand, nb, kRunBlock, 0, s, P, keys, vals, numTiles);
 }
 
 void launchVertexMulti(const DrawParams& P, uint32_t blocks, int maxStride, cudaStream_t s)

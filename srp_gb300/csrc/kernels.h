@@ -42,10 +42,9 @@ struct DrawParams {
 	LineFrag* frags;               /* line draws: kRunFrags records per pair slot */
 	uint32_t primCap;
 	unsigned long long fragCap;    /* records in frags */
-	/* line draws, after the sort: fragment offsets of the sorted runs
-	 * [entryCap + 1], the runs' block sums [runSumWords], and the record
-	 * numbers of the fragments in sorted order [fragCap] */
-	uint32_t* fragOff;
+	/* line draws, after the sort: the sorted runs' block sums
+	 * [runSumWords], and the record numbers of the fragments in sorted order
+	 * [fragCap] */
 	uint32_t* runSums;
 	uint32_t* fragVals;
 	/* (tile, item) pairs */
@@ -165,8 +164,8 @@ void launchBigEntries(const DrawParams& P, uint32_t jobsHint, cudaStream_t s);
 void launchLambdaTables(const DrawParams& P, uint32_t jobsHint, cudaStream_t s);
 void launchLineFrags(const DrawParams& P, cudaStream_t s);
 /* Line draws: turns the sorted runs back into fragments (fragVals, and the
- * tile ranges over them). */
-void launchRunExpand(const DrawParams& P, const uint32_t* vals, uint32_t numTiles, cudaStream_t s);
+ * tile ranges over them, in place of launchTileRanges). */
+void launchRunExpand(const DrawParams& P, const uint32_t* keys, const uint32_t* vals, uint32_t numTiles, cudaStream_t s);
 uint32_t runSumWords(uint32_t entryCap);
 /* Largest pair capacity of a line draw (a run's slot shares its value word
  * with its fragment count). */

@@ -98,9 +98,8 @@ struct Registry {
  * while draw N's shading still reads draw N's winners. */
 struct DrawSet {
 	DeviceBuffer ctr, tileStart, tileEnd, heavy, vary, triR, triA, points, lines, frags, table, winner;
-	/* line draws: the runs' fragment offsets and block sums, and the
-	 * fragments in sorted order */
-	DeviceBuffer fragOff, runSums, fragVals;
+	/* line draws: the runs' block sums, and the fragments in sorted order */
+	DeviceBuffer runSums, fragVals;
 	/* the big-primitive list: written by setup, read by the binning and by
 	 * the lambda tables, which run on another stream than the next front */
 	DeviceBuffer big;
@@ -1711,7 +1710,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		else ok = ok && S.lines.reserve((size_t) primCap * sizeof(LineRec), FN) &&
 		          S.frags.reserve((size_t) entryCap * kRunFrags * sizeof(LineFrag), FN) &&
 		          S.fragVals.reserve((size_t) entryCap * kRunFrags * 4, FN) &&
-		          S.fragOff.reserve(((size_t) entryCap + 2) * 4, FN) && S.runSums.reserve((size_t) runSumWords(entryCap) * 4, FN);
+		          S.runSums.reserve((size_t) runSumWords(entryCap) * 4, FN);
 		if (!ok) return;
 		P.clip = S.clip.as<float4>();
 		P.vset0 = S.vset0.as<float4>();
@@ -1728,7 +1727,6 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		P.primCap = primCap;
 		P.fragCap = kind == kKindLineFrag ? (unsigned long long) entryCap * kRunFrags : 0;
 		P.fragVals = S.fragVals.as<uint32_t>();
-		P.fragOff = S.fragOff.as<uint32_t>();
 		P.runSums = S.runSums.as<uint32_t>();
 		P.keys = S.keys.as<uint32_t>();
 		P.vals = S.vals.as<uint32_t>();
@@ -1784,13 +1782,14 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 			            S.partials.as<uint32_t>(), &sk, &sv, fs);
 			cudaMemsetAsync(P.tileStart, 0, (size_t) numTiles * 4, fs);
 			cudaMemsetAsync(P.tileEnd, 0, (size_t) numTiles * 4, fs);
-			launchTileRanges(P, sk, numTiles, fs);
 			if (kind == kKindLineFrag) {
 				/* the sorted runs back to fragments: the resolve takes one item per fragment */
-				launchRunExpand(P, sv, numTiles, fs);
+				launchRunExpand(P, sk, sv, numTiles, fs);
 				sv = P.fragVals;
+			} else {
+				launchTileRanges(P, sk, numTiles, fs);
 			}
-			stageEnd(SRP_GPU_STAGE_BIN, 2 + 1 + (int) (keyBits / 8) + 1 + (kind == kKindLineFrag ? 4 : 0));
+			stageEnd(SRP_GPU_STAGE_BIN, 2 + 1 + (int) (keyBits / 8) + 1 + (kind == kKindLineFrag ? 2 : 0));
 		};
 		auto resolve = [&]() {
 			stageBegin();
@@ -1817,7 +1816,7 @@ static void runDraw(const SRPIndexBuffer* ibc, const SRPVertexBuffer* vbc, const
 		                         (unsigned long long) (uintptr_t) fs, (unsigned long long) (uintptr_t) rs }),
 		           S, fs, rs, head, lateIb ? ib->ready : nullptr, head2, kind == kKindTri, mid, bin, resolve, !late, shade);
 		g.launches += 4 + (ib && !P.shadeAll ? 1 : 0) + (isTri(prim) ? 1 : 0) + (kind == kKindPoint ? 1 : 2) + 1 +
-		              keyBits / 8 + 1 + (kind == kKindLineFrag ? 4 : 0) +
+		              keyBits / 8 + 1 + (kind == kKindLineFrag ? 2 : 0) +
 		              (late ? 1 : 4);
 		if (!cudaOk(cudaGetLastError(), FN, "launch")) return;
 		/* wait for the setup counters only; the rest of the draw runs on */

@@ -95,10 +95,10 @@ size_t round256(size_t b) { return (b + 255) & ~(size_t) 255; }
 size_t binBytes(size_t E, bool lineFrags)
 {
 	const size_t e = E ? E : 1;
-	/* line draws: kRunFrags records and fragment numbers per pair slot, the
-	 * runs' fragment offsets and their block sums */
+	/* line draws: kRunFrags records and fragment numbers per pair slot, and
+	 * the runs' block sums */
 	const size_t lines = lineFrags ? round256(e * kRunFrags * sizeof(LineFrag)) + round256(e * kRunFrags * 4) +
-	                                     round256((e + 2) * 4) + round256((size_t) runSumWords((uint32_t) e) * 4)
+	                                     round256((size_t) runSumWords((uint32_t) e) * 4)
 	                               : 0;
 	return 4 * round256(e * 4) + lines +
 	       round256(sortHistWords((uint32_t) e) * 4) + round256(sortPartialWords((uint32_t) e) * 4 + 64);
@@ -173,7 +173,7 @@ extern "C" int srpGpuDrawFixedScratch(const SRPIndexBuffer* ib, const SRPVertexB
 	const size_t oTable = cv.take(tableBytes);
 	const size_t binRoom = (size_t) SRP_GPU_FIXED_SCRATCH_BYTES - cv.used;
 	const bool lineFrags = info.kind == kKindLineFrag;
-	size_t entryCap = std::min<size_t>(binRoom / (16 + (lineFrags ? kRunFrags * (sizeof(LineFrag) + 4) + 4 : 0) + 2),
+	size_t entryCap = std::min<size_t>(binRoom / (16 + (lineFrags ? kRunFrags * (sizeof(LineFrag) + 4) + 1 : 0) + 2),
 	                                   lineFrags ? (size_t) kMaxLineEntries : (size_t) 0xF0000000u);
 	while (entryCap > 0 && binBytes(entryCap, lineFrags) > binRoom) entryCap -= entryCap / 64 + 1;
 	const size_t oKeys = cv.take(entryCap * 4);
@@ -182,7 +182,6 @@ extern "C" int srpGpuDrawFixedScratch(const SRPIndexBuffer* ib, const SRPVertexB
 	const size_t oVals2 = cv.take(entryCap * 4);
 	const size_t oFrags = lineFrags ? cv.take(entryCap * kRunFrags * sizeof(LineFrag)) : 0;
 	const size_t oFragVals = lineFrags ? cv.take(entryCap * kRunFrags * 4) : 0;
-	const size_t oFragOff = lineFrags ? cv.take((entryCap + 2) * 4) : 0;
 	const size_t oRunSums = lineFrags ? cv.take((size_t) runSumWords((uint32_t) entryCap) * 4) : 0;
 	const size_t oHist = cv.take(sortHistWords((uint32_t) std::max<size_t>(entryCap, 1)) * 4);
 	const size_t oPartials = cv.take(sortPartialWords((uint32_t) std::max<size_t>(entryCap, 1)) * 4 + 64);
@@ -220,7 +219,6 @@ extern "C" int srpGpuDrawFixedScratch(const SRPIndexBuffer* ib, const SRPVertexB
 	P.fragCap = lineFrags ? (unsigned long long) entryCap * kRunFrags : 0;
 	if (lineFrags) {
 		P.fragVals = (uint32_t*) (base + oFragVals);
-		P.fragOff = (uint32_t*) (base + oFragOff);
 		P.runSums = (uint32_t*) (base + oRunSums);
 	}
 	P.bigJobs = (uint4*) (base + oBig);
@@ -295,12 +293,13 @@ extern "C" int srpGpuDrawFixedScratch(const SRPIndexBuffer* ib, const SRPVertexB
 		launches += 1 + keyBits / 8;
 		cudaMemsetAsync(P.tileStart, 0, (size_t) info.numTiles * 4, s);
 		cudaMemsetAsync(P.tileEnd, 0, (size_t) info.numTiles * 4, s);
-		launchTileRanges(P, sk, info.numTiles, s);
 		if (lineFrags) {
-			/* the sorted runs back to fragments */
-			launchRunExpand(P, sv, info.numTiles, s);
+			/* the sorted runs back to fragments, with their tile ranges */
+			launchRunExpand(P, sk, sv, info.numTiles, s);
 			sv = P.fragVals;
-			launches += 4;
+			launches += 2;
+		} else {
+			launchTileRanges(P, sk, info.numTiles, s);
 		}
 		if (info.late) {
 			launchResolveLate(P, info.kind, sv, info.numTiles, s);
