@@ -53,7 +53,7 @@ typedef struct SRPStdUniform
 	uint32_t extraOffset;    /* srpVsWorld: first extra word appended to varyings */
 	uint32_t extraCount;     /* srpVsWorld: number of extra words (<= 16) */
 	uint32_t varyingOffset;  /* fragment shaders: first varying word they read */
-	uint32_t pad0;
+	float texelScale;        /* srpFsTextureLod: texels per pixel at clip w = 1 */
 	SRPTexture* texture;     /* replaced by a device descriptor on upload */
 } SRPStdUniform;
 
@@ -83,6 +83,7 @@ typedef enum SRPGpuFragmentShaderId
 	SRP_GPU_FS_MIXED = 11,          /* colour from the packed mixed-type block at word o (srpFsMixed) */
 	SRP_GPU_FS_BYTE_PALETTE = 12,   /* 0 red, 1 green, 2 blue, else hashed: uint8 varying at byte 4*o */
 	SRP_GPU_FS_PRIMITIVE_MOD = 13,  /* ((id*97, id*57, id*23) mod 255) / 255 / colour[0] */
+	SRP_GPU_FS_TEXTURE_LOD = 14,    /* texture(uv = varyings[o..o+1]) at lod log2(max(1, texelScale * w)) */
 	SRP_GPU_FS_COUNT
 } SRPGpuFragmentShaderId;
 
@@ -107,6 +108,7 @@ void srpFsFlatInt(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out);
 void srpFsMixed(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out);
 void srpFsBytePalette(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out);
 void srpFsPrimitiveMod(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out);
+void srpFsTextureLod(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out);
 
 #ifdef __cplusplus
 }

@@ -7,8 +7,9 @@
  * nvcc -fmad=false): the vertex transform feeds coverage and depth and has to
  * round exactly like the reference's mat4MultiplyVec4 (src/math/mat.c:16-45).
  *
- * Device builds define SRP_DEVICE_TEXTURE_SAMPLE(tex, u, v, out) before
- * including this header; the host build calls srpTextureGetFilteredColor. */
+ * Device builds define SRP_DEVICE_TEXTURE_SAMPLE(tex, u, v, out) and
+ * SRP_DEVICE_TEXTURE_SAMPLE_LOD(tex, u, v, lod, out) before including this
+ * header; the host build calls srpTextureGetFilteredColor(Lod). */
 #pragma once
 
 #include <math.h>
@@ -24,8 +25,15 @@
 
 #if defined(__CUDA_ARCH__) && !defined(SRP_SHADERLIB_HOST_ONLY)
 #define SRP_TEXTURE_SAMPLE(tex, u, v, out) SRP_DEVICE_TEXTURE_SAMPLE(tex, u, v, out)
+#define SRP_TEXTURE_SAMPLE_LOD(tex, u, v, lod, out) SRP_DEVICE_TEXTURE_SAMPLE_LOD(tex, u, v, lod, out)
+#elif defined(SRP_SHADERLIB_NEAREST_ONLY)
+/* host build linked against a library without the filtering additions of
+ * srp/texture.h (the reference's own): every sample is at level 0 */
+#define SRP_TEXTURE_SAMPLE(tex, u, v, out) srpTextureGetFilteredColor(tex, u, v, out)
+#define SRP_TEXTURE_SAMPLE_LOD(tex, u, v, lod, out) srpTextureGetFilteredColor(tex, u, v, out)
 #else
 #define SRP_TEXTURE_SAMPLE(tex, u, v, out) srpTextureGetFilteredColor(tex, u, v, out)
+#define SRP_TEXTURE_SAMPLE_LOD(tex, u, v, lod, out) srpTextureGetFilteredColorLod(tex, u, v, lod, out)
 #endif
 
 /* Word access through memcpy: user vertex and varying blocks may be byte
@@ -220,6 +228,19 @@ SRP_SHADER_FN void srpslFsTexture(SRPFragmentShaderIn* in, SRPFragmentShaderOut*
 	const SRPStdUniform* u = (const SRPStdUniform*) in->uniform;
 	uint32_t o = u->varyingOffset;
 	SRP_TEXTURE_SAMPLE(u->texture, srpslLoadF(in->varyings, o), srpslLoadF(in->varyings, o + 1), out->color);
+}
+
+/* Texture at a level of detail that grows with the distance: the texture
+ * shrinks on screen as 1 / w (w = fragCoord[3], the interpolated clip w), so
+ * lod = log2(max(1, texelScale * w)), texelScale being the texels a pixel
+ * spans at w = 1. */
+SRP_SHADER_FN void srpslFsTextureLod(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out)
+{
+	const SRPStdUniform* u = (const SRPStdUniform*) in->uniform;
+	uint32_t o = u->varyingOffset;
+	float k = u->texelScale * in->fragCoord[3];
+	float lod = k > 1.0f ? log2f(k) : 0.0f;
+	SRP_TEXTURE_SAMPLE_LOD(u->texture, srpslLoadF(in->varyings, o), srpslLoadF(in->varyings, o + 1), lod, out->color);
 }
 
 SRP_SHADER_FN void srpslFsTextureModulate(SRPFragmentShaderIn* in, SRPFragmentShaderOut* out)

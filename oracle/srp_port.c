@@ -276,7 +276,14 @@ static void ndcToScreen(const SRPFramebuffer* fb, const float* ndc, float* ss)
 
 /* ---------------------------------------------------------------- texture */
 
-struct SRPTexture { uint8_t* data; int width, height, wm1, hm1; SRPTextureWrappingMode wx, wy; };
+struct SRPTexture {
+	uint8_t* data; int width, height, wm1, hm1; SRPTextureWrappingMode wx, wy;
+	/* filtering (an addition: the reference samples the nearest texel only) */
+	int filter, nLevels;
+	int lw[32], lh[32];
+	size_t loff[32];      /* texel offset of each level in mips (levels 1..) */
+	uint8_t* mips;
+};
 
 SRPTexture* srpNewTextureFromMemory(const uint8_t* texels, int w, int h, int ch,
                                     SRPTextureWrappingMode wx, SRPTextureWrappingMode wy)
@@ -290,6 +297,10 @@ SRPTexture* srpNewTextureFromMemory(const uint8_t* texels, int w, int h, int ch,
 	for (size_t i = 0; i < (size_t) w * h; ++i)
 		memcpy(t->data + 3 * i, texels + (size_t) ch * i, 3);
 	t->width = w; t->height = h; t->wm1 = w - 1; t->hm1 = h - 1; t->wx = wx; t->wy = wy;
+	t->filter = SRP_TEXTURE_FILTER_NEAREST;
+	t->nLevels = 1;
+	t->lw[0] = w; t->lh[0] = h; t->loff[0] = 0;
+	t->mips = NULL;
 	return t;
 }
 
@@ -307,12 +318,16 @@ SRPTexture* srpNewTexture(const char* path, SRPTextureWrappingMode wx, SRPTextur
 	return t;
 }
 
-void srpFreeTexture(SRPTexture* t) { if (t) { free(t->data); free(t); } }
+void srpFreeTexture(SRPTexture* t) { if (t) { free(t->data); free(t->mips); free(t); } }
+
+void srpTextureGetFilteredColorLod(const SRPTexture* t, float u, float v, float lod, float out[4]);
 
 void srpTextureGetFilteredColor(const SRPTexture* t, float u, float v, float out[4])
 {
 	/* src/core/texture.c:56-81: wrap only outside [0, 1], nearest texel,
-	 * rows stored top first, alpha 1 (3 stored channels). */
+	 * rows stored top first, alpha 1 (3 stored channels); a texture set to a
+	 * filter (an addition) samples level 0 with it. */
+	if (t->filter != SRP_TEXTURE_FILTER_NEAREST) { srpTextureGetFilteredColorLod(t, u, v, 0.0f, out); return; }
 	if (u < 0 || u > 1) u = (float) (t->wx == TW_REPEAT ? (double) u - floor(u) : fmax(0.0, fmin(1.0, u)));
 	if (v < 0 || v > 1) v = (float) (t->wy == TW_REPEAT ? (double) v - floor(v) : fmax(0.0, fmin(1.0, v)));
 	float x = (float) t->wm1 * u;
@@ -324,6 +339,107 @@ void srpTextureGetFilteredColor(const SRPTexture* t, float u, float v, float out
 	out[0] = p[0] * inv255;
 	out[1] = p[1] * inv255;
 	out[2] = p[2] * inv255;
+	out[3] = 1.f;
+}
+
+/* ------------------------------------------------------ texture filtering
+ * Not in the reference (its README.md:71-72 lists bilinear filtering and
+ * mipmapping as to do): the definition of srp/texture.h, restated here in
+ * plain C as the checker of the device sampler. */
+
+int srpTextureMipLevels(int w, int h)
+{
+	int n = 1;
+	while (w > 1 || h > 1) { w = w > 1 ? w / 2 : 1; h = h > 1 ? h / 2 : 1; ++n; }
+	return n;
+}
+
+static const uint8_t* texel(const SRPTexture* t, int l, int x, int y)
+{
+	if (l == 0) return t->data + 3 * ((size_t) y * t->width + x);
+	return t->mips + 3 * (t->loff[l] + (size_t) y * t->lw[l] + x);
+}
+
+static void buildMips(SRPTexture* t)
+{
+	const int n = srpTextureMipLevels(t->width, t->height);
+	size_t total = 0;
+	int w = t->width, h = t->height;
+	for (int l = 1; l < n; ++l) {
+		w = w > 1 ? w / 2 : 1; h = h > 1 ? h / 2 : 1;
+		t->lw[l] = w; t->lh[l] = h; t->loff[l] = total;
+		total += (size_t) w * h;
+	}
+	t->mips = (uint8_t*) xmalloc(total * 3 + 3);
+	for (int l = 1; l < n; ++l) {
+		const int pw = t->lw[l - 1], ph = t->lh[l - 1];
+		for (int j = 0; j < t->lh[l]; ++j)
+			for (int i = 0; i < t->lw[l]; ++i) {
+				const int x0 = 2 * i < pw ? 2 * i : pw - 1, x1 = 2 * i + 1 < pw ? 2 * i + 1 : pw - 1;
+				const int y0 = 2 * j < ph ? 2 * j : ph - 1, y1 = 2 * j + 1 < ph ? 2 * j + 1 : ph - 1;
+				const uint8_t *a = texel(t, l - 1, x0, y0), *b = texel(t, l - 1, x1, y0);
+				const uint8_t *c = texel(t, l - 1, x0, y1), *d = texel(t, l - 1, x1, y1);
+				uint8_t* o = t->mips + 3 * (t->loff[l] + (size_t) j * t->lw[l] + i);
+				for (int k = 0; k < 3; ++k) o[k] = (uint8_t) ((a[k] + b[k] + c[k] + d[k] + 2) / 4);
+			}
+	}
+	t->nLevels = n;
+}
+
+void srpTextureSetFilter(SRPTexture* t, SRPTextureFilter f)
+{
+	if (f != SRP_TEXTURE_FILTER_NEAREST && f != SRP_TEXTURE_FILTER_BILINEAR && f != SRP_TEXTURE_FILTER_TRILINEAR) {
+		message(SRP_MESSAGE_ERROR, SRP_MESSAGE_SEVERITY_HIGH, "srpTextureSetFilter",
+		        "Unknown texture filter (%i). Falling back to SRP_TEXTURE_FILTER_NEAREST", (int) f);
+		f = SRP_TEXTURE_FILTER_NEAREST;
+	}
+	t->filter = f;
+	if (f == SRP_TEXTURE_FILTER_TRILINEAR && !t->mips) buildMips(t);
+}
+
+SRPTextureFilter srpTextureGetFilter(const SRPTexture* t) { return (SRPTextureFilter) t->filter; }
+
+/* Bilinear sample of level l at wrapped (u, v), channels in 0..255. */
+static void bilinear(const SRPTexture* t, int l, float u, float v, float c[3])
+{
+	const int w = t->lw[l], h = t->lh[l];
+	const float x = (float) (w - 1) * u, y = (float) (h - 1) * (1.0f - v);
+	const float fx0 = floorf(x), fy0 = floorf(y);
+	int x0 = (int) fx0, y0 = (int) fy0;
+	if (x0 < 0) x0 = 0;
+	if (x0 > w - 1) x0 = w - 1;
+	if (y0 < 0) y0 = 0;
+	if (y0 > h - 1) y0 = h - 1;
+	const float fx = x - fx0, fy = y - fy0;
+	const int x1 = x0 + 1 < w ? x0 + 1 : (t->wx == TW_REPEAT ? 0 : w - 1);
+	const int y1 = y0 + 1 < h ? y0 + 1 : (t->wy == TW_REPEAT ? 0 : h - 1);
+	const uint8_t *a = texel(t, l, x0, y0), *b = texel(t, l, x1, y0), *d = texel(t, l, x0, y1), *e = texel(t, l, x1, y1);
+	for (int k = 0; k < 3; ++k) {
+		const float top = (float) a[k] + fx * ((float) b[k] - (float) a[k]);
+		const float bot = (float) d[k] + fx * ((float) e[k] - (float) d[k]);
+		c[k] = top + fy * (bot - top);
+	}
+}
+
+void srpTextureGetFilteredColorLod(const SRPTexture* t, float u, float v, float lod, float out[4])
+{
+	if (t->filter == SRP_TEXTURE_FILTER_NEAREST) { srpTextureGetFilteredColor(t, u, v, out); return; }
+	if (u < 0 || u > 1) u = (float) (t->wx == TW_REPEAT ? (double) u - floor(u) : fmax(0.0, fmin(1.0, u)));
+	if (v < 0 || v > 1) v = (float) (t->wy == TW_REPEAT ? (double) v - floor(v) : fmax(0.0, fmin(1.0, v)));
+	float c[3];
+	bilinear(t, 0, u, v, c);
+	if (t->filter == SRP_TEXTURE_FILTER_TRILINEAR && t->nLevels > 1) {
+		const float top = (float) (t->nLevels - 1);
+		const float ld = lod > 0.0f ? (lod < top ? lod : top) : 0.0f;
+		const int l0 = (int) floorf(ld);
+		const float f = ld - (float) l0;
+		float c0[3], c1[3];
+		bilinear(t, l0, u, v, c0);
+		bilinear(t, l0 + 1 < t->nLevels ? l0 + 1 : l0, u, v, c1);
+		for (int k = 0; k < 3; ++k) c[k] = c0[k] + f * (c1[k] - c0[k]);
+	}
+	const float inv255 = (float) (1. / 255.);
+	for (int k = 0; k < 3; ++k) out[k] = c[k] * inv255;
 	out[3] = 1.f;
 }
 

@@ -106,9 +106,65 @@ __device__ __forceinline__ uint32_t packColor(const float c[4])
 	return r;
 }
 
-/* Nearest texel with the reference's wrap rules (src/core/texture.c:56-81). */
+/* Bilinear sample of mip level l at wrapped (u, v): x = (w - 1) u,
+ * y = (h - 1)(1 - v), the texels at floor(x), floor(y) and +1 (the +1
+ * neighbour wraps or clamps) blended by the fractions, per channel in
+ * 0..255 (srpTextureSetFilter's definition, srp/texture.h). */
+__device__ __forceinline__ void textureBilinear(const TextureDesc* t, int l, float u, float v, float c[3])
+{
+	const int w = t->lw[l], h = t->lh[l];
+	const float x = __fmul_rn((float) (w - 1), u), y = __fmul_rn((float) (h - 1), __fsub_rn(1.0f, v));
+	const float fx0 = floorf(x), fy0 = floorf(y);
+	int x0 = (int) fx0, y0 = (int) fy0;
+	x0 = min(max(x0, 0), w - 1);
+	y0 = min(max(y0, 0), h - 1);
+	const float fx = __fsub_rn(x, fx0), fy = __fsub_rn(y, fy0);
+	const int x1 = x0 + 1 < w ? x0 + 1 : (t->wrapX == 0 ? 0 : w - 1);
+	const int y1 = y0 + 1 < h ? y0 + 1 : (t->wrapY == 0 ? 0 : h - 1);
+	const uint32_t* L = t->texels + t->loff[l];
+	const uint32_t a = __ldg(L + (size_t) y0 * w + x0), b = __ldg(L + (size_t) y0 * w + x1);
+	const uint32_t d = __ldg(L + (size_t) y1 * w + x0), e = __ldg(L + (size_t) y1 * w + x1);
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+		const float ta = (float) ((a >> (8 * k)) & 0xFFu), tb = (float) ((b >> (8 * k)) & 0xFFu);
+		const float td = (float) ((d >> (8 * k)) & 0xFFu), te = (float) ((e >> (8 * k)) & 0xFFu);
+		const float top = __fadd_rn(ta, __fmul_rn(fx, __fsub_rn(tb, ta)));
+		const float bot = __fadd_rn(td, __fmul_rn(fx, __fsub_rn(te, td)));
+		c[k] = __fadd_rn(top, __fmul_rn(fy, __fsub_rn(bot, top)));
+	}
+}
+
+/* Filtered sample at level of detail lod: NEAREST and BILINEAR read level 0,
+ * TRILINEAR blends the bilinear samples of floor(lod) and the next level
+ * (lod clamped to the chain). */
+__device__ __forceinline__ void textureFiltered(const TextureDesc* t, float u, float v, float lod, float out[4])
+{
+	if (u < 0.0f || u > 1.0f) u = t->wrapX == 0 ? __fsub_rn(u, floorf(u)) : fmaxf(0.0f, fminf(1.0f, u));
+	if (v < 0.0f || v > 1.0f) v = t->wrapY == 0 ? __fsub_rn(v, floorf(v)) : fmaxf(0.0f, fminf(1.0f, v));
+	float c[3];
+	textureBilinear(t, 0, u, v, c);
+	if (t->filter == 2 && t->nLevels > 1) {
+		const float top = (float) (t->nLevels - 1);
+		const float ld = lod > 0.0f ? (lod < top ? lod : top) : 0.0f;   /* NaN: level 0 */
+		const int l0 = (int) floorf(ld);
+		const float f = __fsub_rn(ld, (float) l0);
+		float c0[3], c1[3];
+		textureBilinear(t, l0, u, v, c0);
+		textureBilinear(t, l0 + 1 < t->nLevels ? l0 + 1 : l0, u, v, c1);
+#pragma unroll
+		for (int k = 0; k < 3; ++k) c[k] = __fadd_rn(c0[k], __fmul_rn(f, __fsub_rn(c1[k], c0[k])));
+	}
+	const float inv255 = (float) (1. / 255.);
+#pragma unroll
+	for (int k = 0; k < 3; ++k) out[k] = __fmul_rn(c[k], inv255);
+	out[3] = 1.0f;
+}
+
+/* Nearest texel with the reference's wrap rules (src/core/texture.c:56-81);
+ * textures set to a filter go to textureFiltered at level 0. */
 __device__ __forceinline__ void textureSample(const TextureDesc* t, float u, float v, float out[4])
 {
+	if (t->filter != 0) { textureFiltered(t, u, v, 0.0f, out); return; }
 	if (u < 0.0f || u > 1.0f) u = t->wrapX == 0 ? __fsub_rn(u, floorf(u)) : fmaxf(0.0f, fminf(1.0f, u));
 	if (v < 0.0f || v > 1.0f) v = t->wrapY == 0 ? __fsub_rn(v, floorf(v)) : fmaxf(0.0f, fminf(1.0f, v));
 	const float x = __fmul_rn((float) t->wm1, u);
@@ -124,6 +180,13 @@ __device__ __forceinline__ void textureSample(const TextureDesc* t, float u, flo
 	out[1] = __fmul_rn((float) ((texel >> 8) & 0xFFu), inv255);
 	out[2] = __fmul_rn((float) ((texel >> 16) & 0xFFu), inv255);
 	out[3] = 1.0f;
+}
+
+/* srpTextureGetFilteredColorLod on the device. */
+__device__ __forceinline__ void textureSampleLod(const TextureDesc* t, float u, float v, float lod, float out[4])
+{
+	if (t->filter == 0) textureSample(t, u, v, out);
+	else textureFiltered(t, u, v, lod, out);
 }
 
 /* ------------------------------------------------------------ varyings */

@@ -65,12 +65,19 @@ struct DrawState {
 	int pad1;
 };
 
+/* Levels of a mip chain kept on the device (textures up to 2^31 texels wide). */
+constexpr int kMaxMipLevels = 32;
+
 /* Device texture descriptor (RGBA8 texels, alpha unused: the reference keeps
  * three channels and reads alpha as 1). */
 struct TextureDesc {
-	const uint32_t* texels;
+	const uint32_t* texels;          /* level 0, then the mip levels (TRILINEAR) */
 	int width, height, wm1, hm1;
 	int wrapX, wrapY;
+	int filter;                      /* SRPTextureFilter */
+	int nLevels;                     /* levels stored (1 unless TRILINEAR) */
+	int lw[kMaxMipLevels], lh[kMaxMipLevels];
+	uint32_t loff[kMaxMipLevels];    /* first texel of each level */
 };
 
 /* Triangle record read by the tile resolve kernel (64 bytes). */

@@ -26,8 +26,13 @@ __device__ __forceinline__ void devTexSample(const void* tex, float u, float v, 
 {
 	textureSample((const TextureDesc*) tex, u, v, out);
 }
+__device__ __forceinline__ void devTexSampleLod(const void* tex, float u, float v, float lod, float out[4])
+{
+	textureSampleLod((const TextureDesc*) tex, u, v, lod, out);
+}
 }  // namespace srpg
 #define SRP_DEVICE_TEXTURE_SAMPLE(tex, u, v, out) srpg::devTexSample((const void*) (tex), u, v, out)
+#define SRP_DEVICE_TEXTURE_SAMPLE_LOD(tex, u, v, lod, out) srpg::devTexSampleLod((const void*) (tex), u, v, lod, out)
 #include "srp/shaderlib_impl.h"
 
 namespace srpg {

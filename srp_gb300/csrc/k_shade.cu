@@ -341,6 +341,7 @@ static void shadeKind(const DrawParams& P, uint32_t numTiles, cudaStream_t s)
 	case SRP_GPU_FS_MIXED: pdlLaunch(k_shade<KIND, SRP_GPU_FS_MIXED, MULTI, TMA>, b, t, 0, s, P, numTiles); break;
 	case SRP_GPU_FS_BYTE_PALETTE: pdlLaunch(k_shade<KIND, SRP_GPU_FS_BYTE_PALETTE, MULTI, TMA>, b, t, 0, s, P, numTiles); break;
 	case SRP_GPU_FS_PRIMITIVE_MOD: pdlLaunch(k_shade<KIND, SRP_GPU_FS_PRIMITIVE_MOD, MULTI, TMA>, b, t, 0, s, P, numTiles); break;
+	case SRP_GPU_FS_TEXTURE_LOD: pdlLaunch(k_shade<KIND, SRP_GPU_FS_TEXTURE_LOD, MULTI, TMA>, b, t, 0, s, P, numTiles); break;
 	case kFsLearned:
 		if constexpr (KIND == kKindTri) {
 			/* one CTA per SM, its groups looping over the tile pairs */

@@ -20,8 +20,13 @@ __device__ __forceinline__ void rasterTexSample(const void* tex, float u, float 
 {
 	textureSample((const TextureDesc*) tex, u, v, out);
 }
+__device__ __forceinline__ void rasterTexSampleLod(const void* tex, float u, float v, float lod, float out[4])
+{
+	textureSampleLod((const TextureDesc*) tex, u, v, lod, out);
+}
 }  // namespace srpg
 #define SRP_DEVICE_TEXTURE_SAMPLE(tex, u, v, out) srpg::rasterTexSample((const void*) (tex), u, v, out)
+#define SRP_DEVICE_TEXTURE_SAMPLE_LOD(tex, u, v, lod, out) srpg::rasterTexSampleLod((const void*) (tex), u, v, lod, out)
 #include "srp/shaderlib_impl.h"
 
 namespace srpg {
@@ -56,6 +61,7 @@ __device__ __forceinline__ void runFS(SRPFragmentShaderIn* in, SRPFragmentShader
 	case SRP_GPU_FS_MIXED: srpslFsMixed(in, out); break;
 	case SRP_GPU_FS_BYTE_PALETTE: srpslFsBytePalette(in, out); break;
 	case SRP_GPU_FS_PRIMITIVE_MOD: srpslFsPrimitiveMod(in, out); break;
+	case SRP_GPU_FS_TEXTURE_LOD: srpslFsTextureLod(in, out); break;
 	default: break;
 	}
 }

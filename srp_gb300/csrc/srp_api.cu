@@ -1308,31 +1308,115 @@ struct SRPTexture {
 	uint8_t* rgb = nullptr;   /* host copy, 3 channels */
 	int width = 0, height = 0, wm1 = 0, hm1 = 0;
 	SRPTextureWrappingMode wx = TW_REPEAT, wy = TW_REPEAT;
-	uint32_t* texels = nullptr;      /* device RGBA8 */
+	uint32_t* texels = nullptr;      /* device RGBA8: level 0, then the mip levels once built */
 	TextureDesc* desc = nullptr;     /* device descriptor */
 	bool dirty = true;
+	/* filtering (srpTextureSetFilter): the mip chain, built on the host when
+	 * TRILINEAR is first set, levels 1.. stored one after the other */
+	SRPTextureFilter filter = SRP_TEXTURE_FILTER_NEAREST;
+	int nLevels = 1;                 /* levels built */
+	int lw[kMaxMipLevels] = {}, lh[kMaxMipLevels] = {};
+	size_t loff[kMaxMipLevels] = {}; /* first texel of each level, level 0 included */
+	std::vector<uint8_t> mips;       /* RGB8 of levels 1.. */
 };
+
+static const uint8_t* texelAt(const SRPTexture* t, int l, int x, int y)
+{
+	if (l == 0) return t->rgb + 3 * ((size_t) y * t->width + x);
+	return t->mips.data() + 3 * (t->loff[l] - (size_t) t->width * t->height + (size_t) y * t->lw[l] + x);
+}
+
+/* The mip chain of srp/texture.h: level l + 1 is the 2x2 box average of
+ * level l (edge texels repeated for odd sizes), rounded to nearest. */
+static void textureBuildMips(SRPTexture* t)
+{
+	const int n = std::min(srpTextureMipLevels(t->width, t->height), kMaxMipLevels);
+	t->lw[0] = t->width; t->lh[0] = t->height; t->loff[0] = 0;
+	size_t at = (size_t) t->width * t->height;
+	for (int l = 1; l < n; ++l) {
+		t->lw[l] = std::max(1, t->lw[l - 1] / 2);
+		t->lh[l] = std::max(1, t->lh[l - 1] / 2);
+		t->loff[l] = at;
+		at += (size_t) t->lw[l] * t->lh[l];
+	}
+	t->mips.assign((at - (size_t) t->width * t->height) * 3, 0);
+	t->nLevels = n;
+	for (int l = 1; l < n; ++l) {
+		const int pw = t->lw[l - 1], ph = t->lh[l - 1];
+		for (int j = 0; j < t->lh[l]; ++j)
+			for (int i = 0; i < t->lw[l]; ++i) {
+				const int x0 = std::min(2 * i, pw - 1), x1 = std::min(2 * i + 1, pw - 1);
+				const int y0 = std::min(2 * j, ph - 1), y1 = std::min(2 * j + 1, ph - 1);
+				const uint8_t *a = texelAt(t, l - 1, x0, y0), *b = texelAt(t, l - 1, x1, y0);
+				const uint8_t *c = texelAt(t, l - 1, x0, y1), *d = texelAt(t, l - 1, x1, y1);
+				uint8_t* o = (uint8_t*) texelAt(t, l, i, j);
+				for (int k = 0; k < 3; ++k) o[k] = (uint8_t) ((a[k] + b[k] + c[k] + d[k] + 2) / 4);
+			}
+	}
+}
+
+/* Device texels of every level built so far (RGBA8), replacing the old copy. */
+static bool textureUploadLevels(SRPTexture* t, const char* fn)
+{
+	const size_t n = t->loff[t->nLevels - 1] + (size_t) t->lw[t->nLevels - 1] * t->lh[t->nLevels - 1];
+	std::vector<uint32_t> rgba(n);
+	for (int l = 0; l < t->nLevels; ++l)
+		for (int y = 0; y < t->lh[l]; ++y)
+			for (int x = 0; x < t->lw[l]; ++x) {
+				const uint8_t* p = texelAt(t, l, x, y);
+				rgba[t->loff[l] + (size_t) y * t->lw[l] + x] = (uint32_t) p[0] | (uint32_t) p[1] << 8 | (uint32_t) p[2] << 16;
+			}
+	uint32_t* dev = nullptr;
+	if (!cudaOk(cudaMalloc(&dev, n * 4), fn, "cudaMalloc")) return false;
+	cudaMemcpy(dev, rgba.data(), n * 4, cudaMemcpyHostToDevice);
+	if (t->texels) {
+		/* draws queued with the old texels may still read them */
+		cudaDeviceSynchronize();
+		cudaFree(t->texels);
+	}
+	t->texels = dev;
+	t->dirty = true;
+	return true;
+}
 
 static bool textureSync(SRPTexture* t)
 {
 	if (!t->texels) {
-		if (!cudaOk(cudaMalloc(&t->texels, (size_t) t->width * t->height * 4), "srpNewTexture", "cudaMalloc")) return false;
+		t->lw[0] = t->width; t->lh[0] = t->height; t->loff[0] = 0;
 		if (!cudaOk(cudaMalloc(&t->desc, sizeof(TextureDesc)), "srpNewTexture", "cudaMalloc")) return false;
-		std::vector<uint32_t> rgba((size_t) t->width * t->height);
-		for (size_t i = 0; i < rgba.size(); ++i)
-			rgba[i] = (uint32_t) t->rgb[3 * i] | (uint32_t) t->rgb[3 * i + 1] << 8 | (uint32_t) t->rgb[3 * i + 2] << 16;
-		cudaMemcpy(t->texels, rgba.data(), rgba.size() * 4, cudaMemcpyHostToDevice);
+		if (!textureUploadLevels(t, "srpNewTexture")) return false;
 	}
 	if (t->dirty) {
-		TextureDesc d;
+		TextureDesc d = {};
 		d.texels = t->texels;
 		d.width = t->width; d.height = t->height; d.wm1 = t->wm1; d.hm1 = t->hm1;
 		d.wrapX = t->wx; d.wrapY = t->wy;
+		d.filter = t->filter;
+		d.nLevels = t->filter == SRP_TEXTURE_FILTER_TRILINEAR ? t->nLevels : 1;
+		for (int l = 0; l < t->nLevels; ++l) { d.lw[l] = t->lw[l]; d.lh[l] = t->lh[l]; d.loff[l] = (uint32_t) t->loff[l]; }
 		cudaMemcpyAsync(t->desc, &d, sizeof d, cudaMemcpyHostToDevice, g.stream);
 		cudaStreamSynchronize(g.stream);
 		t->dirty = false;
 	}
 	return true;
+}
+
+/* Host bilinear sample of level l (channels in 0..255), as the device's. */
+static void hostBilinear(const SRPTexture* t, int l, float u, float v, float c[3])
+{
+	const int w = t->lw[l], h = t->lh[l];
+	const float x = (float) (w - 1) * u, y = (float) (h - 1) * (1.0f - v);
+	const float fx0 = floorf(x), fy0 = floorf(y);
+	const int x0 = std::min(std::max((int) fx0, 0), w - 1), y0 = std::min(std::max((int) fy0, 0), h - 1);
+	const float fx = x - fx0, fy = y - fy0;
+	const int x1 = x0 + 1 < w ? x0 + 1 : (t->wx == TW_REPEAT ? 0 : w - 1);
+	const int y1 = y0 + 1 < h ? y0 + 1 : (t->wy == TW_REPEAT ? 0 : h - 1);
+	const uint8_t *a = texelAt(t, l, x0, y0), *b = texelAt(t, l, x1, y0), *d = texelAt(t, l, x0, y1), *e = texelAt(t, l, x1, y1);
+	for (int k = 0; k < 3; ++k) {
+		const float top = (float) a[k] + fx * ((float) b[k] - (float) a[k]);
+		const float bot = (float) d[k] + fx * ((float) e[k] - (float) d[k]);
+		c[k] = top + fy * (bot - top);
+	}
 }
 
 extern "C" {
@@ -1376,9 +1460,57 @@ void srpFreeTexture(SRPTexture* t)
 	delete t;
 }
 
+int srpTextureMipLevels(int w, int h)
+{
+	int n = 1;
+	while (w > 1 || h > 1) { w = w > 1 ? w / 2 : 1; h = h > 1 ? h / 2 : 1; ++n; }
+	return n;
+}
+
+void srpTextureSetFilter(SRPTexture* t, SRPTextureFilter f)
+{
+	if (!t) return;
+	if (f != SRP_TEXTURE_FILTER_NEAREST && f != SRP_TEXTURE_FILTER_BILINEAR && f != SRP_TEXTURE_FILTER_TRILINEAR) {
+		SRP_ERROR("srpTextureSetFilter", "Unknown texture filter (%i). Falling back to SRP_TEXTURE_FILTER_NEAREST", (int) f);
+		f = SRP_TEXTURE_FILTER_NEAREST;
+	}
+	if (f == SRP_TEXTURE_FILTER_TRILINEAR && t->nLevels == 1 && srpTextureMipLevels(t->width, t->height) > 1) {
+		/* the chain is built once, here: draws then allocate nothing for it */
+		textureBuildMips(t);
+		if (!textureUploadLevels(t, "srpTextureSetFilter")) return;
+	}
+	t->filter = f;
+	t->dirty = true;
+}
+
+SRPTextureFilter srpTextureGetFilter(const SRPTexture* t) { return t ? t->filter : SRP_TEXTURE_FILTER_NEAREST; }
+
+void srpTextureGetFilteredColorLod(const SRPTexture* t, float u, float v, float lod, float out[4])
+{
+	if (t->filter == SRP_TEXTURE_FILTER_NEAREST) { srpTextureGetFilteredColor(t, u, v, out); return; }
+	if (u < 0 || u > 1) u = (float) (t->wx == TW_REPEAT ? (double) u - floor(u) : fmax(0.0, fmin(1.0, u)));
+	if (v < 0 || v > 1) v = (float) (t->wy == TW_REPEAT ? (double) v - floor(v) : fmax(0.0, fmin(1.0, v)));
+	float c[3];
+	hostBilinear(t, 0, u, v, c);
+	if (t->filter == SRP_TEXTURE_FILTER_TRILINEAR && t->nLevels > 1) {
+		const float top = (float) (t->nLevels - 1);
+		const float ld = lod > 0.0f ? (lod < top ? lod : top) : 0.0f;
+		const int l0 = (int) floorf(ld);
+		const float f = ld - (float) l0;
+		float c0[3], c1[3];
+		hostBilinear(t, l0, u, v, c0);
+		hostBilinear(t, l0 + 1 < t->nLevels ? l0 + 1 : l0, u, v, c1);
+		for (int k = 0; k < 3; ++k) c[k] = c0[k] + f * (c1[k] - c0[k]);
+	}
+	const float inv255 = (float) (1. / 255.);
+	for (int k = 0; k < 3; ++k) out[k] = c[k] * inv255;
+	out[3] = 1.f;
+}
+
 void srpTextureGetFilteredColor(const SRPTexture* t, float u, float v, float out[4])
 {
 	/* host lookup, same arithmetic as the device sampler (texture.c:56-81) */
+	if (t->filter != SRP_TEXTURE_FILTER_NEAREST) { srpTextureGetFilteredColorLod(t, u, v, 0.0f, out); return; }
 	if (u < 0 || u > 1) u = (float) (t->wx == TW_REPEAT ? (double) u - floor(u) : fmax(0.0, fmin(1.0, u)));
 	if (v < 0 || v > 1) v = (float) (t->wy == TW_REPEAT ? (double) v - floor(v) : fmax(0.0, fmin(1.0, v)));
 	float x = (float) t->wm1 * u;
@@ -1452,7 +1584,7 @@ static int lookupFS(void* fn)
 		{ (void*) srpFsMarble, SRP_GPU_FS_MARBLE }, { (void*) srpFsDepthOverwrite, SRP_GPU_FS_DEPTH_OVERWRITE },
 		{ (void*) srpFsFragCoord, SRP_GPU_FS_FRAGCOORD }, { (void*) srpFsFlatInt, SRP_GPU_FS_FLAT_INT },
 		{ (void*) srpFsMixed, SRP_GPU_FS_MIXED }, { (void*) srpFsBytePalette, SRP_GPU_FS_BYTE_PALETTE },
-		{ (void*) srpFsPrimitiveMod, SRP_GPU_FS_PRIMITIVE_MOD },
+		{ (void*) srpFsPrimitiveMod, SRP_GPU_FS_PRIMITIVE_MOD }, { (void*) srpFsTextureLod, SRP_GPU_FS_TEXTURE_LOD },
 	};
 	for (auto& b : builtin) if (b.f == fn) return b.id;
 	for (auto& e : g.reg.fs) if (e.first == fn) return e.second;

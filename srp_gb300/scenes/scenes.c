@@ -139,6 +139,7 @@ struct Scene {
 	SRPType itype[MAX_BUF];
 	/* shading */
 	SRPTexture* tex;
+	SRPTexture* texExtra[2];   /* more textures of a scene (texfilter) */
 	size_t texBytes;
 	int nprog;
 	SRPStdUniform uni[MAX_PROG];
@@ -720,6 +721,82 @@ static void renderInterp(Scene* s, SRPFramebuffer* fb)
 	drawI(s, 0, 0, fb, 2, SRP_PRIM_TRIANGLES, 18, 6);  /* flat int, last vertex */
 	drawI(s, 0, 0, fb, 3, SRP_PRIM_TRIANGLES, 24, 6);  /* fragCoord */
 }
+
+#ifndef SCENES_REF
+/* Texture filtering (an addition: the reference samples the nearest texel
+ * only): three floors receding from z = 1.2 to 40, textured 2 x 10 times
+ * over with one 96 x 64 texture (repeat in u, clamp in v), sampled nearest,
+ * bilinearly, and trilinearly at a level of detail growing with w
+ * (srpFsTextureLod). */
+static void renderTexFilter(Scene* s, SRPFramebuffer* fb)
+{
+	srpDepthTest(true);
+	srpDepthCompareOp(SRP_COMPARE_LESS);
+	srpRasterCullFace(SRP_FACE_NONE);
+	const size_t n = s->ibytes[0] / 4 / 3;
+	for (int k = 0; k < 3; ++k) drawI(s, 0, 0, fb, k, SRP_PRIM_TRIANGLES, (size_t) k * n, n);
+}
+
+static void buildTexFilter(Scene* s, Rng* rng)
+{
+	featureSize(s);
+	enum { G = 12 };   /* quads per floor side */
+	float* v = (float*) malloc(sizeof(float) * 5 * 3 * (G + 1) * (G + 1));
+	uint32_t* idx = (uint32_t*) malloc(sizeof(uint32_t) * 3 * 3 * 6 * G * G);
+	size_t nv = 0, ni = 0;
+	for (int f = 0; f < 3; ++f) {
+		const uint32_t base = (uint32_t) nv;
+		const double x0 = -1.9 + 1.3 * f + 0.05 * rngRange(rng, -1, 1);
+		for (int j = 0; j <= G; ++j)
+			for (int i = 0; i <= G; ++i) {
+				float* p = v + 5 * nv++;
+				const double a = (double) i / G, b = (double) j / G;
+				const double z = 1.2 * pow(40.0 / 1.2, b);
+				p[0] = (float) (x0 + 1.2 * a); p[1] = -0.8f; p[2] = (float) z;
+				p[3] = (float) (2.0 * a); p[4] = (float) (10.0 * b + 0.02 * f);
+			}
+		for (int j = 0; j < G; ++j)
+			for (int i = 0; i < G; ++i) {
+				const uint32_t q = base + (uint32_t) (j * (G + 1) + i);
+				const uint32_t t[6] = { q, q + 1, q + G + 2, q, q + G + 2, q + G + 1 };
+				memcpy(idx + ni, t, sizeof t);
+				ni += 6;
+			}
+	}
+	addVB(s, v, 20, nv * 20);
+	addIB(s, SRP_UINT32, idx, ni * 4);
+	free(v); free(idx);
+	const int tw = 96, th = 64;
+	uint8_t* tex = (uint8_t*) malloc((size_t) tw * th * 3);
+	for (int y = 0; y < th; ++y)
+		for (int x = 0; x < tw; ++x)
+			for (int c = 0; c < 3; ++c) {
+				const int check = ((x / 8) ^ (y / 8)) & 1;
+				tex[3 * (y * tw + x) + c] = (uint8_t) ((check ? 200 : 40) + (int) (rngNext(rng) >> 59) * (c + 1));
+			}
+	s->tex = makeTexture(s, tex, tw, th, TW_REPEAT, TW_CLAMP_TO_EDGE);
+	s->texExtra[0] = makeTexture(s, tex, tw, th, TW_REPEAT, TW_CLAMP_TO_EDGE);
+	s->texExtra[1] = makeTexture(s, tex, tw, th, TW_REPEAT, TW_CLAMP_TO_EDGE);
+	free(tex);
+	srpTextureSetFilter(s->texExtra[0], SRP_TEXTURE_FILTER_BILINEAR);
+	srpTextureSetFilter(s->texExtra[1], SRP_TEXTURE_FILTER_TRILINEAR);
+	SRPVaryingInfo vp[1] = { vi(2, SRP_FLOAT, SRP_INTERPOLATION_MODE_PERSPECTIVE) };
+	for (int k = 0; k < 3; ++k) {
+		SRPStdUniform* u = &s->uni[k];
+		baseUniform(u);
+		u->projection = perspective60((float) s->W / (float) s->H, 0.5f, 60.f);
+		u->passOffset = 3; u->passCount = 2;
+		u->texelScale = 0.45f + 0.05f * (float) rngU(rng);
+		u->texture = k == 0 ? s->tex : s->texExtra[k - 1];
+	}
+	program(s, 0, srpVsTransform, srpFsTexture, 0, 1, vp);
+	program(s, 1, srpVsTransform, srpFsTexture, 0, 1, vp);
+	program(s, 2, srpVsTransform, srpFsTextureLod, 0, 1, vp);
+	s->depthInit = 1.0f;
+	s->render = renderTexFilter;
+	s->draws = 3;
+}
+#endif
 
 /* Four tilted quads (perspective uv, affine uv, flat int with first and last
  * provoking vertex, fragCoord); texture 64x48 with repeat/clamp wrapping. */
@@ -1471,6 +1548,9 @@ static const SceneDef DEFS[] = {
 	{ "clip_lines", buildClipLines },
 	{ "points", buildPoints },
 	{ "interp", buildInterp },
+#ifndef SCENES_REF
+	{ "texfilter", buildTexFilter },
+#endif
 	{ "depth_ops", buildDepthOps },
 	{ "raster_rules", buildRules },
 	{ "scissor", buildScissor },
@@ -1517,6 +1597,8 @@ void sceneDestroy(Scene* s)
 	for (int k = 0; k < s->nvb; ++k) { srpFreeVertexBuffer(s->vb[k]); hostFree(s->vdata[k]); }
 	for (int k = 0; k < s->nib; ++k) { srpFreeIndexBuffer(s->ib[k]); hostFree(s->idata[k]); }
 	if (s->tex) srpFreeTexture(s->tex);
+	for (int k = 0; k < 2; ++k)
+		if (s->texExtra[k]) srpFreeTexture(s->texExtra[k]);
 	free(s);
 }
 

@@ -28,7 +28,8 @@ def test_gpu_matches_reference_fixture(built_library, case):
 SEEDED = [(n, seed, scale) for n, scale in [
     ("sphere", 0.5), ("soup", 0.02), ("clip_tris", 1.0), ("clip_lines", 1.0), ("points", 1.0),
     ("interp", 1.0), ("depth_ops", 1.0), ("raster_rules", 1.0), ("scissor", 1.0), ("stencil", 1.0),
-    ("poly_modes", 1.0), ("topologies", 1.0), ("late_z", 1.0), ("lit", 1.0), ("varyings", 1.0)]
+    ("poly_modes", 1.0), ("topologies", 1.0), ("late_z", 1.0), ("lit", 1.0), ("varyings", 1.0),
+    ("texfilter", 1.0)]
     for seed in (2, 5)]
 
 

@@ -50,8 +50,8 @@ class StdUniform(ctypes.Structure):
                 ("shininess", ctypes.c_float), ("marbleFrequency", ctypes.c_float), ("marbleGain", ctypes.c_float),
                 ("depthScale", ctypes.c_float), ("depthBias", ctypes.c_float)] + \
                [(n, ctypes.c_uint32) for n in ("nLights", "marbleOctaves", "passOffset", "passCount", "normalOffset",
-                                               "uvOffset", "extraOffset", "extraCount", "varyingOffset", "pad0")] + \
-               [("texture", ctypes.c_void_p)]
+                                               "uvOffset", "extraOffset", "extraCount", "varyingOffset")] + \
+               [("texelScale", ctypes.c_float), ("texture", ctypes.c_void_p)]
 
 
 class Api:
