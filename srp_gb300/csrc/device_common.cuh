@@ -20,25 +20,11 @@ namespace srpg {
  * float x this is |x| <= 1e-9f, 1e-9f being the largest float not above 1e-9. */
 __device__ __forceinline__ bool roughlyZero(float x) { return fabsf(x) <= 1e-9f; }
 
-/* One axis of the viewport map: (float) (half * ((double) v + 1.)), half =
- * size / 2. When 2^-12 <= |v| < 2^36 (or v = 0), v + 1 has at most 37
- * significant bits and half (size < 2^16) at most 16, so the double sum and
- * product are exact: the result is the exact real (v + 1) * half rounded
- * once to float, which is what the fused multiply-add computes, without the
- * FP64 pipe (slow on this GPU). Other values take the double path. */
-__device__ __forceinline__ float viewportAxis(float half, float v)
-{
-	const float a = fabsf(v);
-	if (half < 32768.0f && (v == 0.0f || (a >= 0x1p-12f && a < 0x1p36f))) return __fmaf_rn(v, half, half);
-	return (float) ((double) half * ((double) v + 1.));
-}
-
 /* NDC -> screen space in double, then narrowed (src/core/framebuffer.c:48-55). */
 __device__ __forceinline__ void ndcToScreen(int W, int H, float nx, float ny, float& sx, float& sy)
 {
-	/* (double) (float) W / 2. is exact in float for W < 2^24 */
-	sx = viewportAxis(__fmul_rn((float) W, 0.5f), nx);
-	sy = viewportAxis(__fmul_rn((float) H, 0.5f), -ny);
+	sx = (float) (((double) (float) W / 2.) * ((double) nx + 1.));
+	sy = (float) (((double) (float) H / 2.) * (1. - (double) ny));
 }
 
 /* invW = (float)(1.0 / (double) w): a float quotient computed in double and
