@@ -74,7 +74,9 @@ void srpGpuFramebufferFillBatch(const SRPFramebuffer* const* fbs, size_t n, uint
 
 /** srpVertexBufferCopyData without waiting for the copy. Copies run in
  *  order on a copy stream of the library; a draw that reads the buffer waits
- *  for its copy, and nothing else does. */
+ *  for its copy, and nothing else does. A copy into a buffer that earlier
+ *  draws read does not wait for them either: every draw call returns only
+ *  after its device stages have read its vertex and index buffers. */
 void srpGpuVertexBufferCopyDataAsync(SRPVertexBuffer* buffer, size_t stride, size_t nBytes, const void* data);
 /** srpIndexBufferCopyData without waiting for the copy. */
 void srpGpuIndexBufferCopyDataAsync(SRPIndexBuffer* buffer, SRPType type, size_t nBytes, const void* data);
