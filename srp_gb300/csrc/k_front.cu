@@ -1214,6 +1214,7 @@ __device__ unsigned long long walkLineRuns(const DrawParams& P, const LineRec& L
 	unsigned long long passed = 0;
 	const uint32_t invalid = (uint32_t) (P.st.tilesX * P.st.tilesY);
 	const unsigned long long size = (unsigned long long) P.st.W * (unsigned long long) P.st.H;
+	const bool inside = (L.slots & kLineInside) != 0;
 	uint32_t used = 0, runKey = invalid, runN = 0;
 	auto flush = [&]() {
 		if (runN) {
@@ -1231,12 +1232,18 @@ __device__ unsigned long long walkLineRuns(const DrawParams& P, const LineRec& L
 		uint32_t key = invalid;
 		if (scissorPass(P.st, px, py)) {
 			++passed;  /* counted as the reference's fragments are, before the framebuffer bound */
-			const unsigned long long idx = (unsigned long long) (long long) py * (unsigned long long) P.st.W
-			                             + (unsigned long long) (long long) px;
-			if (idx < size) {
-				const uint32_t gx = (uint32_t) (idx % (unsigned long long) P.st.W);
-				const uint32_t gy = (uint32_t) (idx / (unsigned long long) P.st.W);
-				key = (gy / kTile) * (uint32_t) P.st.tilesX + gx / kTile;
+			if (inside) {
+				/* every step of the line lands in the framebuffer (lineRunInfo):
+				 * the pixel is (px, py) itself, no row wraps */
+				key = ((uint32_t) py / kTile) * (uint32_t) P.st.tilesX + (uint32_t) px / kTile;
+			} else {
+				const unsigned long long idx = (unsigned long long) (long long) py * (unsigned long long) P.st.W
+				                             + (unsigned long long) (long long) px;
+				if (idx < size) {
+					const uint32_t gx = (uint32_t) (idx % (unsigned long long) P.st.W);
+					const uint32_t gy = (uint32_t) (idx / (unsigned long long) P.st.W);
+					key = (gy / kTile) * (uint32_t) P.st.tilesX + gx / kTile;
+				}
 			}
 		}
 		if (key != runKey || runN == kRunMaxCount) {

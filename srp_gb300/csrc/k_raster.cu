@@ -296,9 +296,8 @@ __global__ void __launch_bounds__(kResolveWarps * 32) k_resolve_frags(const __gr
 			item = vals[b + lane];
 			const LineFrag F = P.frags[item];
 			/* the logical pixel, as the reference indexes it (px may equal the width) */
-			const unsigned long long at = (unsigned long long) (long long) F.py * (unsigned long long) st.W
-			                            + (unsigned long long) (long long) F.px;
-			const int gx = (int) (at % (unsigned long long) st.W), gy = (int) (at / (unsigned long long) st.W);
+			int gx, gy;
+			lineFragPixel(st.W, F.px, F.py, gx, gy);
 			const int qq = (gy - y0) * kTile + (gx - x0);
 			if (qq >= 0 && qq < 64) q = qq;
 			d = F.depth;

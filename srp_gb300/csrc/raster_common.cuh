@@ -149,6 +149,19 @@ __device__ __forceinline__ void shadeItem(const DrawParams& P, const unsigned ch
 	runShader<FS>(in, out);
 }
 
+/* The pixel a line fragment lands on, as the reference indexes it: its
+ * logical (px, py) when 0 <= px < W and py >= 0; otherwise the row-major
+ * index py * W + px wraps (px may equal the width), and the pixel comes
+ * from it. */
+__device__ __forceinline__ void lineFragPixel(int W, int px, int py, int& gx, int& gy)
+{
+	if ((unsigned) px < (unsigned) W && py >= 0) { gx = px; gy = py; return; }
+	const unsigned long long at = (unsigned long long) (long long) py * (unsigned long long) W
+	                            + (unsigned long long) (long long) px;
+	gx = (int) (at % (unsigned long long) W);
+	gy = (int) (at / (unsigned long long) W);
+}
+
 /* Record of an item, by kind (loaded ahead of use by k_resolve_heavy). */
 template <int KIND> struct RecOf { typedef TriRaster T; };
 template <> struct RecOf<kKindPoint> { typedef PointRec T; };
@@ -226,9 +239,8 @@ __device__ __forceinline__ void coverageRec(const DrawParams& P, const typename 
 	} else {
 		const LineFrag& F = Rec;
 		flags = 1u;
-		const unsigned long long idx = (unsigned long long) (long long) F.py * (unsigned long long) P.st.W
-		                             + (unsigned long long) (long long) F.px;
-		const int gx = (int) (idx % (unsigned long long) P.st.W), gy = (int) (idx / (unsigned long long) P.st.W);
+		int gx, gy;
+		lineFragPixel(P.st.W, F.px, F.py, gx, gy);
 		const int q = (gy - y0) * kTile + (gx - x0);
 		if (q >= 0 && q < 64) { mask = 1ull << q; dep[q] = F.depth; }
 	}
