@@ -937,8 +937,11 @@ __device__ __forceinline__ unsigned long long orderedOffset(const DrawParams& P,
 	return sPrefix + warpExcl + (incl - mine);
 }
 
+/* Filled triangles (millions per draw) run at kSetupBlocksPerSM; the other
+ * modes, with their clip paths inline and far fewer primitives, at 6 blocks
+ * per SM, whose registers hold them without spills. */
 template <int MODE>
-__global__ void __launch_bounds__(kSetupThreads, kSetupBlocksPerSM) k_setup(const __grid_constant__ DrawParams P)
+__global__ void __launch_bounds__(kSetupThreads, MODE == kTriFill ? kSetupBlocksPerSM : 6) k_setup(const __grid_constant__ DrawParams P)
 {
 	gridDepSync();
 	__shared__ uint32_t sBlock;
