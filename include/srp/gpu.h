@@ -269,10 +269,13 @@ int srpGpuMlpGradients(SRPGpuMlp* mlp, const float* samples, size_t n, float* gr
  *  bytes each) and by the framebuffer (about 4 bytes per pixel) must leave at
  *  least 4 MiB of the array free; this is checked before anything runs. What
  *  the draw produces is checked once the setup stage has counted it: tile
- *  entries (about 16 bytes each, 32 for lines) in three quarters of what is
- *  left, barycentric tables of large triangles in the other quarter, at most
- *  16384 vertices created by clipping and 4096 triangles that need clipping
- *  (whose extra triangles are counted in the primitive part).
+ *  entries (about 16 bytes each) in three quarters of what is left,
+ *  barycentric tables of large triangles in the other quarter, at most 16384
+ *  vertices created by clipping and 4096 triangles that need clipping (whose
+ *  extra triangles are counted in the primitive part). A line draw's entries
+ *  are runs of up to 15 fragments in one tile, about one per tile a line
+ *  crosses (one per step for lines that leave the framebuffer), at about
+ *  340 bytes each with their fragment records.
  *  A draw beyond a limit is rejected: it returns -1, says which size was too
  *  large through the message callback and leaves the framebuffer unchanged.
  *
